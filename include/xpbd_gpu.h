@@ -1,0 +1,218 @@
+/*
+ * xpbd_gpu.h -- C ABI of the GB300 (sm_103a) XPBD substep solver.
+ *
+ * The reference (MAVYWAVY902/xpbd-tissue-sim) has no FFI: its solver seam is
+ * the compile-time template interface XPBDSolver<IsFirstOrder, Projectors...>
+ * owned by XPBDMeshObject_ (include/simobject/XPBDMeshObject.hpp:229), chosen
+ * by the YAML key `solver-type` (include/config/simobject/XPBDMeshObjectConfig.hpp:26-34)
+ * in XPBDObjectFactory (include/simobject/XPBDObjectFactory.hpp:53-77). Each
+ * entry point below names the member of that surface it replaces.
+ *
+ * Conventions
+ *  - Every call returns an int status (XPBD_OK = 0) and never aborts; the
+ *    reference instead asserts (include/gpu/resource/GPUResource.hpp:8-19).
+ *    xpbd_last_error() gives a message for the last failing call on a context.
+ *  - Vertex arrays are 3 x V column-major doubles (x0,y0,z0,x1,...), the layout
+ *    of Geometry::Mesh::VerticesMat (include/geometry/Mesh.hpp:29).
+ *  - Tets are 4 x T int32, faces 3 x F int32, 0-based, as TetMesh stores them.
+ *  - One context = one deformable object on one CUDA stream. A context is not
+ *    thread-safe; distinct contexts are independent (the reference drives its
+ *    solver from the single Simulation::update thread, Simulation.cpp:332-336).
+ *  - The device computes in FP32; residual and energy reductions finish in FP64.
+ */
+#ifndef XPBD_GPU_H
+#define XPBD_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define XPBD_ABI_VERSION 1
+
+/* status codes */
+#define XPBD_OK 0
+#define XPBD_ERR_INVALID 1      /* bad argument or size                        */
+#define XPBD_ERR_CUDA 2         /* a CUDA runtime call failed                  */
+#define XPBD_ERR_NUMERIC 3      /* a projection produced a non-finite update   */
+#define XPBD_ERR_NO_DEVICE 4    /* no CUDA device / extension not usable       */
+#define XPBD_ERR_STATE 5        /* call not valid in the context's state       */
+#define XPBD_ERR_CAPACITY 6     /* a fixed capacity was exceeded               */
+
+/* solver-type (XPBDObjectSolverTypeEnum, include/common/XPBDEnumTypes.hpp:6-11).
+ * "Gauss-Seidel" maps to the graph-coloured Gauss-Seidel, "Jacobi" and
+ * "Parallel-Jacobi" to the GPU Jacobi solver. */
+#define XPBD_SOLVER_GAUSS_SEIDEL 0
+#define XPBD_SOLVER_JACOBI 1
+
+/* constraint-type (XPBDMeshObjectConstraintConfigurationEnum) */
+#define XPBD_CONSTRAINT_COMBINED 0   /* "Stable-Neohookean-Combined" (2x2 solve)   */
+#define XPBD_CONSTRAINT_SEPARATE 1   /* "Stable-Neohookean" (Dev, then Hyd)        */
+
+/* residual-policy (XPBDSolverResidualPolicyEnum) */
+#define XPBD_RESIDUAL_NEVER 0
+#define XPBD_RESIDUAL_EVERY_SUBSTEP 1
+#define XPBD_RESIDUAL_EVERY_ITERATION 2  /* records ||r|| before every iteration */
+
+/* Jacobi scatter variant */
+#define XPBD_JACOBI_ATOMIC 0   /* warp-level vector atomics into a delta buffer  */
+#define XPBD_JACOBI_GATHER 1   /* per-tet deltas + vertex->tet CSR gather        */
+
+typedef struct xpbd_ctx xpbd_ctx;
+
+/* Mesh and per-element material, the data XPBDMeshObject_::setup() derives
+ * from the loaded TetMesh and its ElasticMaterial list
+ * (src/simobject/XPBDMeshObject.cpp:103-160, 277-417). */
+typedef struct {
+    int64_t num_vertices;
+    int64_t num_tets;
+    int64_t num_faces;        /* surface faces used by collision detection, may be 0 */
+    const double* vertices;   /* 3 x V, column-major, rest = initial state           */
+    const int32_t* tets;      /* 4 x T                                               */
+    const int32_t* faces;     /* 3 x F or NULL                                       */
+    const double* tet_E;      /* T Young's moduli [Pa]                               */
+    const double* tet_nu;     /* T Poisson ratios                                    */
+    const double* tet_density;/* T densities [kg/m^3]                                */
+} xpbd_mesh_desc;
+
+/* Solver parameters (Simulation + XPBDMeshObjectConfig keys). */
+typedef struct {
+    double dt;                 /* time-step [s]                                    */
+    double g_accel;            /* g-accel [m/s^2], acts along -z                   */
+    double collision_rate;     /* collision-rate [Hz]; <= 0 disables the cadence  */
+    int32_t num_iters;         /* num-solver-iters                                 */
+    int32_t solver_type;       /* XPBD_SOLVER_*                                    */
+    int32_t constraint_type;   /* XPBD_CONSTRAINT_*                                */
+    int32_t residual_policy;   /* XPBD_RESIDUAL_*                                  */
+    int32_t jacobi_variant;    /* XPBD_JACOBI_*                                    */
+    int32_t block_size;        /* threads per block for tet kernels; 0 = default   */
+    int32_t max_contacts_per_face; /* contact slots per surface face; 0 = 4        */
+    int32_t use_graphs;        /* capture each substep in a CUDA graph (1) or not  */
+} xpbd_params;
+
+/* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
+ * SimulationConfig.hpp:185-195): dt 1e-3, g 9.81, collision-rate 100 Hz,
+ * 1 iteration, Gauss-Seidel, combined constraints, residual Never. */
+int xpbd_default_params(xpbd_params* p);
+
+int xpbd_abi_version(void);
+const char* xpbd_status_string(int status);
+
+/* Host-only utility (no GPU needed): greedy vertex-disjoint colouring in item
+ * order, the order the coloured Gauss-Seidel uses. arity = 4 for tets, 3 for
+ * faces. Returns the number of colours (> 0) or -XPBD_ERR_INVALID. */
+int xpbd_colour_items(int64_t n_items, int32_t arity, const int32_t* items, int64_t n_vertices,
+                      int32_t* colour_out);
+
+/* Host-only utility (no GPU needed): hexahedral grid of nx x ny x nz hexes
+ * with spacing (hx, hy, hz), five tets per hex, and its boundary triangles, as
+ * MeshUtils::createBeamMsh builds them (src/utils/MeshUtils.cpp:424-660; x =
+ * width, y = length, z = height). split = 0: the alternating split of the
+ * current generator; split = 1: the uniform split of the revision that wrote
+ * resource/cube/cube{2,4}.msh. X is 3 x V, tets 4 x T, faces 3 x F with the
+ * counts from xpbd_grid_counts. */
+int xpbd_grid_counts(int32_t nx, int32_t ny, int32_t nz, int64_t* nv, int64_t* nt, int64_t* nf);
+int xpbd_grid_mesh(int32_t nx, int32_t ny, int32_t nz, double hx, double hy, double hz, int32_t split, double* X,
+                   int32_t* tets, int32_t* faces);
+
+/* Context lifetime: XPBDMeshObject_ ctor + setup() + XPBDSolver ctor/setup()
+ * (XPBDMeshObject.cpp:60-160; XPBDSolver.hpp:47-61). Uploads the mesh, builds
+ * rest shapes, masses, compliances and the colouring. */
+int xpbd_create(const xpbd_mesh_desc* mesh, const xpbd_params* params, xpbd_ctx** out);
+int xpbd_destroy(xpbd_ctx* ctx);
+const char* xpbd_last_error(const xpbd_ctx* ctx);
+
+/* Iteration count (XPBDSolver::_num_iter, XPBDSolver.hpp:139). */
+int xpbd_set_num_iters(xpbd_ctx* ctx, int32_t num_iters);
+
+/* State transfer between the host mesh (Mesh::vertices()) and the device. */
+int xpbd_set_positions(xpbd_ctx* ctx, const double* x3v);
+int xpbd_get_positions(xpbd_ctx* ctx, double* x3v);
+int xpbd_get_prev_positions(xpbd_ctx* ctx, double* x3v);
+int xpbd_set_velocities(xpbd_ctx* ctx, const double* v3v);
+int xpbd_get_velocities(xpbd_ctx* ctx, double* v3v);
+/* float32 xyz-interleaved variants (3*V floats) for callers that keep FP32 */
+int xpbd_set_positions_f32(xpbd_ctx* ctx, const float* x3v);
+int xpbd_get_positions_f32(xpbd_ctx* ctx, float* x3v);
+/* lumped vertex masses (XPBDMeshObject.cpp:277-331) */
+int xpbd_get_masses(xpbd_ctx* ctx, double* m);
+
+/* XPBDMeshObject_Base_::fixVertex (include/simobject/XPBDMeshObjectBase.hpp:97-99):
+ * mask[i] != 0 fixes vertex i (reset to its previous position after solve). */
+int xpbd_set_fixed(xpbd_ctx* ctx, const uint8_t* mask);
+
+/* Kinematic vertex group: fixed vertices driven to rest + offset, the pattern
+ * of fixVertex + a cursor setPosition (src/simulation/GraspingSimulation.cpp:155,241).
+ * set_group records the current positions of idx as their rest positions and
+ * fixes them; set_offset moves them (stream-ordered, before the next step). */
+int xpbd_set_kinematic_group(xpbd_ctx* ctx, int32_t n, const int32_t* idx);
+int xpbd_set_kinematic_offset(xpbd_ctx* ctx, const double* offset3);
+
+/* Rigid spheres (RigidSphere + SphereSDF, src/geometry/SphereSDF.cpp:16-26),
+ * treated as fixed: detection emits static collision constraints. */
+int xpbd_set_spheres(xpbd_ctx* ctx, int32_t n, const double* centers3n, const double* radii);
+
+/* clearCollisionConstraints (XPBDMeshObject.cpp:233-251). */
+int xpbd_clear_collisions(xpbd_ctx* ctx);
+/* clear + CollisionScene::collideObjects against the spheres
+ * (src/collision/CollisionScene.cpp:171-214, 253-283). */
+int xpbd_detect_collisions(xpbd_ctx* ctx);
+/* addStaticCollisionConstraint (XPBDMeshObject.cpp:180-206). */
+int xpbd_add_static_collision(xpbd_ctx* ctx, int32_t face, double u, double v, double w, const double* p3,
+                              const double* n3);
+/* Active contacts, rows of 12 doubles: slot, face, u, v, w, p(3), n(3), lambda.
+ * *n_out receives the count; at most max_rows rows are written. */
+int xpbd_get_collisions(xpbd_ctx* ctx, int32_t max_rows, double* rows, int32_t* n_out);
+
+/* XPBDMeshObject_::update (XPBDMeshObject.cpp:426-505): prev <- x, inertial
+ * move, solve (lambda <- 0, num_iters sweeps), fixed reset. Asynchronous. */
+int xpbd_update(xpbd_ctx* ctx);
+/* XPBDMeshObject_::velocityUpdate (XPBDMeshObject.cpp:507-535). */
+int xpbd_velocity_update(xpbd_ctx* ctx);
+/* Simulation::_timeStep for this object, n times (Simulation.cpp:197-276):
+ * collision detection on the strict cadence test t - t_last > 1/rate,
+ * update, velocity update, t += dt. Asynchronous. */
+int xpbd_step(xpbd_ctx* ctx, int32_t nsteps);
+/* waits for the context's stream; reports CUDA and numeric errors */
+int xpbd_synchronize(xpbd_ctx* ctx);
+int xpbd_get_time(xpbd_ctx* ctx, double* t);
+
+/* ||r||_2 of the elastic constraint residual r = C + alpha_tilde*lambda at the
+ * current state (XPBDSolver::_calculateConstraintResidual, XPBDSolver.hpp:327-391),
+ * and its ratio to ||r(x_pred, 0)|| of the last update. FP64 reduction. */
+int xpbd_residual(xpbd_ctx* ctx, double* abs_norm, double* rel);
+/* lastConstraintResidual(): 2T values in the reference's order (combined:
+ * [dev_0, hyd_0, dev_1, ...]; separate: all dev, then all hyd). */
+int xpbd_get_constraint_residual(xpbd_ctx* ctx, double* r, int64_t n);
+/* Per-iteration ||r|| of the last update when residual_policy is
+ * EVERY_ITERATION: n = num_iters + 1 values (before each sweep, after the last).
+ * Jacobi values are exact state residuals; Gauss-Seidel values are sweep
+ * residuals (each tet evaluated when it is projected) except the last. */
+int xpbd_residual_history(xpbd_ctx* ctx, double* out, int32_t max_n, int32_t* n_out);
+/* Lagrange multipliers, T x 2 (dev, hyd) in tet order. */
+int xpbd_get_lambda(xpbd_ctx* ctx, double* lam);
+/* totalStrainEnergy: sum of C^2/alpha over Dev and Hyd (XPBDMeshObject.cpp:537-549). */
+int xpbd_total_strain_energy(xpbd_ctx* ctx, double* e);
+/* Counters since the last call: projections with a non-finite update (skipped)
+ * and projections that took the FP64 near-degenerate path (|det F| < 1e-3). */
+int xpbd_health(xpbd_ctx* ctx, int64_t* nonfinite, int64_t* degenerate);
+
+/* Colouring in use (coloured Gauss-Seidel): number of tet colours and the
+ * colour of each tet; contacts follow the surface-face colouring. */
+int xpbd_num_colours(xpbd_ctx* ctx, int32_t* n_tet_colours, int32_t* n_face_colours);
+int xpbd_get_tet_colours(xpbd_ctx* ctx, int32_t* colour_of_tet);
+
+/* Per-kernel timing with CUDA events on the context's stream over n substeps
+ * (no graphs). Fills up to max_k entries: average milliseconds per launch and
+ * launches, for kernel ids 0..max_k-1 (see xpbd_kernel_name). */
+int xpbd_profile_steps(xpbd_ctx* ctx, int32_t nsteps, int32_t max_k, double* avg_ms, int64_t* launches);
+const char* xpbd_kernel_name(int32_t id);
+/* number of kernel launches issued by the library since creation */
+int xpbd_launch_count(xpbd_ctx* ctx, int64_t* n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* XPBD_GPU_H */

@@ -1,0 +1,706 @@
+// XPBD oracle: a CPU restatement of the reference's XPBD substep loop.
+//
+// TEST INFRASTRUCTURE ONLY. Nothing in the shipped library links, calls or
+// executes this file; tests, the smoke check and the benchmark's CPU-baseline
+// leg use it as the checker.
+//
+// PARITY STATUS: the physics is "parity unpinned". The reference ships no
+// golden vectors, known-answer tests or stored outputs for the solver, and
+// its own build needs Eigen/yaml-cpp/gmsh, which are absent, so it cannot be
+// run here. The grid-mesh generator IS pinned: its output is compared with
+// the reference's cube{2,4,8,16}.msh files, which the reference's own
+// MeshUtils::createBeamMsh wrote. The physics is checked by known-answer
+// tests derived from the formulas (rest stability, free fall, Lame
+// parameters, finite-difference gradients).
+//
+// Every function cites the reference file:line it restates. Real is the
+// template parameter: double reproduces the reference's CPU build
+// (include/common/types.hpp:6-11, Real = double without HAVE_CUDA), float
+// gives a same-precision oracle for the GPU kernels.
+#pragma once
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace xo {
+
+// ---------------------------------------------------------------------------
+// Grid mesh: restates MeshUtils::createBeamMsh (src/utils/MeshUtils.cpp:424-660)
+// with the hex counts given directly. Axis mapping follows the reference:
+// width index wi -> x, length index li -> y, height index hi -> z, and vertex
+// index hi + wi*(h+1) + li*(w+1)*(h+1) (MeshUtils.cpp:432-435).
+// ---------------------------------------------------------------------------
+struct GridDims {
+    int w, l, h;  // hexes along x, y, z
+    long long V() const { return (long long)(w + 1) * (l + 1) * (h + 1); }
+    long long T() const { return 5LL * w * l * h; }
+    long long F() const { return 4LL * w * h + 4LL * l * h + 4LL * l * w; }
+};
+
+// split = 0: the alternating 5-tet split and face diagonals of the current
+// createBeamMsh source (conforming across hexes). split = 1: the revision of
+// the generator that wrote the reference's resource/cube/cube2.msh and
+// cube4.msh fixtures: every hex takes the first 5-tet pattern and each
+// boundary quad takes its second triangulation exactly when its two in-plane
+// hex indices have equal parity (inferred from those files).
+inline void grid_mesh(const GridDims& d, double ex, double ey, double ez,
+                      double* X, int* tets, int* faces, int split = 0) {
+    const int w = d.w, l = d.l, h = d.h;
+    const bool legacy = split == 1;
+    auto index = [w, h](int li, int wi, int hi) { return hi + wi * (h + 1) + li * (w + 1) * (h + 1); };
+    // vertices (MeshUtils.cpp:437-449)
+    for (int li = 0; li < l + 1; li++)
+        for (int wi = 0; wi < w + 1; wi++)
+            for (int hi = 0; hi < h + 1; hi++) {
+                long long i = index(li, wi, hi);
+                X[3 * i + 0] = wi * ex;
+                X[3 * i + 1] = li * ey;
+                X[3 * i + 2] = hi * ez;
+            }
+    long long fi = 0;
+    auto put3 = [&](int a, int b, int c) {
+        faces[3 * fi + 0] = a; faces[3 * fi + 1] = b; faces[3 * fi + 2] = c; fi++;
+    };
+    // front/back faces, w*h (MeshUtils.cpp:451-500)
+    for (int wi = 0; wi < w; wi++)
+        for (int hi = 0; hi < h; hi++) {
+            int f1 = index(0, wi, hi), f2 = index(0, wi + 1, hi), f3 = index(0, wi + 1, hi + 1), f4 = index(0, wi, hi + 1);
+            int a = legacy ? (wi % 2 != hi % 2) : (wi % 2 == hi % 2);
+            if (!a) { put3(f1, f2, f4); put3(f2, f3, f4); }
+            else    { put3(f1, f2, f3); put3(f1, f3, f4); }
+            int b1 = index(l, wi, hi), b2 = index(l, wi + 1, hi), b3 = index(l, wi + 1, hi + 1), b4 = index(l, wi, hi + 1);
+            a = legacy ? (wi % 2 != hi % 2) : (wi % 2 == hi % 2) - l % 2;
+            if (!a) { put3(b1, b4, b2); put3(b2, b4, b3); }
+            else    { put3(b1, b3, b2); put3(b1, b4, b3); }
+        }
+    // right/left faces, l*h (MeshUtils.cpp:502-550)
+    for (int hi = 0; hi < h; hi++)
+        for (int li = 0; li < l; li++) {
+            int r1 = index(li, w, hi), r2 = index(li + 1, w, hi), r3 = index(li + 1, w, hi + 1), r4 = index(li, w, hi + 1);
+            int a = legacy ? (hi % 2 != li % 2) : (hi % 2 == li % 2) - w % 2;
+            if (a) { put3(r1, r2, r3); put3(r1, r3, r4); }
+            else   { put3(r1, r2, r4); put3(r2, r3, r4); }
+            int l1 = index(li, 0, hi), l2 = index(li + 1, 0, hi), l3 = index(li + 1, 0, hi + 1), l4 = index(li, 0, hi + 1);
+            a = legacy ? (hi % 2 != li % 2) : (hi % 2 == li % 2);
+            if (!a) { put3(l1, l4, l2); put3(l2, l4, l3); }
+            else    { put3(l1, l3, l2); put3(l1, l4, l3); }
+        }
+    // top/bottom faces, l*w (MeshUtils.cpp:552-600)
+    for (int li = 0; li < l; li++)
+        for (int wi = 0; wi < w; wi++) {
+            int t1 = index(li, wi, h), t2 = index(li, wi + 1, h), t3 = index(li + 1, wi + 1, h), t4 = index(li + 1, wi, h);
+            int a = legacy ? (li % 2 != wi % 2) : (li % 2 == wi % 2) - h % 2;
+            if (a) { put3(t1, t2, t3); put3(t1, t3, t4); }
+            else   { put3(t1, t2, t4); put3(t2, t3, t4); }
+            int b1 = index(li, wi, 0), b2 = index(li, wi + 1, 0), b3 = index(li + 1, wi + 1, 0), b4 = index(li + 1, wi, 0);
+            a = legacy ? (li % 2 != wi % 2) : (li % 2 == wi % 2);
+            if (a) { put3(b1, b3, b2); put3(b1, b4, b3); }
+            else   { put3(b1, b4, b2); put3(b2, b4, b3); }
+        }
+    // tets, 5 per hex; split selector a = (hi%2==wi%2) - li%2, where -1 is
+    // truthy (MeshUtils.cpp:602-660)
+    long long ti = 0;
+    auto put4 = [&](int a, int b, int c, int e) {
+        tets[4 * ti + 0] = a; tets[4 * ti + 1] = b; tets[4 * ti + 2] = c; tets[4 * ti + 3] = e; ti++;
+    };
+    for (int li = 0; li < l; li++)
+        for (int wi = 0; wi < w; wi++)
+            for (int hi = 0; hi < h; hi++) {
+                int a = legacy ? 1 : (hi % 2 == wi % 2) - li % 2;
+                int i1 = index(li, wi, hi), i2 = index(li, wi + 1, hi), i3 = index(li + 1, wi + 1, hi), i4 = index(li + 1, wi, hi);
+                int i5 = index(li, wi, hi + 1), i6 = index(li, wi + 1, hi + 1), i7 = index(li + 1, wi + 1, hi + 1), i8 = index(li + 1, wi, hi + 1);
+                if (a) {
+                    put4(i1, i2, i3, i6); put4(i1, i3, i4, i8); put4(i1, i6, i5, i8); put4(i3, i6, i7, i8); put4(i1, i3, i6, i8);
+                } else {
+                    put4(i1, i4, i2, i5); put4(i2, i4, i3, i7); put4(i2, i6, i5, i7); put4(i4, i5, i8, i7); put4(i2, i4, i5, i7);
+                }
+            }
+}
+
+// ---------------------------------------------------------------------------
+// Small 3x3 helpers (column-major, as Eigen's default Mat3r).
+// ---------------------------------------------------------------------------
+template <typename R>
+inline R det3(const R* m) {
+    // m(r,c) = m[c*3+r]; cofactor expansion down column 0
+    auto M = [m](int r, int c) { return m[c * 3 + r]; };
+    return M(0, 0) * (M(1, 1) * M(2, 2) - M(2, 1) * M(1, 2)) - M(1, 0) * (M(0, 1) * M(2, 2) - M(2, 1) * M(0, 2)) +
+           M(2, 0) * (M(0, 1) * M(1, 2) - M(1, 1) * M(0, 2));
+}
+
+template <typename R>
+inline void inv3(const R* m, R* out) {
+    auto M = [m](int r, int c) { return m[c * 3 + r]; };
+    R c00 = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+    R c10 = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+    R c20 = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+    R det = M(0, 0) * c00 + M(0, 1) * c10 + M(0, 2) * c20;
+    R inv = R(1) / det;
+    // out(r,c) = cofactor(c,r)/det
+    out[0 * 3 + 0] = c00 * inv;
+    out[0 * 3 + 1] = c10 * inv;
+    out[0 * 3 + 2] = c20 * inv;
+    out[1 * 3 + 0] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * inv;
+    out[1 * 3 + 1] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * inv;
+    out[1 * 3 + 2] = (M(0, 1) * M(2, 0) - M(0, 0) * M(2, 1)) * inv;
+    out[2 * 3 + 0] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * inv;
+    out[2 * 3 + 1] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) * inv;
+    out[2 * 3 + 2] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) * inv;
+}
+
+// ---------------------------------------------------------------------------
+// Element constraint pieces.
+// ---------------------------------------------------------------------------
+
+// Q = (X0-X3, X1-X3, X2-X3)^-1 and V = |det|/6 at rest
+// (include/solver/constraint/ElementConstraint.hpp:23-51).
+template <typename R>
+inline void rest_shape(const R* X0, const R* X1, const R* X2, const R* X3, R* Q, R* vol) {
+    R X[9];
+    for (int k = 0; k < 3; k++) { X[k] = X0[k] - X3[k]; X[3 + k] = X1[k] - X3[k]; X[6 + k] = X2[k] - X3[k]; }
+    inv3(X, Q);
+    *vol = std::abs(det3(X) / R(6));
+}
+
+// F = Ds * Q, column-major (ElementConstraint.hpp:78-119)
+template <typename R>
+inline void compute_F(const R* x0, const R* x1, const R* x2, const R* x3, const R* Q, R* F) {
+    R X[9];
+    X[0] = x0[0] - x3[0]; X[1] = x0[1] - x3[1]; X[2] = x0[2] - x3[2];
+    X[3] = x1[0] - x3[0]; X[4] = x1[1] - x3[1]; X[5] = x1[2] - x3[2];
+    X[6] = x2[0] - x3[0]; X[7] = x2[1] - x3[1]; X[8] = x2[2] - x3[2];
+    auto q = [Q](int r, int c) { return Q[c * 3 + r]; };
+    for (int c = 0; c < 3; c++) {
+        F[3 * c + 0] = X[0] * q(0, c) + X[3] * q(1, c) + X[6] * q(2, c);
+        F[3 * c + 1] = X[1] * q(0, c) + X[4] * q(1, c) + X[7] * q(2, c);
+        F[3 * c + 2] = X[2] * q(0, c) + X[5] * q(1, c) + X[8] * q(2, c);
+    }
+}
+
+template <typename R>
+inline R detF(const R* F) {
+    // HydrostaticConstraint.hpp:127 (same term order)
+    return F[0] * F[4] * F[8] - F[0] * F[7] * F[5] - F[3] * F[1] * F[8] + F[3] * F[7] * F[2] + F[6] * F[1] * F[5] -
+           F[6] * F[4] * F[2];
+}
+
+// C_h = -gamma + log J (J >= 1) or its 3-term Taylor series (J < 1)
+// (include/solver/constraint/HydrostaticConstraint.hpp:123-153)
+template <typename R>
+inline R hyd_C(const R* F, R gamma) {
+    R J = detF(F);
+    if (J >= 1) return -gamma + std::log(J);
+    return -gamma + (J - 1) - (J - 1) * (J - 1) / R(2) + (J - 1) * (J - 1) * (J - 1) / R(3);
+}
+
+template <typename R>
+inline void cross3(const R* a, const R* b, R* c) {
+    c[0] = a[1] * b[2] - a[2] * b[1];
+    c[1] = a[2] * b[0] - a[0] * b[2];
+    c[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// grad C_h = fac * [f1 x f2, f2 x f0, f0 x f1] * Q^T, 4th = -sum
+// (HydrostaticConstraint.hpp:158-221)
+template <typename R>
+inline void hyd_grad(const R* F, const R* Q, R* g) {
+    R Fc[9];
+    cross3(F + 3, F + 6, Fc);
+    cross3(F + 6, F, Fc + 3);
+    cross3(F, F + 3, Fc + 6);
+    R J = detF(F);
+    R fac = (J >= R(1.0)) ? R(1) / J : R(1) - (J - 1) + (J - 1) * (J - 1);
+    auto q = [Q](int r, int c) { return Q[c * 3 + r]; };
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) g[3 * i + k] = fac * (Fc[k] * q(i, 0) + Fc[3 + k] * q(i, 1) + Fc[6 + k] * q(i, 2));
+    for (int k = 0; k < 3; k++) g[9 + k] = -g[k] - g[3 + k] - g[6 + k];
+}
+
+// C_d = ||F||_F (include/solver/constraint/DeviatoricConstraint.hpp:112-116)
+template <typename R>
+inline R dev_C(const R* F) {
+    return std::sqrt(F[0] * F[0] + F[1] * F[1] + F[2] * F[2] + F[3] * F[3] + F[4] * F[4] + F[5] * F[5] + F[6] * F[6] +
+                     F[7] * F[7] + F[8] * F[8]);
+}
+
+// grad C_d = (1/C) F Q^T, 4th = -sum (DeviatoricConstraint.hpp:121-152)
+template <typename R>
+inline void dev_grad(const R* F, R C, const R* Q, R* g) {
+    R inv_C = R(1.0) / C;
+    auto q = [Q](int r, int c) { return Q[c * 3 + r]; };
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) g[3 * i + k] = inv_C * (F[k] * q(i, 0) + F[3 + k] * q(i, 1) + F[6 + k] * q(i, 2));
+    for (int k = 0; k < 3; k++) g[9 + k] = -g[k] - g[3 + k] - g[6 + k];
+}
+
+// Combined deviatoric+hydrostatic 2x2 projection, 2nd order
+// (src/solver/xpbd_projector/CombinedNeohookeanConstraintProjector.cpp:98-179).
+// at[0] = alpha_d/dt^2, at[1] = alpha_h/dt^2. Writes 12 position updates.
+template <typename R>
+inline void project_combined(const R* x0, const R* x1, const R* x2, const R* x3, const R* w, const R* Q,
+                             const R* at, R gamma, R* lam, R* dx) {
+    R F[9];
+    compute_F(x0, x1, x2, x3, Q, F);
+    R C[2];
+    R g[24];
+    C[0] = dev_C(F);
+    dev_grad(F, C[0], Q, g);
+    C[1] = hyd_C(F, gamma);
+    hyd_grad(F, Q, g + 12);
+    R L[4];
+    L[0] = at[0]; L[1] = 0; L[2] = 0; L[3] = at[1];
+    for (int ci = 0; ci < 2; ci++) {
+        const R* gi = g + 12 * ci;
+        for (int cj = ci; cj < 2; cj++) {
+            const R* gj = g + 12 * cj;
+            for (int i = 0; i < 4; i++)
+                L[cj * 2 + ci] += w[i] * (gi[3 * i] * gj[3 * i] + gi[3 * i + 1] * gj[3 * i + 1] + gi[3 * i + 2] * gj[3 * i + 2]);
+            L[ci * 2 + cj] = L[cj * 2 + ci];
+        }
+    }
+    R rhs[2] = {-C[0] - at[0] * lam[0], -C[1] - at[1] * lam[1]};
+    const R det = L[0] * L[3] - L[1] * L[2];
+    R dl0 = (rhs[0] * L[3] - rhs[1] * L[2]) / det;
+    R dl1 = (rhs[1] * L[0] - rhs[0] * L[1]) / det;
+    lam[0] += dl0;
+    lam[1] += dl1;
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) dx[3 * i + k] = w[i] * (g[3 * i + k] * dl0 + g[12 + 3 * i + k] * dl1);
+}
+
+// Scalar XPBD projection of one element constraint (Dev or Hyd) for the
+// "Stable-Neohookean" (separate) configuration
+// (include/solver/xpbd_projector/ConstraintProjector.hpp:111-172).
+template <typename R>
+inline void project_single_elem(int which, const R* x0, const R* x1, const R* x2, const R* x3, const R* w, const R* Q,
+                                R at, R gamma, R* lam, R* dx) {
+    R F[9], g[12], C;
+    compute_F(x0, x1, x2, x3, Q, F);
+    if (which == 0) { C = dev_C(F); dev_grad(F, C, Q, g); }
+    else            { C = hyd_C(F, gamma); hyd_grad(F, Q, g); }
+    R L = at;
+    for (int i = 0; i < 4; i++) L += w[i] * (g[3 * i] * g[3 * i] + g[3 * i + 1] * g[3 * i + 1] + g[3 * i + 2] * g[3 * i + 2]);
+    R rhs = -C - at * (*lam);
+    R dl = rhs / L;
+    *lam += dl;
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) dx[3 * i + k] = w[i] * g[3 * i + k] * dl;
+}
+
+// ---------------------------------------------------------------------------
+// Collisions.
+// ---------------------------------------------------------------------------
+template <typename R>
+struct Contact {
+    int sphere;    // which sphere produced it
+    int face;      // surface face index
+    int v[3];      // face vertices
+    R u, v_, w;    // barycentrics
+    R p[3];        // surface point
+    R n[3];        // normal
+    R lambda;
+};
+
+// SphereSDF::evaluate / gradient (src/geometry/SphereSDF.cpp:16-26). Eigen's
+// normalized() leaves a zero vector unchanged.
+template <typename R>
+inline R sphere_sdf(const R* x, const R* c, R r) {
+    R d0 = x[0] - c[0], d1 = x[1] - c[1], d2 = x[2] - c[2];
+    return std::sqrt(d0 * d0 + d1 * d1 + d2 * d2) - r;
+}
+template <typename R>
+inline void sphere_grad(const R* x, const R* c, R* g) {
+    R d0 = x[0] - c[0], d1 = x[1] - c[1], d2 = x[2] - c[2];
+    R n2 = d0 * d0 + d1 * d1 + d2 * d2;
+    if (n2 > R(0)) {
+        R n = std::sqrt(n2);
+        g[0] = d0 / n; g[1] = d1 / n; g[2] = d2 / n;
+    } else {
+        g[0] = d0; g[1] = d1; g[2] = d2;
+    }
+}
+
+// CollisionScene::_frankWolfe (src/collision/CollisionScene.cpp:253-283)
+template <typename R>
+inline void frank_wolfe(const R* c, R r, const R* p1, const R* p2, const R* p3, R* x) {
+    R d1 = sphere_sdf(p1, c, r), d2 = sphere_sdf(p2, c, r), d3 = sphere_sdf(p3, c, r);
+    const R* s0 = (d1 <= d2 && d1 <= d3) ? p1 : ((d2 <= d1 && d2 <= d3) ? p2 : p3);
+    x[0] = s0[0]; x[1] = s0[1]; x[2] = s0[2];
+    for (int i = 0; i < 32; i++) {
+        R alpha = R(2.0) / R(i + 3);
+        R g[3];
+        sphere_grad(x, c, g);
+        R sg1 = p1[0] * g[0] + p1[1] * g[1] + p1[2] * g[2];
+        R sg2 = p2[0] * g[0] + p2[1] * g[1] + p2[2] * g[2];
+        R sg3 = p3[0] * g[0] + p3[1] * g[1] + p3[2] * g[2];
+        const R* s = (sg1 < sg2 && sg1 < sg3) ? p1 : ((sg2 < sg1 && sg2 < sg3) ? p2 : p3);
+        for (int k = 0; k < 3; k++) x[k] = x[k] + alpha * (s[k] - x[k]);
+    }
+}
+
+// GeometryUtils::barycentricCoords (src/utils/GeometryUtils.cpp:6-23)
+template <typename R>
+inline void barycentric(const R* p, const R* a, const R* b, const R* c, R* u, R* v, R* w) {
+    R v0[3], v1[3], v2[3];
+    for (int k = 0; k < 3; k++) { v0[k] = b[k] - a[k]; v1[k] = c[k] - a[k]; v2[k] = p[k] - a[k]; }
+    auto dot = [](const R* x, const R* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+    R d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0), d21 = dot(v2, v1);
+    R denom = d00 * d11 - d01 * d01;
+    *v = (d11 * d20 - d01 * d21) / denom;
+    *w = (d00 * d21 - d01 * d20) / denom;
+    *u = 1 - *v - *w;
+}
+
+// One face against one sphere: centroid cull, Frank-Wolfe, threshold,
+// barycentrics, surface point (CollisionScene.cpp:171-214). Returns true and
+// fills the contact when the face is in contact.
+template <typename R>
+inline bool collide_face_sphere(const R* p1, const R* p2, const R* p3, const R* c, R r, Contact<R>* out) {
+    auto sq = [](const R* a, const R* b) {
+        R d0 = b[0] - a[0], d1 = b[1] - a[1], d2 = b[2] - a[2];
+        return d0 * d0 + d1 * d1 + d2 * d2;
+    };
+    R e12 = sq(p1, p2), e13 = sq(p1, p3), e23 = sq(p2, p3);
+    R max_edge = std::max({e12, e13, e23});
+    R cen[3];
+    for (int k = 0; k < 3; k++) cen[k] = (p1[k] + p2[k] + p3[k]) / R(3);
+    R cd = sphere_sdf(cen, c, r);
+    if (cd * cd > max_edge) return false;
+    R x[3];
+    frank_wolfe(c, r, p1, p2, p3, x);
+    const double distance = (double)sphere_sdf(x, c, r);
+    if (!(distance <= 1e-4)) return false;
+    barycentric(x, p1, p2, p3, &out->u, &out->v_, &out->w);
+    R g[3];
+    sphere_grad(x, c, g);
+    for (int k = 0; k < 3; k++) {
+        out->p[k] = (R)(x[k] - g[k] * distance);
+        out->n[k] = g[k];
+    }
+    out->lambda = 0;
+    return true;
+}
+
+// Static deformable collision projection: C = n.(u x1 + v x2 + w x3 - p),
+// inequality skip when C > 0, alpha = 0
+// (src/solver/constraint/StaticDeformableCollisionConstraint.cpp:20-49;
+//  include/solver/xpbd_projector/ConstraintProjector.hpp:111-172).
+// Returns false when skipped.
+template <typename R>
+inline bool project_contact(const R* x1, const R* x2, const R* x3, const R* wv, Contact<R>& ct, R* dx) {
+    R a[3];
+    for (int k = 0; k < 3; k++) a[k] = ct.u * x1[k] + ct.v_ * x2[k] + ct.w * x3[k];
+    R C = ct.n[0] * (a[0] - ct.p[0]) + ct.n[1] * (a[1] - ct.p[1]) + ct.n[2] * (a[2] - ct.p[2]);
+    if (C > 0) return false;
+    R g[9];
+    R b[3] = {ct.u, ct.v_, ct.w};
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) g[3 * i + k] = b[i] * ct.n[k];
+    R L = 0;  // alpha_tilde = 0 for collision constraints
+    for (int i = 0; i < 3; i++) L += wv[i] * (g[3 * i] * g[3 * i] + g[3 * i + 1] * g[3 * i + 1] + g[3 * i + 2] * g[3 * i + 2]);
+    R rhs = -C - R(0) * ct.lambda;
+    R dl = rhs / L;
+    ct.lambda += dl;
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) dx[3 * i + k] = wv[i] * g[3 * i + k] * dl;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Greedy tet colouring used by the coloured Gauss-Seidel order. Tets are
+// visited in index order; each takes the smallest colour not used by any tet
+// already coloured that shares a vertex. Surface faces use the same rule.
+// This is this project's own ordering (the reference's Gauss-Seidel order is
+// plain projector index order, include/common/VariadicVectorContainer.hpp:83-223).
+// ---------------------------------------------------------------------------
+inline int greedy_colour(long long n_items, int arity, const int* items, long long n_vertices, int* colour_out) {
+    std::vector<std::vector<uint64_t>> used(1, std::vector<uint64_t>((size_t)n_vertices, 0));
+    int ncol = 0;
+    for (long long t = 0; t < n_items; t++) {
+        const int* it = items + arity * t;
+        int c = -1;
+        for (size_t word = 0; c < 0; word++) {
+            if (word == used.size()) used.emplace_back((size_t)n_vertices, 0);
+            uint64_t m = 0;
+            for (int k = 0; k < arity; k++) m |= used[word][(size_t)it[k]];
+            if (~m) c = (int)(64 * word + __builtin_ctzll(~m));
+        }
+        colour_out[t] = c;
+        for (int k = 0; k < arity; k++) used[(size_t)c / 64][(size_t)it[k]] |= (1ULL << (c % 64));
+        ncol = std::max(ncol, c + 1);
+    }
+    return ncol;
+}
+
+// ---------------------------------------------------------------------------
+// The simulated object: XPBDMeshObject_ with a combined (or separate)
+// Stable-Neo-Hookean constraint set, 2nd order.
+// ---------------------------------------------------------------------------
+enum SolverKind { GAUSS_SEIDEL = 0, JACOBI = 1, COLOURED_GS = 2 };
+enum ConstraintKind { COMBINED = 0, SEPARATE = 1 };
+
+template <typename R>
+struct Object {
+    long long V = 0, T = 0, F = 0;
+    std::vector<R> x, prev, vel;     // 3V each
+    std::vector<R> mass, inv_mass;   // V
+    std::vector<uint8_t> fixed;      // V
+    std::vector<int> tets, faces;    // 4T, 3F
+    std::vector<R> Q, vol, alpha_d, alpha_h, gamma;  // 9T, T, T, T, T
+    std::vector<R> lam;              // 2T: [2t]=dev, [2t+1]=hyd
+    std::vector<Contact<R>> contacts;
+    R dt = R(1e-3), g = R(9.81);
+    double dt_host = 1e-3;           // the host loop's time step, always double
+    int num_iter = 1;
+    int solver = GAUSS_SEIDEL;
+    int ckind = COMBINED;
+    // coloured Gauss-Seidel order
+    std::vector<int> tet_order;      // tets in colour order
+    std::vector<int> face_colour;    // F
+    int n_face_colours = 0;
+    // spheres
+    std::vector<R> sph_c, sph_r;
+    // kinematic vertex group
+    std::vector<int> kin_idx;
+    std::vector<R> kin_rest;
+    // collision cadence (Simulation.cpp:197-276), in double as the host loop
+    double time = 0, last_cd = 0, cd_interval = 1e300;
+    // per-iteration residual trajectory of the last update(): ||r||_2
+    std::vector<double> res_history;
+
+    // Setup: rest shape, materials, masses (XPBDMeshObject.cpp:277-331,
+    // 352-417; HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
+    // ElasticMaterial.hpp:31-32).
+    void setup(long long V_, const double* X, long long T_, const int* tets_, long long F_, const int* faces_,
+               const double* E, const double* nu, const double* rho) {
+        V = V_; T = T_; F = F_;
+        x.assign(3 * V, 0);
+        for (long long i = 0; i < 3 * V; i++) x[i] = (R)X[i];
+        prev = x;
+        vel.assign(3 * V, 0);
+        tets.assign(tets_, tets_ + 4 * T);
+        faces.assign(faces_, faces_ + 3 * F);
+        mass.assign(V, 0);
+        fixed.assign(V, 0);
+        Q.assign(9 * T, 0); vol.assign(T, 0); alpha_d.assign(T, 0); alpha_h.assign(T, 0); gamma.assign(T, 0);
+        lam.assign(2 * T, 0);
+        for (long long t = 0; t < T; t++) {
+            const int* e = &tets[4 * t];
+            R v_e;
+            rest_shape(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], &Q[9 * t], &v_e);
+            vol[t] = v_e;
+            R mu = (R)E[t] / (2 * (1 + (R)nu[t]));
+            R la = ((R)E[t] * (R)nu[t]) / ((1 + (R)nu[t]) * (1 - 2 * (R)nu[t]));
+            R em = v_e * (R)rho[t];
+            for (int k = 0; k < 4; k++) mass[e[k]] += em / R(4.0);
+            alpha_h[t] = 1 / (la * v_e);
+            gamma[t] = mu / la;
+            alpha_d[t] = 1 / (mu * v_e);
+        }
+        inv_mass.assign(V, 0);
+        for (long long i = 0; i < V; i++) inv_mass[i] = R(1.0) / mass[i];
+        tet_order.clear();
+        face_colour.assign(F, 0);
+    }
+
+    void use_colouring() {
+        std::vector<int> col(T);
+        int nc = greedy_colour(T, 4, tets.data(), V, col.data());
+        tet_order.clear();
+        for (int c = 0; c < nc; c++)
+            for (long long t = 0; t < T; t++)
+                if (col[t] == c) tet_order.push_back((int)t);
+        n_face_colours = F ? greedy_colour(F, 3, faces.data(), V, face_colour.data()) : 0;
+    }
+
+    R at_d(long long t) const { return alpha_d[t] / (dt * dt); }
+    R at_h(long long t) const { return alpha_h[t] / (dt * dt); }
+
+    void project_tet_combined(long long t, R* dx) {
+        const int* e = &tets[4 * t];
+        R w[4] = {inv_mass[e[0]], inv_mass[e[1]], inv_mass[e[2]], inv_mass[e[3]]};
+        R at[2] = {at_d(t), at_h(t)};
+        project_combined(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], w, &Q[9 * t], at, gamma[t],
+                         &lam[2 * t], dx);
+    }
+    void project_tet_single(long long t, int which, R* dx) {
+        const int* e = &tets[4 * t];
+        R w[4] = {inv_mass[e[0]], inv_mass[e[1]], inv_mass[e[2]], inv_mass[e[3]]};
+        R at = which == 0 ? at_d(t) : at_h(t);
+        project_single_elem(which, &x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], w, &Q[9 * t], at,
+                            gamma[t], &lam[2 * t + which], dx);
+    }
+    void add_tet(long long t, const R* dx) {
+        const int* e = &tets[4 * t];
+        for (int i = 0; i < 4; i++)
+            for (int k = 0; k < 3; k++) x[3 * e[i] + k] += dx[3 * i + k];
+    }
+    bool project_contact_i(Contact<R>& ct, R* dx) {
+        R wv[3] = {inv_mass[ct.v[0]], inv_mass[ct.v[1]], inv_mass[ct.v[2]]};
+        return project_contact(&x[3 * ct.v[0]], &x[3 * ct.v[1]], &x[3 * ct.v[2]], wv, ct, dx);
+    }
+    void add_contact(const Contact<R>& ct, const R* dx) {
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) x[3 * ct.v[i] + k] += dx[3 * i + k];
+    }
+
+    // ||r||^2 over the elastic constraints, r = C + alpha_tilde*lambda
+    // (include/solver/xpbd_solver/XPBDSolver.hpp:327-391)
+    void constraint_residual(std::vector<R>& r) const {
+        r.assign(2 * T, 0);
+        for (long long t = 0; t < T; t++) {
+            const int* e = &tets[4 * t];
+            R F_[9];
+            compute_F(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], &Q[9 * t], F_);
+            R Cd = dev_C(F_), Ch = hyd_C(F_, gamma[t]);
+            if (ckind == COMBINED) {
+                r[2 * t] = Cd + alpha_d[t] / (dt * dt) * lam[2 * t];
+                r[2 * t + 1] = Ch + alpha_h[t] / (dt * dt) * lam[2 * t + 1];
+            } else {  // separate: all Dev residuals, then all Hyd residuals
+                r[t] = Cd + alpha_d[t] / (dt * dt) * lam[2 * t];
+                r[T + t] = Ch + alpha_h[t] / (dt * dt) * lam[2 * t + 1];
+            }
+        }
+    }
+    double residual_norm() const {
+        std::vector<R> r;
+        constraint_residual(r);
+        double s = 0;
+        for (R v : r) s += (double)v * (double)v;
+        return std::sqrt(s);
+    }
+
+    // Sum of C^2/alpha over Dev and Hyd constraints (XPBDMeshObject.cpp:537-549)
+    double total_strain_energy() const {
+        double e_dev = 0, e_hyd = 0;
+        for (long long t = 0; t < T; t++) {
+            const int* e = &tets[4 * t];
+            R F_[9];
+            compute_F(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], &Q[9 * t], F_);
+            R Cd = dev_C(F_), Ch = hyd_C(F_, gamma[t]);
+            e_dev += (double)(Cd * Cd / alpha_d[t]);
+            e_hyd += (double)(Ch * Ch / alpha_h[t]);
+        }
+        return e_dev + e_hyd;
+    }
+
+    // One solver iteration (XPBDGaussSeidelSolver.hpp:29-80,
+    // XPBDJacobiSolver.hpp:79-114). Projector type order: elastic first, then
+    // static collision (include/common/XPBDTypedefs.hpp, StableNeohookeanCombined
+    // / StableNeohookean lists).
+    void iterate() {
+        R dx[12];
+        if (solver == GAUSS_SEIDEL) {
+            if (ckind == COMBINED) {
+                for (long long t = 0; t < T; t++) { project_tet_combined(t, dx); add_tet(t, dx); }
+            } else {
+                for (long long t = 0; t < T; t++) { project_tet_single(t, 0, dx); add_tet(t, dx); }
+                for (long long t = 0; t < T; t++) { project_tet_single(t, 1, dx); add_tet(t, dx); }
+            }
+            for (auto& ct : contacts)
+                if (project_contact_i(ct, dx)) add_contact(ct, dx);
+        } else if (solver == COLOURED_GS) {
+            if (ckind == COMBINED) {
+                for (int t : tet_order) { project_tet_combined(t, dx); add_tet(t, dx); }
+            } else {
+                for (int t : tet_order) { project_tet_single(t, 0, dx); add_tet(t, dx); }
+                for (int t : tet_order) { project_tet_single(t, 1, dx); add_tet(t, dx); }
+            }
+            // contacts: face-colour order, ascending face within a colour,
+            // ascending sphere within a face
+            for (int k = 0; k < n_face_colours; k++)
+                for (auto& ct : contacts)
+                    if (face_colour[ct.face] == k)
+                        if (project_contact_i(ct, dx)) add_contact(ct, dx);
+        } else {  // Jacobi: every projection reads the same x; updates summed, no averaging
+            std::vector<R> acc(3 * V, 0);
+            for (long long t = 0; t < T; t++) {
+                const int* e = &tets[4 * t];
+                if (ckind == COMBINED) {
+                    project_tet_combined(t, dx);
+                    for (int i = 0; i < 4; i++) for (int k = 0; k < 3; k++) acc[3 * e[i] + k] += dx[3 * i + k];
+                } else {
+                    project_tet_single(t, 0, dx);
+                    for (int i = 0; i < 4; i++) for (int k = 0; k < 3; k++) acc[3 * e[i] + k] += dx[3 * i + k];
+                    project_tet_single(t, 1, dx);
+                    for (int i = 0; i < 4; i++) for (int k = 0; k < 3; k++) acc[3 * e[i] + k] += dx[3 * i + k];
+                }
+            }
+            for (auto& ct : contacts)
+                if (project_contact_i(ct, dx))
+                    for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
+            for (long long i = 0; i < 3 * V; i++) x[i] += acc[i];
+        }
+    }
+
+    // XPBDMeshObject_::update = prev <- x; inertial move; project
+    // (XPBDMeshObject.cpp:426-505). record_residual stores ||r|| before each
+    // iteration and after the last one.
+    void update(bool record_residual = false) {
+        prev = x;
+        // _movePositionsInertially, 2nd order (XPBDMeshObject.cpp:446-470)
+        for (long long i = 0; i < V; i++) {
+            for (int k = 0; k < 3; k++) x[3 * i + k] += dt * vel[3 * i + k];
+            x[3 * i + 2] += -g * dt * dt;
+        }
+        // XPBDSolver::solve: lambda <- 0, num_iter sweeps (XPBDSolver.hpp:66-97)
+        std::fill(lam.begin(), lam.end(), R(0));
+        for (auto& ct : contacts) ct.lambda = 0;
+        res_history.clear();
+        for (int it = 0; it < num_iter; it++) {
+            if (record_residual) res_history.push_back(residual_norm());
+            iterate();
+        }
+        if (record_residual) res_history.push_back(residual_norm());
+        // fixed vertices back to previous position (XPBDMeshObject.cpp:497-503)
+        for (long long i = 0; i < V; i++)
+            if (fixed[i])
+                for (int k = 0; k < 3; k++) x[3 * i + k] = prev[3 * i + k];
+    }
+
+    // v = (x - prev)/dt (XPBDMeshObject.cpp:507-535)
+    void velocity_update() {
+        for (long long i = 0; i < 3 * V; i++) vel[i] = (x[i] - prev[i]) / dt;
+    }
+
+    // clearCollisionConstraints + CollisionScene::collideObjects for the
+    // object against every sphere, sphere-major then face order
+    // (XPBDMeshObject.cpp:233-251; CollisionScene.cpp:32-51,171-214).
+    void detect() {
+        contacts.clear();
+        long long S = (long long)sph_r.size();
+        for (long long s = 0; s < S; s++)
+            for (long long f = 0; f < F; f++) {
+                const int* fv = &faces[3 * f];
+                Contact<R> ct;
+                if (collide_face_sphere(&x[3 * fv[0]], &x[3 * fv[1]], &x[3 * fv[2]], &sph_c[3 * s], sph_r[s], &ct)) {
+                    ct.sphere = (int)s;
+                    ct.face = (int)f;
+                    ct.v[0] = fv[0]; ct.v[1] = fv[1]; ct.v[2] = fv[2];
+                    contacts.push_back(ct);
+                }
+            }
+    }
+
+    void set_kinematic_offset(const R* off) {
+        for (size_t j = 0; j < kin_idx.size(); j++)
+            for (int k = 0; k < 3; k++) x[3 * kin_idx[j] + k] = kin_rest[3 * j + k] + off[k];
+    }
+
+    // Simulation::_timeStep for this object (Simulation.cpp:197-276):
+    // collision detection on the strict cadence test, update, velocity, time.
+    void time_step(bool record_residual = false) {
+        bool cd = (time - last_cd > cd_interval);
+        if (cd) detect();
+        update(record_residual);
+        velocity_update();
+        if (time - last_cd > cd_interval) last_cd = time;
+        time += dt_host;
+    }
+};
+
+}  // namespace xo

@@ -1,0 +1,246 @@
+// extern "C" surface of the XPBD oracle for the Python test suite and the
+// benchmark's CPU-baseline leg. TEST INFRASTRUCTURE ONLY: the shipped library
+// never links or calls this. See xpbd_oracle.hpp for the parity status.
+#include <chrono>
+#include <cstdint>
+
+#include "xpbd_oracle.hpp"
+
+namespace {
+
+struct Handle {
+    int precision;  // 32 or 64
+    xo::Object<float> f;
+    xo::Object<double> d;
+};
+
+template <typename Fn>
+auto with(Handle* h, Fn fn) {
+    if (h->precision == 32) return fn(h->f);
+    return fn(h->d);
+}
+
+template <typename R>
+void put_vec(std::vector<R>& dst, const double* src, long long n) {
+    for (long long i = 0; i < n; i++) dst[i] = (R)src[i];
+}
+template <typename R>
+void get_vec(const std::vector<R>& src, double* dst, long long n) {
+    for (long long i = 0; i < n; i++) dst[i] = (double)src[i];
+}
+
+}  // namespace
+
+extern "C" {
+
+void xo_grid_counts(int w, int l, int h, long long* V, long long* T, long long* F) {
+    xo::GridDims d{w, l, h};
+    *V = d.V(); *T = d.T(); *F = d.F();
+}
+
+void xo_grid_mesh(int w, int l, int h, double ex, double ey, double ez, double* X, int* tets, int* faces, int split) {
+    xo::grid_mesh(xo::GridDims{w, l, h}, ex, ey, ez, X, tets, faces, split);
+}
+
+int xo_greedy_colour(long long n, int arity, const int* items, long long nv, int* colour_out) {
+    return xo::greedy_colour(n, arity, items, nv, colour_out);
+}
+
+void* xo_create(int precision, long long V, const double* X, long long T, const int* tets, long long F,
+                const int* faces, const double* E, const double* nu, const double* rho, double dt, double g,
+                int num_iter, int solver, int ckind) {
+    Handle* h = new Handle();
+    h->precision = precision == 32 ? 32 : 64;
+    with(h, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        o.dt = (R)dt;
+        o.dt_host = dt;
+        o.g = (R)g;
+        o.num_iter = num_iter;
+        o.solver = solver;
+        o.ckind = ckind;
+        o.setup(V, X, T, tets, F, faces, E, nu, rho);
+        if (solver == xo::COLOURED_GS) o.use_colouring();
+        return 0;
+    });
+    return h;
+}
+
+void xo_destroy(void* p) { delete (Handle*)p; }
+
+void xo_set_collision_rate(void* p, double rate) {
+    with((Handle*)p, [&](auto& o) { o.cd_interval = 1.0 / rate; return 0; });
+}
+
+void xo_set_num_iter(void* p, int n) {
+    with((Handle*)p, [&](auto& o) { o.num_iter = n; return 0; });
+}
+
+void xo_set_positions(void* p, const double* x) {
+    with((Handle*)p, [&](auto& o) { put_vec(o.x, x, 3 * o.V); return 0; });
+}
+void xo_get_positions(void* p, double* x) {
+    with((Handle*)p, [&](auto& o) { get_vec(o.x, x, 3 * o.V); return 0; });
+}
+void xo_get_prev_positions(void* p, double* x) {
+    with((Handle*)p, [&](auto& o) { get_vec(o.prev, x, 3 * o.V); return 0; });
+}
+void xo_set_velocities(void* p, const double* v) {
+    with((Handle*)p, [&](auto& o) { put_vec(o.vel, v, 3 * o.V); return 0; });
+}
+void xo_get_velocities(void* p, double* v) {
+    with((Handle*)p, [&](auto& o) { get_vec(o.vel, v, 3 * o.V); return 0; });
+}
+void xo_set_fixed(void* p, const uint8_t* m) {
+    with((Handle*)p, [&](auto& o) { for (long long i = 0; i < o.V; i++) o.fixed[i] = m[i] ? 1 : 0; return 0; });
+}
+void xo_get_masses(void* p, double* m) {
+    with((Handle*)p, [&](auto& o) { get_vec(o.mass, m, o.V); return 0; });
+}
+// per tet: Q (9, column-major), vol, alpha_d, alpha_h, gamma
+void xo_get_tet_data(void* p, double* Q, double* vol, double* ad, double* ah, double* gm) {
+    with((Handle*)p, [&](auto& o) {
+        get_vec(o.Q, Q, 9 * o.T); get_vec(o.vol, vol, o.T); get_vec(o.alpha_d, ad, o.T);
+        get_vec(o.alpha_h, ah, o.T); get_vec(o.gamma, gm, o.T);
+        return 0;
+    });
+}
+void xo_get_lambda(void* p, double* lam) {
+    with((Handle*)p, [&](auto& o) { get_vec(o.lam, lam, 2 * o.T); return 0; });
+}
+void xo_set_lambda(void* p, const double* lam) {
+    with((Handle*)p, [&](auto& o) { put_vec(o.lam, lam, 2 * o.T); return 0; });
+}
+
+void xo_set_spheres(void* p, int n, const double* c, const double* r) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        o.sph_c.assign(3 * n, 0); o.sph_r.assign(n, 0);
+        for (int i = 0; i < 3 * n; i++) o.sph_c[i] = (R)c[i];
+        for (int i = 0; i < n; i++) o.sph_r[i] = (R)r[i];
+        return 0;
+    });
+}
+
+void xo_set_kinematic_group(void* p, int n, const int* idx) {
+    with((Handle*)p, [&](auto& o) {
+        o.kin_idx.assign(idx, idx + n);
+        o.kin_rest.assign(3 * n, 0);
+        for (int j = 0; j < n; j++)
+            for (int k = 0; k < 3; k++) o.kin_rest[3 * j + k] = o.x[3 * idx[j] + k];
+        return 0;
+    });
+}
+void xo_set_kinematic_offset(void* p, const double* off) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        R of[3] = {(R)off[0], (R)off[1], (R)off[2]};
+        o.set_kinematic_offset(of);
+        return 0;
+    });
+}
+
+int xo_detect(void* p) {
+    return with((Handle*)p, [&](auto& o) { o.detect(); return (int)o.contacts.size(); });
+}
+int xo_num_contacts(void* p) {
+    return with((Handle*)p, [&](auto& o) { return (int)o.contacts.size(); });
+}
+// contact row: sphere, face, u, v, w, p0..2, n0..2, lambda  (12 doubles)
+void xo_get_contacts(void* p, double* out) {
+    with((Handle*)p, [&](auto& o) {
+        for (size_t i = 0; i < o.contacts.size(); i++) {
+            auto& c = o.contacts[i];
+            double* r = out + 12 * i;
+            r[0] = c.sphere; r[1] = c.face; r[2] = c.u; r[3] = c.v_; r[4] = c.w;
+            for (int k = 0; k < 3; k++) { r[5 + k] = c.p[k]; r[8 + k] = c.n[k]; }
+            r[11] = c.lambda;
+        }
+        return 0;
+    });
+}
+// replace the contact list (rows as above, lambda ignored)
+void xo_set_contacts(void* p, int n, const double* rows) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        o.contacts.clear();
+        for (int i = 0; i < n; i++) {
+            const double* r = rows + 12 * i;
+            xo::Contact<R> c;
+            c.sphere = (int)r[0]; c.face = (int)r[1];
+            for (int k = 0; k < 3; k++) c.v[k] = o.faces[3 * c.face + k];
+            c.u = (R)r[2]; c.v_ = (R)r[3]; c.w = (R)r[4];
+            for (int k = 0; k < 3; k++) { c.p[k] = (R)r[5 + k]; c.n[k] = (R)r[8 + k]; }
+            c.lambda = 0;
+            o.contacts.push_back(c);
+        }
+        return 0;
+    });
+}
+
+void xo_update(void* p, int record) {
+    with((Handle*)p, [&](auto& o) { o.update(record != 0); return 0; });
+}
+void xo_velocity_update(void* p) {
+    with((Handle*)p, [&](auto& o) { o.velocity_update(); return 0; });
+}
+void xo_iterate(void* p) {
+    with((Handle*)p, [&](auto& o) { o.iterate(); return 0; });
+}
+// full time steps; returns wall seconds spent
+double xo_time_steps(void* p, int n, int record) {
+    auto t0 = std::chrono::steady_clock::now();
+    with((Handle*)p, [&](auto& o) { for (int i = 0; i < n; i++) o.time_step(record != 0); return 0; });
+    auto t1 = std::chrono::steady_clock::now();
+    return std::chrono::duration<double>(t1 - t0).count();
+}
+double xo_time(void* p) {
+    return with((Handle*)p, [&](auto& o) { return o.time; });
+}
+int xo_res_history(void* p, double* out) {
+    return with((Handle*)p, [&](auto& o) {
+        if (out) for (size_t i = 0; i < o.res_history.size(); i++) out[i] = o.res_history[i];
+        return (int)o.res_history.size();
+    });
+}
+double xo_residual_norm(void* p) {
+    return with((Handle*)p, [&](auto& o) { return o.residual_norm(); });
+}
+void xo_constraint_residual(void* p, double* out) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        std::vector<R> r;
+        o.constraint_residual(r);
+        get_vec(r, out, (long long)r.size());
+        return 0;
+    });
+}
+double xo_strain_energy(void* p) {
+    return with((Handle*)p, [&](auto& o) { return o.total_strain_energy(); });
+}
+// the coloured Gauss-Seidel order actually used (tets in colour order)
+int xo_tet_order(void* p, int* out) {
+    return with((Handle*)p, [&](auto& o) {
+        if (out) for (size_t i = 0; i < o.tet_order.size(); i++) out[i] = o.tet_order[i];
+        return (int)o.tet_order.size();
+    });
+}
+
+// ---- per-element kernels exposed for unit tests (double precision) ----
+void xo_rest_shape(const double* X4, double* Q, double* vol) {
+    xo::rest_shape(X4, X4 + 3, X4 + 6, X4 + 9, Q, vol);
+}
+void xo_elem_eval(const double* x4, const double* Q, double gamma, double* F, double* Cd, double* Ch, double* gd,
+                  double* gh) {
+    xo::compute_F(x4, x4 + 3, x4 + 6, x4 + 9, Q, F);
+    *Cd = xo::dev_C(F);
+    xo::dev_grad(F, *Cd, Q, gd);
+    *Ch = xo::hyd_C(F, gamma);
+    xo::hyd_grad(F, Q, gh);
+}
+void xo_project_combined(const double* x4, const double* w, const double* Q, const double* at, double gamma,
+                         double* lam, double* dx) {
+    xo::project_combined(x4, x4 + 3, x4 + 6, x4 + 9, w, Q, at, gamma, lam, dx);
+}
+
+}  // extern "C"

@@ -1,0 +1,340 @@
+"""GPU parity: the CUDA path (through the C ABI) against the CPU oracle on the
+same seeded inputs.
+
+Tolerances
+  * Jacobi FP32 vs FP64 oracle, and coloured Gauss-Seidel vs the FP64 oracle run
+    in the same colour order: max vertex error <= 1e-4 x mesh extent after the
+    trajectory (the benchmark spec's bound), tighter on short runs.
+  * single projections vs the FP32 oracle: 1e-5 relative.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+import workloads as W
+import xpbd_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+
+def _extent(X):
+    return float((X.max(0) - X.min(0)).max())
+
+
+def _pair(X, tets, faces, E, nu, rho, solver, iters, dt=1e-3, g=9.81, ckind=G.CONSTRAINT_COMBINED, precision=64,
+          with_faces=False, **kw):
+    s = G.XPBDSolver(X, tets, faces if with_faces else None, E, nu, rho, dt=dt, g_accel=g, num_iters=iters,
+                     solver_type=solver, constraint_type=ckind, **kw)
+    o = O.Oracle(X, tets, faces, E, nu, rho, dt=dt, g=g, num_iter=iters,
+                 solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS,
+                 ckind=O.SEPARATE if ckind == G.CONSTRAINT_SEPARATE else O.COMBINED, precision=precision)
+    return s, o
+
+
+def _noisy_cube(n=4, seed=1, noise=2e-3):
+    X, tets, faces = G.grid_mesh(n, n, n, 1.0 / n)
+    x0 = X + np.random.default_rng(seed).uniform(-noise, noise, X.shape)
+    return X, tets, faces, x0
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
+@pytest.mark.parametrize("ckind", [G.CONSTRAINT_COMBINED, G.CONSTRAINT_SEPARATE])
+def test_single_update_matches_fp32_oracle(lib, solver, ckind):
+    X, tets, faces, x0 = _noisy_cube(3, seed=2, noise=0.02)
+    s, o = _pair(X, tets, faces, 5e3, 0.4, 1000.0, solver, 1, ckind=ckind, precision=32)
+    s.set_positions(x0); o.set_positions(x0)
+    s.update(); o.update()
+    xs, xo = s.positions(), o.positions()
+    scale = np.abs(xo - x0).max()
+    assert np.abs(xs - xo).max() <= 1e-4 * scale + 1e-7
+    np.testing.assert_allclose(s.lambdas(), o.lambdas(), rtol=1e-3, atol=1e-6 * np.abs(o.lambdas()).max())
+    s.close()
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
+def test_cube_trajectory_matches_fp64_oracle(lib, solver):
+    """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise), 100 steps."""
+    w = W.cube()
+    s, o = _pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10)
+    for m in (s, o):
+        m.set_positions(w.x0)
+    s.fix_vertices(w.fixed); o.set_fixed(w.fixed)
+    s.step(100); o.time_steps(100)
+    err = np.abs(s.positions() - o.positions()).max()
+    assert err <= 1e-4 * _extent(w.X), err
+    vt = np.abs(s.velocities() - o.velocities()).max()
+    assert vt <= 1e-4 * _extent(w.X) / w.dt
+    # fixed vertices are exactly back at their previous positions
+    np.testing.assert_array_equal(s.positions()[w.fixed], s.prev_positions()[w.fixed])
+    s.close()
+
+
+def test_gs_colour_order_is_the_oracle_order(lib):
+    w = W.cube(n=6)
+    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, solver_type=G.SOLVER_GAUSS_SEIDEL)
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver=O.COLOURED_GS)
+    np.testing.assert_array_equal(s.gs_order(), o.tet_order())
+    nt, _, col = s.colours()
+    # validator: no two tets of one colour share a vertex
+    for c in range(nt):
+        v = w.tets[col == c].ravel()
+        assert len(np.unique(v)) == len(v)
+    s.close()
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
+def test_separate_constraints_trajectory(lib, solver):
+    X, tets, faces, x0 = _noisy_cube(4, seed=3)
+    s, o = _pair(X, tets, faces, 3e3, 0.45, 1000.0, solver, 8, ckind=G.CONSTRAINT_SEPARATE)
+    fixed = X[:, 2] == 0
+    s.set_positions(x0); o.set_positions(x0)
+    s.fix_vertices(fixed); o.set_fixed(fixed)
+    s.step(50); o.time_steps(50)
+    assert np.abs(s.positions() - o.positions()).max() <= 1e-4 * _extent(X)
+    s.close()
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
+def test_residual_history_and_queries(lib, solver):
+    X, tets, faces, x0 = _noisy_cube(4, seed=4, noise=5e-3)
+    s, o = _pair(X, tets, faces, 2e4, 0.45, 1000.0, solver, 6, residual_policy=G.RESIDUAL_EVERY_ITERATION)
+    fixed = X[:, 2] == 0
+    for m in (s, o):
+        m.set_positions(x0)
+    s.fix_vertices(fixed); o.set_fixed(fixed)
+    s.step(3); o.time_steps(3, record=True)
+    hs, ho = s.residual_history(), o.res_history()
+    assert hs.shape == ho.shape == (7,)
+    np.testing.assert_allclose(hs, ho, rtol=2e-3, atol=1e-6 * ho[0])
+    # constraint residual vector (stored at the end of solve, reference order)
+    r_gpu = s.constraint_residual()
+    assert np.isclose(np.linalg.norm(r_gpu), hs[-1], rtol=1e-3)
+    # exact residual and energy at the current state
+    a, rel = s.residual()
+    ref = o.residual_norm()
+    assert np.isclose(a, ref, rtol=5e-3, atol=1e-5 * ho[0])
+    assert 0 <= rel < 1.5
+    e_s, e_o = s.strain_energy(), o.strain_energy()
+    assert np.isclose(e_s, e_o, rtol=1e-3)
+    np.testing.assert_allclose(s.lambdas(), o.lambdas(), rtol=5e-3, atol=1e-3 * np.abs(o.lambdas()).max())
+    s.close()
+
+
+def test_gather_variant_is_deterministic_and_matches_atomic(lib):
+    w = W.cube(n=6)
+    runs = []
+    for variant in (G.JACOBI_GATHER, G.JACOBI_GATHER, G.JACOBI_ATOMIC):
+        s = W.make_solver(w, num_iters=5, solver_type=G.SOLVER_JACOBI, jacobi_variant=variant)
+        s.step(20)
+        runs.append(s.positions())
+        s.close()
+    np.testing.assert_array_equal(runs[0], runs[1])
+    assert np.abs(runs[0] - runs[2]).max() < 1e-6
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
+def test_graph_and_direct_launch_agree(lib, solver):
+    w = W.cube(n=5)
+    out = []
+    for graphs in (1, 0):
+        s = W.make_solver(w, num_iters=4, solver_type=solver, use_graphs=graphs,
+                          jacobi_variant=G.JACOBI_GATHER)
+        s.step(15)
+        out.append(s.positions())
+        s.close()
+    np.testing.assert_array_equal(out[0], out[1])
+
+
+def _beam_small():
+    w = W.beam(nl=20, nw=4, nh=4, length=0.1)
+    w.sphere_r = 0.02
+    w.sphere_c0 = np.array([w.X[:, 0].max() / 2, w.X[:, 1].max() / 2, w.X[:, 2].max() + 0.02 - 0.002])
+    return w
+
+
+def test_collision_detection_matches_fp32_oracle(lib):
+    w = _beam_small()
+    s = W.make_solver(w, num_iters=1)
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, precision=32)
+    x = w.X.copy()
+    x[:, 2] -= 0.5e-3 * np.sin(np.pi * x[:, 1] / x[:, 1].max())  # a sagged, non-grid state
+    s.set_positions(x); o.set_positions(x)
+    c = w.sphere_centre(0.0)
+    s.set_spheres(c, [w.sphere_r]); o.set_spheres(c, [w.sphere_r])
+    s.detect_collisions()
+    nref = o.detect()
+    cg, co = s.collisions(), o.contacts()
+    assert nref > 0
+    fg = {int(r[1]): r for r in cg}
+    fo = {int(r[1]): r for r in co}
+    common = set(fg) & set(fo)
+    # threshold decisions may flip only for faces right at the 1e-4 cut
+    assert len(set(fg) ^ set(fo)) <= max(1, nref // 50)
+    for f in common:
+        np.testing.assert_allclose(fg[f][2:11], fo[f][2:11], atol=2e-5)
+    s.close()
+
+
+def test_beam_trajectory_with_injected_contacts(lib):
+    """Physics parity with contacts: the GPU's own detections are fed to the
+    FP64 oracle, so detection threshold flips cannot mask projection errors."""
+    w = _beam_small()
+    s = W.make_solver(w, num_iters=10)
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, dt=w.dt, g=w.g, num_iter=10, solver=O.JACOBI)
+    o.set_fixed(w.fixed)
+    t, last, interval = 0.0, 0.0, 1.0 / w.collision_rate
+    ncontacts = 0
+    for k in range(60):
+        if t - last > interval:
+            s.set_spheres(w.sphere_centre(t), [w.sphere_r])
+            s.detect_collisions()
+            rows = s.collisions()
+            ncontacts += len(rows)
+            o.set_contacts(rows)
+        s.update(); s.velocity_update()
+        o.update(); o.velocity_update()
+        if t - last > interval:
+            last = t
+        t += w.dt
+    assert ncontacts > 0
+    err = np.abs(s.positions() - o.positions()).max()
+    assert err <= 1e-4 * _extent(w.X), err
+    s.close()
+
+
+def test_step_loop_detection_cadence(lib):
+    """xpbd_step runs detection on the reference's strict cadence; the built-in
+    loop equals the manual detect/update/velocity loop."""
+    w = _beam_small()
+    # Gauss-Seidel: contacts update in place, so both loops are bit-reproducible
+    a = W.make_solver(w, num_iters=5, solver_type=G.SOLVER_GAUSS_SEIDEL)
+    b = W.make_solver(w, num_iters=5, solver_type=G.SOLVER_GAUSS_SEIDEL)
+    t, last, interval = 0.0, 0.0, 1.0 / w.collision_rate
+    for k in range(35):
+        a.set_spheres(w.sphere_centre(a.time), [w.sphere_r])
+        a.step(1)
+        if t - last > interval:
+            b.set_spheres(w.sphere_centre(t), [w.sphere_r])
+            b.detect_collisions()
+        b.update(); b.velocity_update()
+        if t - last > interval:
+            last = t
+        t += w.dt
+    assert abs(a.time - t) == 0.0
+    np.testing.assert_array_equal(a.positions(), b.positions())
+    a.close(); b.close()
+
+
+def test_coloured_gs_contacts_match_oracle_order(lib):
+    w = _beam_small()
+    s = W.make_solver(w, num_iters=6, solver_type=G.SOLVER_GAUSS_SEIDEL)
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, num_iter=6, solver=O.COLOURED_GS)
+    o.set_fixed(w.fixed)
+    s.set_spheres(w.sphere_centre(0.0), [w.sphere_r])
+    s.detect_collisions()
+    o.set_contacts(s.collisions())
+    for _ in range(5):
+        s.update(); s.velocity_update(); o.update(); o.velocity_update()
+    assert np.abs(s.positions() - o.positions()).max() <= 1e-4 * _extent(w.X)
+
+
+def test_add_static_collision_api(lib):
+    X, tets, faces, x0 = _noisy_cube(3, seed=5)
+    s = G.XPBDSolver(X, tets, faces, 3e3, 0.45, 1000.0, num_iters=4, solver_type=G.SOLVER_JACOBI)
+    o = O.Oracle(X, tets, faces, 3e3, 0.45, 1000.0, num_iter=4, solver=O.JACOBI)
+    # a plane contact pushing the bottom faces up by 1 mm
+    bottom = [f for f in range(len(faces)) if np.all(X[faces[f], 2] == 0)]
+    rows = []
+    for f in bottom:
+        p = X[faces[f]].mean(0) + np.array([0, 0, 1e-3])
+        n = np.array([0.0, 0.0, 1.0])
+        s.add_static_collision(f, 1 / 3, 1 / 3, 1 / 3, p, n)
+        rows.append([0, f, 1 / 3, 1 / 3, 1 / 3, *p, *n, 0])
+    o.set_contacts(np.array(rows))
+    s.update(); o.update()
+    assert np.abs(s.positions() - o.positions()).max() < 1e-6
+    assert len(s.collisions()) == len(bottom)
+    s.clear_collisions()
+    assert len(s.collisions()) == 0
+    s.close()
+
+
+def test_kinematic_block_matches_oracle(lib):
+    w = W.block(n=6, iters=8)
+    s = W.make_solver(w)
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, dt=w.dt, g=w.g, num_iter=8, solver=O.COLOURED_GS)
+    o.set_fixed(w.fixed)
+    o.set_kinematic_group(w.kin_idx)
+    for k in range(40):
+        off = w.kin_offset(k + 1)
+        s.set_kinematic_offset(off); o.set_kinematic_offset(off)
+        s.step(1); o.time_steps(1)
+    xs = s.positions()
+    assert np.abs(xs - o.positions()).max() <= 1e-4 * _extent(w.X)
+    np.testing.assert_allclose(xs[w.kin_idx], w.X[w.kin_idx] + w.kin_offset(40), atol=1e-6)
+    s.close()
+
+
+def test_health_counts_degenerate_elements(lib):
+    X, tets, faces = G.grid_mesh(2, 2, 2, 0.5)
+    s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=1, solver_type=G.SOLVER_JACOBI, g_accel=0.0)
+    x = X.copy()
+    x[:, 2] *= 1e-4  # flatten: every tet has |det F| ~ 1e-4
+    s.set_positions(x)
+    s.update()
+    nonfinite, degenerate = s.health()
+    assert degenerate > 0 and nonfinite == 0
+    assert np.isfinite(s.positions()).all()
+    s.close()
+
+
+def test_invalid_inputs_return_status(lib):
+    X, tets, faces = G.grid_mesh(2, 2, 2, 0.5)
+    bad = tets.copy()
+    bad[0, 0] = 10_000
+    with pytest.raises(G.XPBDError) as e:
+        G.XPBDSolver(X, bad, None)
+    assert e.value.status == G.XPBD_ERR_INVALID
+    s = G.XPBDSolver(X, tets, faces)
+    with pytest.raises(G.XPBDError) as e:
+        s.set_spheres(np.zeros((20, 3)), np.ones(20))
+    assert e.value.status == G.XPBD_ERR_INVALID
+    with pytest.raises(G.XPBDError):
+        s.set_kinematic_group([0, 10_000])
+    s.close()
+
+
+# ---- full-size workloads: size-independent properties ----
+
+def test_block_full_size_properties(lib):
+    w = W.block()
+    s = W.make_solver(w, residual_policy=G.RESIDUAL_EVERY_ITERATION)
+    for k in range(3):
+        W.drive_gpu(s, w, k + 1)
+        s.step(1)
+    s.synchronize()
+    x = s.positions()
+    assert np.isfinite(x).all()
+    np.testing.assert_allclose(x[w.fixed], w.X[w.fixed], atol=1e-7)  # float32 storage of the rest state
+    np.testing.assert_allclose(x[w.kin_idx], w.X[w.kin_idx] + w.kin_offset(3), atol=1e-6)
+    h = s.residual_history()
+    assert h.shape == (w.iters + 1,) and np.all(np.isfinite(h)) and h[-1] < h[0]
+    nonfinite, _ = s.health()
+    assert nonfinite == 0
+    s.close()
+
+
+def test_beam_full_size_with_sphere(lib):
+    w = W.beam()
+    s = W.make_solver(w)
+    seen = 0
+    for k in range(40):
+        W.drive_gpu(s, w, k)
+        s.step(1)
+        if k in (11, 21, 31):
+            seen += len(s.collisions())
+    x = s.positions()
+    assert seen > 0
+    assert np.isfinite(x).all()
+    np.testing.assert_allclose(x[w.fixed], w.X[w.fixed], atol=1e-7)
+    s.close()

@@ -1,0 +1,1110 @@
+// C ABI of the GB300 XPBD solver (declared in include/xpbd_gpu.h).
+//
+// Host side of one XPBDMeshObject_ + XPBDSolver pair: builds the device
+// layout (rest shapes, compliances, lumped masses, colouring, CSR), drives the
+// substep on one CUDA stream, captures the substep into a CUDA graph, and
+// reports errors as status codes instead of the reference's assert(0)
+// (include/gpu/resource/GPUResource.hpp:8-19).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/xpbd_gpu.h"
+#include "xpbd_kernels.cuh"
+
+using namespace xg;
+
+namespace {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc((void**)&p, count * sizeof(T));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<int> ids;  // kernel id per recorded pair
+    size_t used = 0;
+};
+
+}  // namespace
+
+struct xpbd_ctx {
+    xpbd_params prm{};
+    int V = 0, T = 0, F = 0;
+    int block = 256;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    long long launches = 0;
+
+    // host mirrors
+    std::vector<double> inv_mass_h;     // V, positive
+    std::vector<uint8_t> fixed_h;       // V
+    std::vector<double> mass_h;         // V
+    std::vector<int> tet_of_slot;       // T
+    std::vector<int> tets_h, faces_h;   // 4T, 3F (original order)
+    std::vector<int> col_off;           // tet colour ranges over slots
+    std::vector<int> tet_colour;        // T, by original index
+    std::vector<int> fcol_off;          // face colour ranges over face_list
+    int n_tet_colours = 1, n_face_colours = 0;
+    std::vector<float> alpha_t_d, alpha_t_h;  // per slot, for energy
+
+    // device state
+    DevBuf<float4> x, prev, vel, dx, dxt;
+    DevBuf<int4> tet_idx;
+    DevBuf<float4> q0, q1, q2;
+    DevBuf<float2> lam;
+    DevBuf<int> perm, csr_off, csr_ent;
+    DevBuf<int4> faces;
+    DevBuf<int> face_list;
+    DevBuf<float4> c_bary, c_p, c_n;
+    DevBuf<float> c_lam;
+    int S = 4;
+    SphereSet spheres{};
+    DevBuf<int> kin_idx;
+    DevBuf<float4> kin_rest;
+    int nkin = 0;
+    DevBuf<Flags> flags;
+    DevBuf<double> res_partial, res_rows, energy_partial;
+    DevBuf<float> rvec;
+    int res_stride = 0;   // doubles per residual row
+    int gs_blocks = 0;    // residual slots used by one Gauss-Seidel sweep
+    bool have_rvec = false;
+    std::vector<int> api_slots;  // contacts added through the API per face
+
+    // pinned staging
+    float4* h_stage = nullptr;
+    double* h_rows = nullptr;
+    int h_rows_cap = 0;
+    int last_rows = 0;
+    bool rows_pending = false;
+
+    // host simulation clock (Simulation.cpp:197-276)
+    double time = 0, last_cd = 0;
+
+    // graphs: [write_vel]
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};  // kernels captured in each graph
+    bool graph_dirty = true;
+
+    Prof prof;
+
+    TetArrays tets() {
+        return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
+    }
+    ContactArrays contacts() {
+        return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
+    }
+};
+
+namespace {
+
+int fail(xpbd_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+int cuda_check(xpbd_ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return XPBD_OK;
+    return fail(c, XPBD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define XPBD_CU(ctx, call)                                         \
+    do {                                                           \
+        int _st = cuda_check((ctx), (call), #call);                \
+        if (_st != XPBD_OK) return _st;                            \
+    } while (0)
+
+int after_launches(xpbd_ctx* c, const char* what) {
+    return cuda_check(c, cudaGetLastError(), what);
+}
+
+// ---- profiling brackets (only when prof.on) ----
+void prof_begin(xpbd_ctx* c, int id) {
+    if (!c->prof.on) return;
+    if (c->prof.used + 2 > c->prof.pool.size()) {
+        size_t old = c->prof.pool.size();
+        c->prof.pool.resize(std::max<size_t>(256, old * 2));
+        for (size_t i = old; i < c->prof.pool.size(); i++) cudaEventCreate(&c->prof.pool[i]);
+    }
+    cudaEventRecord(c->prof.pool[c->prof.used], c->stream);
+    c->prof.ids.push_back(id);
+}
+void prof_end(xpbd_ctx* c) {
+    if (!c->prof.on) return;
+    cudaEventRecord(c->prof.pool[c->prof.used + 1], c->stream);
+    c->prof.used += 2;
+}
+
+struct Scope {
+    xpbd_ctx* c;
+    Scope(xpbd_ctx* c_, int id) : c(c_) {
+        prof_begin(c, id);
+        c->launches++;
+    }
+    ~Scope() { prof_end(c); }
+};
+
+bool valid_params(const xpbd_params& p) {
+    return p.dt > 0 && std::isfinite(p.dt) && std::isfinite(p.g_accel) && p.num_iters >= 0 &&
+           (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL || p.solver_type == XPBD_SOLVER_JACOBI) &&
+           (p.constraint_type == XPBD_CONSTRAINT_COMBINED || p.constraint_type == XPBD_CONSTRAINT_SEPARATE) &&
+           p.residual_policy >= XPBD_RESIDUAL_NEVER && p.residual_policy <= XPBD_RESIDUAL_EVERY_ITERATION &&
+           (p.jacobi_variant == XPBD_JACOBI_ATOMIC || p.jacobi_variant == XPBD_JACOBI_GATHER) &&
+           (p.block_size == 0 || (p.block_size >= 32 && p.block_size <= 256 && p.block_size % 32 == 0)) &&
+           p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres;
+}
+
+// greedy vertex-disjoint colouring in item order (smallest free colour)
+int greedy_colour(long long n, int arity, const int* items, long long nv, int* out) {
+    std::vector<std::vector<uint64_t>> used;
+    used.emplace_back((size_t)nv, 0);
+    int ncol = 0;
+    for (long long t = 0; t < n; t++) {
+        const int* it = items + (size_t)arity * t;
+        int c = -1;
+        for (size_t w = 0; c < 0; w++) {
+            if (w == used.size()) used.emplace_back((size_t)nv, 0);
+            uint64_t m = 0;
+            for (int k = 0; k < arity; k++) m |= used[w][(size_t)it[k]];
+            if (~m) c = (int)(64 * w) + __builtin_ctzll(~m);
+        }
+        out[t] = c;
+        for (int k = 0; k < arity; k++) used[(size_t)c / 64][(size_t)it[k]] |= 1ull << (c % 64);
+        ncol = std::max(ncol, c + 1);
+    }
+    return ncol;
+}
+
+// ---- residual bookkeeping ----
+bool tracking(const xpbd_ctx* c) { return c->prm.residual_policy != XPBD_RESIDUAL_NEVER; }
+
+ResidualSink no_sink() { return ResidualSink{nullptr, 0, 0, 0}; }
+ResidualSink sink(xpbd_ctx* c, int row, int offset) { return ResidualSink{c->res_partial.p, row, c->res_stride, offset}; }
+
+// Residual scratch: `rows` rows of per-block partials, their FP64 sums and a
+// pinned host copy. Growing a buffer invalidates captured graphs, which hold
+// its address.
+int ensure_residual_rows(xpbd_ctx* c, int rows) {
+    const size_t need = (size_t)rows * c->res_stride;
+    if (c->res_partial.n < need) {
+        XPBD_CU(c, cudaStreamSynchronize(c->stream));
+        c->res_partial.release();
+        XPBD_CU(c, c->res_partial.alloc(need));
+        c->graph_dirty = true;
+    }
+    if (c->res_rows.n < (size_t)rows) {
+        XPBD_CU(c, cudaStreamSynchronize(c->stream));
+        c->res_rows.release();
+        XPBD_CU(c, c->res_rows.alloc(rows));
+        c->graph_dirty = true;
+    }
+    if (c->h_rows_cap < rows) {
+        XPBD_CU(c, cudaStreamSynchronize(c->stream));
+        double* nh = nullptr;
+        XPBD_CU(c, cudaMallocHost((void**)&nh, sizeof(double) * rows));
+        std::fill(nh, nh + rows, 0.0);
+        if (c->h_rows) {
+            std::copy(c->h_rows, c->h_rows + c->h_rows_cap, nh);
+            cudaFreeHost(c->h_rows);
+        }
+        c->h_rows = nh;
+        c->h_rows_cap = rows;
+        c->graph_dirty = true;
+    }
+    return XPBD_OK;
+}
+
+void exact_residual_row(xpbd_ctx* c, int row, bool with_vec) {
+    Scope s(c, K_RESIDUAL);
+    launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
+                    c->perm.p, with_vec ? c->rvec.p : nullptr, sink(c, row, 0), nullptr,
+                    (float)(c->prm.dt * c->prm.dt));
+}
+
+// ---- the substep body (XPBDMeshObject_::update, XPBDMeshObject.cpp:426-505) ----
+int enqueue_update(xpbd_ctx* c, bool write_vel) {
+    const xpbd_params& p = c->prm;
+    const int iters = p.num_iters;
+    const bool track = tracking(c);
+    const bool every_iter = p.residual_policy == XPBD_RESIDUAL_EVERY_ITERATION;
+    const bool separate = p.constraint_type == XPBD_CONSTRAINT_SEPARATE;
+    const float dt = (float)p.dt;
+    const float dz = (float)(-p.g_accel * p.dt * p.dt);
+    cudaStream_t s = c->stream;
+    const ContactArrays ca = c->contacts();
+    const bool have_faces = c->F > 0;
+    {
+        Scope sc(c, K_PREDICT);
+        launch_predict(s, c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
+    }
+    if (track) {
+        // lambda <- 0 (XPBDSolver.hpp:71-77) before the r(x_pred, 0) evaluation
+        cudaMemsetAsync(c->lam.p, 0, sizeof(float2) * (size_t)c->T, s);
+        cudaMemsetAsync(c->res_partial.p, 0, sizeof(double) * (size_t)c->res_stride * (iters + 1), s);
+    }
+    const bool jacobi = p.solver_type == XPBD_SOLVER_JACOBI;
+    const bool fuse_final = !track;
+    if (jacobi) {
+        const bool gather = p.jacobi_variant == XPBD_JACOBI_GATHER;
+        if (track && !every_iter) exact_residual_row(c, 0, false);
+        for (int it = 0; it < iters; it++) {
+            const bool first = it == 0;
+            const ResidualSink rs = every_iter ? sink(c, it, 0) : no_sink();
+            const bool last = it == iters - 1;
+            if (gather) {
+                {
+                    Scope sc(c, K_PROJECT_JACOBI);
+                    launch_project_jacobi_gather_write(s, c->block, c->tets(), c->T, c->x.p, c->dxt.p, first,
+                                                       separate, rs, c->flags.p);
+                }
+                if (have_faces) {
+                    Scope sc(c, K_CONTACT);
+                    launch_contacts_jacobi(s, ca, c->x.p, c->dx.p, first);
+                }
+                Scope sc(c, K_GATHER);
+                launch_gather_apply(s, c->x.p, c->dxt.p, c->csr_off.p, c->csr_ent.p, c->dx.p, c->V, c->prev.p,
+                                    c->vel.p, last && fuse_final, dt, write_vel);
+            } else {
+                {
+                    Scope sc(c, K_PROJECT_JACOBI);
+                    launch_project_jacobi(s, c->block, c->tets(), c->T, c->x.p, c->dx.p, first, separate, rs,
+                                          c->flags.p);
+                }
+                if (have_faces) {
+                    Scope sc(c, K_CONTACT);
+                    launch_contacts_jacobi(s, ca, c->x.p, c->dx.p, first);
+                }
+                Scope sc(c, K_APPLY);
+                launch_apply(s, c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
+            }
+        }
+    } else {
+        if (track && !every_iter) exact_residual_row(c, 0, false);
+        for (int it = 0; it < iters; it++) {
+            const bool first = it == 0;
+            if (every_iter) exact_residual_row(c, it, false);
+            const int passes = separate ? 2 : 1;
+            for (int pass = 0; pass < passes; pass++) {
+                const int which = separate ? pass : 2;
+                // in the separate form the second pass (Hyd) of iteration 0
+                // must not re-zero the Dev multipliers updated by pass 0
+                const bool f = first && (!separate || pass == 0);
+                for (int col = 0; col < c->n_tet_colours; col++) {
+                    Scope sc(c, K_PROJECT_GS);
+                    launch_project_gs(s, c->block, c->tets(), c->col_off[col], c->col_off[col + 1], c->x.p, f,
+                                      which, no_sink(), c->flags.p);
+                }
+            }
+            if (have_faces) {
+                for (int fc = 0; fc < c->n_face_colours; fc++) {
+                    Scope sc(c, K_CONTACT);
+                    launch_contacts_gs(s, ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
+                }
+            }
+        }
+    }
+    if (track) {
+        exact_residual_row(c, iters, true);
+        {
+            Scope sc(c, K_REDUCE);
+            launch_reduce_rows(s, c->res_partial.p, iters + 1, c->res_stride, c->res_rows.p);
+        }
+        cudaMemcpyAsync(c->h_rows, c->res_rows.p, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, s);
+    }
+    if (!jacobi || !fuse_final || iters == 0) {
+        Scope sc(c, K_FINALIZE);
+        launch_finalize(s, c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
+    }
+    return XPBD_OK;
+}
+
+int prepare_update(xpbd_ctx* c) {
+    if (tracking(c)) {
+        // one extra row for on-demand residual queries
+        int st = ensure_residual_rows(c, c->prm.num_iters + 2);
+        if (st) return st;
+    }
+    return XPBD_OK;
+}
+
+void drop_graphs(xpbd_ctx* c) {
+    for (auto& g : c->gexec)
+        if (g) {
+            cudaGraphExecDestroy(g);
+            g = nullptr;
+        }
+    c->graph_kernels[0] = c->graph_kernels[1] = 0;
+    c->graph_dirty = false;
+}
+
+int run_update(xpbd_ctx* c, bool write_vel) {
+    int st = prepare_update(c);
+    if (st) return st;
+    if (c->graph_dirty) drop_graphs(c);
+    if (c->prm.use_graphs && !c->prof.on) {
+        cudaGraphExec_t& ge = c->gexec[write_vel ? 1 : 0];
+        if (!ge) {
+            cudaGraph_t g = nullptr;
+            XPBD_CU(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            const long long before = c->launches;
+            enqueue_update(c, write_vel);
+            c->graph_kernels[write_vel ? 1 : 0] = c->launches - before;
+            c->launches = before;
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (e != cudaSuccess) return cuda_check(c, e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) {
+                ge = nullptr;
+                return cuda_check(c, e, "cudaGraphInstantiate");
+            }
+        }
+        XPBD_CU(c, cudaGraphLaunch(ge, c->stream));
+        c->launches += c->graph_kernels[write_vel ? 1 : 0];
+    } else {
+        enqueue_update(c, write_vel);
+    }
+    c->rows_pending = tracking(c);
+    c->last_rows = c->prm.num_iters + 1;
+    if (tracking(c)) c->have_rvec = true;
+    return after_launches(c, "update");
+}
+
+int detect(xpbd_ctx* c) {
+    if (c->F == 0) return XPBD_OK;
+    {
+        Scope sc(c, K_DETECT);
+        launch_detect(c->stream, c->contacts(), c->x.p, c->spheres);
+    }
+    std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
+    return after_launches(c, "detect");
+}
+
+int stage_positions_to_device(xpbd_ctx* c, const double* x3v, const float* x3f) {
+    for (int i = 0; i < c->V; i++) {
+        const float w = (float)c->inv_mass_h[i] * (c->fixed_h[i] ? -1.f : 1.f);
+        if (x3v)
+            c->h_stage[i] = make_float4((float)x3v[3 * i], (float)x3v[3 * i + 1], (float)x3v[3 * i + 2], w);
+        else
+            c->h_stage[i] = make_float4(x3f[3 * i], x3f[3 * i + 1], x3f[3 * i + 2], w);
+    }
+    XPBD_CU(c, cudaMemcpyAsync(c->x.p, c->h_stage, sizeof(float4) * c->V, cudaMemcpyHostToDevice, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+
+int fetch(xpbd_ctx* c, const float4* src) {
+    XPBD_CU(c, cudaMemcpyAsync(c->h_stage, src, sizeof(float4) * c->V, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+
+void release(xpbd_ctx* c) {
+    drop_graphs(c);
+    for (auto e : c->prof.pool) cudaEventDestroy(e);
+    c->x.release(); c->prev.release(); c->vel.release(); c->dx.release(); c->dxt.release();
+    c->tet_idx.release(); c->q0.release(); c->q1.release(); c->q2.release(); c->lam.release();
+    c->perm.release(); c->csr_off.release(); c->csr_ent.release(); c->faces.release(); c->face_list.release();
+    c->c_bary.release(); c->c_p.release(); c->c_n.release(); c->c_lam.release();
+    c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
+    c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
+    if (c->h_stage) cudaFreeHost(c->h_stage);
+    if (c->h_rows) cudaFreeHost(c->h_rows);
+    c->h_stage = nullptr;
+    c->h_rows = nullptr;
+    if (c->stream) cudaStreamDestroy(c->stream);
+    c->stream = nullptr;
+}
+
+int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
+    const int V = c->V, T = c->T, F = c->F;
+    const xpbd_params& p = c->prm;
+    c->block = p.block_size ? p.block_size : 256;
+    c->S = p.max_contacts_per_face ? p.max_contacts_per_face : 4;
+    c->tets_h.assign(m->tets, m->tets + 4 * (size_t)T);
+    if (F) c->faces_h.assign(m->faces, m->faces + 3 * (size_t)F);
+    for (int v : c->tets_h)
+        if (v < 0 || v >= V) return fail(c, XPBD_ERR_INVALID, "tet vertex index %d out of range [0,%d)", v, V);
+    for (int v : c->faces_h)
+        if (v < 0 || v >= V) return fail(c, XPBD_ERR_INVALID, "face vertex index %d out of range [0,%d)", v, V);
+
+    // rest shape, compliance, lumped mass (ElementConstraint.hpp:23-51;
+    // HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
+    // ElasticMaterial.hpp:31-32; XPBDMeshObject.cpp:277-331)
+    const double* X = m->vertices;
+    std::vector<double> Q(9 * (size_t)T), ad(T), ah(T), gm(T);
+    c->mass_h.assign(V, 0.0);
+    for (int t = 0; t < T; t++) {
+        const int* e = &c->tets_h[4 * (size_t)t];
+        double D[9];
+        for (int i = 0; i < 3; i++)
+            for (int k = 0; k < 3; k++) D[3 * i + k] = X[3 * (size_t)e[i] + k] - X[3 * (size_t)e[3] + k];
+        auto M = [&D](int r, int cc) { return D[cc * 3 + r]; };
+        const double c00 = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
+        const double c10 = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
+        const double c20 = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
+        const double det = M(0, 0) * c00 + M(0, 1) * c10 + M(0, 2) * c20;
+        if (!(std::fabs(det) > 0) || !std::isfinite(det))
+            return fail(c, XPBD_ERR_INVALID, "tet %d is degenerate at rest (det = %g)", t, det);
+        const double inv = 1.0 / det;
+        double* q = &Q[9 * (size_t)t];
+        q[0] = c00 * inv; q[1] = c10 * inv; q[2] = c20 * inv;
+        q[3] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * inv;
+        q[4] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * inv;
+        q[5] = (M(0, 1) * M(2, 0) - M(0, 0) * M(2, 1)) * inv;
+        q[6] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * inv;
+        q[7] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) * inv;
+        q[8] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) * inv;
+        const double vol = std::fabs(det / 6.0);
+        const double E = m->tet_E[t], nu = m->tet_nu[t], rho = m->tet_density[t];
+        if (!(E > 0) || !(nu > -1 && nu < 0.5) || !(rho > 0))
+            return fail(c, XPBD_ERR_INVALID, "tet %d has invalid material E=%g nu=%g rho=%g", t, E, nu, rho);
+        const double mu = E / (2 * (1 + nu));
+        const double la = (E * nu) / ((1 + nu) * (1 - 2 * nu));
+        ad[t] = 1 / (mu * vol);
+        ah[t] = 1 / (la * vol);
+        gm[t] = mu / la;
+        const double em = vol * rho;
+        for (int k = 0; k < 4; k++) c->mass_h[e[k]] += em / 4.0;
+    }
+    c->inv_mass_h.assign(V, 0.0);
+    for (int i = 0; i < V; i++) {
+        if (!(c->mass_h[i] > 0))
+            return fail(c, XPBD_ERR_INVALID, "vertex %d belongs to no tet (zero mass)", i);
+        c->inv_mass_h[i] = 1.0 / c->mass_h[i];
+    }
+    c->fixed_h.assign(V, 0);
+
+    // slot order: colour-sorted for Gauss-Seidel, identity for Jacobi
+    c->tet_colour.assign(T, 0);
+    c->n_tet_colours = T ? greedy_colour(T, 4, c->tets_h.data(), V, c->tet_colour.data()) : 0;
+    c->tet_of_slot.resize(T);
+    if (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
+        c->col_off.assign(c->n_tet_colours + 1, 0);
+        for (int t = 0; t < T; t++) c->col_off[c->tet_colour[t] + 1]++;
+        for (int k = 0; k < c->n_tet_colours; k++) c->col_off[k + 1] += c->col_off[k];
+        std::vector<int> fill(c->col_off.begin(), c->col_off.end() - 1);
+        for (int t = 0; t < T; t++) c->tet_of_slot[fill[c->tet_colour[t]]++] = t;
+    } else {
+        for (int t = 0; t < T; t++) c->tet_of_slot[t] = t;
+        c->col_off = {0, T};
+    }
+    const double dt2 = p.dt * p.dt;
+    std::vector<int4> hidx(T);
+    std::vector<float4> h0(T), h1(T), h2(T);
+    c->alpha_t_d.resize(T);
+    c->alpha_t_h.resize(T);
+    for (int sidx = 0; sidx < T; sidx++) {
+        const int t = c->tet_of_slot[sidx];
+        const int* e = &c->tets_h[4 * (size_t)t];
+        const double* q = &Q[9 * (size_t)t];
+        hidx[sidx] = make_int4(e[0], e[1], e[2], e[3]);
+        const float atd = (float)(ad[t] / dt2), ath = (float)(ah[t] / dt2);
+        h0[sidx] = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
+        h1[sidx] = make_float4((float)q[4], (float)q[5], (float)q[6], (float)q[7]);
+        h2[sidx] = make_float4((float)q[8], atd, ath, (float)gm[t]);
+        c->alpha_t_d[sidx] = atd;
+        c->alpha_t_h[sidx] = ath;
+    }
+
+    // faces and their colouring (Gauss-Seidel contact order)
+    std::vector<int4> hf(F);
+    for (int f = 0; f < F; f++) hf[f] = make_int4(c->faces_h[3 * f], c->faces_h[3 * f + 1], c->faces_h[3 * f + 2], 0);
+    std::vector<int> fcol(F, 0), flist(F);
+    c->n_face_colours = F ? greedy_colour(F, 3, c->faces_h.data(), V, fcol.data()) : 0;
+    c->fcol_off.assign(c->n_face_colours + 1, 0);
+    for (int f = 0; f < F; f++) c->fcol_off[fcol[f] + 1]++;
+    for (int k = 0; k < c->n_face_colours; k++) c->fcol_off[k + 1] += c->fcol_off[k];
+    {
+        std::vector<int> fill(c->fcol_off.begin(), c->fcol_off.end() - 1);
+        for (int f = 0; f < F; f++) flist[fill[fcol[f]]++] = f;
+    }
+    c->api_slots.assign(F, 0);
+
+    // CSR vertex -> (slot, local vertex) for the gather variant
+    std::vector<int> off(V + 1, 0), ent(4 * (size_t)T);
+    if (p.solver_type == XPBD_SOLVER_JACOBI && p.jacobi_variant == XPBD_JACOBI_GATHER) {
+        for (int sidx = 0; sidx < T; sidx++) {
+            const int4 e = hidx[sidx];
+            off[e.x + 1]++; off[e.y + 1]++; off[e.z + 1]++; off[e.w + 1]++;
+        }
+        for (int i = 0; i < V; i++) off[i + 1] += off[i];
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        for (int sidx = 0; sidx < T; sidx++) {
+            const int4 e = hidx[sidx];
+            const int vs[4] = {e.x, e.y, e.z, e.w};
+            for (int k = 0; k < 4; k++) ent[fill[vs[k]]++] = 4 * sidx + k;
+        }
+    }
+
+    // device allocation + upload
+    XPBD_CU(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    XPBD_CU(c, c->x.alloc(V));
+    XPBD_CU(c, c->prev.alloc(V));
+    XPBD_CU(c, c->vel.alloc(V));
+    XPBD_CU(c, c->dx.alloc(V));
+    XPBD_CU(c, c->tet_idx.alloc(T));
+    XPBD_CU(c, c->q0.alloc(T));
+    XPBD_CU(c, c->q1.alloc(T));
+    XPBD_CU(c, c->q2.alloc(T));
+    XPBD_CU(c, c->lam.alloc(T));
+    XPBD_CU(c, c->perm.alloc(T));
+    XPBD_CU(c, c->flags.alloc(1));
+    XPBD_CU(c, c->rvec.alloc(2 * (size_t)T));
+    XPBD_CU(c, c->energy_partial.alloc(residual_blocks(T, c->block) + 1));
+    XPBD_CU(c, cudaMallocHost((void**)&c->h_stage, sizeof(float4) * (size_t)std::max(V, 1)));
+    if (F) {
+        XPBD_CU(c, c->faces.alloc(F));
+        XPBD_CU(c, c->face_list.alloc(F));
+        const size_t ns = (size_t)c->S * F;
+        XPBD_CU(c, c->c_bary.alloc(ns));
+        XPBD_CU(c, c->c_p.alloc(ns));
+        XPBD_CU(c, c->c_n.alloc(ns));
+        XPBD_CU(c, c->c_lam.alloc(ns));
+        XPBD_CU(c, cudaMemset(c->c_bary.p, 0, sizeof(float4) * ns));
+        XPBD_CU(c, cudaMemset(c->c_lam.p, 0, sizeof(float) * ns));
+        XPBD_CU(c, cudaMemcpy(c->faces.p, hf.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->face_list.p, flist.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+    }
+    if (p.solver_type == XPBD_SOLVER_JACOBI && p.jacobi_variant == XPBD_JACOBI_GATHER) {
+        XPBD_CU(c, c->dxt.alloc(3 * (size_t)T));
+        XPBD_CU(c, c->csr_off.alloc(V + 1));
+        XPBD_CU(c, c->csr_ent.alloc(4 * (size_t)T));
+        XPBD_CU(c, cudaMemcpy(c->csr_off.p, off.data(), sizeof(int) * (V + 1), cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->csr_ent.p, ent.data(), sizeof(int) * 4 * (size_t)T, cudaMemcpyHostToDevice));
+    }
+    XPBD_CU(c, cudaMemcpy(c->tet_idx.p, hidx.data(), sizeof(int4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->q0.p, h0.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->q1.p, h1.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->q2.p, h2.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->perm.p, c->tet_of_slot.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemset(c->lam.p, 0, sizeof(float2) * T));
+    XPBD_CU(c, cudaMemset(c->dx.p, 0, sizeof(float4) * V));
+    XPBD_CU(c, cudaMemset(c->vel.p, 0, sizeof(float4) * V));
+    XPBD_CU(c, cudaMemset(c->flags.p, 0, sizeof(Flags)));
+    c->res_stride = residual_blocks(T, c->block) + 1;
+    int st = stage_positions_to_device(c, X, nullptr);
+    if (st) return st;
+    XPBD_CU(c, cudaMemcpy(c->prev.p, c->x.p, sizeof(float4) * V, cudaMemcpyDeviceToDevice));
+    return XPBD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int xpbd_abi_version(void) { return XPBD_ABI_VERSION; }
+
+const char* xpbd_status_string(int st) {
+    switch (st) {
+        case XPBD_OK: return "ok";
+        case XPBD_ERR_INVALID: return "invalid argument";
+        case XPBD_ERR_CUDA: return "CUDA error";
+        case XPBD_ERR_NUMERIC: return "non-finite projection update";
+        case XPBD_ERR_NO_DEVICE: return "no CUDA device";
+        case XPBD_ERR_STATE: return "invalid state";
+        case XPBD_ERR_CAPACITY: return "capacity exceeded";
+        default: return "unknown status";
+    }
+}
+
+int xpbd_default_params(xpbd_params* p) {
+    if (!p) return XPBD_ERR_INVALID;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 1e-3;
+    p->g_accel = 9.81;
+    p->collision_rate = 100.0;
+    p->num_iters = 1;
+    p->solver_type = XPBD_SOLVER_GAUSS_SEIDEL;
+    p->constraint_type = XPBD_CONSTRAINT_COMBINED;
+    p->residual_policy = XPBD_RESIDUAL_NEVER;
+    p->jacobi_variant = XPBD_JACOBI_ATOMIC;
+    p->block_size = 0;
+    p->max_contacts_per_face = 0;
+    p->use_graphs = 1;
+    return XPBD_OK;
+}
+
+int xpbd_colour_items(int64_t n, int32_t arity, const int32_t* items, int64_t nv, int32_t* out) {
+    if (n < 0 || nv <= 0 || arity < 1 || arity > 8 || (n > 0 && (!items || !out))) return -XPBD_ERR_INVALID;
+    for (int64_t i = 0; i < n * arity; i++)
+        if (items[i] < 0 || items[i] >= nv) return -XPBD_ERR_INVALID;
+    return n ? greedy_colour(n, arity, items, nv, out) : 0;
+}
+
+int xpbd_create(const xpbd_mesh_desc* m, const xpbd_params* p, xpbd_ctx** out) {
+    if (!out) return XPBD_ERR_INVALID;
+    *out = nullptr;
+    if (!m || !p || !m->vertices || !m->tets || !m->tet_E || !m->tet_nu || !m->tet_density) return XPBD_ERR_INVALID;
+    if (m->num_vertices <= 0 || m->num_tets <= 0 || m->num_faces < 0 || (m->num_faces > 0 && !m->faces))
+        return XPBD_ERR_INVALID;
+    if (m->num_vertices > (1LL << 30) || m->num_tets > (1LL << 29) || m->num_faces > (1LL << 28))
+        return XPBD_ERR_CAPACITY;
+    if (!valid_params(*p)) return XPBD_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return XPBD_ERR_NO_DEVICE;
+    }
+    xpbd_ctx* c = new (std::nothrow) xpbd_ctx();
+    if (!c) return XPBD_ERR_CAPACITY;
+    c->prm = *p;
+    c->V = (int)m->num_vertices;
+    c->T = (int)m->num_tets;
+    c->F = (int)m->num_faces;
+    int st = build(c, m);
+    if (st) {
+        fprintf(stderr, "xpbd_create: %s\n", c->err.c_str());
+        release(c);
+        delete c;
+        return st;
+    }
+    *out = c;
+    return XPBD_OK;
+}
+
+int xpbd_destroy(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    release(c);
+    delete c;
+    return XPBD_OK;
+}
+
+const char* xpbd_last_error(const xpbd_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int xpbd_set_num_iters(xpbd_ctx* c, int32_t n) {
+    if (!c || n < 0) return XPBD_ERR_INVALID;
+    if (n != c->prm.num_iters) {
+        c->prm.num_iters = n;
+        c->graph_dirty = true;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_set_positions(xpbd_ctx* c, const double* x) {
+    if (!c || !x) return XPBD_ERR_INVALID;
+    return stage_positions_to_device(c, x, nullptr);
+}
+
+int xpbd_set_positions_f32(xpbd_ctx* c, const float* x) {
+    if (!c || !x) return XPBD_ERR_INVALID;
+    return stage_positions_to_device(c, nullptr, x);
+}
+
+static int get_xyz(xpbd_ctx* c, const float4* src, double* out) {
+    int st = fetch(c, src);
+    if (st) return st;
+    for (int i = 0; i < c->V; i++) {
+        out[3 * i] = c->h_stage[i].x;
+        out[3 * i + 1] = c->h_stage[i].y;
+        out[3 * i + 2] = c->h_stage[i].z;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_get_positions(xpbd_ctx* c, double* x) {
+    if (!c || !x) return XPBD_ERR_INVALID;
+    return get_xyz(c, c->x.p, x);
+}
+
+int xpbd_get_positions_f32(xpbd_ctx* c, float* x) {
+    if (!c || !x) return XPBD_ERR_INVALID;
+    int st = fetch(c, c->x.p);
+    if (st) return st;
+    for (int i = 0; i < c->V; i++) {
+        x[3 * i] = c->h_stage[i].x;
+        x[3 * i + 1] = c->h_stage[i].y;
+        x[3 * i + 2] = c->h_stage[i].z;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_get_prev_positions(xpbd_ctx* c, double* x) {
+    if (!c || !x) return XPBD_ERR_INVALID;
+    return get_xyz(c, c->prev.p, x);
+}
+
+int xpbd_set_velocities(xpbd_ctx* c, const double* v) {
+    if (!c || !v) return XPBD_ERR_INVALID;
+    for (int i = 0; i < c->V; i++)
+        c->h_stage[i] = make_float4((float)v[3 * i], (float)v[3 * i + 1], (float)v[3 * i + 2], 0.f);
+    XPBD_CU(c, cudaMemcpyAsync(c->vel.p, c->h_stage, sizeof(float4) * c->V, cudaMemcpyHostToDevice, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+
+int xpbd_get_velocities(xpbd_ctx* c, double* v) {
+    if (!c || !v) return XPBD_ERR_INVALID;
+    return get_xyz(c, c->vel.p, v);
+}
+
+int xpbd_get_masses(xpbd_ctx* c, double* m) {
+    if (!c || !m) return XPBD_ERR_INVALID;
+    std::copy(c->mass_h.begin(), c->mass_h.end(), m);
+    return XPBD_OK;
+}
+
+int xpbd_set_fixed(xpbd_ctx* c, const uint8_t* mask) {
+    if (!c || !mask) return XPBD_ERR_INVALID;
+    // the fixed flag lives in the sign of x.w (and prev.w): re-stage both
+    int st = fetch(c, c->x.p);
+    if (st) return st;
+    for (int i = 0; i < c->V; i++) {
+        c->fixed_h[i] = mask[i] ? 1 : 0;
+        c->h_stage[i].w = (float)c->inv_mass_h[i] * (c->fixed_h[i] ? -1.f : 1.f);
+    }
+    XPBD_CU(c, cudaMemcpyAsync(c->x.p, c->h_stage, sizeof(float4) * c->V, cudaMemcpyHostToDevice, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    st = fetch(c, c->prev.p);
+    if (st) return st;
+    for (int i = 0; i < c->V; i++) c->h_stage[i].w = (float)c->inv_mass_h[i] * (c->fixed_h[i] ? -1.f : 1.f);
+    XPBD_CU(c, cudaMemcpyAsync(c->prev.p, c->h_stage, sizeof(float4) * c->V, cudaMemcpyHostToDevice, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+
+int xpbd_set_kinematic_group(xpbd_ctx* c, int32_t n, const int32_t* idx) {
+    if (!c || n < 0 || (n > 0 && !idx)) return XPBD_ERR_INVALID;
+    for (int j = 0; j < n; j++)
+        if (idx[j] < 0 || idx[j] >= c->V) return fail(c, XPBD_ERR_INVALID, "kinematic index %d out of range", idx[j]);
+    std::vector<uint8_t> mask(c->fixed_h);
+    for (int j = 0; j < n; j++) mask[idx[j]] = 1;
+    int st = xpbd_set_fixed(c, mask.data());
+    if (st) return st;
+    st = fetch(c, c->x.p);
+    if (st) return st;
+    std::vector<float4> rest(n);
+    for (int j = 0; j < n; j++) rest[j] = c->h_stage[idx[j]];
+    c->kin_idx.release();
+    c->kin_rest.release();
+    c->nkin = n;
+    if (n) {
+        XPBD_CU(c, c->kin_idx.alloc(n));
+        XPBD_CU(c, c->kin_rest.alloc(n));
+        XPBD_CU(c, cudaMemcpy(c->kin_idx.p, idx, sizeof(int) * n, cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->kin_rest.p, rest.data(), sizeof(float4) * n, cudaMemcpyHostToDevice));
+    }
+    return XPBD_OK;
+}
+
+int xpbd_set_kinematic_offset(xpbd_ctx* c, const double* off) {
+    if (!c || !off) return XPBD_ERR_INVALID;
+    if (c->nkin == 0) return XPBD_OK;
+    {
+        Scope sc(c, K_KINEMATIC);
+        launch_kinematic(c->stream, c->x.p, c->kin_idx.p, c->kin_rest.p, c->nkin, (float)off[0], (float)off[1],
+                         (float)off[2]);
+    }
+    return after_launches(c, "kinematic offset");
+}
+
+int xpbd_set_spheres(xpbd_ctx* c, int32_t n, const double* ctr, const double* rad) {
+    if (!c || n < 0 || n > kMaxSpheres || (n > 0 && (!ctr || !rad)))
+        return c ? fail(c, XPBD_ERR_INVALID, "sphere count %d outside [0,%d]", n, kMaxSpheres) : XPBD_ERR_INVALID;
+    if (n > c->S) return fail(c, XPBD_ERR_CAPACITY, "%d spheres exceed %d contact slots per face", n, c->S);
+    c->spheres.n = n;
+    for (int i = 0; i < n; i++)
+        c->spheres.s[i] = make_float4((float)ctr[3 * i], (float)ctr[3 * i + 1], (float)ctr[3 * i + 2], (float)rad[i]);
+    return XPBD_OK;
+}
+
+int xpbd_clear_collisions(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (c->F) {
+        XPBD_CU(c, cudaMemsetAsync(c->c_bary.p, 0, sizeof(float4) * (size_t)c->S * c->F, c->stream));
+        XPBD_CU(c, cudaMemsetAsync(c->c_lam.p, 0, sizeof(float) * (size_t)c->S * c->F, c->stream));
+    }
+    std::fill(c->api_slots.begin(), c->api_slots.end(), 0);
+    return XPBD_OK;
+}
+
+int xpbd_detect_collisions(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    return detect(c);
+}
+
+int xpbd_add_static_collision(xpbd_ctx* c, int32_t face, double u, double v, double w, const double* p3,
+                              const double* n3) {
+    if (!c || !p3 || !n3) return XPBD_ERR_INVALID;
+    if (face < 0 || face >= c->F) return fail(c, XPBD_ERR_INVALID, "face %d out of range", face);
+    if (c->api_slots[face] < 0) {
+        // slots were filled by a detection: count the active ones
+        std::vector<float4> b((size_t)c->S * c->F);
+        XPBD_CU(c, cudaMemcpyAsync(b.data(), c->c_bary.p, sizeof(float4) * b.size(), cudaMemcpyDeviceToHost,
+                                   c->stream));
+        XPBD_CU(c, cudaStreamSynchronize(c->stream));
+        for (int f = 0; f < c->F; f++) {
+            int k = 0;
+            for (int s = 0; s < c->S; s++)
+                if (b[(size_t)s * c->F + f].w != 0.f) k = s + 1;
+            c->api_slots[f] = k;
+        }
+    }
+    const int s = c->api_slots[face];
+    if (s >= c->S) return fail(c, XPBD_ERR_CAPACITY, "face %d already has %d contacts", face, c->S);
+    const size_t slot = (size_t)s * c->F + face;
+    const float4 b = make_float4((float)u, (float)v, (float)w, 1.f);
+    const float4 pp = make_float4((float)p3[0], (float)p3[1], (float)p3[2], 0.f);
+    const float4 nn = make_float4((float)n3[0], (float)n3[1], (float)n3[2], 0.f);
+    const float z = 0.f;
+    XPBD_CU(c, cudaMemcpy(c->c_p.p + slot, &pp, sizeof pp, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->c_n.p + slot, &nn, sizeof nn, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->c_lam.p + slot, &z, sizeof z, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->c_bary.p + slot, &b, sizeof b, cudaMemcpyHostToDevice));
+    c->api_slots[face] = s + 1;
+    return XPBD_OK;
+}
+
+int xpbd_get_collisions(xpbd_ctx* c, int32_t max_rows, double* rows, int32_t* n_out) {
+    if (!c || !n_out || max_rows < 0 || (max_rows > 0 && !rows)) return XPBD_ERR_INVALID;
+    *n_out = 0;
+    if (!c->F) return XPBD_OK;
+    const size_t ns = (size_t)c->S * c->F;
+    std::vector<float4> b(ns), pp(ns), nn(ns);
+    std::vector<float> l(ns);
+    XPBD_CU(c, cudaMemcpyAsync(b.data(), c->c_bary.p, sizeof(float4) * ns, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaMemcpyAsync(pp.data(), c->c_p.p, sizeof(float4) * ns, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaMemcpyAsync(nn.data(), c->c_n.p, sizeof(float4) * ns, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaMemcpyAsync(l.data(), c->c_lam.p, sizeof(float) * ns, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    int k = 0;
+    for (size_t sl = 0; sl < ns; sl++) {
+        if (b[sl].w == 0.f) continue;
+        if (k < max_rows) {
+            double* r = rows + 12 * (size_t)k;
+            r[0] = (double)(sl / c->F); r[1] = (double)(sl % c->F);
+            r[2] = b[sl].x; r[3] = b[sl].y; r[4] = b[sl].z;
+            r[5] = pp[sl].x; r[6] = pp[sl].y; r[7] = pp[sl].z;
+            r[8] = nn[sl].x; r[9] = nn[sl].y; r[10] = nn[sl].z;
+            r[11] = l[sl];
+        }
+        k++;
+    }
+    *n_out = k;
+    return XPBD_OK;
+}
+
+int xpbd_update(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    return run_update(c, false);
+}
+
+int xpbd_velocity_update(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    {
+        Scope sc(c, K_VELOCITY);
+        launch_velocity(c->stream, c->x.p, c->prev.p, c->vel.p, c->V, (float)c->prm.dt);
+    }
+    return after_launches(c, "velocity update");
+}
+
+int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
+    if (!c || nsteps < 0) return XPBD_ERR_INVALID;
+    const double interval = c->prm.collision_rate > 0 ? 1.0 / c->prm.collision_rate : 1e300;
+    for (int k = 0; k < nsteps; k++) {
+        const bool cd = (c->time - c->last_cd > interval);
+        if (cd && c->spheres.n > 0) {
+            int st = detect(c);
+            if (st) return st;
+        } else if (cd) {
+            int st = xpbd_clear_collisions(c);
+            if (st) return st;
+        }
+        int st = run_update(c, true);
+        if (st) return st;
+        if (c->time - c->last_cd > interval) c->last_cd = c->time;
+        c->time += c->prm.dt;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_synchronize(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    Flags f{};
+    XPBD_CU(c, cudaMemcpy(&f, c->flags.p, sizeof f, cudaMemcpyDeviceToHost));
+    if (f.nonfinite) return fail(c, XPBD_ERR_NUMERIC, "%llu projections produced non-finite updates", f.nonfinite);
+    return XPBD_OK;
+}
+
+int xpbd_get_time(xpbd_ctx* c, double* t) {
+    if (!c || !t) return XPBD_ERR_INVALID;
+    *t = c->time;
+    return XPBD_OK;
+}
+
+int xpbd_residual_history(xpbd_ctx* c, double* out, int32_t max_n, int32_t* n_out) {
+    if (!c || !n_out || max_n < 0 || (max_n > 0 && !out)) return XPBD_ERR_INVALID;
+    *n_out = 0;
+    if (!c->rows_pending && c->last_rows == 0) return XPBD_OK;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    if (!tracking(c)) return XPBD_OK;
+    const int n = c->last_rows;
+    if (c->prm.residual_policy == XPBD_RESIDUAL_EVERY_SUBSTEP) {
+        // only r(x_pred, 0) and the final residual are evaluated
+        if (max_n > 0) out[0] = std::sqrt(c->h_rows[0]);
+        if (max_n > 1) out[1] = std::sqrt(c->h_rows[n - 1]);
+        *n_out = 2;
+        return XPBD_OK;
+    }
+    for (int i = 0; i < n && i < max_n; i++) out[i] = std::sqrt(c->h_rows[i]);
+    *n_out = n;
+    return XPBD_OK;
+}
+
+int xpbd_residual(xpbd_ctx* c, double* abs_norm, double* rel) {
+    if (!c || !abs_norm) return XPBD_ERR_INVALID;
+    // exact residual at the current state into a scratch row past the history
+    const int row = std::max(c->last_rows, c->prm.num_iters + 1);
+    int st = ensure_residual_rows(c, row + 1);
+    if (st) return st;
+    XPBD_CU(c, cudaMemsetAsync(c->res_partial.p + (size_t)row * c->res_stride, 0, sizeof(double) * c->res_stride,
+                               c->stream));
+    exact_residual_row(c, row, false);
+    launch_reduce_rows(c->stream, c->res_partial.p + (size_t)row * c->res_stride, 1, c->res_stride,
+                       c->res_rows.p + row);
+    double v = 0;
+    XPBD_CU(c, cudaMemcpyAsync(&v, c->res_rows.p + row, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    *abs_norm = std::sqrt(v);
+    if (rel) {
+        *rel = -1.0;
+        if (tracking(c) && c->last_rows > 0) {
+            const double r0 = std::sqrt(c->h_rows[0]);
+            *rel = r0 > 0 ? *abs_norm / r0 : 0.0;
+        }
+    }
+    return after_launches(c, "residual");
+}
+
+int xpbd_get_constraint_residual(xpbd_ctx* c, double* r, int64_t n) {
+    if (!c || !r || n < 2LL * c->T) return XPBD_ERR_INVALID;
+    if (!c->have_rvec) {
+        // no stored residual: evaluate at the current state
+        launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p,
+                        c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE, c->perm.p, c->rvec.p, no_sink(), nullptr,
+                        (float)(c->prm.dt * c->prm.dt));
+    }
+    std::vector<float> h(2 * (size_t)c->T);
+    XPBD_CU(c, cudaMemcpyAsync(h.data(), c->rvec.p, sizeof(float) * h.size(), cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    for (size_t i = 0; i < h.size(); i++) r[i] = h[i];
+    return after_launches(c, "constraint residual");
+}
+
+int xpbd_get_lambda(xpbd_ctx* c, double* lam) {
+    if (!c || !lam) return XPBD_ERR_INVALID;
+    std::vector<float2> h(c->T);
+    XPBD_CU(c, cudaMemcpyAsync(h.data(), c->lam.p, sizeof(float2) * c->T, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    for (int sidx = 0; sidx < c->T; sidx++) {
+        const int t = c->tet_of_slot[sidx];
+        lam[2 * (size_t)t] = h[sidx].x;
+        lam[2 * (size_t)t + 1] = h[sidx].y;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_total_strain_energy(xpbd_ctx* c, double* e) {
+    if (!c || !e) return XPBD_ERR_INVALID;
+    const int nb = residual_blocks(c->T, c->block);
+    launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
+                    c->perm.p, nullptr, no_sink(), c->energy_partial.p, (float)(c->prm.dt * c->prm.dt));
+    launch_reduce_rows(c->stream, c->energy_partial.p, 1, nb, c->energy_partial.p + nb);
+    double v = 0;
+    XPBD_CU(c, cudaMemcpyAsync(&v, c->energy_partial.p + nb, sizeof v, cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    *e = v;
+    return after_launches(c, "strain energy");
+}
+
+int xpbd_health(xpbd_ctx* c, int64_t* nonfinite, int64_t* degenerate) {
+    if (!c) return XPBD_ERR_INVALID;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    Flags f{};
+    XPBD_CU(c, cudaMemcpy(&f, c->flags.p, sizeof f, cudaMemcpyDeviceToHost));
+    XPBD_CU(c, cudaMemset(c->flags.p, 0, sizeof f));
+    if (nonfinite) *nonfinite = (int64_t)f.nonfinite;
+    if (degenerate) *degenerate = (int64_t)f.degenerate;
+    return XPBD_OK;
+}
+
+int xpbd_num_colours(xpbd_ctx* c, int32_t* nt, int32_t* nf) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (nt) *nt = c->n_tet_colours;
+    if (nf) *nf = c->n_face_colours;
+    return XPBD_OK;
+}
+
+int xpbd_get_tet_colours(xpbd_ctx* c, int32_t* col) {
+    if (!c || !col) return XPBD_ERR_INVALID;
+    std::copy(c->tet_colour.begin(), c->tet_colour.end(), col);
+    return XPBD_OK;
+}
+
+static const char* kNames[K_COUNT] = {"predict",  "project_jacobi", "apply",    "project_gs",
+                                      "contacts", "detect",         "finalize", "residual",
+                                      "reduce",   "kinematic",      "gather_apply", "velocity"};
+
+const char* xpbd_kernel_name(int32_t id) { return (id >= 0 && id < K_COUNT) ? kNames[id] : "?"; }
+
+int xpbd_profile_steps(xpbd_ctx* c, int32_t nsteps, int32_t max_k, double* avg_ms, int64_t* launches) {
+    if (!c || nsteps < 0 || max_k < 0 || (max_k > 0 && (!avg_ms || !launches))) return XPBD_ERR_INVALID;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    c->prof.on = true;
+    c->prof.used = 0;
+    c->prof.ids.clear();
+    int st = xpbd_step(c, nsteps);
+    c->prof.on = false;
+    if (st) return st;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    std::vector<double> tot(K_COUNT, 0.0);
+    std::vector<long long> cnt(K_COUNT, 0);
+    for (size_t i = 0; i < c->prof.ids.size(); i++) {
+        float ms = 0;
+        XPBD_CU(c, cudaEventElapsedTime(&ms, c->prof.pool[2 * i], c->prof.pool[2 * i + 1]));
+        tot[c->prof.ids[i]] += ms;
+        cnt[c->prof.ids[i]]++;
+    }
+    for (int k = 0; k < max_k; k++) {
+        avg_ms[k] = (k < K_COUNT && cnt[k]) ? tot[k] / cnt[k] : 0.0;
+        launches[k] = k < K_COUNT ? cnt[k] : 0;
+    }
+    return XPBD_OK;
+}
+
+int xpbd_launch_count(xpbd_ctx* c, int64_t* n) {
+    if (!c || !n) return XPBD_ERR_INVALID;
+    *n = c->launches;
+    return XPBD_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,797 @@
+// sm_103a kernels of the XPBD substep: prediction, Stable-Neo-Hookean
+// tetrahedral projection (combined 2x2 and separate scalar forms), Jacobi
+// scatter/apply, coloured Gauss-Seidel sweeps, SDF sphere collision detection
+// and projection, fixed-vertex reset + velocity update, and FP64-finished
+// residual/energy reductions.
+//
+// Semantics follow the reference's CPU path:
+//   projection   src/solver/xpbd_projector/CombinedNeohookeanConstraintProjector.cpp:98-179
+//                include/solver/xpbd_projector/ConstraintProjector.hpp:111-172
+//   constraints  include/solver/constraint/{Hydrostatic,Deviatoric}Constraint.hpp
+//   Jacobi       include/solver/xpbd_solver/XPBDJacobiSolver.hpp:79-114 (plain sum)
+//   predict      src/simobject/XPBDMeshObject.cpp:446-470
+//   fixed/vel    src/simobject/XPBDMeshObject.cpp:497-535
+//   collisions   src/collision/CollisionScene.cpp:171-214,253-283
+//                src/solver/constraint/StaticDeformableCollisionConstraint.cpp:20-49
+// Every kernel is memory-bound; see the HBM layout in xpbd_kernels.cuh.
+#include <cuda_runtime.h>
+
+#include "xpbd_kernels.cuh"
+
+namespace xg {
+
+namespace {
+
+constexpr float kDegenerateJ = 1e-3f;  // |det F| below this takes the FP64 path
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Fixed-order block sum: FP32 inside a warp, FP64 across warps.
+__device__ __forceinline__ void block_sum_store(float v, double* slot) {
+    __shared__ double sw[32];
+    v = warp_sum(v);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) sw[wid] = (double)v;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        const int nw = (blockDim.x + 31) >> 5;
+        for (int i = 0; i < nw; i++) s += sw[i];
+        *slot = s;
+    }
+}
+
+__device__ __forceinline__ void add_vec4(float4* addr, float a, float b, float c) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+    atomicAdd(addr, make_float4(a, b, c, 0.f));  // one 16-byte vector reduction at L2
+#else
+    atomicAdd(&addr->x, a);
+    atomicAdd(&addr->y, b);
+    atomicAdd(&addr->z, c);
+#endif
+}
+
+// ---------------------------------------------------------------------------
+// Per-tet math, templated on the arithmetic type (float fast path, double for
+// near-degenerate elements).
+// ---------------------------------------------------------------------------
+template <typename R>
+struct TetState {
+    R p[4][3];
+    R w[4];
+    R q[9];  // Q column-major: q[3c + r] = Q(r, c)
+    R atd, ath, gam;
+};
+
+template <typename R>
+__device__ __forceinline__ R dev_log(R v) { return log(v); }
+template <>
+__device__ __forceinline__ float dev_log<float>(float v) { return logf(v); }
+template <typename R>
+__device__ __forceinline__ R dev_sqrt(R v) { return sqrt(v); }
+template <>
+__device__ __forceinline__ float dev_sqrt<float>(float v) { return sqrtf(v); }
+
+// F = Ds Q (ElementConstraint.hpp:78-119), its Frobenius norm (C_dev) and det.
+template <typename R>
+__device__ __forceinline__ void tet_F(const TetState<R>& s, R F[9]) {
+    R X[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) X[3 * i + k] = s.p[i][k] - s.p[3][k];
+#pragma unroll
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            F[3 * c + k] = X[k] * s.q[3 * c + 0] + X[3 + k] * s.q[3 * c + 1] + X[6 + k] * s.q[3 * c + 2];
+}
+
+template <typename R>
+__device__ __forceinline__ R tet_detF(const R F[9]) {
+    return F[0] * F[4] * F[8] - F[0] * F[7] * F[5] - F[3] * F[1] * F[8] + F[3] * F[7] * F[2] + F[6] * F[1] * F[5] -
+           F[6] * F[4] * F[2];
+}
+
+// Values and gradients of both constraints (HydrostaticConstraint.hpp:123-221,
+// DeviatoricConstraint.hpp:112-152). gd/gh hold vertices 0..2; vertex 3 is
+// minus their sum.
+template <typename R>
+__device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R gd[9], R gh[9], R& J) {
+    R F[9];
+    tet_F(s, F);
+    R ss = 0;
+#pragma unroll
+    for (int i = 0; i < 9; i++) ss += F[i] * F[i];
+    Cd = dev_sqrt(ss);
+    const R invC = R(1) / Cd;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            gd[3 * i + k] = invC * (F[k] * s.q[i] + F[3 + k] * s.q[3 + i] + F[6 + k] * s.q[6 + i]);
+    J = tet_detF(F);
+    R fac;
+    if (J >= R(1)) {
+        Ch = -s.gam + dev_log(J);
+        fac = R(1) / J;
+    } else {
+        const R d = J - R(1);
+        Ch = -s.gam + d - d * d / R(2) + d * d * d / R(3);
+        fac = R(1) - d + d * d;
+    }
+    R Fc[9];
+    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
+    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
+    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
+}
+
+// Combined 2x2 projection. Returns the pre-update residuals r = C + at*lam and
+// the lambda increments; writes the 4 vertex updates to d[4][3].
+template <typename R>
+__device__ __forceinline__ void tet_project_combined(const TetState<R>& s, R lam0, R lam1, R& r0, R& r1, R& dl0,
+                                                     R& dl1, R d[4][3], R& J) {
+    R Cd, Ch, gd[9], gh[9];
+    tet_eval(s, Cd, Ch, gd, gh, J);
+    R gd3[3], gh3[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        gd3[k] = -gd[k] - gd[3 + k] - gd[6 + k];
+        gh3[k] = -gh[k] - gh[3 + k] - gh[6 + k];
+    }
+    R L00 = s.atd, L01 = 0, L11 = s.ath;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const R* a = i < 3 ? gd + 3 * i : gd3;
+        const R* b = i < 3 ? gh + 3 * i : gh3;
+        L00 += s.w[i] * (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+        L01 += s.w[i] * (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
+        L11 += s.w[i] * (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
+    }
+    r0 = Cd + s.atd * lam0;
+    r1 = Ch + s.ath * lam1;
+    const R det = L00 * L11 - L01 * L01;
+    dl0 = (-r0 * L11 + r1 * L01) / det;
+    dl1 = (-r1 * L00 + r0 * L01) / det;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const R* a = i < 3 ? gd + 3 * i : gd3;
+        const R* b = i < 3 ? gh + 3 * i : gh3;
+#pragma unroll
+        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * (a[k] * dl0 + b[k] * dl1);
+    }
+}
+
+// Scalar projection of one element constraint (which = 0 dev, 1 hyd).
+template <typename R>
+__device__ __forceinline__ void tet_project_single(const TetState<R>& s, int which, R lam, R& r, R& dl, R d[4][3],
+                                                   R& J) {
+    R Cd, Ch, gd[9], gh[9];
+    tet_eval(s, Cd, Ch, gd, gh, J);
+    const R* g = which == 0 ? gd : gh;
+    const R at = which == 0 ? s.atd : s.ath;
+    const R C = which == 0 ? Cd : Ch;
+    R g3[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) g3[k] = -g[k] - g[3 + k] - g[6 + k];
+    R L = at;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const R* a = i < 3 ? g + 3 * i : g3;
+        L += s.w[i] * (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    }
+    r = C + at * lam;
+    dl = -r / L;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const R* a = i < 3 ? g + 3 * i : g3;
+#pragma unroll
+        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * a[k] * dl;
+    }
+}
+
+__device__ __forceinline__ void load_tet(const TetArrays& t, int slot, const float4* __restrict__ x, int4& e,
+                                         TetState<float>& s, float4 xp[4]) {
+    e = __ldg(t.idx + slot);
+    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
+    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
+    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
+    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
+    xp[0] = x[e.x]; xp[1] = x[e.y]; xp[2] = x[e.z]; xp[3] = x[e.w];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        s.p[i][0] = xp[i].x; s.p[i][1] = xp[i].y; s.p[i][2] = xp[i].z;
+        s.w[i] = fabsf(xp[i].w);
+    }
+}
+
+// FP64 guard path for near-degenerate / inverted elements. Kept out of line so
+// the FP32 path keeps its register budget.
+__device__ __noinline__ void project_combined_fp64(const TetState<float>& sf, float lam0, float lam1, float* r,
+                                                   float* dl, float* d) {
+    TetState<double> s;
+    for (int i = 0; i < 4; i++) {
+        for (int k = 0; k < 3; k++) s.p[i][k] = sf.p[i][k];
+        s.w[i] = sf.w[i];
+    }
+    for (int i = 0; i < 9; i++) s.q[i] = sf.q[i];
+    s.atd = sf.atd; s.ath = sf.ath; s.gam = sf.gam;
+    double r0, r1, dl0, dl1, dd[4][3], J;
+    tet_project_combined(s, (double)lam0, (double)lam1, r0, r1, dl0, dl1, dd, J);
+    r[0] = (float)r0; r[1] = (float)r1; dl[0] = (float)dl0; dl[1] = (float)dl1;
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) d[3 * i + k] = (float)dd[i][k];
+}
+
+__device__ __noinline__ void project_single_fp64(const TetState<float>& sf, int which, float lam, float* r, float* dl,
+                                                 float* d) {
+    TetState<double> s;
+    for (int i = 0; i < 4; i++) {
+        for (int k = 0; k < 3; k++) s.p[i][k] = sf.p[i][k];
+        s.w[i] = sf.w[i];
+    }
+    for (int i = 0; i < 9; i++) s.q[i] = sf.q[i];
+    s.atd = sf.atd; s.ath = sf.ath; s.gam = sf.gam;
+    double rr, dd_l, dd[4][3], J;
+    tet_project_single(s, which, (double)lam, rr, dd_l, dd, J);
+    *r = (float)rr; *dl = (float)dd_l;
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) d[3 * i + k] = (float)dd[i][k];
+}
+
+// One tet projection in the chosen constraint form. On return d holds the
+// vertex updates, lam the updated multipliers and rsq the squared residual of
+// the state the projection saw. Returns false when the update is non-finite
+// (then nothing may be applied).
+template <bool SEPARATE>
+__device__ __forceinline__ bool project_one(const TetState<float>& s, float2& lam, float d[4][3], float& rsq,
+                                            Flags* flags) {
+    float J;
+    if (!SEPARATE) {
+        float r0, r1, dl0, dl1;
+        tet_project_combined(s, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
+        if (fabsf(J) < kDegenerateJ) {
+            float r[2], dl[2];
+            project_combined_fp64(s, lam.x, lam.y, r, dl, &d[0][0]);
+            r0 = r[0]; r1 = r[1]; dl0 = dl[0]; dl1 = dl[1];
+            atomicAdd(&flags->degenerate, 1ull);
+        }
+        rsq = r0 * r0 + r1 * r1;
+        if (!(isfinite(dl0) && isfinite(dl1))) {
+            atomicAdd(&flags->nonfinite, 1ull);
+            return false;
+        }
+        lam.x += dl0;
+        lam.y += dl1;
+    } else {
+        // Jacobi form of the separate configuration: Dev and Hyd both see the
+        // same positions, their updates are summed.
+        float r0, r1, dl0, dl1, d1[4][3];
+        tet_project_single(s, 0, lam.x, r0, dl0, d, J);
+        tet_project_single(s, 1, lam.y, r1, dl1, d1, J);
+        if (fabsf(J) < kDegenerateJ) {
+            project_single_fp64(s, 0, lam.x, &r0, &dl0, &d[0][0]);
+            project_single_fp64(s, 1, lam.y, &r1, &dl1, &d1[0][0]);
+            atomicAdd(&flags->degenerate, 1ull);
+        }
+        rsq = r0 * r0 + r1 * r1;
+        if (!(isfinite(dl0) && isfinite(dl1))) {
+            atomicAdd(&flags->nonfinite, 1ull);
+            return false;
+        }
+        lam.x += dl0;
+        lam.y += dl1;
+#pragma unroll
+        for (int i = 0; i < 4; i++)
+#pragma unroll
+            for (int k = 0; k < 3; k++) d[i][k] += d1[i][k];
+    }
+    return true;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+__global__ void k_predict(float4* __restrict__ x, float4* __restrict__ prev, const float4* __restrict__ vel, int V,
+                          float dt, float dz) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float4 p = x[i];
+    const float4 v = vel[i];
+    prev[i] = p;
+    x[i] = make_float4(p.x + dt * v.x, p.y + dt * v.y, (p.z + dt * v.z) + dz, p.w);
+}
+
+__global__ void k_kinematic(float4* __restrict__ x, const int* __restrict__ idx, const float4* __restrict__ rest,
+                            int n, float ox, float oy, float oz) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int i = idx[j];
+    const float4 r = rest[j];
+    const float w = x[i].w;
+    x[i] = make_float4(r.x + ox, r.y + oy, r.z + oz, w);
+}
+
+// Jacobi sweep: every tet reads the same x, its updates are summed into dx by
+// 16-byte vector reductions (XPBDJacobiSolver.hpp:79-114, plain summation).
+template <bool FIRST, bool SEPARATE, bool RES>
+__global__ void __launch_bounds__(256) k_project_jacobi(TetArrays t, int T, const float4* __restrict__ x,
+                                                        float4* __restrict__ dx, ResidualSink res, Flags* flags) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    float rsq = 0.f;
+    if (slot < T) {
+        int4 e;
+        TetState<float> s;
+        float4 xp[4];
+        load_tet(t, slot, x, e, s, xp);
+        float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
+        float d[4][3];
+        if (project_one<SEPARATE>(s, lam, d, rsq, flags)) {
+            add_vec4(dx + e.x, d[0][0], d[0][1], d[0][2]);
+            add_vec4(dx + e.y, d[1][0], d[1][1], d[1][2]);
+            add_vec4(dx + e.z, d[2][0], d[2][1], d[2][2]);
+            add_vec4(dx + e.w, d[3][0], d[3][1], d[3][2]);
+        }
+        t.lam[slot] = lam;
+    }
+    if (RES) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
+}
+
+// Deterministic Jacobi variant, pass 1: per-tet updates to a [T][3] float4
+// buffer (12 floats per tet).
+template <bool FIRST, bool SEPARATE, bool RES>
+__global__ void __launch_bounds__(256) k_project_jacobi_write(TetArrays t, int T, const float4* __restrict__ x,
+                                                              float4* __restrict__ dxt, ResidualSink res,
+                                                              Flags* flags) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    float rsq = 0.f;
+    if (slot < T) {
+        int4 e;
+        TetState<float> s;
+        float4 xp[4];
+        load_tet(t, slot, x, e, s, xp);
+        float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
+        float d[4][3];
+        if (!project_one<SEPARATE>(s, lam, d, rsq, flags)) {
+#pragma unroll
+            for (int i = 0; i < 4; i++) d[i][0] = d[i][1] = d[i][2] = 0.f;
+        }
+        dxt[3 * (size_t)slot + 0] = make_float4(d[0][0], d[0][1], d[0][2], d[1][0]);
+        dxt[3 * (size_t)slot + 1] = make_float4(d[1][1], d[1][2], d[2][0], d[2][1]);
+        dxt[3 * (size_t)slot + 2] = make_float4(d[2][2], d[3][0], d[3][1], d[3][2]);
+        t.lam[slot] = lam;
+    }
+    if (RES) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
+}
+
+// Fixed vertices go back to their previous position (XPBDMeshObject.cpp:497-503);
+// with write_vel the velocity update v = (x - prev)/dt (XPBDMeshObject.cpp:507-535)
+// is fused in.
+__device__ __forceinline__ void finalize_vertex(float4* __restrict__ x, const float4* __restrict__ prev,
+                                                float4* __restrict__ vel, int i, float4 xx, float dt,
+                                                bool write_vel) {
+    const float4 p = prev[i];
+    if (p.w < 0.f) xx = p;
+    x[i] = xx;
+    if (write_vel) vel[i] = make_float4((xx.x - p.x) / dt, (xx.y - p.y) / dt, (xx.z - p.z) / dt, 0.f);
+}
+
+// Pass 2: each vertex sums its tets' updates in CSR (ascending tet) order.
+template <bool FINAL>
+__global__ void k_gather_apply(float4* __restrict__ x, const float* __restrict__ dxt, const int* __restrict__ off,
+                               const int* __restrict__ ent, float4* __restrict__ dx, int V,
+                               const float4* __restrict__ prev, float4* __restrict__ vel, float dt, bool write_vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    const int b = off[i], e = off[i + 1];
+    for (int j = b; j < e; j++) {
+        const int code = ent[j];  // slot * 4 + local vertex
+        const float* p = dxt + 12 * (size_t)(code >> 2) + 3 * (code & 3);
+        sx += p[0]; sy += p[1]; sz += p[2];
+    }
+    // contact updates arrive through dx
+    const float4 dc = dx[i];
+    dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float4 xx = x[i];
+    xx.x += sx + dc.x; xx.y += sy + dc.y; xx.z += sz + dc.z;
+    if (FINAL) finalize_vertex(x, prev, vel, i, xx, dt, write_vel);
+    else x[i] = xx;
+}
+
+template <bool FINAL>
+__global__ void k_apply(float4* __restrict__ x, float4* __restrict__ dx, int V, const float4* __restrict__ prev,
+                        float4* __restrict__ vel, float dt, bool write_vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    float4 xx = x[i];
+    const float4 d = dx[i];
+    xx.x += d.x; xx.y += d.y; xx.z += d.z;
+    dx[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (FINAL) finalize_vertex(x, prev, vel, i, xx, dt, write_vel);
+    else x[i] = xx;
+}
+
+// Coloured Gauss-Seidel: one launch per colour; tets of a colour share no
+// vertex, so each thread updates its 4 vertices in place.
+template <bool FIRST, int WHICH, bool RES>
+__global__ void __launch_bounds__(256) k_project_gs(TetArrays t, int begin, int end, float4* __restrict__ x,
+                                                    ResidualSink res, Flags* flags) {
+    const int slot = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    float rsq = 0.f;
+    if (slot < end) {
+        int4 e;
+        TetState<float> s;
+        float4 xp[4];
+        load_tet(t, slot, x, e, s, xp);
+        float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
+        float d[4][3];
+        bool ok;
+        if (WHICH == 2) {
+            ok = project_one<false>(s, lam, d, rsq, flags);
+        } else {
+            float J, r, dl;
+            float lw = WHICH == 0 ? lam.x : lam.y;
+            tet_project_single(s, WHICH, lw, r, dl, d, J);
+            if (fabsf(J) < kDegenerateJ) {
+                project_single_fp64(s, WHICH, lw, &r, &dl, &d[0][0]);
+                atomicAdd(&flags->degenerate, 1ull);
+            }
+            rsq = r * r;
+            ok = isfinite(dl);
+            if (!ok) atomicAdd(&flags->nonfinite, 1ull);
+            else if (WHICH == 0) lam.x += dl;
+            else lam.y += dl;
+        }
+        if (ok) {
+            x[e.x] = make_float4(xp[0].x + d[0][0], xp[0].y + d[0][1], xp[0].z + d[0][2], xp[0].w);
+            x[e.y] = make_float4(xp[1].x + d[1][0], xp[1].y + d[1][1], xp[1].z + d[1][2], xp[1].w);
+            x[e.z] = make_float4(xp[2].x + d[2][0], xp[2].y + d[2][1], xp[2].z + d[2][2], xp[2].w);
+            x[e.w] = make_float4(xp[3].x + d[3][0], xp[3].y + d[3][1], xp[3].z + d[3][2], xp[3].w);
+        }
+        t.lam[slot] = lam;
+    }
+    if (RES) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
+}
+
+// Static collision projection of one contact slot: C = n.(u x1 + v x2 + w x3 - p),
+// skipped when C > 0, alpha = 0. Returns false when skipped.
+__device__ __forceinline__ bool contact_update(const ContactArrays& c, int slot, const float4 xs[3], float d[3][3],
+                                               float& lam) {
+    const float4 b = c.bary[slot];
+    const float4 p = c.p[slot];
+    const float4 n = c.n[slot];
+    const float a0 = b.x * xs[0].x + b.y * xs[1].x + b.z * xs[2].x;
+    const float a1 = b.x * xs[0].y + b.y * xs[1].y + b.z * xs[2].y;
+    const float a2 = b.x * xs[0].z + b.y * xs[1].z + b.z * xs[2].z;
+    const float C = n.x * (a0 - p.x) + n.y * (a1 - p.y) + n.z * (a2 - p.z);
+    if (C > 0.f) return false;
+    const float bb[3] = {b.x, b.y, b.z};
+    float L = 0.f;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float gx = bb[i] * n.x, gy = bb[i] * n.y, gz = bb[i] * n.z;
+        L += fabsf(xs[i].w) * (gx * gx + gy * gy + gz * gz);
+    }
+    const float dl = -C / L;
+    if (!isfinite(dl)) return false;
+    lam += dl;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float wi = fabsf(xs[i].w);
+        d[i][0] = wi * (bb[i] * n.x) * dl;
+        d[i][1] = wi * (bb[i] * n.y) * dl;
+        d[i][2] = wi * (bb[i] * n.z) * dl;
+    }
+    return true;
+}
+
+template <bool FIRST>
+__global__ void k_contacts_jacobi(ContactArrays c, const float4* __restrict__ x, float4* __restrict__ dx) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= c.S * c.F) return;
+    if (c.bary[slot].w == 0.f) return;
+    const int f = slot % c.F;
+    const int4 fv = c.faces[f];
+    const float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
+    float lam = FIRST ? 0.f : c.lam[slot];
+    float d[3][3];
+    if (contact_update(c, slot, xs, d, lam)) {
+        add_vec4(dx + fv.x, d[0][0], d[0][1], d[0][2]);
+        add_vec4(dx + fv.y, d[1][0], d[1][1], d[1][2]);
+        add_vec4(dx + fv.z, d[2][0], d[2][1], d[2][2]);
+    }
+    c.lam[slot] = lam;
+}
+
+// Gauss-Seidel contacts: one launch per surface-face colour; a thread owns a
+// face and walks its slots in order, updating positions in place.
+template <bool FIRST>
+__global__ void k_contacts_gs(ContactArrays c, const int* __restrict__ face_list, int begin, int end,
+                              float4* __restrict__ x) {
+    const int j = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= end) return;
+    const int f = face_list[j];
+    const int4 fv = c.faces[f];
+    for (int s = 0; s < c.S; s++) {
+        const int slot = s * c.F + f;
+        if (c.bary[slot].w == 0.f) continue;
+        float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
+        float lam = FIRST ? 0.f : c.lam[slot];
+        float d[3][3];
+        if (contact_update(c, slot, xs, d, lam)) {
+            x[fv.x] = make_float4(xs[0].x + d[0][0], xs[0].y + d[0][1], xs[0].z + d[0][2], xs[0].w);
+            x[fv.y] = make_float4(xs[1].x + d[1][0], xs[1].y + d[1][1], xs[1].z + d[1][2], xs[1].w);
+            x[fv.z] = make_float4(xs[2].x + d[2][0], xs[2].y + d[2][1], xs[2].z + d[2][2], xs[2].w);
+        }
+        c.lam[slot] = lam;
+    }
+}
+
+// ---- collision detection (one thread per (sphere slot, face)) ----
+__device__ __forceinline__ float sdf_sphere(float px, float py, float pz, float4 sph) {
+    const float a = px - sph.x, b = py - sph.y, c = pz - sph.z;
+    return sqrtf(a * a + b * b + c * c) - sph.w;
+}
+__device__ __forceinline__ void grad_sphere(float px, float py, float pz, float4 sph, float g[3]) {
+    const float a = px - sph.x, b = py - sph.y, c = pz - sph.z;
+    const float n2 = a * a + b * b + c * c;
+    if (n2 > 0.f) {
+        const float n = sqrtf(n2);
+        g[0] = a / n; g[1] = b / n; g[2] = c / n;
+    } else {
+        g[0] = a; g[1] = b; g[2] = c;
+    }
+}
+
+__global__ void k_detect(ContactArrays c, const float4* __restrict__ x, SphereSet sph) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= c.S * c.F) return;
+    const int s = slot / c.F, f = slot - s * c.F;
+    float4 bary = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (s < sph.n) {
+        const float4 S = sph.s[s];
+        const int4 fv = c.faces[f];
+        const float4 q1 = x[fv.x], q2 = x[fv.y], q3 = x[fv.z];
+        const float p1[3] = {q1.x, q1.y, q1.z}, p2[3] = {q2.x, q2.y, q2.z}, p3[3] = {q3.x, q3.y, q3.z};
+        auto sq = [](const float* a, const float* b) {
+            const float d0 = b[0] - a[0], d1 = b[1] - a[1], d2 = b[2] - a[2];
+            return d0 * d0 + d1 * d1 + d2 * d2;
+        };
+        const float me = fmaxf(fmaxf(sq(p1, p2), sq(p1, p3)), sq(p2, p3));
+        const float cd = sdf_sphere((p1[0] + p2[0] + p3[0]) / 3.f, (p1[1] + p2[1] + p3[1]) / 3.f,
+                                    (p1[2] + p2[2] + p3[2]) / 3.f, S);
+        if (!(cd * cd > me)) {
+            // Frank-Wolfe over the triangle, 32 iterations, from the vertex of
+            // smallest SDF (CollisionScene.cpp:253-283)
+            const float d1 = sdf_sphere(p1[0], p1[1], p1[2], S), d2 = sdf_sphere(p2[0], p2[1], p2[2], S),
+                        d3 = sdf_sphere(p3[0], p3[1], p3[2], S);
+            const float* s0 = (d1 <= d2 && d1 <= d3) ? p1 : ((d2 <= d1 && d2 <= d3) ? p2 : p3);
+            float xx[3] = {s0[0], s0[1], s0[2]};
+            for (int i = 0; i < 32; i++) {
+                const float alpha = 2.0f / (float)(i + 3);
+                float g[3];
+                grad_sphere(xx[0], xx[1], xx[2], S, g);
+                const float sg1 = p1[0] * g[0] + p1[1] * g[1] + p1[2] * g[2];
+                const float sg2 = p2[0] * g[0] + p2[1] * g[1] + p2[2] * g[2];
+                const float sg3 = p3[0] * g[0] + p3[1] * g[1] + p3[2] * g[2];
+                const float* sv = (sg1 < sg2 && sg1 < sg3) ? p1 : ((sg2 < sg1 && sg2 < sg3) ? p2 : p3);
+#pragma unroll
+                for (int k = 0; k < 3; k++) xx[k] = xx[k] + alpha * (sv[k] - xx[k]);
+            }
+            const float dist = sdf_sphere(xx[0], xx[1], xx[2], S);
+            if ((double)dist <= 1e-4) {
+                // barycentrics (GeometryUtils.cpp:6-23)
+                float v0[3], v1[3], v2[3];
+                for (int k = 0; k < 3; k++) { v0[k] = p2[k] - p1[k]; v1[k] = p3[k] - p1[k]; v2[k] = xx[k] - p1[k]; }
+                auto dot = [](const float* a, const float* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+                const float d00 = dot(v0, v0), d01 = dot(v0, v1), d11 = dot(v1, v1), d20 = dot(v2, v0),
+                            d21 = dot(v2, v1);
+                const float den = d00 * d11 - d01 * d01;
+                const float bv = (d11 * d20 - d01 * d21) / den;
+                const float bw = (d00 * d21 - d01 * d20) / den;
+                const float bu = 1.f - bv - bw;
+                float g[3];
+                grad_sphere(xx[0], xx[1], xx[2], S, g);
+                bary = make_float4(bu, bv, bw, 1.f);
+                c.p[slot] = make_float4(xx[0] - g[0] * dist, xx[1] - g[1] * dist, xx[2] - g[2] * dist, 0.f);
+                c.n[slot] = make_float4(g[0], g[1], g[2], 0.f);
+                c.lam[slot] = 0.f;
+            }
+        }
+    }
+    c.bary[slot] = bary;
+}
+
+__global__ void k_finalize(float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel, int V,
+                           float dt, bool write_vel) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    finalize_vertex(x, prev, vel, i, x[i], dt, write_vel);
+}
+
+// v = (x - prev)/dt alone (XPBDMeshObject_::velocityUpdate)
+__global__ void k_velocity(const float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel,
+                           int V, float dt) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float4 xx = x[i], p = prev[i];
+    vel[i] = make_float4((xx.x - p.x) / dt, (xx.y - p.y) / dt, (xx.z - p.z) / dt, 0.f);
+}
+
+// Exact residual / energy at the current state. rvec (optional) receives the
+// per-constraint residuals in the reference's order via the slot->tet map.
+__global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const float4* __restrict__ x, bool separate,
+                                                  const int* __restrict__ perm, float* __restrict__ rvec,
+                                                  ResidualSink res, double* __restrict__ energy_partial, float dt2) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    float rsq = 0.f, en = 0.f;
+    if (slot < T) {
+        int4 e;
+        TetState<float> s;
+        float4 xp[4];
+        load_tet(t, slot, x, e, s, xp);
+        const float2 lam = t.lam[slot];
+        float Cd, Ch, gd[9], gh[9], J;
+        tet_eval(s, Cd, Ch, gd, gh, J);
+        const float r0 = Cd + s.atd * lam.x, r1 = Ch + s.ath * lam.y;
+        rsq = r0 * r0 + r1 * r1;
+        en = Cd * Cd / (s.atd * dt2) + Ch * Ch / (s.ath * dt2);
+        if (rvec) {
+            const int tt = perm ? perm[slot] : slot;
+            if (!separate) { rvec[2 * (size_t)tt] = r0; rvec[2 * (size_t)tt + 1] = r1; }
+            else { rvec[tt] = r0; rvec[(size_t)T + tt] = r1; }
+        }
+    }
+    if (res.partial) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
+    if (energy_partial) {
+        __syncthreads();
+        block_sum_store(en, energy_partial + blockIdx.x);
+    }
+}
+
+// One block per row: FP64 sum of `stride` partials, fixed order.
+__global__ void k_reduce_rows(const double* __restrict__ partial, int stride, double* __restrict__ out) {
+    __shared__ double sh[256];
+    const int row = blockIdx.x;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < stride; i += blockDim.x) s += partial[(size_t)row * stride + i];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) out[row] = sh[0];
+}
+
+inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
+
+}  // namespace
+
+int residual_blocks(int T, int block) { return nblk(T, block); }
+
+void launch_predict(cudaStream_t s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz) {
+    if (V > 0) k_predict<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt, dz);
+}
+
+void launch_kinematic(cudaStream_t s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
+                      float oz) {
+    if (n > 0) k_kinematic<<<nblk(n, 256), 256, 0, s>>>(x, idx, rest, n, ox, oy, oz);
+}
+
+#define XG_DISPATCH_FSR(KERNEL, GRID, BLOCK, STREAM, ...)                                               \
+    do {                                                                                                \
+        const bool _r = res.partial != nullptr;                                                         \
+        if (first) {                                                                                    \
+            if (separate) { if (_r) KERNEL<true, true, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);  \
+                            else KERNEL<true, true, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }  \
+            else { if (_r) KERNEL<true, false, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);          \
+                   else KERNEL<true, false, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }          \
+        } else {                                                                                        \
+            if (separate) { if (_r) KERNEL<false, true, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
+                            else KERNEL<false, true, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); } \
+            else { if (_r) KERNEL<false, false, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);         \
+                   else KERNEL<false, false, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }         \
+        }                                                                                               \
+    } while (0)
+
+void launch_project_jacobi(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
+                           bool first, bool separate, ResidualSink res, Flags* flags) {
+    if (T <= 0) return;
+    XG_DISPATCH_FSR(k_project_jacobi, nblk(T, block), block, s, t, T, x, dx, res, flags);
+}
+
+void launch_project_jacobi_gather_write(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x,
+                                        float4* dxt, bool first, bool separate, ResidualSink res, Flags* flags) {
+    if (T <= 0) return;
+    XG_DISPATCH_FSR(k_project_jacobi_write, nblk(T, block), block, s, t, T, x, dxt, res, flags);
+}
+
+void launch_gather_apply(cudaStream_t s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
+                         float4* dx, int V, float4* prev, float4* vel, bool final_step, float dt, bool write_vel) {
+    if (V <= 0) return;
+    const float* d = (const float*)dxt;
+    if (final_step)
+        k_gather_apply<true><<<nblk(V, 256), 256, 0, s>>>(x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
+    else
+        k_gather_apply<false><<<nblk(V, 256), 256, 0, s>>>(x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
+}
+
+void launch_apply(cudaStream_t s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
+                  float dt, bool write_vel) {
+    if (V <= 0) return;
+    if (final_step) k_apply<true><<<nblk(V, 256), 256, 0, s>>>(x, dx, V, prev, vel, dt, write_vel);
+    else k_apply<false><<<nblk(V, 256), 256, 0, s>>>(x, dx, V, prev, vel, dt, write_vel);
+}
+
+void launch_project_gs(cudaStream_t s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
+                       int which, ResidualSink res, Flags* flags) {
+    const int n = end - begin;
+    if (n <= 0) return;
+    const int g = nblk(n, block);
+    const bool r = res.partial != nullptr;
+#define XG_GS(F, W, R) k_project_gs<F, W, R><<<g, block, 0, s>>>(t, begin, end, x, res, flags)
+    if (which == 2) {
+        if (first) { if (r) XG_GS(true, 2, true); else XG_GS(true, 2, false); }
+        else { if (r) XG_GS(false, 2, true); else XG_GS(false, 2, false); }
+    } else if (which == 0) {
+        if (first) { if (r) XG_GS(true, 0, true); else XG_GS(true, 0, false); }
+        else { if (r) XG_GS(false, 0, true); else XG_GS(false, 0, false); }
+    } else {
+        if (first) { if (r) XG_GS(true, 1, true); else XG_GS(true, 1, false); }
+        else { if (r) XG_GS(false, 1, true); else XG_GS(false, 1, false); }
+    }
+#undef XG_GS
+}
+
+void launch_contacts_jacobi(cudaStream_t s, const ContactArrays& c, const float4* x, float4* dx, bool first) {
+    const int n = c.S * c.F;
+    if (n <= 0) return;
+    if (first) k_contacts_jacobi<true><<<nblk(n, 256), 256, 0, s>>>(c, x, dx);
+    else k_contacts_jacobi<false><<<nblk(n, 256), 256, 0, s>>>(c, x, dx);
+}
+
+void launch_contacts_gs(cudaStream_t s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
+                        bool first) {
+    const int n = end - begin;
+    if (n <= 0) return;
+    if (first) k_contacts_gs<true><<<nblk(n, 128), 128, 0, s>>>(c, face_list, begin, end, x);
+    else k_contacts_gs<false><<<nblk(n, 128), 128, 0, s>>>(c, face_list, begin, end, x);
+}
+
+void launch_detect(cudaStream_t s, const ContactArrays& c, const float4* x, const SphereSet& spheres) {
+    const int n = c.S * c.F;
+    if (n <= 0) return;
+    k_detect<<<nblk(n, 128), 128, 0, s>>>(c, x, spheres);
+}
+
+void launch_finalize(cudaStream_t s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel) {
+    if (V > 0) k_finalize<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt, write_vel);
+}
+
+void launch_velocity(cudaStream_t s, const float4* x, const float4* prev, float4* vel, int V, float dt) {
+    if (V > 0) k_velocity<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt);
+}
+
+void launch_residual(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, bool separate,
+                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2) {
+    if (T <= 0) return;
+    k_residual<<<nblk(T, block), block, 0, s>>>(t, T, x, separate, perm, rvec, res, energy_partial, dt2);
+}
+
+void launch_reduce_rows(cudaStream_t s, const double* partial, int rows, int stride, double* out) {
+    if (rows > 0) k_reduce_rows<<<rows, 256, 0, s>>>(partial, stride, out);
+}
+
+}  // namespace xg

@@ -1,0 +1,100 @@
+// Device data layout and kernel launchers of the GB300 XPBD solver.
+//
+// HBM layout (all arrays 16-byte aligned, structure-of-arrays):
+//   x      float4[V]  position xyz, w = inverse mass; w < 0 marks a fixed vertex
+//   prev   float4[V]  position at the start of the substep (w copied from x)
+//   vel    float4[V]  velocity xyz
+//   dx     float4[V]  Jacobi accumulator (zero between sweeps)
+//   tet_idx int4[T]   vertex indices, in solver slot order
+//   tet_q0  float4[T] Q(0,0) Q(1,0) Q(2,0) Q(0,1)      (Q = Dm^-1, column-major)
+//   tet_q1  float4[T] Q(1,1) Q(2,1) Q(0,2) Q(1,2)
+//   tet_q2  float4[T] Q(2,2) alpha_tilde_dev alpha_tilde_hyd gamma
+//   lam     float2[T] (lambda_dev, lambda_hyd)
+// One tet costs 16 + 48 + 8 (+8 write) = 80 bytes of streamed data per sweep.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace xg {
+
+// kernel ids for per-kernel profiling
+enum KernelId {
+    K_PREDICT = 0,
+    K_PROJECT_JACOBI,
+    K_APPLY,
+    K_PROJECT_GS,
+    K_CONTACT,
+    K_DETECT,
+    K_FINALIZE,
+    K_RESIDUAL,
+    K_REDUCE,
+    K_KINEMATIC,
+    K_GATHER,
+    K_VELOCITY,
+    K_COUNT
+};
+
+struct TetArrays {
+    const int4* idx;
+    const float4* q0;
+    const float4* q1;
+    const float4* q2;
+    float2* lam;
+};
+
+struct ContactArrays {
+    float4* bary;   // u, v, w, active (1/0)           [S*F]
+    float4* p;      // surface point                    [S*F]
+    float4* n;      // normal                           [S*F]
+    float* lam;     //                                  [S*F]
+    const int4* faces;  // face vertex indices (w unused) [F]
+    int F;
+    int S;
+};
+
+constexpr int kMaxSpheres = 16;
+struct SphereSet {
+    float4 s[kMaxSpheres];  // centre xyz, radius
+    int n;
+};
+
+struct Flags {
+    unsigned long long nonfinite;
+    unsigned long long degenerate;
+};
+
+// residual partial sums: one double per block per record row
+struct ResidualSink {
+    double* partial;  // nullptr = off
+    int row;          // record row (iteration)
+    int stride;       // doubles per row
+    int offset;       // first slot of this launch in the row
+};
+
+// ---- launchers (all asynchronous on `s`) ----
+void launch_predict(cudaStream_t s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz);
+void launch_kinematic(cudaStream_t s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
+                      float oz);
+void launch_project_jacobi(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
+                           bool first, bool separate, ResidualSink res, Flags* flags);
+void launch_project_jacobi_gather_write(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x,
+                                        float4* dxt, bool first, bool separate, ResidualSink res, Flags* flags);
+void launch_gather_apply(cudaStream_t s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
+                         float4* dx, int V, float4* prev, float4* vel, bool final_step, float dt, bool write_vel);
+void launch_apply(cudaStream_t s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
+                  float dt, bool write_vel);
+void launch_project_gs(cudaStream_t s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
+                       int which, ResidualSink res, Flags* flags);
+void launch_contacts_jacobi(cudaStream_t s, const ContactArrays& c, const float4* x, float4* dx, bool first);
+void launch_contacts_gs(cudaStream_t s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
+                        bool first);
+void launch_detect(cudaStream_t s, const ContactArrays& c, const float4* x, const SphereSet& spheres);
+void launch_finalize(cudaStream_t s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);
+void launch_velocity(cudaStream_t s, const float4* x, const float4* prev, float4* vel, int V, float dt);
+void launch_residual(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, bool separate,
+                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2);
+void launch_reduce_rows(cudaStream_t s, const double* partial, int rows, int stride, double* out);
+int residual_blocks(int T, int block);
+
+}  // namespace xg

@@ -1,0 +1,383 @@
+"""Python binding of libxpbd_gpu.so (include/xpbd_gpu.h) through ctypes.
+
+The product path is the CUDA library: there is no CPU fallback. Loading fails
+loudly when the shared library is missing, and XPBDSolver raises when the C ABI
+returns an error status.
+
+Object model mirrors the reference's XPBDMeshObject_ + XPBDSolver surface:
+  update()              XPBDMeshObject_::update        (src/simobject/XPBDMeshObject.cpp:426-505)
+  velocity_update()     XPBDMeshObject_::velocityUpdate (XPBDMeshObject.cpp:507-535)
+  step(n)               Simulation::_timeStep           (src/simulation/Simulation.cpp:197-276)
+  fix_vertices(mask)    XPBDMeshObject_Base_::fixVertex (include/simobject/XPBDMeshObjectBase.hpp:97-99)
+  constraint_residual() XPBDSolver::constraintResidual  (include/solver/xpbd_solver/XPBDSolver.hpp:135)
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+LIB_PATH = os.path.join(HERE, "_build", "libxpbd_gpu.so")
+HEADER = os.path.join(ROOT, "include", "xpbd_gpu.h")
+
+XPBD_OK, XPBD_ERR_INVALID, XPBD_ERR_CUDA, XPBD_ERR_NUMERIC, XPBD_ERR_NO_DEVICE, XPBD_ERR_STATE, XPBD_ERR_CAPACITY = range(7)
+SOLVER_GAUSS_SEIDEL, SOLVER_JACOBI = 0, 1
+CONSTRAINT_COMBINED, CONSTRAINT_SEPARATE = 0, 1
+RESIDUAL_NEVER, RESIDUAL_EVERY_SUBSTEP, RESIDUAL_EVERY_ITERATION = 0, 1, 2
+JACOBI_ATOMIC, JACOBI_GATHER = 0, 1
+
+# YAML `solver-type` strings (include/config/simobject/XPBDMeshObjectConfig.hpp:26-34)
+# plus the GPU names; "Parallel-Jacobi" aliases the GPU Jacobi solver.
+SOLVER_TYPES = {
+    "Gauss-Seidel": SOLVER_GAUSS_SEIDEL,
+    "GPU-Gauss-Seidel": SOLVER_GAUSS_SEIDEL,
+    "Jacobi": SOLVER_JACOBI,
+    "GPU-Jacobi": SOLVER_JACOBI,
+    "Parallel-Jacobi": SOLVER_JACOBI,
+}
+CONSTRAINT_TYPES = {"Stable-Neohookean-Combined": CONSTRAINT_COMBINED, "Stable-Neohookean": CONSTRAINT_SEPARATE}
+RESIDUAL_POLICIES = {"Never": RESIDUAL_NEVER, "Every-Substep": RESIDUAL_EVERY_SUBSTEP,
+                     "Every-Iteration": RESIDUAL_EVERY_ITERATION}
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_int64), ("num_tets", C.c_int64), ("num_faces", C.c_int64),
+        ("vertices", C.c_void_p), ("tets", C.c_void_p), ("faces", C.c_void_p),
+        ("tet_E", C.c_void_p), ("tet_nu", C.c_void_p), ("tet_density", C.c_void_p),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("g_accel", C.c_double), ("collision_rate", C.c_double),
+        ("num_iters", C.c_int32), ("solver_type", C.c_int32), ("constraint_type", C.c_int32),
+        ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
+        ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32),
+    ]
+
+
+class XPBDError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"xpbd status {status}: {msg}")
+        self.status = status
+
+
+_lib = None
+
+
+def header_functions() -> list[str]:
+    """Names of the entry points include/xpbd_gpu.h declares."""
+    import re
+    text = open(HEADER).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return re.findall(r"\b(xpbd_[a-z0-9_]+)\s*\(", text)
+
+
+def load(path: str | None = None):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise RuntimeError(f"libxpbd_gpu.so not found at {path}: run __graft_entry__.build() "
+                           f"(the solver has no CPU fallback)")
+    L = C.CDLL(path)
+    P, I32, I64, D = C.c_void_p, C.c_int32, C.c_int64, C.c_double
+    sig = {
+        "xpbd_abi_version": ([], C.c_int),
+        "xpbd_status_string": ([C.c_int], C.c_char_p),
+        "xpbd_default_params": ([P], C.c_int),
+        "xpbd_colour_items": ([I64, I32, P, I64, P], C.c_int),
+        "xpbd_grid_counts": ([I32, I32, I32, P, P, P], C.c_int),
+        "xpbd_grid_mesh": ([I32, I32, I32, D, D, D, I32, P, P, P], C.c_int),
+        "xpbd_create": ([P, P, P], C.c_int),
+        "xpbd_destroy": ([P], C.c_int),
+        "xpbd_last_error": ([P], C.c_char_p),
+        "xpbd_set_num_iters": ([P, I32], C.c_int),
+        "xpbd_set_positions": ([P, P], C.c_int),
+        "xpbd_get_positions": ([P, P], C.c_int),
+        "xpbd_get_prev_positions": ([P, P], C.c_int),
+        "xpbd_set_velocities": ([P, P], C.c_int),
+        "xpbd_get_velocities": ([P, P], C.c_int),
+        "xpbd_set_positions_f32": ([P, P], C.c_int),
+        "xpbd_get_positions_f32": ([P, P], C.c_int),
+        "xpbd_get_masses": ([P, P], C.c_int),
+        "xpbd_set_fixed": ([P, P], C.c_int),
+        "xpbd_set_kinematic_group": ([P, I32, P], C.c_int),
+        "xpbd_set_kinematic_offset": ([P, P], C.c_int),
+        "xpbd_set_spheres": ([P, I32, P, P], C.c_int),
+        "xpbd_clear_collisions": ([P], C.c_int),
+        "xpbd_detect_collisions": ([P], C.c_int),
+        "xpbd_add_static_collision": ([P, I32, D, D, D, P, P], C.c_int),
+        "xpbd_get_collisions": ([P, I32, P, P], C.c_int),
+        "xpbd_update": ([P], C.c_int),
+        "xpbd_velocity_update": ([P], C.c_int),
+        "xpbd_step": ([P, I32], C.c_int),
+        "xpbd_synchronize": ([P], C.c_int),
+        "xpbd_get_time": ([P, P], C.c_int),
+        "xpbd_residual": ([P, P, P], C.c_int),
+        "xpbd_get_constraint_residual": ([P, P, I64], C.c_int),
+        "xpbd_residual_history": ([P, P, I32, P], C.c_int),
+        "xpbd_get_lambda": ([P, P], C.c_int),
+        "xpbd_total_strain_energy": ([P, P], C.c_int),
+        "xpbd_health": ([P, P, P], C.c_int),
+        "xpbd_num_colours": ([P, P, P], C.c_int),
+        "xpbd_get_tet_colours": ([P, P], C.c_int),
+        "xpbd_profile_steps": ([P, I32, I32, P, P], C.c_int),
+        "xpbd_kernel_name": ([I32], C.c_char_p),
+        "xpbd_launch_count": ([P, P], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load().xpbd_default_params(C.byref(p))
+    for k, v in kw.items():
+        if k == "solver_type" and isinstance(v, str):
+            v = SOLVER_TYPES[v]
+        if k == "constraint_type" and isinstance(v, str):
+            v = CONSTRAINT_TYPES[v]
+        if k == "residual_policy" and isinstance(v, str):
+            v = RESIDUAL_POLICIES[v]
+        setattr(p, k, v)
+    return p
+
+
+def colour_items(items: np.ndarray, n_vertices: int):
+    items = np.ascontiguousarray(items, np.int32)
+    out = np.zeros(items.shape[0], np.int32)
+    n = load().xpbd_colour_items(items.shape[0], items.shape[1], _p(items), n_vertices, _p(out))
+    if n < 0:
+        raise XPBDError(-n, "bad colouring input")
+    return n, out
+
+
+def grid_mesh(nx: int, ny: int, nz: int, hx: float, hy: float | None = None, hz: float | None = None,
+              split: int = 0):
+    """Hex grid with five tets per hex (createBeamMsh layout). Returns X (V,3),
+    tets (T,4) int32, faces (F,3) int32."""
+    hy = hx if hy is None else hy
+    hz = hx if hz is None else hz
+    L = load()
+    nv, nt, nf = C.c_int64(), C.c_int64(), C.c_int64()
+    st = L.xpbd_grid_counts(nx, ny, nz, C.byref(nv), C.byref(nt), C.byref(nf))
+    if st != XPBD_OK:
+        raise XPBDError(st, "bad grid size")
+    X = np.zeros((nv.value, 3))
+    tets = np.zeros((nt.value, 4), np.int32)
+    faces = np.zeros((nf.value, 3), np.int32)
+    st = L.xpbd_grid_mesh(nx, ny, nz, hx, hy, hz, split, _p(X), _p(tets), _p(faces))
+    if st != XPBD_OK:
+        raise XPBDError(st, "grid generation failed")
+    return X, tets, faces
+
+
+class XPBDSolver:
+    """One deformable tet-mesh object solved on the GPU."""
+
+    def __init__(self, X, tets, faces=None, E=3e3, nu=0.45, density=1000.0, **params):
+        self.L = load()
+        self.X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
+        self.tets = np.ascontiguousarray(tets, np.int32).reshape(-1, 4)
+        self.faces = None if faces is None else np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
+        self.V, self.T = self.X.shape[0], self.tets.shape[0]
+        self.F = 0 if self.faces is None else self.faces.shape[0]
+        bc = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64), (self.T,)))
+        self._E, self._nu, self._rho = bc(E), bc(nu), bc(density)
+        self.params = default_params(**params)
+        desc = MeshDesc(self.V, self.T, self.F, _p(self.X).value, _p(self.tets).value,
+                        None if self.faces is None else _p(self.faces).value,
+                        _p(self._E).value, _p(self._nu).value, _p(self._rho).value)
+        h = C.c_void_p()
+        st = self.L.xpbd_create(C.byref(desc), C.byref(self.params), C.byref(h))
+        if st != XPBD_OK:
+            raise XPBDError(st, self.L.xpbd_status_string(st).decode())
+        self.h = h
+
+    # ---- lifetime ----
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.xpbd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _ck(self, st):
+        if st != XPBD_OK:
+            raise XPBDError(st, self.L.xpbd_last_error(self.h).decode())
+
+    # ---- state ----
+    def positions(self) -> np.ndarray:
+        out = np.zeros((self.V, 3))
+        self._ck(self.L.xpbd_get_positions(self.h, _p(out)))
+        return out
+
+    def prev_positions(self) -> np.ndarray:
+        out = np.zeros((self.V, 3))
+        self._ck(self.L.xpbd_get_prev_positions(self.h, _p(out)))
+        return out
+
+    def set_positions(self, x):
+        x = np.ascontiguousarray(x, np.float64)
+        self._ck(self.L.xpbd_set_positions(self.h, _p(x)))
+
+    def velocities(self) -> np.ndarray:
+        out = np.zeros((self.V, 3))
+        self._ck(self.L.xpbd_get_velocities(self.h, _p(out)))
+        return out
+
+    def set_velocities(self, v):
+        v = np.ascontiguousarray(v, np.float64)
+        self._ck(self.L.xpbd_set_velocities(self.h, _p(v)))
+
+    def positions_f32(self, out=None) -> np.ndarray:
+        out = np.zeros((self.V, 3), np.float32) if out is None else out
+        self._ck(self.L.xpbd_get_positions_f32(self.h, _p(out)))
+        return out
+
+    def set_positions_f32(self, x):
+        self._ck(self.L.xpbd_set_positions_f32(self.h, _p(np.ascontiguousarray(x, np.float32))))
+
+    def masses(self) -> np.ndarray:
+        out = np.zeros(self.V)
+        self._ck(self.L.xpbd_get_masses(self.h, _p(out)))
+        return out
+
+    def fix_vertices(self, mask):
+        m = np.ascontiguousarray(mask, np.uint8)
+        self._ck(self.L.xpbd_set_fixed(self.h, _p(m)))
+
+    def set_kinematic_group(self, idx):
+        idx = np.ascontiguousarray(idx, np.int32)
+        self._ck(self.L.xpbd_set_kinematic_group(self.h, len(idx), _p(idx)))
+
+    def set_kinematic_offset(self, off):
+        self._ck(self.L.xpbd_set_kinematic_offset(self.h, _p(np.ascontiguousarray(off, np.float64))))
+
+    def set_num_iters(self, n):
+        self._ck(self.L.xpbd_set_num_iters(self.h, int(n)))
+
+    # ---- collisions ----
+    def set_spheres(self, centers, radii):
+        c = np.ascontiguousarray(centers, np.float64).reshape(-1, 3)
+        r = np.ascontiguousarray(radii, np.float64).reshape(-1)
+        self._ck(self.L.xpbd_set_spheres(self.h, len(r), _p(c), _p(r)))
+
+    def clear_collisions(self):
+        self._ck(self.L.xpbd_clear_collisions(self.h))
+
+    def detect_collisions(self):
+        self._ck(self.L.xpbd_detect_collisions(self.h))
+
+    def add_static_collision(self, face, u, v, w, p, n):
+        self._ck(self.L.xpbd_add_static_collision(self.h, int(face), u, v, w,
+                                                  _p(np.ascontiguousarray(p, np.float64)),
+                                                  _p(np.ascontiguousarray(n, np.float64))))
+
+    def collisions(self) -> np.ndarray:
+        n = C.c_int32()
+        self._ck(self.L.xpbd_get_collisions(self.h, 0, None, C.byref(n)))
+        out = np.zeros((n.value, 12))
+        if n.value:
+            self._ck(self.L.xpbd_get_collisions(self.h, n.value, _p(out), C.byref(n)))
+        return out
+
+    # ---- stepping ----
+    def update(self):
+        self._ck(self.L.xpbd_update(self.h))
+
+    def velocity_update(self):
+        self._ck(self.L.xpbd_velocity_update(self.h))
+
+    def step(self, n=1):
+        self._ck(self.L.xpbd_step(self.h, int(n)))
+
+    def synchronize(self):
+        self._ck(self.L.xpbd_synchronize(self.h))
+
+    @property
+    def time(self) -> float:
+        t = C.c_double()
+        self._ck(self.L.xpbd_get_time(self.h, C.byref(t)))
+        return t.value
+
+    # ---- queries ----
+    def residual(self):
+        a, r = C.c_double(), C.c_double()
+        self._ck(self.L.xpbd_residual(self.h, C.byref(a), C.byref(r)))
+        return a.value, r.value
+
+    def residual_history(self) -> np.ndarray:
+        n = C.c_int32()
+        buf = np.zeros(int(self.params.num_iters) + 2)
+        self._ck(self.L.xpbd_residual_history(self.h, _p(buf), len(buf), C.byref(n)))
+        return buf[: n.value].copy()
+
+    def constraint_residual(self) -> np.ndarray:
+        out = np.zeros(2 * self.T)
+        self._ck(self.L.xpbd_get_constraint_residual(self.h, _p(out), out.size))
+        return out
+
+    def lambdas(self) -> np.ndarray:
+        out = np.zeros((self.T, 2))
+        self._ck(self.L.xpbd_get_lambda(self.h, _p(out)))
+        return out
+
+    def strain_energy(self) -> float:
+        e = C.c_double()
+        self._ck(self.L.xpbd_total_strain_energy(self.h, C.byref(e)))
+        return e.value
+
+    def health(self):
+        a, b = C.c_int64(), C.c_int64()
+        self._ck(self.L.xpbd_health(self.h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    def colours(self):
+        nt, nf = C.c_int32(), C.c_int32()
+        self._ck(self.L.xpbd_num_colours(self.h, C.byref(nt), C.byref(nf)))
+        col = np.zeros(self.T, np.int32)
+        self._ck(self.L.xpbd_get_tet_colours(self.h, _p(col)))
+        return nt.value, nf.value, col
+
+    def gs_order(self) -> np.ndarray:
+        """Tets in the coloured Gauss-Seidel order (colour, then index)."""
+        _, _, col = self.colours()
+        return np.lexsort((np.arange(self.T), col)).astype(np.int32)
+
+    def profile_steps(self, n):
+        K = 16
+        ms = np.zeros(K)
+        cnt = np.zeros(K, np.int64)
+        self._ck(self.L.xpbd_profile_steps(self.h, int(n), K, _p(ms), _p(cnt)))
+        return {self.L.xpbd_kernel_name(k).decode(): (ms[k], int(cnt[k])) for k in range(K) if cnt[k]}
+
+    def launch_count(self) -> int:
+        n = C.c_int64()
+        self._ck(self.L.xpbd_launch_count(self.h, C.byref(n)))
+        return n.value
