@@ -1,0 +1,394 @@
+"""Benchmark of the GB300 XPBD substep (one JSON line on rank 0).
+
+Workload (default `block`): the 1,310,720-tet block (64^3 hexes x 5 tets,
+274,625 vertices, 0.1 m, per-tet E log-uniform in [1e3, 1e5] Pa, nu 0.45,
+bottom fixed, top face raised 1 cm over 100 steps), graph-coloured
+Gauss-Seidel, 30 iterations per substep, FP32 on the device. A step is one
+substep (Simulation::_timeStep). `beam` (50,000 tets, GPU Jacobi, 20
+iterations, sphere collisions) and `cube` (5,000 tets, 10 iterations) are
+selectable with --workload.
+
+value      substeps/s, device-timed with CUDA events on the solver's stream,
+           inputs resident in HBM, L2 flushed between steps outside the events
+e2e        the same metric through the C ABI with host buffers: per step
+           xpbd_set_positions (H2D), xpbd_step, xpbd_get_positions (D2H)
+roofline   the dominant kernel's algorithmic bytes / its event-timed average
+           launch duration, against MEASURED_PEAKS.json hbm_gbs
+cpu_baseline  the FP64 oracle (the reference's sequential Gauss-Seidel or
+           Jacobi order, 1 thread) on a bounded sample of the same workload
+
+--impl reference times that CPU implementation alone (rank 0) and prints the
+same line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path[:0] = [os.path.join(ROOT, "xpbd-tissue-sim_gb300"), os.path.join(ROOT, "oracle")]
+
+METRIC = "substeps/sec & tet-projections/sec at 1e-3 rel. residual: plain vs batched+learned"
+UNIT = "substeps/s"
+
+
+def env_int(name, default):
+    try:
+        return int(os.environ.get(name, default))
+    except ValueError:
+        return default
+
+
+def workload(name):
+    import workloads as W
+    if name == "block":
+        return W.block()
+    if name == "beam":
+        return W.beam()
+    if name == "cube":
+        return W.cube()
+    raise SystemExit(f"unknown workload {name}")
+
+
+def describe(w):
+    import xpbd_gb300 as G
+    solver = "coloured Gauss-Seidel" if w.solver == G.SOLVER_GAUSS_SEIDEL else "Jacobi (vector atomics)"
+    d = {
+        "workload": f"{w.name}: {w.T:,} tets, {w.V:,} vertices",
+        "solver": solver,
+        "iterations": w.iters,
+        "dt": w.dt,
+        "global_batch": 1,
+        "parallelism": "replicas",
+        "l2": "flushed (256 MiB write) between timed steps, outside the per-step events",
+    }
+    if w.name == "block":
+        d["workload"] += ", 0.1 m cube of 64^3 hexes x 5 tets, per-tet E log-uniform [1e3,1e5] Pa, nu 0.45, " \
+                         "bottom fixed, top face +1 cm over 100 steps"
+    if w.name == "beam":
+        d["workload"] += ", 0.5x0.05x0.05 m, 100x10x10 hexes, E 1e4, nu 0.49, y-min clamped, sphere r 0.03 m " \
+                         "descending 0.05 m/s, collision-rate 100 Hz"
+    return d
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle sampling during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active," \
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown," \
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.lines = []
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(gpu_index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(kernel, workload_name):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(f"{workload_name}/{kernel}")
+    return None if e is None else e.get("dram_bytes_per_launch")
+
+
+def algorithmic_bytes(w, kernel):
+    """Algorithmic bytes per launch: per sweep 80 B/tet (16 B indices, 48 B
+    Dm^-1 + compliances, 8 B lambda read, 8 B written) plus 28 B/vertex
+    (12 B read, 12 B written, 4 B inverse mass), apportioned to launches."""
+    import xpbd_gb300 as G
+    b_sweep = 80.0 * w.T + 28.0 * w.V
+    if kernel == "project_gs":
+        return b_sweep  # divided by the number of colour launches by the caller
+    if kernel == "project_jacobi":
+        return 80.0 * w.T
+    return None
+
+
+def cpu_sample(w, target_s=15.0, threads_note="1 thread"):
+    """FP64 oracle on the full mesh, the reference's own order: sequential
+    Gauss-Seidel (element order) for Gauss-Seidel workloads, Jacobi otherwise.
+    Times a step with k of the configured iterations and a step with none, and
+    scales to the configured count. Returns (substeps/s, sample text)."""
+    import numpy as np
+
+    import oracle as O
+    import xpbd_gb300 as G
+    solver = O.GAUSS_SEIDEL if w.solver == G.SOLVER_GAUSS_SEIDEL else O.JACOBI
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, dt=w.dt, g=w.g, num_iter=0, solver=solver)
+    o.set_positions(w.x0)
+    o.set_fixed(w.fixed)
+    if w.kin_idx is not None:
+        o.set_kinematic_group(w.kin_idx)
+    o.set_num_iter(0)
+    t0 = o.time_steps(2) / 2
+    # pick k so the sample lasts about target_s
+    o.set_num_iter(1)
+    t1 = o.time_steps(1)
+    per_iter = max(t1 - t0, 1e-9)
+    k = int(max(1, min(w.iters, (target_s / 2 - t0) / per_iter)))
+    o.set_num_iter(k)
+    tk = o.time_steps(2) / 2
+    per_iter = max((tk - t0) / k, 1e-12)
+    t_full = t0 + w.iters * per_iter
+    order = "sequential Gauss-Seidel (element order)" if solver == O.GAUSS_SEIDEL else "Jacobi (plain sum)"
+    sample = (f"FP64 oracle port, {order}, {threads_note}; full {w.T:,}-tet mesh; 2 steps with {k} of "
+              f"{w.iters} iterations and 2 with none, scaled to {w.iters} iterations "
+              f"({t_full * 1e3:.0f} ms per substep)")
+    o.close()
+    return 1.0 / t_full, sample, t_full
+
+
+def run_reference(args):
+    """The reference's CPU algorithm (FP64 oracle port, reference order, 1
+    thread): W warm-up and K timed steps on the full mesh. Each step runs k of
+    the configured iterations (k chosen so the run stays within ~2 minutes) and
+    its time is scaled to the full count with the per-iteration cost measured
+    against zero-iteration steps."""
+    rank = env_int("RANK", 0)
+    if rank != 0:
+        return 0
+    import oracle as O
+    import xpbd_gb300 as G
+    w = workload(args.workload)
+    solver = O.GAUSS_SEIDEL if w.solver == G.SOLVER_GAUSS_SEIDEL else O.JACOBI
+    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, dt=w.dt, g=w.g, num_iter=0, solver=solver)
+    o.set_positions(w.x0)
+    o.set_fixed(w.fixed)
+    if w.kin_idx is not None:
+        o.set_kinematic_group(w.kin_idx)
+    t0 = o.time_steps(2) / 2
+    o.set_num_iter(1)
+    c1 = max(o.time_steps(1) - t0, 1e-9)
+    budget = 120.0 / (args.steps + args.warmup)
+    k = int(max(1, min(w.iters, (budget - t0) / c1)))
+    o.set_num_iter(k)
+    for _ in range(args.warmup):
+        o.time_steps(1)
+    times = [o.time_steps(1) for _ in range(args.steps)]
+    per_iter = max((statistics.mean(times) - t0) / k, 1e-12)
+    t_full = t0 + w.iters * per_iter
+    sub = 1.0 / t_full
+    order = "sequential Gauss-Seidel (element order)" if solver == O.GAUSS_SEIDEL else "Jacobi (plain sum)"
+    sample = (f"FP64 oracle port, {order}, 1 thread (the reference solver is single-threaded); full "
+              f"{w.T:,}-tet mesh; each step runs {k} of {w.iters} iterations, scaled to {w.iters}")
+    line = {
+        "metric": METRIC, "value": sub, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_full * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": describe(w), "impl": "reference",
+        "tet_projections_per_s": sub * w.iters * w.T,
+        "cpu_baseline": {"value": sub, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
+        "e2e": {"value": sub, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    o.close()
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import workloads as W
+    import xpbd_gb300 as G
+
+    rank, world, local = env_int("RANK", 0), env_int("WORLD_SIZE", 1), env_int("LOCAL_RANK", 0)
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    w = workload(args.workload)
+    s = W.make_solver(w)
+    step_no = 0
+
+    def one_step():
+        nonlocal step_no
+        step_no += 1
+        W.drive_gpu(s, w, step_no)
+        s.step(1)
+
+    for _ in range(args.warmup):
+        one_step()
+    s.synchronize()
+
+    stream = torch.cuda.ExternalStream(s.stream_handle())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    clocks = ClockSampler(local)
+    time.sleep(0.4)
+    launches0 = s.launch_count()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()  # evict the working set (L2 is 129 MB)
+        evs[k][0].record(stream)
+        one_step()
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    launches = s.launch_count() - launches0
+    ms = sum(a.elapsed_time(b) for a, b in evs)
+    s.synchronize()
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    substeps = world * 1e3 / ms_step
+    if args.quick:
+        # timed region only (used for profiler runs)
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": substeps, "unit": UNIT, "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+                              "gpu_launches": int(launches), "config": describe(w), "quick": True}), flush=True)
+        s.close()
+        if dist:
+            dist.destroy_process_group()
+        return 0
+
+    # ---- end to end through the C ABI with host buffers ----
+    x_host = s.positions()
+    s.synchronize()
+    e2e_steps = max(3, min(args.steps, 20))
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        s.set_positions(x_host)           # H2D of the step's input state
+        one_step()
+        x_host = s.positions()            # D2H of the step's result (synchronises)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d = d2h = 16 * w.V
+
+    # ---- kernel roofline: event-timed launches over the same workload ----
+    prof = s.profile_steps(3)
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0] * kv[1][1])[0]
+    ms_launch, nl = prof[dom]
+    nl_step = nl / 3
+    sweep_bytes = algorithmic_bytes(w, dom)
+    roofline = None
+    if sweep_bytes is not None:
+        per_launch = sweep_bytes / (nl_step / w.iters) if dom == "project_gs" else sweep_bytes
+        achieved = per_launch / (ms_launch * 1e-3) / 1e9
+        traffic = profiled_traffic(dom, w.name)
+        roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                    "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
+                    "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": ms_launch,
+                    "launches_per_step": nl_step, "traffic": traffic}
+    kernel_share = {k: v[0] * v[1] / 3 for k, v in prof.items()}
+
+    # ---- convergence at the configured iteration count ----
+    sr = W.make_solver(w, residual_policy=G.RESIDUAL_EVERY_ITERATION)
+    for k in range(3):
+        W.drive_gpu(sr, w, k + 1)
+        sr.step(1)
+    hist = sr.residual_history()
+    rel = hist / hist[0]
+    below = np.nonzero(rel <= 1e-3)[0]
+    sr.close()
+
+    line = {
+        "metric": METRIC, "value": substeps, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": describe(w),
+        "tet_projections_per_s": substeps * w.iters * w.T,
+        "rel_residual_after_iters": float(rel[-1]),
+        "iters_to_1e-3": int(below[0]) if len(below) else None,
+        "e2e": {"value": world / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(launches),
+        "roofline": roofline,
+        "kernel_ms_per_step": kernel_share,
+        "clocks": clk,
+    }
+    if rank == 0 and not args.no_cpu:
+        sub, sample, _ = cpu_sample(w)
+        line["cpu_baseline"] = {"value": sub, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    s.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="block", choices=["block", "beam", "cube"])
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--quick", action="store_true", help="timed steps only (no e2e/roofline/CPU legs)")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

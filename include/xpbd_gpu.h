@@ -89,6 +89,7 @@ typedef struct {
     int32_t block_size;        /* threads per block for tet kernels; 0 = default   */
     int32_t max_contacts_per_face; /* contact slots per surface face; 0 = 4        */
     int32_t use_graphs;        /* capture each substep in a CUDA graph (1) or not  */
+    int32_t use_pdl;           /* programmatic dependent launch between kernels    */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -210,6 +211,9 @@ int xpbd_profile_steps(xpbd_ctx* ctx, int32_t nsteps, int32_t max_k, double* avg
 const char* xpbd_kernel_name(int32_t id);
 /* number of kernel launches issued by the library since creation */
 int xpbd_launch_count(xpbd_ctx* ctx, int64_t* n);
+/* the context's CUDA stream (a cudaStream_t), for callers that time or order
+ * their own work against the solver's */
+int xpbd_get_stream(xpbd_ctx* ctx, void** stream);
 
 #ifdef __cplusplus
 }

@@ -122,12 +122,15 @@ void xo_set_spheres(void* p, int n, const double* c, const double* r) {
     });
 }
 
+// kinematic vertices are fixed vertices driven to rest + offset
 void xo_set_kinematic_group(void* p, int n, const int* idx) {
     with((Handle*)p, [&](auto& o) {
         o.kin_idx.assign(idx, idx + n);
         o.kin_rest.assign(3 * n, 0);
-        for (int j = 0; j < n; j++)
+        for (int j = 0; j < n; j++) {
+            o.fixed[idx[j]] = 1;
             for (int k = 0; k < 3; k++) o.kin_rest[3 * j + k] = o.x[3 * idx[j] + k];
+        }
         return 0;
     });
 }

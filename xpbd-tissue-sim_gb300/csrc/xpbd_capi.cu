@@ -111,6 +111,7 @@ struct xpbd_ctx {
     TetArrays tets() {
         return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
     }
+    Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
     ContactArrays contacts() {
         return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
     }
@@ -178,7 +179,8 @@ bool valid_params(const xpbd_params& p) {
            p.residual_policy >= XPBD_RESIDUAL_NEVER && p.residual_policy <= XPBD_RESIDUAL_EVERY_ITERATION &&
            (p.jacobi_variant == XPBD_JACOBI_ATOMIC || p.jacobi_variant == XPBD_JACOBI_GATHER) &&
            (p.block_size == 0 || (p.block_size >= 32 && p.block_size <= 256 && p.block_size % 32 == 0)) &&
-           p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres;
+           p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres &&
+           (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1);
 }
 
 // greedy vertex-disjoint colouring in item order (smallest free colour)
@@ -243,7 +245,7 @@ int ensure_residual_rows(xpbd_ctx* c, int rows) {
 
 void exact_residual_row(xpbd_ctx* c, int row, bool with_vec) {
     Scope s(c, K_RESIDUAL);
-    launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
+    launch_residual(c->L(), c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
                     c->perm.p, with_vec ? c->rvec.p : nullptr, sink(c, row, 0), nullptr,
                     (float)(c->prm.dt * c->prm.dt));
 }
@@ -262,7 +264,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     const bool have_faces = c->F > 0;
     {
         Scope sc(c, K_PREDICT);
-        launch_predict(s, c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
+        launch_predict(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
     }
     if (track) {
         // lambda <- 0 (XPBDSolver.hpp:71-77) before the r(x_pred, 0) evaluation
@@ -281,28 +283,28 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
             if (gather) {
                 {
                     Scope sc(c, K_PROJECT_JACOBI);
-                    launch_project_jacobi_gather_write(s, c->block, c->tets(), c->T, c->x.p, c->dxt.p, first,
+                    launch_project_jacobi_gather_write(c->L(), c->block, c->tets(), c->T, c->x.p, c->dxt.p, first,
                                                        separate, rs, c->flags.p);
                 }
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
-                    launch_contacts_jacobi(s, ca, c->x.p, c->dx.p, first);
+                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first);
                 }
                 Scope sc(c, K_GATHER);
-                launch_gather_apply(s, c->x.p, c->dxt.p, c->csr_off.p, c->csr_ent.p, c->dx.p, c->V, c->prev.p,
+                launch_gather_apply(c->L(), c->x.p, c->dxt.p, c->csr_off.p, c->csr_ent.p, c->dx.p, c->V, c->prev.p,
                                     c->vel.p, last && fuse_final, dt, write_vel);
             } else {
                 {
                     Scope sc(c, K_PROJECT_JACOBI);
-                    launch_project_jacobi(s, c->block, c->tets(), c->T, c->x.p, c->dx.p, first, separate, rs,
+                    launch_project_jacobi(c->L(), c->block, c->tets(), c->T, c->x.p, c->dx.p, first, separate, rs,
                                           c->flags.p);
                 }
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
-                    launch_contacts_jacobi(s, ca, c->x.p, c->dx.p, first);
+                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first);
                 }
                 Scope sc(c, K_APPLY);
-                launch_apply(s, c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
+                launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
     } else {
@@ -318,14 +320,14 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 const bool f = first && (!separate || pass == 0);
                 for (int col = 0; col < c->n_tet_colours; col++) {
                     Scope sc(c, K_PROJECT_GS);
-                    launch_project_gs(s, c->block, c->tets(), c->col_off[col], c->col_off[col + 1], c->x.p, f,
+                    launch_project_gs(c->L(), c->block, c->tets(), c->col_off[col], c->col_off[col + 1], c->x.p, f,
                                       which, no_sink(), c->flags.p);
                 }
             }
             if (have_faces) {
                 for (int fc = 0; fc < c->n_face_colours; fc++) {
                     Scope sc(c, K_CONTACT);
-                    launch_contacts_gs(s, ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
+                    launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
                 }
             }
         }
@@ -334,13 +336,13 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         exact_residual_row(c, iters, true);
         {
             Scope sc(c, K_REDUCE);
-            launch_reduce_rows(s, c->res_partial.p, iters + 1, c->res_stride, c->res_rows.p);
+            launch_reduce_rows(c->L(), c->res_partial.p, iters + 1, c->res_stride, c->res_rows.p);
         }
         cudaMemcpyAsync(c->h_rows, c->res_rows.p, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, s);
     }
     if (!jacobi || !fuse_final || iters == 0) {
         Scope sc(c, K_FINALIZE);
-        launch_finalize(s, c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
+        launch_finalize(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
     }
     return XPBD_OK;
 }
@@ -401,7 +403,7 @@ int detect(xpbd_ctx* c) {
     if (c->F == 0) return XPBD_OK;
     {
         Scope sc(c, K_DETECT);
-        launch_detect(c->stream, c->contacts(), c->x.p, c->spheres);
+        launch_detect(c->L(), c->contacts(), c->x.p, c->spheres);
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
     return after_launches(c, "detect");
@@ -649,6 +651,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->block_size = 0;
     p->max_contacts_per_face = 0;
     p->use_graphs = 1;
+    p->use_pdl = 1;
     return XPBD_OK;
 }
 
@@ -820,7 +823,7 @@ int xpbd_set_kinematic_offset(xpbd_ctx* c, const double* off) {
     if (c->nkin == 0) return XPBD_OK;
     {
         Scope sc(c, K_KINEMATIC);
-        launch_kinematic(c->stream, c->x.p, c->kin_idx.p, c->kin_rest.p, c->nkin, (float)off[0], (float)off[1],
+        launch_kinematic(c->L(), c->x.p, c->kin_idx.p, c->kin_rest.p, c->nkin, (float)off[0], (float)off[1],
                          (float)off[2]);
     }
     return after_launches(c, "kinematic offset");
@@ -921,7 +924,7 @@ int xpbd_velocity_update(xpbd_ctx* c) {
     if (!c) return XPBD_ERR_INVALID;
     {
         Scope sc(c, K_VELOCITY);
-        launch_velocity(c->stream, c->x.p, c->prev.p, c->vel.p, c->V, (float)c->prm.dt);
+        launch_velocity(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, (float)c->prm.dt);
     }
     return after_launches(c, "velocity update");
 }
@@ -989,7 +992,7 @@ int xpbd_residual(xpbd_ctx* c, double* abs_norm, double* rel) {
     XPBD_CU(c, cudaMemsetAsync(c->res_partial.p + (size_t)row * c->res_stride, 0, sizeof(double) * c->res_stride,
                                c->stream));
     exact_residual_row(c, row, false);
-    launch_reduce_rows(c->stream, c->res_partial.p + (size_t)row * c->res_stride, 1, c->res_stride,
+    launch_reduce_rows(c->L(), c->res_partial.p + (size_t)row * c->res_stride, 1, c->res_stride,
                        c->res_rows.p + row);
     double v = 0;
     XPBD_CU(c, cudaMemcpyAsync(&v, c->res_rows.p + row, sizeof v, cudaMemcpyDeviceToHost, c->stream));
@@ -1009,7 +1012,7 @@ int xpbd_get_constraint_residual(xpbd_ctx* c, double* r, int64_t n) {
     if (!c || !r || n < 2LL * c->T) return XPBD_ERR_INVALID;
     if (!c->have_rvec) {
         // no stored residual: evaluate at the current state
-        launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p,
+        launch_residual(c->L(), c->block, c->tets(), c->T, c->x.p,
                         c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE, c->perm.p, c->rvec.p, no_sink(), nullptr,
                         (float)(c->prm.dt * c->prm.dt));
     }
@@ -1036,9 +1039,9 @@ int xpbd_get_lambda(xpbd_ctx* c, double* lam) {
 int xpbd_total_strain_energy(xpbd_ctx* c, double* e) {
     if (!c || !e) return XPBD_ERR_INVALID;
     const int nb = residual_blocks(c->T, c->block);
-    launch_residual(c->stream, c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
+    launch_residual(c->L(), c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
                     c->perm.p, nullptr, no_sink(), c->energy_partial.p, (float)(c->prm.dt * c->prm.dt));
-    launch_reduce_rows(c->stream, c->energy_partial.p, 1, nb, c->energy_partial.p + nb);
+    launch_reduce_rows(c->L(), c->energy_partial.p, 1, nb, c->energy_partial.p + nb);
     double v = 0;
     XPBD_CU(c, cudaMemcpyAsync(&v, c->energy_partial.p + nb, sizeof v, cudaMemcpyDeviceToHost, c->stream));
     XPBD_CU(c, cudaStreamSynchronize(c->stream));
@@ -1104,6 +1107,12 @@ int xpbd_profile_steps(xpbd_ctx* c, int32_t nsteps, int32_t max_k, double* avg_m
 int xpbd_launch_count(xpbd_ctx* c, int64_t* n) {
     if (!c || !n) return XPBD_ERR_INVALID;
     *n = c->launches;
+    return XPBD_OK;
+}
+
+int xpbd_get_stream(xpbd_ctx* c, void** stream) {
+    if (!c || !stream) return XPBD_ERR_INVALID;
+    *stream = (void*)c->stream;
     return XPBD_OK;
 }
 

@@ -16,6 +16,8 @@
 // Every kernel is memory-bound; see the HBM layout in xpbd_kernels.cuh.
 #include <cuda_runtime.h>
 
+#include <utility>
+
 #include "xpbd_kernels.cuh"
 
 namespace xg {
@@ -23,6 +25,17 @@ namespace xg {
 namespace {
 
 constexpr float kDegenerateJ = 1e-3f;  // |det F| below this takes the FP64 path
+
+// Programmatic dependent launch: a kernel may start while its predecessor on
+// the stream still runs; it must wait before touching anything the
+// predecessor writes. Dependents are released only after this kernel's own
+// wait, so a pre-wait prologue overlaps at most the direct predecessor.
+__device__ __forceinline__ void pdl_wait_then_release() {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+#endif
+}
 
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
@@ -199,13 +212,18 @@ __device__ __forceinline__ void tet_project_single(const TetState<R>& s, int whi
     }
 }
 
-__device__ __forceinline__ void load_tet(const TetArrays& t, int slot, const float4* __restrict__ x, int4& e,
-                                         TetState<float>& s, float4 xp[4]) {
+// Static per-tet data (indices, Dm^-1, compliances): never written while the
+// solver runs, so it may be loaded before the dependency wait.
+__device__ __forceinline__ void load_tet_static(const TetArrays& t, int slot, int4& e, TetState<float>& s) {
     e = __ldg(t.idx + slot);
     const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
     s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
     s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
     s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
+}
+
+__device__ __forceinline__ void gather_tet(const float4* __restrict__ x, const int4& e, TetState<float>& s,
+                                           float4 xp[4]) {
     xp[0] = x[e.x]; xp[1] = x[e.y]; xp[2] = x[e.z]; xp[3] = x[e.w];
 #pragma unroll
     for (int i = 0; i < 4; i++) {
@@ -304,6 +322,7 @@ __device__ __forceinline__ bool project_one(const TetState<float>& s, float2& la
 
 __global__ void k_predict(float4* __restrict__ x, float4* __restrict__ prev, const float4* __restrict__ vel, int V,
                           float dt, float dz) {
+    pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     const float4 p = x[i];
@@ -314,6 +333,7 @@ __global__ void k_predict(float4* __restrict__ x, float4* __restrict__ prev, con
 
 __global__ void k_kinematic(float4* __restrict__ x, const int* __restrict__ idx, const float4* __restrict__ rest,
                             int n, float ox, float oy, float oz) {
+    pdl_wait_then_release();
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int i = idx[j];
@@ -329,11 +349,13 @@ __global__ void __launch_bounds__(256) k_project_jacobi(TetArrays t, int T, cons
                                                         float4* __restrict__ dx, ResidualSink res, Flags* flags) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     float rsq = 0.f;
+    int4 e;
+    TetState<float> s;
+    if (slot < T) load_tet_static(t, slot, e, s);
+    pdl_wait_then_release();
     if (slot < T) {
-        int4 e;
-        TetState<float> s;
         float4 xp[4];
-        load_tet(t, slot, x, e, s, xp);
+        gather_tet(x, e, s, xp);
         float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
         float d[4][3];
         if (project_one<SEPARATE>(s, lam, d, rsq, flags)) {
@@ -355,11 +377,13 @@ __global__ void __launch_bounds__(256) k_project_jacobi_write(TetArrays t, int T
                                                               Flags* flags) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     float rsq = 0.f;
+    int4 e;
+    TetState<float> s;
+    if (slot < T) load_tet_static(t, slot, e, s);
+    pdl_wait_then_release();
     if (slot < T) {
-        int4 e;
-        TetState<float> s;
         float4 xp[4];
-        load_tet(t, slot, x, e, s, xp);
+        gather_tet(x, e, s, xp);
         float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
         float d[4][3];
         if (!project_one<SEPARATE>(s, lam, d, rsq, flags)) {
@@ -391,6 +415,7 @@ template <bool FINAL>
 __global__ void k_gather_apply(float4* __restrict__ x, const float* __restrict__ dxt, const int* __restrict__ off,
                                const int* __restrict__ ent, float4* __restrict__ dx, int V,
                                const float4* __restrict__ prev, float4* __restrict__ vel, float dt, bool write_vel) {
+    pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float sx = 0.f, sy = 0.f, sz = 0.f;
@@ -412,6 +437,7 @@ __global__ void k_gather_apply(float4* __restrict__ x, const float* __restrict__
 template <bool FINAL>
 __global__ void k_apply(float4* __restrict__ x, float4* __restrict__ dx, int V, const float4* __restrict__ prev,
                         float4* __restrict__ vel, float dt, bool write_vel) {
+    pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float4 xx = x[i];
@@ -429,11 +455,13 @@ __global__ void __launch_bounds__(256) k_project_gs(TetArrays t, int begin, int 
                                                     ResidualSink res, Flags* flags) {
     const int slot = begin + blockIdx.x * blockDim.x + threadIdx.x;
     float rsq = 0.f;
+    int4 e;
+    TetState<float> s;
+    if (slot < end) load_tet_static(t, slot, e, s);
+    pdl_wait_then_release();
     if (slot < end) {
-        int4 e;
-        TetState<float> s;
         float4 xp[4];
-        load_tet(t, slot, x, e, s, xp);
+        gather_tet(x, e, s, xp);
         float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
         float d[4][3];
         bool ok;
@@ -498,6 +526,7 @@ __device__ __forceinline__ bool contact_update(const ContactArrays& c, int slot,
 
 template <bool FIRST>
 __global__ void k_contacts_jacobi(ContactArrays c, const float4* __restrict__ x, float4* __restrict__ dx) {
+    pdl_wait_then_release();
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= c.S * c.F) return;
     if (c.bary[slot].w == 0.f) return;
@@ -519,6 +548,7 @@ __global__ void k_contacts_jacobi(ContactArrays c, const float4* __restrict__ x,
 template <bool FIRST>
 __global__ void k_contacts_gs(ContactArrays c, const int* __restrict__ face_list, int begin, int end,
                               float4* __restrict__ x) {
+    pdl_wait_then_release();
     const int j = begin + blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= end) return;
     const int f = face_list[j];
@@ -555,6 +585,7 @@ __device__ __forceinline__ void grad_sphere(float px, float py, float pz, float4
 }
 
 __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, SphereSet sph) {
+    pdl_wait_then_release();
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= c.S * c.F) return;
     const int s = slot / c.F, f = slot - s * c.F;
@@ -615,6 +646,7 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, SphereSe
 
 __global__ void k_finalize(float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel, int V,
                            float dt, bool write_vel) {
+    pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     finalize_vertex(x, prev, vel, i, x[i], dt, write_vel);
@@ -623,6 +655,7 @@ __global__ void k_finalize(float4* __restrict__ x, const float4* __restrict__ pr
 // v = (x - prev)/dt alone (XPBDMeshObject_::velocityUpdate)
 __global__ void k_velocity(const float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel,
                            int V, float dt) {
+    pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     const float4 xx = x[i], p = prev[i];
@@ -636,11 +669,13 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
                                                   ResidualSink res, double* __restrict__ energy_partial, float dt2) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     float rsq = 0.f, en = 0.f;
+    int4 e;
+    TetState<float> s;
+    if (slot < T) load_tet_static(t, slot, e, s);
+    pdl_wait_then_release();
     if (slot < T) {
-        int4 e;
-        TetState<float> s;
         float4 xp[4];
-        load_tet(t, slot, x, e, s, xp);
+        gather_tet(x, e, s, xp);
         const float2 lam = t.lam[slot];
         float Cd, Ch, gd[9], gh[9], J;
         tet_eval(s, Cd, Ch, gd, gh, J);
@@ -662,6 +697,7 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
 
 // One block per row: FP64 sum of `stride` partials, fixed order.
 __global__ void k_reduce_rows(const double* __restrict__ partial, int stride, double* __restrict__ out) {
+    pdl_wait_then_release();
     __shared__ double sh[256];
     const int row = blockIdx.x;
     double s = 0.0;
@@ -677,71 +713,92 @@ __global__ void k_reduce_rows(const double* __restrict__ partial, int stride, do
 
 inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
 
+// cudaLaunchKernelEx with programmatic stream serialization when L.pdl.
+template <typename... KArgs, typename... Args>
+void go(void (*kernel)(KArgs...), int grid, int block, const Launch& L, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3((unsigned)block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = L.s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = L.pdl ? 1 : 0;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 }  // namespace
 
 int residual_blocks(int T, int block) { return nblk(T, block); }
 
-void launch_predict(cudaStream_t s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz) {
-    if (V > 0) k_predict<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt, dz);
+void launch_predict(const Launch& s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz) {
+    if (V > 0) go(k_predict, nblk(V, 256), 256, s, x, prev, vel, V, dt, dz);
 }
 
-void launch_kinematic(cudaStream_t s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
+void launch_kinematic(const Launch& s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
                       float oz) {
-    if (n > 0) k_kinematic<<<nblk(n, 256), 256, 0, s>>>(x, idx, rest, n, ox, oy, oz);
+    if (n > 0) go(k_kinematic, nblk(n, 256), 256, s, x, idx, rest, n, ox, oy, oz);
 }
 
-#define XG_DISPATCH_FSR(KERNEL, GRID, BLOCK, STREAM, ...)                                               \
-    do {                                                                                                \
-        const bool _r = res.partial != nullptr;                                                         \
-        if (first) {                                                                                    \
-            if (separate) { if (_r) KERNEL<true, true, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);  \
-                            else KERNEL<true, true, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }  \
-            else { if (_r) KERNEL<true, false, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);          \
-                   else KERNEL<true, false, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }          \
-        } else {                                                                                        \
-            if (separate) { if (_r) KERNEL<false, true, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); \
-                            else KERNEL<false, true, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); } \
-            else { if (_r) KERNEL<false, false, true><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__);         \
-                   else KERNEL<false, false, false><<<GRID, BLOCK, 0, STREAM>>>(__VA_ARGS__); }         \
-        }                                                                                               \
+// FIRST x SEPARATE x RES instantiations of the tet sweep kernels
+#define XG_SWEEP(KERNEL, GRID, BLOCK, ...)                                                      \
+    do {                                                                                        \
+        const bool _r = res.partial != nullptr;                                                 \
+        if (first) {                                                                            \
+            if (separate) {                                                                     \
+                if (_r) go(KERNEL<true, true, true>, GRID, BLOCK, s, __VA_ARGS__);              \
+                else go(KERNEL<true, true, false>, GRID, BLOCK, s, __VA_ARGS__);                \
+            } else {                                                                            \
+                if (_r) go(KERNEL<true, false, true>, GRID, BLOCK, s, __VA_ARGS__);             \
+                else go(KERNEL<true, false, false>, GRID, BLOCK, s, __VA_ARGS__);               \
+            }                                                                                   \
+        } else {                                                                                \
+            if (separate) {                                                                     \
+                if (_r) go(KERNEL<false, true, true>, GRID, BLOCK, s, __VA_ARGS__);             \
+                else go(KERNEL<false, true, false>, GRID, BLOCK, s, __VA_ARGS__);               \
+            } else {                                                                            \
+                if (_r) go(KERNEL<false, false, true>, GRID, BLOCK, s, __VA_ARGS__);            \
+                else go(KERNEL<false, false, false>, GRID, BLOCK, s, __VA_ARGS__);              \
+            }                                                                                   \
+        }                                                                                       \
     } while (0)
 
-void launch_project_jacobi(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
+void launch_project_jacobi(const Launch& s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
                            bool first, bool separate, ResidualSink res, Flags* flags) {
     if (T <= 0) return;
-    XG_DISPATCH_FSR(k_project_jacobi, nblk(T, block), block, s, t, T, x, dx, res, flags);
+    XG_SWEEP(k_project_jacobi, nblk(T, block), block, t, T, x, dx, res, flags);
 }
 
-void launch_project_jacobi_gather_write(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x,
+void launch_project_jacobi_gather_write(const Launch& s, int block, const TetArrays& t, int T, const float4* x,
                                         float4* dxt, bool first, bool separate, ResidualSink res, Flags* flags) {
     if (T <= 0) return;
-    XG_DISPATCH_FSR(k_project_jacobi_write, nblk(T, block), block, s, t, T, x, dxt, res, flags);
+    XG_SWEEP(k_project_jacobi_write, nblk(T, block), block, t, T, x, dxt, res, flags);
 }
 
-void launch_gather_apply(cudaStream_t s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
+void launch_gather_apply(const Launch& s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
                          float4* dx, int V, float4* prev, float4* vel, bool final_step, float dt, bool write_vel) {
     if (V <= 0) return;
     const float* d = (const float*)dxt;
-    if (final_step)
-        k_gather_apply<true><<<nblk(V, 256), 256, 0, s>>>(x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
-    else
-        k_gather_apply<false><<<nblk(V, 256), 256, 0, s>>>(x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
+    if (final_step) go(k_gather_apply<true>, nblk(V, 256), 256, s, x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
+    else go(k_gather_apply<false>, nblk(V, 256), 256, s, x, d, csr_off, csr_ent, dx, V, prev, vel, dt, write_vel);
 }
 
-void launch_apply(cudaStream_t s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
+void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
                   float dt, bool write_vel) {
     if (V <= 0) return;
-    if (final_step) k_apply<true><<<nblk(V, 256), 256, 0, s>>>(x, dx, V, prev, vel, dt, write_vel);
-    else k_apply<false><<<nblk(V, 256), 256, 0, s>>>(x, dx, V, prev, vel, dt, write_vel);
+    if (final_step) go(k_apply<true>, nblk(V, 256), 256, s, x, dx, V, prev, vel, dt, write_vel);
+    else go(k_apply<false>, nblk(V, 256), 256, s, x, dx, V, prev, vel, dt, write_vel);
 }
 
-void launch_project_gs(cudaStream_t s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
+void launch_project_gs(const Launch& s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
                        int which, ResidualSink res, Flags* flags) {
     const int n = end - begin;
     if (n <= 0) return;
     const int g = nblk(n, block);
     const bool r = res.partial != nullptr;
-#define XG_GS(F, W, R) k_project_gs<F, W, R><<<g, block, 0, s>>>(t, begin, end, x, res, flags)
+#define XG_GS(F, W, R) go(k_project_gs<F, W, R>, g, block, s, t, begin, end, x, res, flags)
     if (which == 2) {
         if (first) { if (r) XG_GS(true, 2, true); else XG_GS(true, 2, false); }
         else { if (r) XG_GS(false, 2, true); else XG_GS(false, 2, false); }
@@ -755,43 +812,43 @@ void launch_project_gs(cudaStream_t s, int block, const TetArrays& t, int begin,
 #undef XG_GS
 }
 
-void launch_contacts_jacobi(cudaStream_t s, const ContactArrays& c, const float4* x, float4* dx, bool first) {
+void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first) {
     const int n = c.S * c.F;
     if (n <= 0) return;
-    if (first) k_contacts_jacobi<true><<<nblk(n, 256), 256, 0, s>>>(c, x, dx);
-    else k_contacts_jacobi<false><<<nblk(n, 256), 256, 0, s>>>(c, x, dx);
+    if (first) go(k_contacts_jacobi<true>, nblk(n, 256), 256, s, c, x, dx);
+    else go(k_contacts_jacobi<false>, nblk(n, 256), 256, s, c, x, dx);
 }
 
-void launch_contacts_gs(cudaStream_t s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
+void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first) {
     const int n = end - begin;
     if (n <= 0) return;
-    if (first) k_contacts_gs<true><<<nblk(n, 128), 128, 0, s>>>(c, face_list, begin, end, x);
-    else k_contacts_gs<false><<<nblk(n, 128), 128, 0, s>>>(c, face_list, begin, end, x);
+    if (first) go(k_contacts_gs<true>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
+    else go(k_contacts_gs<false>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
 }
 
-void launch_detect(cudaStream_t s, const ContactArrays& c, const float4* x, const SphereSet& spheres) {
+void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const SphereSet& spheres) {
     const int n = c.S * c.F;
     if (n <= 0) return;
-    k_detect<<<nblk(n, 128), 128, 0, s>>>(c, x, spheres);
+    go(k_detect, nblk(n, 128), 128, s, c, x, spheres);
 }
 
-void launch_finalize(cudaStream_t s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel) {
-    if (V > 0) k_finalize<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt, write_vel);
+void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel) {
+    if (V > 0) go(k_finalize, nblk(V, 256), 256, s, x, prev, vel, V, dt, write_vel);
 }
 
-void launch_velocity(cudaStream_t s, const float4* x, const float4* prev, float4* vel, int V, float dt) {
-    if (V > 0) k_velocity<<<nblk(V, 256), 256, 0, s>>>(x, prev, vel, V, dt);
+void launch_velocity(const Launch& s, const float4* x, const float4* prev, float4* vel, int V, float dt) {
+    if (V > 0) go(k_velocity, nblk(V, 256), 256, s, x, prev, vel, V, dt);
 }
 
-void launch_residual(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, bool separate,
+void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
                      const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2) {
     if (T <= 0) return;
-    k_residual<<<nblk(T, block), block, 0, s>>>(t, T, x, separate, perm, rvec, res, energy_partial, dt2);
+    go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2);
 }
 
-void launch_reduce_rows(cudaStream_t s, const double* partial, int rows, int stride, double* out) {
-    if (rows > 0) k_reduce_rows<<<rows, 256, 0, s>>>(partial, stride, out);
+void launch_reduce_rows(const Launch& s, const double* partial, int rows, int stride, double* out) {
+    if (rows > 0) go(k_reduce_rows, rows, 256, s, partial, stride, out);
 }
 
 }  // namespace xg

@@ -72,29 +72,36 @@ struct ResidualSink {
     int offset;       // first slot of this launch in the row
 };
 
-// ---- launchers (all asynchronous on `s`) ----
-void launch_predict(cudaStream_t s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz);
-void launch_kinematic(cudaStream_t s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
+// Where and how to launch: the stream, and whether the kernel may start
+// before its predecessor finishes (programmatic dependent launch).
+struct Launch {
+    cudaStream_t s;
+    bool pdl;
+};
+
+// ---- launchers (all asynchronous on L.s) ----
+void launch_predict(const Launch& s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz);
+void launch_kinematic(const Launch& s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
                       float oz);
-void launch_project_jacobi(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
+void launch_project_jacobi(const Launch& s, int block, const TetArrays& t, int T, const float4* x, float4* dx,
                            bool first, bool separate, ResidualSink res, Flags* flags);
-void launch_project_jacobi_gather_write(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x,
+void launch_project_jacobi_gather_write(const Launch& s, int block, const TetArrays& t, int T, const float4* x,
                                         float4* dxt, bool first, bool separate, ResidualSink res, Flags* flags);
-void launch_gather_apply(cudaStream_t s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
+void launch_gather_apply(const Launch& s, float4* x, const float4* dxt, const int* csr_off, const int* csr_ent,
                          float4* dx, int V, float4* prev, float4* vel, bool final_step, float dt, bool write_vel);
-void launch_apply(cudaStream_t s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
+void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
                   float dt, bool write_vel);
-void launch_project_gs(cudaStream_t s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
+void launch_project_gs(const Launch& s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
                        int which, ResidualSink res, Flags* flags);
-void launch_contacts_jacobi(cudaStream_t s, const ContactArrays& c, const float4* x, float4* dx, bool first);
-void launch_contacts_gs(cudaStream_t s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
+void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
+void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);
-void launch_detect(cudaStream_t s, const ContactArrays& c, const float4* x, const SphereSet& spheres);
-void launch_finalize(cudaStream_t s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);
-void launch_velocity(cudaStream_t s, const float4* x, const float4* prev, float4* vel, int V, float dt);
-void launch_residual(cudaStream_t s, int block, const TetArrays& t, int T, const float4* x, bool separate,
+void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const SphereSet& spheres);
+void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);
+void launch_velocity(const Launch& s, const float4* x, const float4* prev, float4* vel, int V, float dt);
+void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
                      const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2);
-void launch_reduce_rows(cudaStream_t s, const double* partial, int rows, int stride, double* out);
+void launch_reduce_rows(const Launch& s, const double* partial, int rows, int stride, double* out);
 int residual_blocks(int T, int block);
 
 }  // namespace xg

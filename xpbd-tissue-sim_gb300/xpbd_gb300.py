@@ -56,7 +56,7 @@ class Params(C.Structure):
         ("dt", C.c_double), ("g_accel", C.c_double), ("collision_rate", C.c_double),
         ("num_iters", C.c_int32), ("solver_type", C.c_int32), ("constraint_type", C.c_int32),
         ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
-        ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32),
+        ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
     ]
 
 
@@ -131,6 +131,7 @@ def load(path: str | None = None):
         "xpbd_profile_steps": ([P, I32, I32, P, P], C.c_int),
         "xpbd_kernel_name": ([I32], C.c_char_p),
         "xpbd_launch_count": ([P, P], C.c_int),
+        "xpbd_get_stream": ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -376,6 +377,12 @@ class XPBDSolver:
         cnt = np.zeros(K, np.int64)
         self._ck(self.L.xpbd_profile_steps(self.h, int(n), K, _p(ms), _p(cnt)))
         return {self.L.xpbd_kernel_name(k).decode(): (ms[k], int(cnt[k])) for k in range(K) if cnt[k]}
+
+    def stream_handle(self) -> int:
+        """The context's cudaStream_t as an integer (for torch.cuda.ExternalStream)."""
+        h = C.c_void_p()
+        self._ck(self.L.xpbd_get_stream(self.h, C.byref(h)))
+        return h.value or 0
 
     def launch_count(self) -> int:
         n = C.c_int64()
