@@ -90,6 +90,8 @@ typedef struct {
     int32_t max_contacts_per_face; /* contact slots per surface face; 0 = 4        */
     int32_t use_graphs;        /* capture each substep in a CUDA graph (1) or not  */
     int32_t use_pdl;           /* programmatic dependent launch between kernels    */
+    int32_t gs_patch_tets;     /* Gauss-Seidel patch size in tets (1..5); 0 = 5;   */
+                               /* 1 = plain per-tet colouring                      */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -199,10 +201,18 @@ int xpbd_total_strain_energy(xpbd_ctx* ctx, double* e);
  * and projections that took the FP64 near-degenerate path (|det F| < 1e-3). */
 int xpbd_health(xpbd_ctx* ctx, int64_t* nonfinite, int64_t* degenerate);
 
-/* Colouring in use (coloured Gauss-Seidel): number of tet colours and the
- * colour of each tet; contacts follow the surface-face colouring. */
+/* Colouring in use (coloured Gauss-Seidel). Tets are grouped into patches
+ * (runs of up to gs_patch_tets consecutive tets on at most 8 vertices) and the
+ * patches are coloured so that patches of one colour share no vertex; each
+ * colour is one kernel launch. n_tet_colours is the number of these sweep
+ * colours, colour_of_tet the colour of each tet's patch; contacts follow the
+ * surface-face colouring. */
 int xpbd_num_colours(xpbd_ctx* ctx, int32_t* n_tet_colours, int32_t* n_face_colours);
 int xpbd_get_tet_colours(xpbd_ctx* ctx, int32_t* colour_of_tet);
+/* The order in which one Gauss-Seidel sweep projects the tets (T tet indices):
+ * colour by colour, patch by patch, tets of a patch in index order. The FP64
+ * oracle replays this order for parity. */
+int xpbd_get_sweep_order(xpbd_ctx* ctx, int32_t* order);
 
 /* Per-kernel timing with CUDA events on the context's stream over n substeps
  * (no graphs). Fills up to max_k entries: average milliseconds per launch and

@@ -222,6 +222,12 @@ class Oracle:
     def strain_energy(self):
         return self.L.xo_strain_energy(self.h)
 
+    def set_order(self, order):
+        """Replay a given Gauss-Seidel order (a permutation of the tets)."""
+        order = np.ascontiguousarray(order, np.int32)
+        if self.L.xo_set_order(C.c_void_p(self.h), len(order), _p(order)) != 0:
+            raise ValueError("not a permutation of the tets")
+
     def tet_order(self):
         n = self.L.xo_tet_order(C.c_void_p(self.h), None)
         out = np.zeros(n, np.int32)

@@ -221,6 +221,22 @@ void xo_constraint_residual(void* p, double* out) {
 double xo_strain_energy(void* p) {
     return with((Handle*)p, [&](auto& o) { return o.total_strain_energy(); });
 }
+// replace the coloured Gauss-Seidel order (a permutation of the tets), e.g.
+// with the sweep order the GPU library reports
+int xo_set_order(void* p, int n, const int* order) {
+    return with((Handle*)p, [&](auto& o) {
+        if (n != (int)o.T) return 1;
+        std::vector<int> seen(o.T, 0);
+        for (int i = 0; i < n; i++) {
+            if (order[i] < 0 || order[i] >= (int)o.T || seen[order[i]]++) return 1;
+        }
+        o.tet_order.assign(order, order + n);
+        if (o.face_colour.size() != (size_t)o.F || (o.F && o.n_face_colours == 0))
+            o.n_face_colours = o.F ? xo::greedy_colour(o.F, 3, o.faces.data(), o.V, o.face_colour.data()) : 0;
+        return 0;
+    });
+}
+
 // the coloured Gauss-Seidel order actually used (tets in colour order)
 int xo_tet_order(void* p, int* out) {
     return with((Handle*)p, [&](auto& o) {

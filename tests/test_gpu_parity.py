@@ -32,6 +32,8 @@ def _pair(X, tets, faces, E, nu, rho, solver, iters, dt=1e-3, g=9.81, ckind=G.CO
     o = O.Oracle(X, tets, faces, E, nu, rho, dt=dt, g=g, num_iter=iters,
                  solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS,
                  ckind=O.SEPARATE if ckind == G.CONSTRAINT_SEPARATE else O.COMBINED, precision=precision)
+    if solver == G.SOLVER_GAUSS_SEIDEL:
+        o.set_order(s.sweep_order())  # replay the GPU's colour/patch order
     return s, o
 
 
@@ -55,19 +57,25 @@ def test_single_update_matches_fp32_oracle(lib, solver, ckind):
     s.close()
 
 
-def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, **kw):
-    mk = lambda prec: O.Oracle(X, tets, faces, E, nu, rho, num_iter=iters,
-                               solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS, precision=prec, **kw)
+def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, gpu=None, **kw):
+    """FP32 and FP64 oracles; for Gauss-Seidel they replay the GPU's sweep order."""
+    def mk(prec):
+        o = O.Oracle(X, tets, faces, E, nu, rho, num_iter=iters,
+                     solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS, precision=prec, **kw)
+        if solver == G.SOLVER_GAUSS_SEIDEL:
+            o.set_order(gpu.sweep_order())
+        return o
     return mk(32), mk(64)
 
 
-@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
-def test_cube_trajectory_matches_fp64_oracle(lib, solver):
+@pytest.mark.parametrize("solver,cap", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 5), (G.SOLVER_GAUSS_SEIDEL, 1)])
+def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap):
     """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise): 20 steps at the
-    spec bound, then 100 steps within the FP32 band."""
+    spec bound, then 100 steps within the FP32 band. Gauss-Seidel runs
+    with hex patches (cap 5) and with per-tet colouring (cap 1)."""
     w = W.cube()
-    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver)
-    o32, o64 = _oracle_pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10)
+    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver, gs_patch_tets=cap)
+    o32, o64 = _oracle_pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10, gpu=s)
     s.set_positions(w.x0)
     s.fix_vertices(w.fixed)
     for o in (o32, o64):
@@ -87,16 +95,40 @@ def test_cube_trajectory_matches_fp64_oracle(lib, solver):
     s.close()
 
 
-def test_gs_colour_order_is_the_oracle_order(lib):
+def _patches(tets, cap, max_verts=8):
+    """Independent restatement of the library's patch rule: runs of
+    consecutive tets, each sharing a vertex with the run, at most `cap` tets
+    and `max_verts` vertices."""
+    runs, cur, verts = [], [], []
+    for t, e in enumerate(tets):
+        fresh = [v for v in e if v not in verts]
+        if cur and (len(cur) == cap or len(fresh) == 4 or len(verts) + len(fresh) > max_verts):
+            runs.append(cur); cur, verts = [], []
+            fresh = list(e)
+        cur.append(t); verts.extend(fresh)
+    runs.append(cur)
+    return runs
+
+
+@pytest.mark.parametrize("cap", [1, 5])
+def test_gs_sweep_order_is_patch_colouring(lib, cap):
     w = W.cube(n=6)
-    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, solver_type=G.SOLVER_GAUSS_SEIDEL)
-    o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver=O.COLOURED_GS)
-    np.testing.assert_array_equal(s.gs_order(), o.tet_order())
+    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, solver_type=G.SOLVER_GAUSS_SEIDEL, gs_patch_tets=cap)
     nt, _, col = s.colours()
-    # validator: no two tets of one colour share a vertex
+    order = s.sweep_order()
+    runs = _patches(w.tets, cap)
+    assert sorted(order.tolist()) == list(range(w.T))
+    if cap == 5:
+        assert all(len(r) == 5 for r in runs) and nt == 8  # hex patches of the grid: 8 colours
+    # colours are non-decreasing along the sweep, each patch keeps one colour
+    assert np.all(np.diff(col[order]) >= 0)
+    for r in runs:
+        assert len(set(col[r])) == 1
+    # patches of one colour share no vertex
     for c in range(nt):
-        v = w.tets[col == c].ravel()
-        assert len(np.unique(v)) == len(v)
+        vs = [set(w.tets[r].ravel()) for r in runs if col[r[0]] == c]
+        allv = [v for st in vs for v in st]
+        assert len(allv) == len(set(allv))
     s.close()
 
 
@@ -105,7 +137,7 @@ def test_separate_constraints_trajectory(lib, solver):
     X, tets, faces, x0 = _noisy_cube(4, seed=3)
     s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=8, solver_type=solver,
                      constraint_type=G.CONSTRAINT_SEPARATE)
-    o32, o64 = _oracle_pair(X, tets, faces, 3e3, 0.45, 1000.0, solver, 8, ckind=O.SEPARATE)
+    o32, o64 = _oracle_pair(X, tets, faces, 3e3, 0.45, 1000.0, solver, 8, gpu=s, ckind=O.SEPARATE)
     fixed = X[:, 2] == 0
     s.set_positions(x0); s.fix_vertices(fixed)
     for o in (o32, o64):
@@ -203,17 +235,21 @@ def test_beam_trajectory_with_injected_contacts(lib, solver):
     """Physics parity with contacts: the GPU's own detections are fed to the
     FP64 oracle, so detection threshold flips cannot mask projection errors.
     The reference's un-averaged Jacobi diverges on the nu = 0.49 beam (both here
-    and in the oracle), so the Jacobi case uses nu = 0.3, where it is stable."""
+    and in the oracle), and with overlapping face contacts it diverges after
+    ~40 steps even at nu = 0.3; the Jacobi case runs 30 steps at nu = 0.3
+    (two detections), the Gauss-Seidel case 60 steps on the beam material."""
     w = _beam_small()
+    nsteps = 60
     if solver == G.SOLVER_JACOBI:
         w.nu = np.full(w.T, 0.3)
+        nsteps = 30
     s = W.make_solver(w, num_iters=10, solver_type=solver)
-    oracles = _oracle_pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10, dt=w.dt, g=w.g)
+    oracles = _oracle_pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10, gpu=s, dt=w.dt, g=w.g)
     for o in oracles:
         o.set_fixed(w.fixed)
     t, last, interval = 0.0, 0.0, 1.0 / w.collision_rate
     ncontacts = 0
-    for k in range(60):
+    for k in range(nsteps):
         if t - last > interval:
             s.set_spheres(w.sphere_centre(t), [w.sphere_r])
             s.detect_collisions()
@@ -262,6 +298,7 @@ def test_coloured_gs_contacts_match_oracle_order(lib):
     w = _beam_small()
     s = W.make_solver(w, num_iters=6, solver_type=G.SOLVER_GAUSS_SEIDEL)
     o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, num_iter=6, solver=O.COLOURED_GS)
+    o.set_order(s.sweep_order())
     o.set_fixed(w.fixed)
     s.set_spheres(w.sphere_centre(0.0), [w.sphere_r])
     s.detect_collisions()
@@ -296,6 +333,7 @@ def test_kinematic_block_matches_oracle(lib):
     w = W.block(n=6, iters=8)
     s = W.make_solver(w)
     o = O.Oracle(w.X, w.tets, w.faces, w.E, w.nu, w.rho, dt=w.dt, g=w.g, num_iter=8, solver=O.COLOURED_GS)
+    o.set_order(s.sweep_order())
     o.set_fixed(w.fixed)
     o.set_kinematic_group(w.kin_idx)
     for k in range(40):

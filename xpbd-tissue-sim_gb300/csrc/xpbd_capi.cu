@@ -62,7 +62,6 @@ struct xpbd_ctx {
     std::vector<double> mass_h;         // V
     std::vector<int> tet_of_slot;       // T
     std::vector<int> tets_h, faces_h;   // 4T, 3F (original order)
-    std::vector<int> col_off;           // tet colour ranges over slots
     std::vector<int> tet_colour;        // T, by original index
     std::vector<int> fcol_off;          // face colour ranges over face_list
     int n_tet_colours = 1, n_face_colours = 0;
@@ -76,6 +75,8 @@ struct xpbd_ctx {
     DevBuf<int> perm, csr_off, csr_ent;
     DevBuf<int4> faces;
     DevBuf<int> face_list;
+    DevBuf<int4> patch_meta, patch_verts;
+    std::vector<int> pcol_off;           // patch colour ranges (Gauss-Seidel)
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -87,7 +88,6 @@ struct xpbd_ctx {
     DevBuf<double> res_partial, res_rows, energy_partial;
     DevBuf<float> rvec;
     int res_stride = 0;   // doubles per residual row
-    int gs_blocks = 0;    // residual slots used by one Gauss-Seidel sweep
     bool have_rvec = false;
     std::vector<int> api_slots;  // contacts added through the API per face
 
@@ -112,6 +112,7 @@ struct xpbd_ctx {
         return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
     }
     Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
+    PatchArrays patches() const { return PatchArrays{patch_meta.p, patch_verts.p}; }
     ContactArrays contacts() {
         return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
     }
@@ -180,10 +181,59 @@ bool valid_params(const xpbd_params& p) {
            (p.jacobi_variant == XPBD_JACOBI_ATOMIC || p.jacobi_variant == XPBD_JACOBI_GATHER) &&
            (p.block_size == 0 || (p.block_size >= 32 && p.block_size <= 256 && p.block_size % 32 == 0)) &&
            p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres &&
-           (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1);
+           (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
+           p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets;
 }
 
-// greedy vertex-disjoint colouring in item order (smallest free colour)
+// Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
+// vertices, each tet sharing a vertex with the run.
+struct HostPatch {
+    int first = 0, n = 0, nv = 0;
+    int v[kMaxPatchVerts] = {-1, -1, -1, -1, -1, -1, -1, -1};
+    unsigned long long loc = 0;
+    int local(int vert) const {
+        for (int k = 0; k < nv; k++)
+            if (v[k] == vert) return k;
+        return -1;
+    }
+};
+
+std::vector<HostPatch> build_patches(const std::vector<int>& tets, int T, int cap) {
+    std::vector<HostPatch> out;
+    HostPatch cur;
+    for (int t = 0; t < T; t++) {
+        const int* e = &tets[4 * (size_t)t];
+        bool fits = cur.n > 0 && cur.n < cap;
+        if (fits) {
+            int fresh = 0;
+            bool shares = false;
+            for (int k = 0; k < 4; k++) {
+                if (cur.local(e[k]) >= 0) shares = true;
+                else fresh++;
+            }
+            fits = shares && cur.nv + fresh <= kMaxPatchVerts;
+        }
+        if (!fits && cur.n > 0) {
+            out.push_back(cur);
+            cur = HostPatch();
+        }
+        if (cur.n == 0) cur.first = t;
+        for (int k = 0; k < 4; k++) {
+            int l = cur.local(e[k]);
+            if (l < 0) {
+                l = cur.nv;
+                cur.v[cur.nv++] = e[k];
+            }
+            cur.loc |= (unsigned long long)l << (12 * cur.n + 3 * k);
+        }
+        cur.n++;
+    }
+    if (cur.n > 0) out.push_back(cur);
+    return out;
+}
+
+// greedy vertex-disjoint colouring in item order (smallest free colour);
+// entries < 0 in an item are padding
 int greedy_colour(long long n, int arity, const int* items, long long nv, int* out) {
     std::vector<std::vector<uint64_t>> used;
     used.emplace_back((size_t)nv, 0);
@@ -194,11 +244,13 @@ int greedy_colour(long long n, int arity, const int* items, long long nv, int* o
         for (size_t w = 0; c < 0; w++) {
             if (w == used.size()) used.emplace_back((size_t)nv, 0);
             uint64_t m = 0;
-            for (int k = 0; k < arity; k++) m |= used[w][(size_t)it[k]];
+            for (int k = 0; k < arity; k++)
+                if (it[k] >= 0) m |= used[w][(size_t)it[k]];
             if (~m) c = (int)(64 * w) + __builtin_ctzll(~m);
         }
         out[t] = c;
-        for (int k = 0; k < arity; k++) used[(size_t)c / 64][(size_t)it[k]] |= 1ull << (c % 64);
+        for (int k = 0; k < arity; k++)
+            if (it[k] >= 0) used[(size_t)c / 64][(size_t)it[k]] |= 1ull << (c % 64);
         ncol = std::max(ncol, c + 1);
     }
     return ncol;
@@ -320,8 +372,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 const bool f = first && (!separate || pass == 0);
                 for (int col = 0; col < c->n_tet_colours; col++) {
                     Scope sc(c, K_PROJECT_GS);
-                    launch_project_gs(c->L(), c->block, c->tets(), c->col_off[col], c->col_off[col + 1], c->x.p, f,
-                                      which, no_sink(), c->flags.p);
+                    launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
+                                           c->x.p, f, which, c->flags.p);
                 }
             }
             if (have_faces) {
@@ -436,6 +488,7 @@ void release(xpbd_ctx* c) {
     c->perm.release(); c->csr_off.release(); c->csr_ent.release(); c->faces.release(); c->face_list.release();
     c->c_bary.release(); c->c_p.release(); c->c_n.release(); c->c_lam.release();
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
+    c->patch_meta.release(); c->patch_verts.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_rows) cudaFreeHost(c->h_rows);
@@ -504,19 +557,41 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
     }
     c->fixed_h.assign(V, 0);
 
-    // slot order: colour-sorted for Gauss-Seidel, identity for Jacobi
+    // slot order: Gauss-Seidel sorts patches by colour (tets of a patch stay
+    // consecutive); Jacobi keeps the tet order
     c->tet_colour.assign(T, 0);
-    c->n_tet_colours = T ? greedy_colour(T, 4, c->tets_h.data(), V, c->tet_colour.data()) : 0;
     c->tet_of_slot.resize(T);
+    std::vector<int4> pmeta, pverts;
     if (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
-        c->col_off.assign(c->n_tet_colours + 1, 0);
-        for (int t = 0; t < T; t++) c->col_off[c->tet_colour[t] + 1]++;
-        for (int k = 0; k < c->n_tet_colours; k++) c->col_off[k + 1] += c->col_off[k];
-        std::vector<int> fill(c->col_off.begin(), c->col_off.end() - 1);
-        for (int t = 0; t < T; t++) c->tet_of_slot[fill[c->tet_colour[t]]++] = t;
+        const int cap = p.gs_patch_tets ? p.gs_patch_tets : kMaxPatchTets;
+        const std::vector<HostPatch> patches = build_patches(c->tets_h, T, cap);
+        const int P = (int)patches.size();
+        std::vector<int> plist((size_t)P * kMaxPatchVerts), pcol(P);
+        for (int q = 0; q < P; q++)
+            for (int k = 0; k < kMaxPatchVerts; k++) plist[(size_t)q * kMaxPatchVerts + k] = patches[q].v[k];
+        c->n_tet_colours = greedy_colour(P, kMaxPatchVerts, plist.data(), V, pcol.data());
+        c->pcol_off.assign(c->n_tet_colours + 1, 0);
+        for (int q = 0; q < P; q++) c->pcol_off[pcol[q] + 1]++;
+        for (int k = 0; k < c->n_tet_colours; k++) c->pcol_off[k + 1] += c->pcol_off[k];
+        std::vector<int> sorted(P), fill(c->pcol_off.begin(), c->pcol_off.end() - 1);
+        for (int q = 0; q < P; q++) sorted[fill[pcol[q]]++] = q;
+        pmeta.resize(P);
+        pverts.resize(2 * (size_t)P);
+        int slot = 0;
+        for (int r = 0; r < P; r++) {
+            const HostPatch& hp = patches[sorted[r]];
+            pmeta[r] = make_int4(slot, hp.n | (hp.nv << 8), (int)(unsigned)(hp.loc & 0xffffffffull),
+                                 (int)(unsigned)(hp.loc >> 32));
+            pverts[2 * (size_t)r] = make_int4(hp.v[0], hp.v[1], hp.v[2], hp.v[3]);
+            pverts[2 * (size_t)r + 1] = make_int4(hp.v[4], hp.v[5], hp.v[6], hp.v[7]);
+            for (int i = 0; i < hp.n; i++) {
+                c->tet_of_slot[slot++] = hp.first + i;
+                c->tet_colour[hp.first + i] = pcol[sorted[r]];
+            }
+        }
     } else {
         for (int t = 0; t < T; t++) c->tet_of_slot[t] = t;
-        c->col_off = {0, T};
+        c->n_tet_colours = 1;
     }
     const double dt2 = p.dt * p.dt;
     std::vector<int4> hidx(T);
@@ -595,6 +670,12 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
         XPBD_CU(c, cudaMemcpy(c->faces.p, hf.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
         XPBD_CU(c, cudaMemcpy(c->face_list.p, flist.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
     }
+    if (!pmeta.empty()) {
+        XPBD_CU(c, c->patch_meta.alloc(pmeta.size()));
+        XPBD_CU(c, c->patch_verts.alloc(pverts.size()));
+        XPBD_CU(c, cudaMemcpy(c->patch_meta.p, pmeta.data(), sizeof(int4) * pmeta.size(), cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->patch_verts.p, pverts.data(), sizeof(int4) * pverts.size(), cudaMemcpyHostToDevice));
+    }
     if (p.solver_type == XPBD_SOLVER_JACOBI && p.jacobi_variant == XPBD_JACOBI_GATHER) {
         XPBD_CU(c, c->dxt.alloc(3 * (size_t)T));
         XPBD_CU(c, c->csr_off.alloc(V + 1));
@@ -652,6 +733,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->max_contacts_per_face = 0;
     p->use_graphs = 1;
     p->use_pdl = 1;
+    p->gs_patch_tets = 0;
     return XPBD_OK;
 }
 
@@ -1070,6 +1152,12 @@ int xpbd_num_colours(xpbd_ctx* c, int32_t* nt, int32_t* nf) {
 int xpbd_get_tet_colours(xpbd_ctx* c, int32_t* col) {
     if (!c || !col) return XPBD_ERR_INVALID;
     std::copy(c->tet_colour.begin(), c->tet_colour.end(), col);
+    return XPBD_OK;
+}
+
+int xpbd_get_sweep_order(xpbd_ctx* c, int32_t* order) {
+    if (!c || !order) return XPBD_ERR_INVALID;
+    std::copy(c->tet_of_slot.begin(), c->tet_of_slot.end(), order);
     return XPBD_OK;
 }
 

@@ -448,48 +448,91 @@ __global__ void k_apply(float4* __restrict__ x, float4* __restrict__ dx, int V, 
     else x[i] = xx;
 }
 
-// Coloured Gauss-Seidel: one launch per colour; tets of a colour share no
-// vertex, so each thread updates its 4 vertices in place.
-template <bool FIRST, int WHICH, bool RES>
-__global__ void __launch_bounds__(256) k_project_gs(TetArrays t, int begin, int end, float4* __restrict__ x,
-                                                    ResidualSink res, Flags* flags) {
-    const int slot = begin + blockIdx.x * blockDim.x + threadIdx.x;
-    float rsq = 0.f;
-    int4 e;
-    TetState<float> s;
-    if (slot < end) load_tet_static(t, slot, e, s);
+// Coloured Gauss-Seidel over patches: a patch is a run of up to
+// kMaxPatchTets consecutive tets on at most kMaxPatchVerts vertices. Patches of
+// one colour share no vertex, so each thread owns one patch: it stages the
+// patch's vertices in shared memory, projects the patch's tets in order on
+// them, and writes the vertices back once. One launch per patch colour. A
+// patch of one tet is plain per-tet colouring.
+template <bool FIRST, int WHICH>
+__global__ void __launch_bounds__(kPatchBlock) k_project_patch(TetArrays t, PatchArrays pa, int pbegin, int pend,
+                                                               float4* __restrict__ x, Flags* flags) {
+    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    const int tid = threadIdx.x;
+    const int p = pbegin + blockIdx.x * kPatchBlock + tid;
+    const bool active = p < pend;
+    int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
+    TetState<float> st[kMaxPatchTets];
+    int ntets = 0, nverts = 0;
+    if (active) {
+        meta = __ldg(pa.meta + p);
+        va = __ldg(pa.verts + 2 * (size_t)p);
+        vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+        ntets = meta.y & 0xff;
+        nverts = meta.y >> 8;
+        // static tet data does not depend on the predecessor: load it before the wait
+#pragma unroll
+        for (int i = 0; i < kMaxPatchTets; i++) {
+            if (i < ntets) {
+                int4 dummy;
+                load_tet_static(t, meta.x + i, dummy, st[i]);
+            }
+        }
+    }
     pdl_wait_then_release();
-    if (slot < end) {
+    if (!active) return;
+    // one round trip: all vertex and multiplier loads are issued together
+    const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+    float2 lams[kMaxPatchTets];
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++)
+        lams[i] = (!FIRST && i < ntets) ? t.lam[meta.x + i] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kMaxPatchVerts; k++)
+        if (k < nverts) sv[k][tid] = x[vid[k]];
+    const unsigned long long loc = (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++) {
+        if (i >= ntets) break;
+        const int slot = meta.x + i;
+        int l[4];
         float4 xp[4];
-        gather_tet(x, e, s, xp);
-        float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            l[j] = (int)((loc >> (12 * i + 3 * j)) & 7ull);
+            xp[j] = sv[l[j]][tid];
+            st[i].p[j][0] = xp[j].x; st[i].p[j][1] = xp[j].y; st[i].p[j][2] = xp[j].z;
+            st[i].w[j] = fabsf(xp[j].w);
+        }
+        float2 lam = lams[i];
         float d[4][3];
         bool ok;
         if (WHICH == 2) {
-            ok = project_one<false>(s, lam, d, rsq, flags);
+            float rsq;
+            ok = project_one<false>(st[i], lam, d, rsq, flags);
         } else {
             float J, r, dl;
-            float lw = WHICH == 0 ? lam.x : lam.y;
-            tet_project_single(s, WHICH, lw, r, dl, d, J);
+            const float lw = WHICH == 0 ? lam.x : lam.y;
+            tet_project_single(st[i], WHICH, lw, r, dl, d, J);
             if (fabsf(J) < kDegenerateJ) {
-                project_single_fp64(s, WHICH, lw, &r, &dl, &d[0][0]);
+                project_single_fp64(st[i], WHICH, lw, &r, &dl, &d[0][0]);
                 atomicAdd(&flags->degenerate, 1ull);
             }
-            rsq = r * r;
             ok = isfinite(dl);
             if (!ok) atomicAdd(&flags->nonfinite, 1ull);
             else if (WHICH == 0) lam.x += dl;
             else lam.y += dl;
         }
         if (ok) {
-            x[e.x] = make_float4(xp[0].x + d[0][0], xp[0].y + d[0][1], xp[0].z + d[0][2], xp[0].w);
-            x[e.y] = make_float4(xp[1].x + d[1][0], xp[1].y + d[1][1], xp[1].z + d[1][2], xp[1].w);
-            x[e.z] = make_float4(xp[2].x + d[2][0], xp[2].y + d[2][1], xp[2].z + d[2][2], xp[2].w);
-            x[e.w] = make_float4(xp[3].x + d[3][0], xp[3].y + d[3][1], xp[3].z + d[3][2], xp[3].w);
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                sv[l[j]][tid] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
         }
         t.lam[slot] = lam;
     }
-    if (RES) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
+#pragma unroll
+    for (int k = 0; k < kMaxPatchVerts; k++)
+        if (k < nverts) x[vid[k]] = sv[k][tid];
 }
 
 // Static collision projection of one contact slot: C = n.(u x1 + v x2 + w x3 - p),
@@ -792,24 +835,16 @@ void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, f
     else go(k_apply<false>, nblk(V, 256), 256, s, x, dx, V, prev, vel, dt, write_vel);
 }
 
-void launch_project_gs(const Launch& s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
-                       int which, ResidualSink res, Flags* flags) {
-    const int n = end - begin;
+void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
+                            float4* x, bool first, int which, Flags* flags) {
+    const int n = pend - pbegin;
     if (n <= 0) return;
-    const int g = nblk(n, block);
-    const bool r = res.partial != nullptr;
-#define XG_GS(F, W, R) go(k_project_gs<F, W, R>, g, block, s, t, begin, end, x, res, flags)
-    if (which == 2) {
-        if (first) { if (r) XG_GS(true, 2, true); else XG_GS(true, 2, false); }
-        else { if (r) XG_GS(false, 2, true); else XG_GS(false, 2, false); }
-    } else if (which == 0) {
-        if (first) { if (r) XG_GS(true, 0, true); else XG_GS(true, 0, false); }
-        else { if (r) XG_GS(false, 0, true); else XG_GS(false, 0, false); }
-    } else {
-        if (first) { if (r) XG_GS(true, 1, true); else XG_GS(true, 1, false); }
-        else { if (r) XG_GS(false, 1, true); else XG_GS(false, 1, false); }
-    }
-#undef XG_GS
+    const int g = nblk(n, kPatchBlock);
+#define XG_PATCH(F, W) go(k_project_patch<F, W>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
+    if (which == 2) { if (first) XG_PATCH(true, 2); else XG_PATCH(false, 2); }
+    else if (which == 0) { if (first) XG_PATCH(true, 0); else XG_PATCH(false, 0); }
+    else { if (first) XG_PATCH(true, 1); else XG_PATCH(false, 1); }
+#undef XG_PATCH
 }
 
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first) {

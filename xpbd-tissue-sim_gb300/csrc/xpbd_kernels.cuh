@@ -53,6 +53,17 @@ struct ContactArrays {
     int S;
 };
 
+// Gauss-Seidel patches: up to kMaxPatchTets consecutive tets on at most
+// kMaxPatchVerts vertices, one thread each.
+constexpr int kMaxPatchTets = 5;
+constexpr int kMaxPatchVerts = 8;
+constexpr int kPatchBlock = 64;
+struct PatchArrays {
+    const int4* meta;   // [P] x: first slot, y: ntets | nverts << 8, z/w: local vertex ids, 3 bits per
+                        //     (tet i, corner j) at bit 12 i + 3 j of the 64-bit word (z low, w high)
+    const int4* verts;  // [2P] the patch's vertex indices
+};
+
 constexpr int kMaxSpheres = 16;
 struct SphereSet {
     float4 s[kMaxSpheres];  // centre xyz, radius
@@ -91,8 +102,8 @@ void launch_gather_apply(const Launch& s, float4* x, const float4* dxt, const in
                          float4* dx, int V, float4* prev, float4* vel, bool final_step, float dt, bool write_vel);
 void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
                   float dt, bool write_vel);
-void launch_project_gs(const Launch& s, int block, const TetArrays& t, int begin, int end, float4* x, bool first,
-                       int which, ResidualSink res, Flags* flags);
+void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
+                            float4* x, bool first, int which, Flags* flags);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);

@@ -57,6 +57,7 @@ class Params(C.Structure):
         ("num_iters", C.c_int32), ("solver_type", C.c_int32), ("constraint_type", C.c_int32),
         ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
         ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
+        ("gs_patch_tets", C.c_int32),
     ]
 
 
@@ -128,6 +129,7 @@ def load(path: str | None = None):
         "xpbd_health": ([P, P, P], C.c_int),
         "xpbd_num_colours": ([P, P, P], C.c_int),
         "xpbd_get_tet_colours": ([P, P], C.c_int),
+        "xpbd_get_sweep_order": ([P, P], C.c_int),
         "xpbd_profile_steps": ([P, I32, I32, P, P], C.c_int),
         "xpbd_kernel_name": ([I32], C.c_char_p),
         "xpbd_launch_count": ([P, P], C.c_int),
@@ -366,10 +368,12 @@ class XPBDSolver:
         self._ck(self.L.xpbd_get_tet_colours(self.h, _p(col)))
         return nt.value, nf.value, col
 
-    def gs_order(self) -> np.ndarray:
-        """Tets in the coloured Gauss-Seidel order (colour, then index)."""
-        _, _, col = self.colours()
-        return np.lexsort((np.arange(self.T), col)).astype(np.int32)
+    def sweep_order(self) -> np.ndarray:
+        """Tets in the order one sweep projects them (Gauss-Seidel: colour by
+        colour, patch by patch; Jacobi: index order)."""
+        out = np.zeros(self.T, np.int32)
+        self._ck(self.L.xpbd_get_sweep_order(self.h, _p(out)))
+        return out
 
     def profile_steps(self, n):
         K = 16
