@@ -123,6 +123,17 @@ int xpbd_grid_mesh(int32_t nx, int32_t ny, int32_t nz, double hx, double hy, dou
  * (XPBDMeshObject.cpp:60-160; XPBDSolver.hpp:47-61). Uploads the mesh, builds
  * rest shapes, masses, compliances and the colouring. */
 int xpbd_create(const xpbd_mesh_desc* mesh, const xpbd_params* params, xpbd_ctx** out);
+/* Batched instances: n independent objects (one XPBDMeshObject_ each, as a
+ * Simulation holding many objects steps them, Simulation.cpp:246-255) advanced
+ * together by the same kernel launches. Instance k's vertices, tets and faces
+ * follow instance k-1's in the context's arrays (xpbd_instance_offsets); state
+ * transfer, fixing and kinematic groups use these concatenated indices. */
+int xpbd_create_batch(const xpbd_mesh_desc* meshes, int32_t n_instances, const xpbd_params* params,
+                      xpbd_ctx** out);
+int xpbd_num_instances(xpbd_ctx* ctx, int32_t* n);
+/* offsets of each instance into the concatenated arrays, n + 1 entries each
+ * (any pointer may be NULL) */
+int xpbd_instance_offsets(xpbd_ctx* ctx, int64_t* vertex_offsets, int64_t* tet_offsets, int64_t* face_offsets);
 int xpbd_destroy(xpbd_ctx* ctx);
 const char* xpbd_last_error(const xpbd_ctx* ctx);
 
@@ -155,6 +166,9 @@ int xpbd_set_kinematic_offset(xpbd_ctx* ctx, const double* offset3);
 /* Rigid spheres (RigidSphere + SphereSDF, src/geometry/SphereSDF.cpp:16-26),
  * treated as fixed: detection emits static collision constraints. */
 int xpbd_set_spheres(xpbd_ctx* ctx, int32_t n, const double* centers3n, const double* radii);
+/* the same for one instance of a batch (xpbd_set_spheres addresses instance 0) */
+int xpbd_set_instance_spheres(xpbd_ctx* ctx, int32_t instance, int32_t n, const double* centers3n,
+                              const double* radii);
 
 /* clearCollisionConstraints (XPBDMeshObject.cpp:233-251). */
 int xpbd_clear_collisions(xpbd_ctx* ctx);
@@ -221,6 +235,14 @@ int xpbd_profile_steps(xpbd_ctx* ctx, int32_t nsteps, int32_t max_k, double* avg
 const char* xpbd_kernel_name(int32_t id);
 /* number of kernel launches issued by the library since creation */
 int xpbd_launch_count(xpbd_ctx* ctx, int64_t* n);
+/* Autotuner: builds trial contexts from the meshes, times trial_steps substeps
+ * (CUDA events, graphs on) for each candidate launch configuration -- Gauss-
+ * Seidel: patch size (tet colours folded into one launch) x programmatic
+ * dependent launch; Jacobi: block size x scatter/gather variant x programmatic
+ * dependent launch -- and writes the fastest into *params. report (if
+ * report_len > 0) receives a JSON list of the candidates and their ms/step. */
+int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_instances, xpbd_params* params, int32_t trial_steps,
+                  char* report, int32_t report_len);
 /* the context's CUDA stream (a cudaStream_t), for callers that time or order
  * their own work against the solver's */
 int xpbd_get_stream(xpbd_ctx* ctx, void** stream);

@@ -80,7 +80,14 @@ struct xpbd_ctx {
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
-    SphereSet spheres{};
+    // instances (batched objects): offsets into the concatenated arrays
+    int n_inst = 1;
+    std::vector<int64_t> voff, toff, foff;
+    std::vector<float4> sphere_tab_h;  // [n_inst * S], radius < 0 = empty
+    DevBuf<float4> sphere_tab;
+    DevBuf<int> face_inst;
+    bool sphere_dirty = true;
+    int n_spheres_total = 0;
     DevBuf<int> kin_idx;
     DevBuf<float4> kin_rest;
     int nkin = 0;
@@ -453,9 +460,16 @@ int run_update(xpbd_ctx* c, bool write_vel) {
 
 int detect(xpbd_ctx* c) {
     if (c->F == 0) return XPBD_OK;
+    if (c->sphere_dirty) {
+        // pageable source: the copy is staged before the call returns, so the
+        // host table may change right after; the upload is stream-ordered
+        XPBD_CU(c, cudaMemcpyAsync(c->sphere_tab.p, c->sphere_tab_h.data(), sizeof(float4) * c->sphere_tab_h.size(),
+                                   cudaMemcpyHostToDevice, c->stream));
+        c->sphere_dirty = false;
+    }
     {
         Scope sc(c, K_DETECT);
-        launch_detect(c->L(), c->contacts(), c->x.p, c->spheres);
+        launch_detect(c->L(), c->contacts(), c->x.p, c->sphere_tab.p, c->face_inst.p);
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
     return after_launches(c, "detect");
@@ -488,6 +502,7 @@ void release(xpbd_ctx* c) {
     c->perm.release(); c->csr_off.release(); c->csr_ent.release(); c->faces.release(); c->face_list.release();
     c->c_bary.release(); c->c_p.release(); c->c_n.release(); c->c_lam.release();
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
+    c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     if (c->h_stage) cudaFreeHost(c->h_stage);
@@ -498,22 +513,54 @@ void release(xpbd_ctx* c) {
     c->stream = nullptr;
 }
 
-int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
+int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     const int V = c->V, T = c->T, F = c->F;
     const xpbd_params& p = c->prm;
     c->block = p.block_size ? p.block_size : 256;
     c->S = p.max_contacts_per_face ? p.max_contacts_per_face : 4;
-    c->tets_h.assign(m->tets, m->tets + 4 * (size_t)T);
-    if (F) c->faces_h.assign(m->faces, m->faces + 3 * (size_t)F);
-    for (int v : c->tets_h)
-        if (v < 0 || v >= V) return fail(c, XPBD_ERR_INVALID, "tet vertex index %d out of range [0,%d)", v, V);
-    for (int v : c->faces_h)
-        if (v < 0 || v >= V) return fail(c, XPBD_ERR_INVALID, "face vertex index %d out of range [0,%d)", v, V);
+    // concatenate the instances; indices are shifted by the vertex offsets
+    c->n_inst = n_inst;
+    c->voff.assign(n_inst + 1, 0);
+    c->toff.assign(n_inst + 1, 0);
+    c->foff.assign(n_inst + 1, 0);
+    for (int k = 0; k < n_inst; k++) {
+        c->voff[k + 1] = c->voff[k] + ms[k].num_vertices;
+        c->toff[k + 1] = c->toff[k] + ms[k].num_tets;
+        c->foff[k + 1] = c->foff[k] + ms[k].num_faces;
+    }
+    std::vector<double> Xcat(3 * (size_t)V), Ecat(T), nucat(T), rhocat(T);
+    c->tets_h.resize(4 * (size_t)T);
+    c->faces_h.resize(3 * (size_t)F);
+    std::vector<int> finst(F);
+    for (int k = 0; k < n_inst; k++) {
+        const xpbd_mesh_desc& m = ms[k];
+        const int64_t vo = c->voff[k], to = c->toff[k], fo = c->foff[k];
+        std::copy(m.vertices, m.vertices + 3 * m.num_vertices, Xcat.begin() + 3 * vo);
+        std::copy(m.tet_E, m.tet_E + m.num_tets, Ecat.begin() + to);
+        std::copy(m.tet_nu, m.tet_nu + m.num_tets, nucat.begin() + to);
+        std::copy(m.tet_density, m.tet_density + m.num_tets, rhocat.begin() + to);
+        for (int64_t i = 0; i < 4 * m.num_tets; i++) {
+            const int v = m.tets[i];
+            if (v < 0 || v >= m.num_vertices)
+                return fail(c, XPBD_ERR_INVALID, "instance %d: tet vertex index %d out of range [0,%lld)", k, v,
+                            (long long)m.num_vertices);
+            c->tets_h[4 * to + i] = (int)(v + vo);
+        }
+        for (int64_t i = 0; i < 3 * m.num_faces; i++) {
+            const int v = m.faces[i];
+            if (v < 0 || v >= m.num_vertices)
+                return fail(c, XPBD_ERR_INVALID, "instance %d: face vertex index %d out of range [0,%lld)", k, v,
+                            (long long)m.num_vertices);
+            c->faces_h[3 * fo + i] = (int)(v + vo);
+        }
+        for (int64_t f = 0; f < m.num_faces; f++) finst[fo + f] = k;
+    }
+    c->sphere_tab_h.assign((size_t)n_inst * c->S, make_float4(0.f, 0.f, 0.f, -1.f));
 
     // rest shape, compliance, lumped mass (ElementConstraint.hpp:23-51;
     // HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
     // ElasticMaterial.hpp:31-32; XPBDMeshObject.cpp:277-331)
-    const double* X = m->vertices;
+    const double* X = Xcat.data();
     std::vector<double> Q(9 * (size_t)T), ad(T), ah(T), gm(T);
     c->mass_h.assign(V, 0.0);
     for (int t = 0; t < T; t++) {
@@ -538,7 +585,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
         q[7] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) * inv;
         q[8] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) * inv;
         const double vol = std::fabs(det / 6.0);
-        const double E = m->tet_E[t], nu = m->tet_nu[t], rho = m->tet_density[t];
+        const double E = Ecat[t], nu = nucat[t], rho = rhocat[t];
         if (!(E > 0) || !(nu > -1 && nu < 0.5) || !(rho > 0))
             return fail(c, XPBD_ERR_INVALID, "tet %d has invalid material E=%g nu=%g rho=%g", t, E, nu, rho);
         const double mu = E / (2 * (1 + nu));
@@ -657,7 +704,10 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* m) {
     XPBD_CU(c, c->rvec.alloc(2 * (size_t)T));
     XPBD_CU(c, c->energy_partial.alloc(residual_blocks(T, c->block) + 1));
     XPBD_CU(c, cudaMallocHost((void**)&c->h_stage, sizeof(float4) * (size_t)std::max(V, 1)));
+    XPBD_CU(c, c->sphere_tab.alloc(c->sphere_tab_h.size()));
     if (F) {
+        XPBD_CU(c, c->face_inst.alloc(F));
+        XPBD_CU(c, cudaMemcpy(c->face_inst.p, finst.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
         XPBD_CU(c, c->faces.alloc(F));
         XPBD_CU(c, c->face_list.alloc(F));
         const size_t ns = (size_t)c->S * F;
@@ -745,13 +795,24 @@ int xpbd_colour_items(int64_t n, int32_t arity, const int32_t* items, int64_t nv
 }
 
 int xpbd_create(const xpbd_mesh_desc* m, const xpbd_params* p, xpbd_ctx** out) {
+    return xpbd_create_batch(m, 1, p, out);
+}
+
+int xpbd_create_batch(const xpbd_mesh_desc* ms, int32_t n_inst, const xpbd_params* p, xpbd_ctx** out) {
     if (!out) return XPBD_ERR_INVALID;
     *out = nullptr;
-    if (!m || !p || !m->vertices || !m->tets || !m->tet_E || !m->tet_nu || !m->tet_density) return XPBD_ERR_INVALID;
-    if (m->num_vertices <= 0 || m->num_tets <= 0 || m->num_faces < 0 || (m->num_faces > 0 && !m->faces))
-        return XPBD_ERR_INVALID;
-    if (m->num_vertices > (1LL << 30) || m->num_tets > (1LL << 29) || m->num_faces > (1LL << 28))
-        return XPBD_ERR_CAPACITY;
+    if (!ms || !p || n_inst <= 0) return XPBD_ERR_INVALID;
+    long long V = 0, T = 0, F = 0;
+    for (int k = 0; k < n_inst; k++) {
+        const xpbd_mesh_desc* m = ms + k;
+        if (!m->vertices || !m->tets || !m->tet_E || !m->tet_nu || !m->tet_density) return XPBD_ERR_INVALID;
+        if (m->num_vertices <= 0 || m->num_tets <= 0 || m->num_faces < 0 || (m->num_faces > 0 && !m->faces))
+            return XPBD_ERR_INVALID;
+        V += m->num_vertices;
+        T += m->num_tets;
+        F += m->num_faces;
+    }
+    if (V > (1LL << 30) || T > (1LL << 29) || F > (1LL << 28)) return XPBD_ERR_CAPACITY;
     if (!valid_params(*p)) return XPBD_ERR_INVALID;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
@@ -761,10 +822,10 @@ int xpbd_create(const xpbd_mesh_desc* m, const xpbd_params* p, xpbd_ctx** out) {
     xpbd_ctx* c = new (std::nothrow) xpbd_ctx();
     if (!c) return XPBD_ERR_CAPACITY;
     c->prm = *p;
-    c->V = (int)m->num_vertices;
-    c->T = (int)m->num_tets;
-    c->F = (int)m->num_faces;
-    int st = build(c, m);
+    c->V = (int)V;
+    c->T = (int)T;
+    c->F = (int)F;
+    int st = build(c, ms, n_inst);
     if (st) {
         fprintf(stderr, "xpbd_create: %s\n", c->err.c_str());
         release(c);
@@ -911,13 +972,41 @@ int xpbd_set_kinematic_offset(xpbd_ctx* c, const double* off) {
     return after_launches(c, "kinematic offset");
 }
 
-int xpbd_set_spheres(xpbd_ctx* c, int32_t n, const double* ctr, const double* rad) {
-    if (!c || n < 0 || n > kMaxSpheres || (n > 0 && (!ctr || !rad)))
-        return c ? fail(c, XPBD_ERR_INVALID, "sphere count %d outside [0,%d]", n, kMaxSpheres) : XPBD_ERR_INVALID;
+int xpbd_set_instance_spheres(xpbd_ctx* c, int32_t inst, int32_t n, const double* ctr, const double* rad) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (inst < 0 || inst >= c->n_inst) return fail(c, XPBD_ERR_INVALID, "instance %d out of range", inst);
+    if (n < 0 || n > kMaxSpheres || (n > 0 && (!ctr || !rad)))
+        return fail(c, XPBD_ERR_INVALID, "sphere count %d outside [0,%d]", n, kMaxSpheres);
     if (n > c->S) return fail(c, XPBD_ERR_CAPACITY, "%d spheres exceed %d contact slots per face", n, c->S);
-    c->spheres.n = n;
     for (int i = 0; i < n; i++)
-        c->spheres.s[i] = make_float4((float)ctr[3 * i], (float)ctr[3 * i + 1], (float)ctr[3 * i + 2], (float)rad[i]);
+        if (!(rad[i] >= 0) || !std::isfinite(ctr[3 * i]) || !std::isfinite(ctr[3 * i + 1]) ||
+            !std::isfinite(ctr[3 * i + 2]))
+            return fail(c, XPBD_ERR_INVALID, "sphere %d has a bad centre or radius", i);
+    float4* row = &c->sphere_tab_h[(size_t)inst * c->S];
+    for (int k = 0; k < c->S; k++)
+        row[k] = k < n ? make_float4((float)ctr[3 * k], (float)ctr[3 * k + 1], (float)ctr[3 * k + 2], (float)rad[k])
+                       : make_float4(0.f, 0.f, 0.f, -1.f);
+    c->n_spheres_total = 0;
+    for (const float4& e : c->sphere_tab_h) c->n_spheres_total += e.w >= 0.f ? 1 : 0;
+    c->sphere_dirty = true;
+    return XPBD_OK;
+}
+
+int xpbd_set_spheres(xpbd_ctx* c, int32_t n, const double* ctr, const double* rad) {
+    return xpbd_set_instance_spheres(c, 0, n, ctr, rad);
+}
+
+int xpbd_num_instances(xpbd_ctx* c, int32_t* n) {
+    if (!c || !n) return XPBD_ERR_INVALID;
+    *n = c->n_inst;
+    return XPBD_OK;
+}
+
+int xpbd_instance_offsets(xpbd_ctx* c, int64_t* voff, int64_t* toff, int64_t* foff) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (voff) std::copy(c->voff.begin(), c->voff.end(), voff);
+    if (toff) std::copy(c->toff.begin(), c->toff.end(), toff);
+    if (foff) std::copy(c->foff.begin(), c->foff.end(), foff);
     return XPBD_OK;
 }
 
@@ -1016,7 +1105,7 @@ int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
     const double interval = c->prm.collision_rate > 0 ? 1.0 / c->prm.collision_rate : 1e300;
     for (int k = 0; k < nsteps; k++) {
         const bool cd = (c->time - c->last_cd > interval);
-        if (cd && c->spheres.n > 0) {
+        if (cd && c->n_spheres_total > 0) {
             int st = detect(c);
             if (st) return st;
         } else if (cd) {
@@ -1195,6 +1284,82 @@ int xpbd_profile_steps(xpbd_ctx* c, int32_t nsteps, int32_t max_k, double* avg_m
 int xpbd_launch_count(xpbd_ctx* c, int64_t* n) {
     if (!c || !n) return XPBD_ERR_INVALID;
     *n = c->launches;
+    return XPBD_OK;
+}
+
+// Autotuner: times candidate launch configurations on trial contexts built
+// from the caller's meshes and keeps the fastest. Trials start from the rest
+// state with gravity off, so every candidate does the same, stable work.
+int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* params, int32_t trial_steps,
+                  char* report, int32_t report_len) {
+    if (!meshes || n_inst <= 0 || !params || trial_steps <= 0 || (report_len > 0 && !report)) return XPBD_ERR_INVALID;
+    if (!valid_params(*params)) return XPBD_ERR_INVALID;
+    std::vector<xpbd_params> cands;
+    xpbd_params base = *params;
+    base.g_accel = 0.0;
+    base.residual_policy = XPBD_RESIDUAL_NEVER;
+    base.use_graphs = 1;
+    if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
+        for (int patch : {1, 2, 3, 5})
+            for (int pdl : {0, 1}) {
+                xpbd_params q = base;
+                q.gs_patch_tets = patch;
+                q.use_pdl = pdl;
+                cands.push_back(q);
+            }
+    } else {
+        for (int block : {64, 128, 256})
+            for (int variant : {XPBD_JACOBI_ATOMIC, XPBD_JACOBI_GATHER})
+                for (int pdl : {0, 1}) {
+                    xpbd_params q = base;
+                    q.block_size = block;
+                    q.jacobi_variant = variant;
+                    q.use_pdl = pdl;
+                    cands.push_back(q);
+                }
+    }
+    std::string rep = "[";
+    double best = 1e300;
+    int best_i = -1;
+    for (size_t i = 0; i < cands.size(); i++) {
+        xpbd_ctx* c = nullptr;
+        int st = xpbd_create_batch(meshes, n_inst, &cands[i], &c);
+        if (st) return st;
+        double ms = -1;
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        if (cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess &&
+            xpbd_step(c, 2) == XPBD_OK && cudaStreamSynchronize(c->stream) == cudaSuccess) {
+            cudaEventRecord(e0, c->stream);
+            st = xpbd_step(c, trial_steps);
+            cudaEventRecord(e1, c->stream);
+            float f = 0;
+            if (st == XPBD_OK && cudaEventSynchronize(e1) == cudaSuccess && cudaEventElapsedTime(&f, e0, e1) == cudaSuccess)
+                ms = f / trial_steps;
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        xpbd_destroy(c);
+        char buf[256];
+        snprintf(buf, sizeof buf, "%s{\"gs_patch_tets\":%d,\"block_size\":%d,\"jacobi_variant\":%d,\"use_pdl\":%d,"
+                 "\"ms_per_step\":%.6f}", i ? "," : "", cands[i].gs_patch_tets, cands[i].block_size,
+                 cands[i].jacobi_variant, cands[i].use_pdl, ms);
+        rep += buf;
+        if (ms > 0 && ms < best) {
+            best = ms;
+            best_i = (int)i;
+        }
+    }
+    rep += "]";
+    if (report_len > 0) {
+        std::strncpy(report, rep.c_str(), (size_t)report_len - 1);
+        report[report_len - 1] = 0;
+    }
+    if (best_i < 0) return XPBD_ERR_CUDA;
+    const xpbd_params& w = cands[best_i];
+    params->gs_patch_tets = w.gs_patch_tets;
+    params->block_size = w.block_size;
+    params->jacobi_variant = w.jacobi_variant;
+    params->use_pdl = w.use_pdl;
     return XPBD_OK;
 }
 

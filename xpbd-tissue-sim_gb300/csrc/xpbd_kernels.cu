@@ -627,14 +627,17 @@ __device__ __forceinline__ void grad_sphere(float px, float py, float pz, float4
     }
 }
 
-__global__ void k_detect(ContactArrays c, const float4* __restrict__ x, SphereSet sph) {
+// Sphere table: table[instance * S + slot] = (centre, radius); radius < 0
+// marks an empty slot. face_inst maps a surface face to its instance.
+__global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const float4* __restrict__ table,
+                         const int* __restrict__ face_inst) {
     pdl_wait_then_release();
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     if (slot >= c.S * c.F) return;
     const int s = slot / c.F, f = slot - s * c.F;
     float4 bary = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (s < sph.n) {
-        const float4 S = sph.s[s];
+    const float4 S = table[(size_t)face_inst[f] * c.S + s];
+    if (S.w >= 0.f) {
         const int4 fv = c.faces[f];
         const float4 q1 = x[fv.x], q2 = x[fv.y], q3 = x[fv.z];
         const float p1[3] = {q1.x, q1.y, q1.z}, p2[3] = {q2.x, q2.y, q2.z}, p3[3] = {q3.x, q3.y, q3.z};
@@ -862,10 +865,11 @@ void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face
     else go(k_contacts_gs<false>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
 }
 
-void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const SphereSet& spheres) {
+void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const float4* sphere_table,
+                   const int* face_inst) {
     const int n = c.S * c.F;
     if (n <= 0) return;
-    go(k_detect, nblk(n, 128), 128, s, c, x, spheres);
+    go(k_detect, nblk(n, 128), 128, s, c, x, sphere_table, face_inst);
 }
 
 void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel) {

@@ -64,11 +64,7 @@ struct PatchArrays {
     const int4* verts;  // [2P] the patch's vertex indices
 };
 
-constexpr int kMaxSpheres = 16;
-struct SphereSet {
-    float4 s[kMaxSpheres];  // centre xyz, radius
-    int n;
-};
+constexpr int kMaxSpheres = 16;  // sphere slots per instance
 
 struct Flags {
     unsigned long long nonfinite;
@@ -107,7 +103,8 @@ void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArra
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);
-void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const SphereSet& spheres);
+void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const float4* sphere_table,
+                   const int* face_inst);
 void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);
 void launch_velocity(const Launch& s, const float4* x, const float4* prev, float4* vel, int V, float dt);
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,

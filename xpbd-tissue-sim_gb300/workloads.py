@@ -108,6 +108,84 @@ def block(n: int = 64, size: float = 0.1, seed: int = 0, E_range=(1e3, 1e5), ite
                     kin_idx=top, kin_dir=np.array([0.0, 0.0, 0.01]), kin_ramp_steps=100)
 
 
+@dataclass
+class Batch:
+    """Independent instances advanced together (concatenated in instance order)."""
+    instances: list
+    name: str = "batched"
+
+    @property
+    def T(self):
+        return sum(w.T for w in self.instances)
+
+    @property
+    def V(self):
+        return sum(w.V for w in self.instances)
+
+    @property
+    def iters(self):
+        return self.instances[0].iters
+
+    @property
+    def dt(self):
+        return self.instances[0].dt
+
+
+def batched(n: int = 256, seed: int = 0, t_range=(2_000, 100_000), iters: int = 20,
+            solver: int = G.SOLVER_GAUSS_SEIDEL) -> Batch:
+    """n cube/beam instances with tet counts log-uniform in t_range (seeded grid
+    dims, T = 5 nx ny nz), E log-uniform in [1e3, 1e5] Pa, nu in [0.40, 0.49],
+    rho 1000, bottom fixed, 1-4 seeded spheres descending at 0.05 m/s onto the
+    top surface."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n):
+        target = np.exp(rng.uniform(np.log(t_range[0]), np.log(t_range[1]))) / 5.0
+        if rng.random() < 0.5:  # cube
+            m = max(2, int(round(target ** (1 / 3))))
+            nx, ny, nz = m, m, m
+        else:  # beam: length 4x the section
+            m = max(2, int(round((target / 4) ** (1 / 3))))
+            nx, ny, nz = m, 4 * m, m
+        h = 0.05 / nx
+        X, tets, faces = G.grid_mesh(nx, ny, nz, h)
+        T = tets.shape[0]
+        E = np.full(T, float(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))))
+        nu = np.full(T, float(rng.uniform(0.40, 0.49)))
+        w = Workload(f"inst{k}", X, tets, faces, E, nu, np.full(T, 1000.0), fixed=X[:, 2] == X[:, 2].min(),
+                     x0=X.copy(), iters=iters, solver=solver, steps=100)
+        ns = int(rng.integers(1, 5))
+        top = X[:, 2].max()
+        r = rng.uniform(0.2, 0.4, ns) * X[:, 0].max()
+        cx = rng.uniform(0.2, 0.8, ns) * X[:, 0].max()
+        cy = rng.uniform(0.2, 0.8, ns) * X[:, 1].max()
+        w.meta["spheres"] = (np.stack([cx, cy, top + r - 0.1 * r], 1), r)
+        w.sphere_r = float(r[0])
+        w.sphere_c0 = w.meta["spheres"][0][0]
+        w.sphere_v = np.array([0.0, 0.0, -0.05])
+        out.append(w)
+    return Batch(out)
+
+
+def make_batch_solver(b: Batch, **params) -> G.XPBDSolver:
+    """One context holding every instance of the batch."""
+    w0 = b.instances[0]
+    kw = dict(dt=w0.dt, g_accel=w0.g, num_iters=w0.iters, solver_type=w0.solver, collision_rate=w0.collision_rate)
+    kw.update(params)
+    s = G.XPBDSolver(instances=[(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances], **kw)
+    s.fix_vertices(np.concatenate([w.fixed for w in b.instances]))
+    s.set_positions(np.concatenate([w.x0 for w in b.instances]))
+    return s
+
+
+def drive_batch(s: G.XPBDSolver, b: Batch):
+    """Sphere centres of every instance at the solver's current time."""
+    t = s.time
+    for k, w in enumerate(b.instances):
+        c, r = w.meta["spheres"]
+        s.set_spheres(c + w.sphere_v * t, r, instance=k)
+
+
 def make_solver(w: Workload, **params) -> G.XPBDSolver:
     """GPU solver set up for a workload: fixed vertices, kinematic group,
     initial positions, spheres."""

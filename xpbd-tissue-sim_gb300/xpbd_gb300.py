@@ -134,6 +134,11 @@ def load(path: str | None = None):
         "xpbd_kernel_name": ([I32], C.c_char_p),
         "xpbd_launch_count": ([P, P], C.c_int),
         "xpbd_get_stream": ([P, P], C.c_int),
+        "xpbd_create_batch": ([P, I32, P, P], C.c_int),
+        "xpbd_num_instances": ([P, P], C.c_int),
+        "xpbd_instance_offsets": ([P, P, P, P], C.c_int),
+        "xpbd_set_instance_spheres": ([P, I32, I32, P, P], C.c_int),
+        "xpbd_autotune": ([P, I32, P, I32, P, I32], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -190,27 +195,60 @@ def grid_mesh(nx: int, ny: int, nz: int, hx: float, hy: float | None = None, hz:
     return X, tets, faces
 
 
-class XPBDSolver:
-    """One deformable tet-mesh object solved on the GPU."""
+class _Mesh:
+    """Host copies of one instance's arrays (kept alive for the C ABI call)."""
 
-    def __init__(self, X, tets, faces=None, E=3e3, nu=0.45, density=1000.0, **params):
-        self.L = load()
+    def __init__(self, X, tets, faces, E, nu, density):
         self.X = np.ascontiguousarray(X, np.float64).reshape(-1, 3)
         self.tets = np.ascontiguousarray(tets, np.int32).reshape(-1, 4)
         self.faces = None if faces is None else np.ascontiguousarray(faces, np.int32).reshape(-1, 3)
-        self.V, self.T = self.X.shape[0], self.tets.shape[0]
-        self.F = 0 if self.faces is None else self.faces.shape[0]
-        bc = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64), (self.T,)))
-        self._E, self._nu, self._rho = bc(E), bc(nu), bc(density)
-        self.params = default_params(**params)
-        desc = MeshDesc(self.V, self.T, self.F, _p(self.X).value, _p(self.tets).value,
+        T = self.tets.shape[0]
+        bc = lambda a: np.ascontiguousarray(np.broadcast_to(np.asarray(a, np.float64), (T,)))
+        self.E, self.nu, self.rho = bc(E), bc(nu), bc(density)
+
+    def desc(self) -> MeshDesc:
+        F = 0 if self.faces is None else self.faces.shape[0]
+        return MeshDesc(self.X.shape[0], self.tets.shape[0], F, _p(self.X).value, _p(self.tets).value,
                         None if self.faces is None else _p(self.faces).value,
-                        _p(self._E).value, _p(self._nu).value, _p(self._rho).value)
+                        _p(self.E).value, _p(self.nu).value, _p(self.rho).value)
+
+
+def autotune(instances, trial_steps=5, **params):
+    """Times the candidate launch configurations on the given meshes
+    (instances=[(X, tets, faces, E, nu, density), ...]) and returns
+    (best Params, list of candidate results)."""
+    import json
+    L = load()
+    meshes = [_Mesh(*inst) for inst in instances]
+    descs = (MeshDesc * len(meshes))(*[m.desc() for m in meshes])
+    p = default_params(**params)
+    buf = C.create_string_buffer(1 << 16)
+    st = L.xpbd_autotune(descs, len(meshes), C.byref(p), int(trial_steps), buf, len(buf))
+    if st != XPBD_OK:
+        raise XPBDError(st, L.xpbd_status_string(st).decode())
+    return p, json.loads(buf.value.decode())
+
+
+class XPBDSolver:
+    """One deformable tet-mesh object solved on the GPU, or a batch of
+    independent objects (instances=[(X, tets, faces, E, nu, density), ...])."""
+
+    def __init__(self, X=None, tets=None, faces=None, E=3e3, nu=0.45, density=1000.0, instances=None, **params):
+        self.L = load()
+        meshes = [_Mesh(*inst) for inst in instances] if instances is not None else \
+            [_Mesh(X, tets, faces, E, nu, density)]
+        self.n_instances = len(meshes)
+        self.V = sum(m.X.shape[0] for m in meshes)
+        self.T = sum(m.tets.shape[0] for m in meshes)
+        self.F = sum(0 if m.faces is None else m.faces.shape[0] for m in meshes)
+        self.params = default_params(**params)
+        descs = (MeshDesc * len(meshes))(*[m.desc() for m in meshes])
         h = C.c_void_p()
-        st = self.L.xpbd_create(C.byref(desc), C.byref(self.params), C.byref(h))
+        st = self.L.xpbd_create_batch(descs, len(meshes), C.byref(self.params), C.byref(h))
         if st != XPBD_OK:
             raise XPBDError(st, self.L.xpbd_status_string(st).decode())
         self.h = h
+        self._meshes = meshes
 
     # ---- lifetime ----
     def close(self):
@@ -286,10 +324,17 @@ class XPBDSolver:
         self._ck(self.L.xpbd_set_num_iters(self.h, int(n)))
 
     # ---- collisions ----
-    def set_spheres(self, centers, radii):
+    def set_spheres(self, centers, radii, instance=0):
         c = np.ascontiguousarray(centers, np.float64).reshape(-1, 3)
         r = np.ascontiguousarray(radii, np.float64).reshape(-1)
-        self._ck(self.L.xpbd_set_spheres(self.h, len(r), _p(c), _p(r)))
+        self._ck(self.L.xpbd_set_instance_spheres(self.h, int(instance), len(r), _p(c), _p(r)))
+
+    def instance_offsets(self):
+        """(vertex, tet, face) offsets of each instance, n + 1 entries each."""
+        n = self.n_instances + 1
+        v, t, f = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n, np.int64)
+        self._ck(self.L.xpbd_instance_offsets(self.h, _p(v), _p(t), _p(f)))
+        return v, t, f
 
     def clear_collisions(self):
         self._ck(self.L.xpbd_clear_collisions(self.h))
