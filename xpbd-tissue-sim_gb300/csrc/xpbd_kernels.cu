@@ -148,6 +148,81 @@ __device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R g
             gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
 }
 
+// FP32 fast path of tet_eval: the same quantities with a shorter dependency
+// chain -- tree-shaped sums instead of left-to-right accumulation, 1/||F||
+// from rsqrt, 1/J from the hardware reciprocal. Results differ from tet_eval
+// only by FP32 rounding (a few ulp); near-degenerate elements never use it.
+__device__ __forceinline__ void tet_eval_fast(const TetState<float>& s, float& Cd, float& Ch, float gd[9], float gh[9],
+                                              float& J) {
+    float F[9];
+    tet_F(s, F);
+    const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
+                      (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
+    const float invC = rsqrtf(ss);
+    Cd = ss * invC;
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            gd[3 * i + k] = invC * fmaf(F[k], s.q[i], fmaf(F[3 + k], s.q[3 + i], F[6 + k] * s.q[6 + i]));
+    float Fc[9];
+    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
+    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
+    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
+    // det F = f0 . (f1 x f2), the same cofactors as the gradient
+    J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
+    float fac;
+    if (J >= 1.f) {
+        Ch = -s.gam + logf(J);
+        fac = __frcp_rn(J);
+    } else {
+        const float d = J - 1.f;
+        Ch = -s.gam + d - d * d * 0.5f + d * d * d * (1.f / 3.f);
+        fac = fmaf(d, d, 1.f - d);
+    }
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            gh[3 * i + k] = fac * fmaf(Fc[k], s.q[i], fmaf(Fc[3 + k], s.q[3 + i], Fc[6 + k] * s.q[6 + i]));
+}
+
+__device__ __forceinline__ float dot3(const float* a, const float* b) {
+    return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
+}
+
+// FP32 fast path of the combined 2x2 projection (same contract as
+// tet_project_combined below).
+__device__ __forceinline__ void tet_project_combined_fast(const TetState<float>& s, float lam0, float lam1, float& r0,
+                                                          float& r1, float& dl0, float& dl1, float d[4][3], float& J) {
+    float Cd, Ch, gd[9], gh[9];
+    tet_eval_fast(s, Cd, Ch, gd, gh, J);
+    float gd3[3], gh3[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+        gd3[k] = -(gd[k] + gd[3 + k]) - gd[6 + k];
+        gh3[k] = -(gh[k] + gh[3 + k]) - gh[6 + k];
+    }
+    const float aa[4] = {dot3(gd, gd), dot3(gd + 3, gd + 3), dot3(gd + 6, gd + 6), dot3(gd3, gd3)};
+    const float ab[4] = {dot3(gd, gh), dot3(gd + 3, gh + 3), dot3(gd + 6, gh + 6), dot3(gd3, gh3)};
+    const float bb[4] = {dot3(gh, gh), dot3(gh + 3, gh + 3), dot3(gh + 6, gh + 6), dot3(gh3, gh3)};
+    const float L00 = s.atd + (fmaf(s.w[0], aa[0], s.w[1] * aa[1]) + fmaf(s.w[2], aa[2], s.w[3] * aa[3]));
+    const float L01 = fmaf(s.w[0], ab[0], s.w[1] * ab[1]) + fmaf(s.w[2], ab[2], s.w[3] * ab[3]);
+    const float L11 = s.ath + (fmaf(s.w[0], bb[0], s.w[1] * bb[1]) + fmaf(s.w[2], bb[2], s.w[3] * bb[3]));
+    r0 = fmaf(s.atd, lam0, Cd);
+    r1 = fmaf(s.ath, lam1, Ch);
+    const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
+    dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
+    dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        const float* a = i < 3 ? gd + 3 * i : gd3;
+        const float* b = i < 3 ? gh + 3 * i : gh3;
+#pragma unroll
+        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * fmaf(a[k], dl0, b[k] * dl1);
+    }
+}
+
 // Combined 2x2 projection. Returns the pre-update residuals r = C + at*lam and
 // the lambda increments; writes the 4 vertex updates to d[4][3].
 template <typename R>
@@ -232,38 +307,52 @@ __device__ __forceinline__ void gather_tet(const float4* __restrict__ x, const i
     }
 }
 
-// FP64 guard path for near-degenerate / inverted elements. Kept out of line so
-// the FP32 path keeps its register budget.
-__device__ __noinline__ void project_combined_fp64(const TetState<float>& sf, float lam0, float lam1, float* r,
-                                                   float* dl, float* d) {
+// FP64 guard path for near-degenerate / inverted elements. Kept out of line
+// so the FP32 path keeps its register budget; everything crosses the call by
+// value (static tet data is re-read by slot) so no caller array needs an
+// address.
+struct Fp64Out {
+    float r0, r1, dl0, dl1;
+    float d[12];
+};
+
+__device__ __forceinline__ TetState<double> fp64_state(const TetArrays& t, int slot, float4 p0, float4 p1, float4 p2,
+                                                       float4 p3) {
     TetState<double> s;
+    const float4 ps[4] = {p0, p1, p2, p3};
     for (int i = 0; i < 4; i++) {
-        for (int k = 0; k < 3; k++) s.p[i][k] = sf.p[i][k];
-        s.w[i] = sf.w[i];
+        s.p[i][0] = ps[i].x; s.p[i][1] = ps[i].y; s.p[i][2] = ps[i].z;
+        s.w[i] = fabsf(ps[i].w);
     }
-    for (int i = 0; i < 9; i++) s.q[i] = sf.q[i];
-    s.atd = sf.atd; s.ath = sf.ath; s.gam = sf.gam;
-    double r0, r1, dl0, dl1, dd[4][3], J;
-    tet_project_combined(s, (double)lam0, (double)lam1, r0, r1, dl0, dl1, dd, J);
-    r[0] = (float)r0; r[1] = (float)r1; dl[0] = (float)dl0; dl[1] = (float)dl1;
-    for (int i = 0; i < 4; i++)
-        for (int k = 0; k < 3; k++) d[3 * i + k] = (float)dd[i][k];
+    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
+    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
+    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
+    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
+    return s;
 }
 
-__device__ __noinline__ void project_single_fp64(const TetState<float>& sf, int which, float lam, float* r, float* dl,
-                                                 float* d) {
-    TetState<double> s;
-    for (int i = 0; i < 4; i++) {
-        for (int k = 0; k < 3; k++) s.p[i][k] = sf.p[i][k];
-        s.w[i] = sf.w[i];
-    }
-    for (int i = 0; i < 9; i++) s.q[i] = sf.q[i];
-    s.atd = sf.atd; s.ath = sf.ath; s.gam = sf.gam;
-    double rr, dd_l, dd[4][3], J;
-    tet_project_single(s, which, (double)lam, rr, dd_l, dd, J);
-    *r = (float)rr; *dl = (float)dd_l;
+__device__ __noinline__ Fp64Out project_combined_fp64(TetArrays t, int slot, float4 p0, float4 p1, float4 p2,
+                                                      float4 p3, float lam0, float lam1) {
+    const TetState<double> s = fp64_state(t, slot, p0, p1, p2, p3);
+    double r0, r1, dl0, dl1, dd[4][3], J;
+    tet_project_combined(s, (double)lam0, (double)lam1, r0, r1, dl0, dl1, dd, J);
+    Fp64Out o;
+    o.r0 = (float)r0; o.r1 = (float)r1; o.dl0 = (float)dl0; o.dl1 = (float)dl1;
     for (int i = 0; i < 4; i++)
-        for (int k = 0; k < 3; k++) d[3 * i + k] = (float)dd[i][k];
+        for (int k = 0; k < 3; k++) o.d[3 * i + k] = (float)dd[i][k];
+    return o;
+}
+
+__device__ __noinline__ Fp64Out project_single_fp64(TetArrays t, int slot, float4 p0, float4 p1, float4 p2, float4 p3,
+                                                    int which, float lam) {
+    const TetState<double> s = fp64_state(t, slot, p0, p1, p2, p3);
+    double rr, dl, dd[4][3], J;
+    tet_project_single(s, which, (double)lam, rr, dl, dd, J);
+    Fp64Out o;
+    o.r0 = (float)rr; o.r1 = 0.f; o.dl0 = (float)dl; o.dl1 = 0.f;
+    for (int i = 0; i < 4; i++)
+        for (int k = 0; k < 3; k++) o.d[3 * i + k] = (float)dd[i][k];
+    return o;
 }
 
 // One tet projection in the chosen constraint form. On return d holds the
@@ -271,16 +360,19 @@ __device__ __noinline__ void project_single_fp64(const TetState<float>& sf, int 
 // the state the projection saw. Returns false when the update is non-finite
 // (then nothing may be applied).
 template <bool SEPARATE>
-__device__ __forceinline__ bool project_one(const TetState<float>& s, float2& lam, float d[4][3], float& rsq,
-                                            Flags* flags) {
+__device__ __forceinline__ bool project_one(const TetState<float>& s, const TetArrays& t, int slot, const float4 xp[4],
+                                            float2& lam, float d[4][3], float& rsq, Flags* flags) {
     float J;
     if (!SEPARATE) {
         float r0, r1, dl0, dl1;
-        tet_project_combined(s, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
+        tet_project_combined_fast(s, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
         if (fabsf(J) < kDegenerateJ) {
-            float r[2], dl[2];
-            project_combined_fp64(s, lam.x, lam.y, r, dl, &d[0][0]);
-            r0 = r[0]; r1 = r[1]; dl0 = dl[0]; dl1 = dl[1];
+            const Fp64Out o = project_combined_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], lam.x, lam.y);
+            r0 = o.r0; r1 = o.r1; dl0 = o.dl0; dl1 = o.dl1;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) d[i][k] = o.d[3 * i + k];
             atomicAdd(&flags->degenerate, 1ull);
         }
         rsq = r0 * r0 + r1 * r1;
@@ -297,8 +389,16 @@ __device__ __forceinline__ bool project_one(const TetState<float>& s, float2& la
         tet_project_single(s, 0, lam.x, r0, dl0, d, J);
         tet_project_single(s, 1, lam.y, r1, dl1, d1, J);
         if (fabsf(J) < kDegenerateJ) {
-            project_single_fp64(s, 0, lam.x, &r0, &dl0, &d[0][0]);
-            project_single_fp64(s, 1, lam.y, &r1, &dl1, &d1[0][0]);
+            const Fp64Out a = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], 0, lam.x);
+            const Fp64Out b = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], 1, lam.y);
+            r0 = a.r0; dl0 = a.dl0; r1 = b.r0; dl1 = b.dl0;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) {
+                    d[i][k] = a.d[3 * i + k];
+                    d1[i][k] = b.d[3 * i + k];
+                }
             atomicAdd(&flags->degenerate, 1ull);
         }
         rsq = r0 * r0 + r1 * r1;
@@ -358,7 +458,7 @@ __global__ void __launch_bounds__(256) k_project_jacobi(TetArrays t, int T, cons
         gather_tet(x, e, s, xp);
         float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
         float d[4][3];
-        if (project_one<SEPARATE>(s, lam, d, rsq, flags)) {
+        if (project_one<SEPARATE>(s, t, slot, xp, lam, d, rsq, flags)) {
             add_vec4(dx + e.x, d[0][0], d[0][1], d[0][2]);
             add_vec4(dx + e.y, d[1][0], d[1][1], d[1][2]);
             add_vec4(dx + e.z, d[2][0], d[2][1], d[2][2]);
@@ -386,7 +486,7 @@ __global__ void __launch_bounds__(256) k_project_jacobi_write(TetArrays t, int T
         gather_tet(x, e, s, xp);
         float2 lam = FIRST ? make_float2(0.f, 0.f) : t.lam[slot];
         float d[4][3];
-        if (!project_one<SEPARATE>(s, lam, d, rsq, flags)) {
+        if (!project_one<SEPARATE>(s, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
             for (int i = 0; i < 4; i++) d[i][0] = d[i][1] = d[i][2] = 0.f;
         }
@@ -509,13 +609,18 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch(TetArrays t, Patc
         bool ok;
         if (WHICH == 2) {
             float rsq;
-            ok = project_one<false>(st[i], lam, d, rsq, flags);
+            ok = project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags);
         } else {
             float J, r, dl;
             const float lw = WHICH == 0 ? lam.x : lam.y;
             tet_project_single(st[i], WHICH, lw, r, dl, d, J);
             if (fabsf(J) < kDegenerateJ) {
-                project_single_fp64(st[i], WHICH, lw, &r, &dl, &d[0][0]);
+                const Fp64Out o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], WHICH, lw);
+                r = o.r0; dl = o.dl0;
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) d[a][k] = o.d[3 * a + k];
                 atomicAdd(&flags->degenerate, 1ull);
             }
             ok = isfinite(dl);
