@@ -268,8 +268,9 @@ def run_batched(args):
         best, cand = G.autotune([(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances], trial_steps=3,
                                 num_iters=b.iters, solver_type=b.instances[0].solver)
         extra.update(gs_patch_tets=best.gs_patch_tets, use_pdl=best.use_pdl, block_size=best.block_size,
-                     jacobi_variant=best.jacobi_variant)
-        tune = {"chosen": {k: getattr(best, k) for k in ["gs_patch_tets", "use_pdl", "block_size", "jacobi_variant"]},
+                     jacobi_variant=best.jacobi_variant, gs_min_blocks=best.gs_min_blocks)
+        tune = {"chosen": {k: getattr(best, k) for k in ["gs_patch_tets", "gs_min_blocks", "use_pdl", "block_size",
+                                                         "jacobi_variant"]},
                 "candidates": cand}
     s = W.make_batch_solver(b, **extra)
     for _ in range(args.warmup):
@@ -354,6 +355,8 @@ def run_ours(args):
         extra["gs_patch_tets"] = args.patch_tets
     if args.no_pdl:
         extra["use_pdl"] = 0
+    if args.min_blocks:
+        extra["gs_min_blocks"] = args.min_blocks
     s = W.make_solver(w, **extra)
     step_no = 0
 
@@ -491,6 +494,7 @@ def main():
     ap.add_argument("--solver", default=None, choices=["Gauss-Seidel", "Jacobi"], help="override the workload's solver")
     ap.add_argument("--patch-tets", type=int, default=None, help="Gauss-Seidel patch size (1 = per-tet colouring)")
     ap.add_argument("--no-pdl", action="store_true", help="disable programmatic dependent launch")
+    ap.add_argument("--min-blocks", type=int, default=0, choices=[0, 6, 8], help="patch kernel blocks/SM target")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

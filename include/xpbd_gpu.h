@@ -39,6 +39,7 @@ extern "C" {
 #define XPBD_ERR_NO_DEVICE 4    /* no CUDA device / extension not usable       */
 #define XPBD_ERR_STATE 5        /* call not valid in the context's state       */
 #define XPBD_ERR_CAPACITY 6     /* a fixed capacity was exceeded               */
+#define XPBD_ERR_TIMEOUT 7      /* a bounded device wait gave up (work skipped) */
 
 /* solver-type (XPBDObjectSolverTypeEnum, include/common/XPBDEnumTypes.hpp:6-11).
  * "Gauss-Seidel" maps to the graph-coloured Gauss-Seidel, "Jacobi" and
@@ -92,6 +93,8 @@ typedef struct {
     int32_t use_pdl;           /* programmatic dependent launch between kernels    */
     int32_t gs_patch_tets;     /* Gauss-Seidel patch size in tets (1..5); 0 = 5;   */
                                /* 1 = plain per-tet colouring                      */
+    int32_t gs_min_blocks;     /* patch kernel occupancy target, blocks/SM: 6 or 8 */
+                               /* (8 caps registers at 128); 0 = 6                 */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -191,7 +194,8 @@ int xpbd_velocity_update(xpbd_ctx* ctx);
  * collision detection on the strict cadence test t - t_last > 1/rate,
  * update, velocity update, t += dt. Asynchronous. */
 int xpbd_step(xpbd_ctx* ctx, int32_t nsteps);
-/* waits for the context's stream; reports CUDA and numeric errors */
+/* waits for the context's stream; reports CUDA errors, device waits that
+ * timed out (XPBD_ERR_TIMEOUT) and non-finite projections (XPBD_ERR_NUMERIC) */
 int xpbd_synchronize(xpbd_ctx* ctx);
 int xpbd_get_time(xpbd_ctx* ctx, double* t);
 

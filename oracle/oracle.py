@@ -193,6 +193,12 @@ class Oracle:
     def update(self, record=False):
         self.L.xo_update(C.c_void_p(self.h), int(record))
 
+    def update_warm(self, lam0, record=False, fallback=True):
+        """Warm-started update from multipliers lam0 (T x 2, dev/hyd); returns
+        True when the warm start was kept (not rejected by the residual test)."""
+        lam0 = np.ascontiguousarray(lam0, np.float64)
+        return bool(self.L.xo_update_warm(C.c_void_p(self.h), _p(lam0), int(record), int(fallback)))
+
     def velocity_update(self):
         self.L.xo_velocity_update(self.h)
 

@@ -637,6 +637,54 @@ struct Object {
         }
     }
 
+    // Warm-started update: the multipliers start at lam0 (2 per tet, dev/hyd)
+    // and the positions take the matching correction x += M^-1 grad C(x)^T lam0
+    // (summed over tets at the predicted positions) before the sweeps; the
+    // sweeps then continue from lam0 instead of 0. fallback: when the residual
+    // after the correction exceeds the plain residual r(x_pred, 0), the plain
+    // initialisation is restored. Returns true when the warm start was kept.
+    bool update_warm(const std::vector<R>& lam0, bool record_residual, bool fallback) {
+        prev = x;
+        for (long long i = 0; i < V; i++) {
+            for (int k = 0; k < 3; k++) x[3 * i + k] += dt * vel[3 * i + k];
+            x[3 * i + 2] += -g * dt * dt;
+        }
+        std::fill(lam.begin(), lam.end(), R(0));
+        for (auto& ct : contacts) ct.lambda = 0;
+        const double r_plain = residual_norm();
+        const std::vector<R> x_pred = x;
+        std::vector<R> acc(3 * V, 0);
+        for (long long t = 0; t < T; t++) {
+            const int* e = &tets[4 * t];
+            R F_[9], gd[12], gh[12];
+            compute_F(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], &Q[9 * t], F_);
+            R Cd = dev_C(F_);
+            dev_grad(F_, Cd, &Q[9 * t], gd);
+            hyd_grad(F_, &Q[9 * t], gh);
+            for (int i = 0; i < 4; i++)
+                for (int k = 0; k < 3; k++)
+                    acc[3 * e[i] + k] += inv_mass[e[i]] * (gd[3 * i + k] * lam0[2 * t] + gh[3 * i + k] * lam0[2 * t + 1]);
+        }
+        for (long long i = 0; i < 3 * V; i++) x[i] += acc[i];
+        lam = lam0;
+        bool kept = true;
+        if (fallback && residual_norm() > r_plain) {
+            x = x_pred;
+            std::fill(lam.begin(), lam.end(), R(0));
+            kept = false;
+        }
+        res_history.clear();
+        for (int it = 0; it < num_iter; it++) {
+            if (record_residual) res_history.push_back(residual_norm());
+            iterate();
+        }
+        if (record_residual) res_history.push_back(residual_norm());
+        for (long long i = 0; i < V; i++)
+            if (fixed[i])
+                for (int k = 0; k < 3; k++) x[3 * i + k] = prev[3 * i + k];
+        return kept;
+    }
+
     // XPBDMeshObject_::update = prev <- x; inertial move; project
     // (XPBDMeshObject.cpp:426-505). record_residual stores ||r|| before each
     // iteration and after the last one.

@@ -181,6 +181,15 @@ void xo_set_contacts(void* p, int n, const double* rows) {
     });
 }
 
+int xo_update_warm(void* p, const double* lam0, int record, int fallback) {
+    return with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        std::vector<R> l(2 * o.T);
+        for (long long i = 0; i < 2 * o.T; i++) l[i] = (R)lam0[i];
+        return o.update_warm(l, record != 0, fallback != 0) ? 1 : 0;
+    });
+}
+
 void xo_update(void* p, int record) {
     with((Handle*)p, [&](auto& o) { o.update(record != 0); return 0; });
 }

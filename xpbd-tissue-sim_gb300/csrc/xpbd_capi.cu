@@ -189,7 +189,8 @@ bool valid_params(const xpbd_params& p) {
            (p.block_size == 0 || (p.block_size >= 32 && p.block_size <= 256 && p.block_size % 32 == 0)) &&
            p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres &&
            (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
-           p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets;
+           p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
+           (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8);
 }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
@@ -380,7 +381,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 for (int col = 0; col < c->n_tet_colours; col++) {
                     Scope sc(c, K_PROJECT_GS);
                     launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
-                                           c->x.p, f, which, c->flags.p);
+                                           c->x.p, f, which, c->flags.p, c->prm.gs_min_blocks ? c->prm.gs_min_blocks : 6);
                 }
             }
             if (have_faces) {
@@ -764,6 +765,7 @@ const char* xpbd_status_string(int st) {
         case XPBD_ERR_NO_DEVICE: return "no CUDA device";
         case XPBD_ERR_STATE: return "invalid state";
         case XPBD_ERR_CAPACITY: return "capacity exceeded";
+        case XPBD_ERR_TIMEOUT: return "a bounded device wait timed out";
         default: return "unknown status";
     }
 }
@@ -784,6 +786,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->use_graphs = 1;
     p->use_pdl = 1;
     p->gs_patch_tets = 0;
+    p->gs_min_blocks = 0;
     return XPBD_OK;
 }
 
@@ -1125,6 +1128,8 @@ int xpbd_synchronize(xpbd_ctx* c) {
     XPBD_CU(c, cudaStreamSynchronize(c->stream));
     Flags f{};
     XPBD_CU(c, cudaMemcpy(&f, c->flags.p, sizeof f, cudaMemcpyDeviceToHost));
+    if (f.timeouts)
+        return fail(c, XPBD_ERR_TIMEOUT, "%llu blocks gave up waiting for their staged data (work skipped)", f.timeouts);
     if (f.nonfinite) return fail(c, XPBD_ERR_NUMERIC, "%llu projections produced non-finite updates", f.nonfinite);
     return XPBD_OK;
 }
@@ -1301,12 +1306,14 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     base.use_graphs = 1;
     if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
         for (int patch : {1, 2, 3, 5})
-            for (int pdl : {0, 1}) {
-                xpbd_params q = base;
-                q.gs_patch_tets = patch;
-                q.use_pdl = pdl;
-                cands.push_back(q);
-            }
+            for (int pdl : {0, 1})
+                for (int minb : {6, 8}) {
+                    xpbd_params q = base;
+                    q.gs_patch_tets = patch;
+                    q.use_pdl = pdl;
+                    q.gs_min_blocks = minb;
+                    cands.push_back(q);
+                }
     } else {
         for (int block : {64, 128, 256})
             for (int variant : {XPBD_JACOBI_ATOMIC, XPBD_JACOBI_GATHER})
@@ -1340,8 +1347,10 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
         if (e1) cudaEventDestroy(e1);
         xpbd_destroy(c);
         char buf[256];
-        snprintf(buf, sizeof buf, "%s{\"gs_patch_tets\":%d,\"block_size\":%d,\"jacobi_variant\":%d,\"use_pdl\":%d,"
-                 "\"ms_per_step\":%.6f}", i ? "," : "", cands[i].gs_patch_tets, cands[i].block_size,
+        snprintf(buf, sizeof buf,
+                 "%s{\"gs_patch_tets\":%d,\"gs_min_blocks\":%d,\"block_size\":%d,\"jacobi_variant\":%d,"
+                 "\"use_pdl\":%d,\"ms_per_step\":%.6f}",
+                 i ? "," : "", cands[i].gs_patch_tets, cands[i].gs_min_blocks, cands[i].block_size,
                  cands[i].jacobi_variant, cands[i].use_pdl, ms);
         rep += buf;
         if (ms > 0 && ms < best) {
@@ -1360,6 +1369,7 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     params->block_size = w.block_size;
     params->jacobi_variant = w.jacobi_variant;
     params->use_pdl = w.use_pdl;
+    params->gs_min_blocks = w.gs_min_blocks;
     return XPBD_OK;
 }
 

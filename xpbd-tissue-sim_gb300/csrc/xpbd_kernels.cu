@@ -37,6 +37,46 @@ __device__ __forceinline__ void pdl_wait_then_release() {
 #endif
 }
 
+// ---- TMA (bulk async copy) + mbarrier helpers ----
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+
+// 1-D bulk copy global -> shared; both addresses 16-byte aligned, bytes a
+// multiple of 16; completion is counted on the mbarrier.
+__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_u32(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of the barrier: false after `limit` tries.
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, unsigned limit) {
+    for (unsigned i = 0; i < limit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+constexpr unsigned kWaitLimit = 1u << 20;
+
 __device__ __forceinline__ float warp_sum(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -554,15 +594,34 @@ __global__ void k_apply(float4* __restrict__ x, float4* __restrict__ dx, int V, 
 // patch's vertices in shared memory, projects the patch's tets in order on
 // them, and writes the vertices back once. One launch per patch colour. A
 // patch of one tet is plain per-tet colouring.
-template <bool FIRST, int WHICH>
-__global__ void __launch_bounds__(kPatchBlock) k_project_patch(TetArrays t, PatchArrays pa, int pbegin, int pend,
+template <bool FIRST, int WHICH, int MINB>
+__global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t, PatchArrays pa, int pbegin, int pend,
                                                                float4* __restrict__ x, Flags* flags) {
+    // the block's patches own the contiguous slot range [s0, s1): their static
+    // tet records arrive by three bulk copies (q0, q1, q2) before the
+    // dependency wait, costing no registers
+    __shared__ __align__(128) float4 sq[3][kPatchBlock * kMaxPatchTets];
     __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int s_first;
     const int tid = threadIdx.x;
-    const int p = pbegin + blockIdx.x * kPatchBlock + tid;
+    const int p0 = pbegin + blockIdx.x * kPatchBlock;
+    const int p = p0 + tid;
     const bool active = p < pend;
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+        const int plast = min(p0 + kPatchBlock - 1, pend - 1);
+        const int4 m0 = __ldg(pa.meta + p0), m1 = __ldg(pa.meta + plast);
+        const int s0 = m0.x, s1 = m1.x + (m1.y & 0xff);
+        const unsigned bytes = (unsigned)(s1 - s0) * 16u;
+        s_first = s0;
+        mbar_arrive_expect_tx(&bar, 3u * bytes);
+        tma_load_1d(sq[0], t.q0 + s0, bytes, &bar);
+        tma_load_1d(sq[1], t.q1 + s0, bytes, &bar);
+        tma_load_1d(sq[2], t.q2 + s0, bytes, &bar);
+    }
     int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
-    TetState<float> st[kMaxPatchTets];
     int ntets = 0, nverts = 0;
     if (active) {
         meta = __ldg(pa.meta + p);
@@ -570,17 +629,8 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch(TetArrays t, Patc
         vb = __ldg(pa.verts + 2 * (size_t)p + 1);
         ntets = meta.y & 0xff;
         nverts = meta.y >> 8;
-        // static tet data does not depend on the predecessor: load it before the wait
-#pragma unroll
-        for (int i = 0; i < kMaxPatchTets; i++) {
-            if (i < ntets) {
-                int4 dummy;
-                load_tet_static(t, meta.x + i, dummy, st[i]);
-            }
-        }
     }
     pdl_wait_then_release();
-    if (!active) return;
     // one round trip: all vertex and multiplier loads are issued together
     const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
     float2 lams[kMaxPatchTets];
@@ -590,30 +640,50 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch(TetArrays t, Patc
 #pragma unroll
     for (int k = 0; k < kMaxPatchVerts; k++)
         if (k < nverts) sv[k][tid] = x[vid[k]];
+    __syncthreads();  // s_first visible
+    const bool staged = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (!staged) {
+        // the copies never completed: record it, give them a second bounded
+        // chance to land before the block exits, and change nothing
+        if (tid == 0) {
+            atomicAdd(&flags->timeouts, 1ull);
+            mbar_wait_bounded(&bar, 0, kWaitLimit);
+        }
+        return;
+    }
+    if (!active) return;
+    const int base = meta.x - s_first;
     const unsigned long long loc = (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
 #pragma unroll
     for (int i = 0; i < kMaxPatchTets; i++) {
         if (i >= ntets) break;
         const int slot = meta.x + i;
+        TetState<float> st;
+        {
+            const float4 a = sq[0][base + i], b = sq[1][base + i], c = sq[2][base + i];
+            st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
+            st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
+            st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
+        }
         int l[4];
         float4 xp[4];
 #pragma unroll
         for (int j = 0; j < 4; j++) {
             l[j] = (int)((loc >> (12 * i + 3 * j)) & 7ull);
             xp[j] = sv[l[j]][tid];
-            st[i].p[j][0] = xp[j].x; st[i].p[j][1] = xp[j].y; st[i].p[j][2] = xp[j].z;
-            st[i].w[j] = fabsf(xp[j].w);
+            st.p[j][0] = xp[j].x; st.p[j][1] = xp[j].y; st.p[j][2] = xp[j].z;
+            st.w[j] = fabsf(xp[j].w);
         }
         float2 lam = lams[i];
         float d[4][3];
         bool ok;
         if (WHICH == 2) {
             float rsq;
-            ok = project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags);
+            ok = project_one<false>(st, t, slot, xp, lam, d, rsq, flags);
         } else {
             float J, r, dl;
             const float lw = WHICH == 0 ? lam.x : lam.y;
-            tet_project_single(st[i], WHICH, lw, r, dl, d, J);
+            tet_project_single(st, WHICH, lw, r, dl, d, J);
             if (fabsf(J) < kDegenerateJ) {
                 const Fp64Out o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], WHICH, lw);
                 r = o.r0; dl = o.dl0;
@@ -944,14 +1014,16 @@ void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, f
 }
 
 void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
-                            float4* x, bool first, int which, Flags* flags) {
+                            float4* x, bool first, int which, Flags* flags, int min_blocks) {
     const int n = pend - pbegin;
     if (n <= 0) return;
     const int g = nblk(n, kPatchBlock);
-#define XG_PATCH(F, W) go(k_project_patch<F, W>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
-    if (which == 2) { if (first) XG_PATCH(true, 2); else XG_PATCH(false, 2); }
-    else if (which == 0) { if (first) XG_PATCH(true, 0); else XG_PATCH(false, 0); }
-    else { if (first) XG_PATCH(true, 1); else XG_PATCH(false, 1); }
+#define XG_PATCH(F, W, M) go(k_project_patch<F, W, M>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
+#define XG_PATCH_M(F, W) do { if (min_blocks == 8) XG_PATCH(F, W, 8); else XG_PATCH(F, W, 6); } while (0)
+    if (which == 2) { if (first) XG_PATCH_M(true, 2); else XG_PATCH_M(false, 2); }
+    else if (which == 0) { if (first) XG_PATCH_M(true, 0); else XG_PATCH_M(false, 0); }
+    else { if (first) XG_PATCH_M(true, 1); else XG_PATCH_M(false, 1); }
+#undef XG_PATCH_M
 #undef XG_PATCH
 }
 

@@ -69,6 +69,7 @@ constexpr int kMaxSpheres = 16;  // sphere slots per instance
 struct Flags {
     unsigned long long nonfinite;
     unsigned long long degenerate;
+    unsigned long long timeouts;  // bounded waits that gave up (the work was skipped)
 };
 
 // residual partial sums: one double per block per record row
@@ -99,7 +100,7 @@ void launch_gather_apply(const Launch& s, float4* x, const float4* dxt, const in
 void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
                   float dt, bool write_vel);
 void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
-                            float4* x, bool first, int which, Flags* flags);
+                            float4* x, bool first, int which, Flags* flags, int min_blocks);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);

@@ -23,7 +23,8 @@ ROOT = os.path.dirname(HERE)
 LIB_PATH = os.path.join(HERE, "_build", "libxpbd_gpu.so")
 HEADER = os.path.join(ROOT, "include", "xpbd_gpu.h")
 
-XPBD_OK, XPBD_ERR_INVALID, XPBD_ERR_CUDA, XPBD_ERR_NUMERIC, XPBD_ERR_NO_DEVICE, XPBD_ERR_STATE, XPBD_ERR_CAPACITY = range(7)
+(XPBD_OK, XPBD_ERR_INVALID, XPBD_ERR_CUDA, XPBD_ERR_NUMERIC, XPBD_ERR_NO_DEVICE, XPBD_ERR_STATE, XPBD_ERR_CAPACITY,
+ XPBD_ERR_TIMEOUT) = range(8)
 SOLVER_GAUSS_SEIDEL, SOLVER_JACOBI = 0, 1
 CONSTRAINT_COMBINED, CONSTRAINT_SEPARATE = 0, 1
 RESIDUAL_NEVER, RESIDUAL_EVERY_SUBSTEP, RESIDUAL_EVERY_ITERATION = 0, 1, 2
@@ -57,7 +58,7 @@ class Params(C.Structure):
         ("num_iters", C.c_int32), ("solver_type", C.c_int32), ("constraint_type", C.c_int32),
         ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
         ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
-        ("gs_patch_tets", C.c_int32),
+        ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32),
     ]
 
 
