@@ -93,8 +93,12 @@ typedef struct {
     int32_t use_pdl;           /* programmatic dependent launch between kernels    */
     int32_t gs_patch_tets;     /* Gauss-Seidel patch size in tets (1..5); 0 = 5;   */
                                /* 1 = plain per-tet colouring                      */
-    int32_t gs_min_blocks;     /* patch kernel occupancy target, blocks/SM: 6 or 8 */
+    int32_t gs_min_blocks;     /* variant-1 occupancy target, blocks/SM: 6 or 8   */
                                /* (8 caps registers at 128); 0 = 6                 */
+    int32_t gs_variant;        /* sweep kernel: 0 one lane per patch, tet records  */
+                               /* prefetched into registers; 1 one lane, records   */
+                               /* staged in shared memory by bulk (TMA) copies;    */
+                               /* 2 four lanes per patch (one per tet corner)      */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -241,8 +245,9 @@ const char* xpbd_kernel_name(int32_t id);
 int xpbd_launch_count(xpbd_ctx* ctx, int64_t* n);
 /* Autotuner: builds trial contexts from the meshes, times trial_steps substeps
  * (CUDA events, graphs on) for each candidate launch configuration -- Gauss-
- * Seidel: patch size (tet colours folded into one launch) x programmatic
- * dependent launch; Jacobi: block size x scatter/gather variant x programmatic
+ * Seidel: patch size (tet colours folded into one launch) x sweep kernel
+ * variant and occupancy x programmatic dependent launch; Jacobi: block size x
+ * scatter/gather variant x programmatic
  * dependent launch -- and writes the fastest into *params. report (if
  * report_len > 0) receives a JSON list of the candidates and their ms/step. */
 int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_instances, xpbd_params* params, int32_t trial_steps,

@@ -100,19 +100,21 @@ def test_batch_full_size_runs(lib):
     s.close()
 
 
-@pytest.mark.parametrize("solver,ncand", [(G.SOLVER_GAUSS_SEIDEL, 16), (G.SOLVER_JACOBI, 12)])
+@pytest.mark.parametrize("solver,ncand", [(G.SOLVER_GAUSS_SEIDEL, 32), (G.SOLVER_JACOBI, 12)])
 def test_autotuner_times_every_candidate_and_keeps_the_fastest(lib, solver, ncand):
     b = _small_batch(n=3)
     inst = [(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances]
     best, results = G.autotune(inst, trial_steps=3, solver_type=solver, num_iters=5)
     assert len(results) == ncand and all(r["ms_per_step"] > 0 for r in results)
     fastest = min(results, key=lambda r: r["ms_per_step"])
-    keys = ["gs_patch_tets", "gs_min_blocks", "use_pdl"] if solver == G.SOLVER_GAUSS_SEIDEL else ["block_size", "jacobi_variant", "use_pdl"]
+    keys = ["gs_patch_tets", "gs_variant", "gs_min_blocks", "use_pdl"] if solver == G.SOLVER_GAUSS_SEIDEL \
+        else ["block_size", "jacobi_variant", "use_pdl"]
     for k in keys:
         assert getattr(best, k) == fastest[k]
     # the chosen configuration runs
     s = G.XPBDSolver(instances=inst, num_iters=5, solver_type=solver,
-                     **{k: getattr(best, k) for k in ["gs_patch_tets", "gs_min_blocks", "block_size", "jacobi_variant", "use_pdl"]})
+                     **{k: getattr(best, k) for k in ["gs_patch_tets", "gs_variant", "gs_min_blocks", "block_size",
+                                                      "jacobi_variant", "use_pdl"]})
     s.step(2)
     s.synchronize()
     s.close()

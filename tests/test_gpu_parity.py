@@ -68,13 +68,17 @@ def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, gpu=None, **kw):
     return mk(32), mk(64)
 
 
-@pytest.mark.parametrize("solver,cap", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 5), (G.SOLVER_GAUSS_SEIDEL, 1)])
-def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap):
+@pytest.mark.parametrize("solver,cap,var", [(G.SOLVER_JACOBI, 0, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 0),
+                                            (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1),
+                                            (G.SOLVER_GAUSS_SEIDEL, 5, 2)])
+def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap, var):
     """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise): 20 steps at the
     spec bound, then 100 steps within the FP32 band. Gauss-Seidel runs
-    with hex patches (cap 5) and with per-tet colouring (cap 1)."""
+    with hex patches (cap 5), per-tet colouring (cap 1), and every sweep
+    kernel variant (registers, shared-memory staging, four lanes per patch)."""
     w = W.cube()
-    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver, gs_patch_tets=cap)
+    s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver, gs_patch_tets=cap,
+                     gs_variant=var)
     o32, o64 = _oracle_pair(w.X, w.tets, w.faces, w.E, w.nu, w.rho, solver, 10, gpu=s)
     s.set_positions(w.x0)
     s.fix_vertices(w.fixed)
@@ -132,11 +136,12 @@ def test_gs_sweep_order_is_patch_colouring(lib, cap):
     s.close()
 
 
-@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
-def test_separate_constraints_trajectory(lib, solver):
+@pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
+                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
+def test_separate_constraints_trajectory(lib, solver, var):
     X, tets, faces, x0 = _noisy_cube(4, seed=3)
     s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=8, solver_type=solver,
-                     constraint_type=G.CONSTRAINT_SEPARATE)
+                     constraint_type=G.CONSTRAINT_SEPARATE, gs_variant=var)
     o32, o64 = _oracle_pair(X, tets, faces, 3e3, 0.45, 1000.0, solver, 8, gpu=s, ckind=O.SEPARATE)
     fixed = X[:, 2] == 0
     s.set_positions(x0); s.fix_vertices(fixed)
@@ -187,13 +192,14 @@ def test_gather_variant_is_deterministic_and_matches_atomic(lib):
     assert np.abs(runs[0] - runs[2]).max() < 1e-6
 
 
-@pytest.mark.parametrize("solver", [G.SOLVER_JACOBI, G.SOLVER_GAUSS_SEIDEL])
-def test_graph_and_direct_launch_agree(lib, solver):
+@pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
+                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
+def test_graph_and_direct_launch_agree(lib, solver, var):
     w = W.cube(n=5)
     out = []
     for graphs in (1, 0):
         s = W.make_solver(w, num_iters=4, solver_type=solver, use_graphs=graphs,
-                          jacobi_variant=G.JACOBI_GATHER)
+                          jacobi_variant=G.JACOBI_GATHER, gs_variant=var)
         s.step(15)
         out.append(s.positions())
         s.close()

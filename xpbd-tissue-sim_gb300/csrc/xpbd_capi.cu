@@ -190,7 +190,8 @@ bool valid_params(const xpbd_params& p) {
            p.max_contacts_per_face >= 0 && p.max_contacts_per_face <= kMaxSpheres &&
            (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
            p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
-           (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8);
+           (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8) &&
+           p.gs_variant >= 0 && p.gs_variant < kGsVariants;
 }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
@@ -381,7 +382,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 for (int col = 0; col < c->n_tet_colours; col++) {
                     Scope sc(c, K_PROJECT_GS);
                     launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
-                                           c->x.p, f, which, c->flags.p, c->prm.gs_min_blocks ? c->prm.gs_min_blocks : 6);
+                                           c->x.p, f, which, c->flags.p, c->prm.gs_min_blocks ? c->prm.gs_min_blocks : 6,
+                                           c->prm.gs_variant);
                 }
             }
             if (have_faces) {
@@ -787,6 +789,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->use_pdl = 1;
     p->gs_patch_tets = 0;
     p->gs_min_blocks = 0;
+    p->gs_variant = 0;
     return XPBD_OK;
 }
 
@@ -1307,11 +1310,12 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
         for (int patch : {1, 2, 3, 5})
             for (int pdl : {0, 1})
-                for (int minb : {6, 8}) {
+                for (int var_minb : {6, 16, 18, 26}) {  // variant x min blocks: (0,-) (1,6) (1,8) (2,-)
                     xpbd_params q = base;
                     q.gs_patch_tets = patch;
                     q.use_pdl = pdl;
-                    q.gs_min_blocks = minb;
+                    q.gs_variant = var_minb / 10;
+                    q.gs_min_blocks = var_minb % 10;
                     cands.push_back(q);
                 }
     } else {
@@ -1348,10 +1352,10 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
         xpbd_destroy(c);
         char buf[256];
         snprintf(buf, sizeof buf,
-                 "%s{\"gs_patch_tets\":%d,\"gs_min_blocks\":%d,\"block_size\":%d,\"jacobi_variant\":%d,"
-                 "\"use_pdl\":%d,\"ms_per_step\":%.6f}",
-                 i ? "," : "", cands[i].gs_patch_tets, cands[i].gs_min_blocks, cands[i].block_size,
-                 cands[i].jacobi_variant, cands[i].use_pdl, ms);
+                 "%s{\"gs_patch_tets\":%d,\"gs_variant\":%d,\"gs_min_blocks\":%d,\"block_size\":%d,"
+                 "\"jacobi_variant\":%d,\"use_pdl\":%d,\"ms_per_step\":%.6f}",
+                 i ? "," : "", cands[i].gs_patch_tets, cands[i].gs_variant, cands[i].gs_min_blocks,
+                 cands[i].block_size, cands[i].jacobi_variant, cands[i].use_pdl, ms);
         rep += buf;
         if (ms > 0 && ms < best) {
             best = ms;
@@ -1370,6 +1374,7 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     params->jacobi_variant = w.jacobi_variant;
     params->use_pdl = w.use_pdl;
     params->gs_min_blocks = w.gs_min_blocks;
+    params->gs_variant = w.gs_variant;
     return XPBD_OK;
 }
 

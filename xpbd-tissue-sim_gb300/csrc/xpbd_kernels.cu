@@ -710,6 +710,293 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t
         if (k < nverts) x[vid[k]] = sv[k][tid];
 }
 
+// One lane per patch, static tet records prefetched into registers before the
+// dependency wait (shortest prologue; for latency-bound sweeps).
+template <bool FIRST, int WHICH>
+__global__ void __launch_bounds__(kPatchBlock) k_project_patch_reg(TetArrays t, PatchArrays pa, int pbegin, int pend,
+                                                               float4* __restrict__ x, Flags* flags) {
+    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    const int tid = threadIdx.x;
+    const int p = pbegin + blockIdx.x * kPatchBlock + tid;
+    const bool active = p < pend;
+    int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
+    TetState<float> st[kMaxPatchTets];
+    int ntets = 0, nverts = 0;
+    if (active) {
+        meta = __ldg(pa.meta + p);
+        va = __ldg(pa.verts + 2 * (size_t)p);
+        vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+        ntets = meta.y & 0xff;
+        nverts = meta.y >> 8;
+        // static tet data does not depend on the predecessor: load it before the wait
+#pragma unroll
+        for (int i = 0; i < kMaxPatchTets; i++) {
+            if (i < ntets) {
+                int4 dummy;
+                load_tet_static(t, meta.x + i, dummy, st[i]);
+            }
+        }
+    }
+    pdl_wait_then_release();
+    if (!active) return;
+    // one round trip: all vertex and multiplier loads are issued together
+    const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+    float2 lams[kMaxPatchTets];
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++)
+        lams[i] = (!FIRST && i < ntets) ? t.lam[meta.x + i] : make_float2(0.f, 0.f);
+#pragma unroll
+    for (int k = 0; k < kMaxPatchVerts; k++)
+        if (k < nverts) sv[k][tid] = x[vid[k]];
+    const unsigned long long loc = (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++) {
+        if (i >= ntets) break;
+        const int slot = meta.x + i;
+        int l[4];
+        float4 xp[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            l[j] = (int)((loc >> (12 * i + 3 * j)) & 7ull);
+            xp[j] = sv[l[j]][tid];
+            st[i].p[j][0] = xp[j].x; st[i].p[j][1] = xp[j].y; st[i].p[j][2] = xp[j].z;
+            st[i].w[j] = fabsf(xp[j].w);
+        }
+        float2 lam = lams[i];
+        float d[4][3];
+        bool ok;
+        if (WHICH == 2) {
+            float rsq;
+            ok = project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags);
+        } else {
+            float J, r, dl;
+            const float lw = WHICH == 0 ? lam.x : lam.y;
+            tet_project_single(st[i], WHICH, lw, r, dl, d, J);
+            if (fabsf(J) < kDegenerateJ) {
+                const Fp64Out o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], WHICH, lw);
+                r = o.r0; dl = o.dl0;
+#pragma unroll
+                for (int a = 0; a < 4; a++)
+#pragma unroll
+                    for (int k = 0; k < 3; k++) d[a][k] = o.d[3 * a + k];
+                atomicAdd(&flags->degenerate, 1ull);
+            }
+            ok = isfinite(dl);
+            if (!ok) atomicAdd(&flags->nonfinite, 1ull);
+            else if (WHICH == 0) lam.x += dl;
+            else lam.y += dl;
+        }
+        if (ok) {
+#pragma unroll
+            for (int j = 0; j < 4; j++)
+                sv[l[j]][tid] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
+        }
+        t.lam[slot] = lam;
+    }
+#pragma unroll
+    for (int k = 0; k < kMaxPatchVerts; k++)
+        if (k < nverts) x[vid[k]] = sv[k][tid];
+}
+
+// register-resident selection by a lane-dependent index (no local memory)
+template <typename T>
+__device__ __forceinline__ T sel4(int j, T a, T b, T c, T d) {
+    return j == 0 ? a : (j == 1 ? b : (j == 2 ? c : d));
+}
+
+// Four lanes per patch: lane j of a patch's group owns corner j of the tet
+// being projected. F, det F and ||F|| are computed by every lane; each lane
+// forms only its corner's gradients (corner 3 through the extended row
+// Q(3,c) = -sum_i Q(i,c)), the 2x2 system is summed over the group with two
+// xor shuffles, and each lane writes its own corner. The sequential order of
+// tets within a patch (and of patches within a colour) is that of the
+// one-lane kernel, so results differ only by FP32 summation order.
+template <bool FIRST, int WHICH>
+__global__ void __launch_bounds__(4 * kPatchBlock) k_project_patch_x4(TetArrays t, PatchArrays pa, int pbegin,
+                                                                     int pend, float4* __restrict__ x, Flags* flags) {
+    __shared__ __align__(128) float4 sq[3][kPatchBlock * kMaxPatchTets];
+    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    __shared__ __align__(8) unsigned long long bar;
+    __shared__ int s_first;
+    const int tid = threadIdx.x;
+    const int pl = tid >> 2;  // patch within the block
+    const int j = tid & 3;    // corner owned by this lane
+    const unsigned gmask = 0xFu << (threadIdx.x & 28);
+    const int p0 = pbegin + blockIdx.x * kPatchBlock;
+    const int p = p0 + pl;
+    const bool active = p < pend;
+    if (tid == 0) mbar_init(&bar, 1);
+    __syncthreads();
+    if (tid == 0) {
+        const int plast = min(p0 + kPatchBlock - 1, pend - 1);
+        const int4 m0 = __ldg(pa.meta + p0), m1 = __ldg(pa.meta + plast);
+        const int s0 = m0.x, s1 = m1.x + (m1.y & 0xff);
+        const unsigned bytes = (unsigned)(s1 - s0) * 16u;
+        s_first = s0;
+        mbar_arrive_expect_tx(&bar, 3u * bytes);
+        tma_load_1d(sq[0], t.q0 + s0, bytes, &bar);
+        tma_load_1d(sq[1], t.q1 + s0, bytes, &bar);
+        tma_load_1d(sq[2], t.q2 + s0, bytes, &bar);
+    }
+    int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
+    int ntets = 0, nverts = 0;
+    if (active) {
+        meta = __ldg(pa.meta + p);
+        va = __ldg(pa.verts + 2 * (size_t)p);
+        vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+        ntets = meta.y & 0xff;
+        nverts = meta.y >> 8;
+    }
+    pdl_wait_then_release();
+    // lane j stages vertices j and j + 4; lane 0 holds the patch's multipliers
+    const int my_v0 = sel4(j, va.x, va.y, va.z, va.w), my_v1 = sel4(j, vb.x, vb.y, vb.z, vb.w);
+    if (j < nverts) sv[j][pl] = x[my_v0];
+    if (j + 4 < nverts) sv[j + 4][pl] = x[my_v1];
+    float2 lams[kMaxPatchTets];
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++)
+        lams[i] = (!FIRST && j == 0 && i < ntets) ? t.lam[meta.x + i] : make_float2(0.f, 0.f);
+    __syncthreads();  // s_first and the staged vertices are visible
+    const bool staged = mbar_wait_bounded(&bar, 0, kWaitLimit);
+    if (!staged) {
+        if (tid == 0) {
+            atomicAdd(&flags->timeouts, 1ull);
+            mbar_wait_bounded(&bar, 0, kWaitLimit);
+        }
+        return;
+    }
+    if (!active) return;
+    const int base = meta.x - s_first;
+    const unsigned long long loc = (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++) {
+        if (i >= ntets) break;
+        const int slot = meta.x + i;
+        TetState<float> st;
+        {
+            const float4 a = sq[0][base + i], b = sq[1][base + i], c = sq[2][base + i];
+            st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
+            st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
+            st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
+        }
+        float4 xp[4];
+        int l[4];
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            l[k] = (int)((loc >> (12 * i + 3 * k)) & 7ull);
+            xp[k] = sv[l[k]][pl];
+            st.p[k][0] = xp[k].x; st.p[k][1] = xp[k].y; st.p[k][2] = xp[k].z;
+            st.w[k] = fabsf(xp[k].w);
+        }
+        float F[9];
+        tet_F(st, F);
+        float Fc[9];
+        Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
+        Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
+        Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
+        const float J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
+        // this lane's row of Q (corner 3: minus the sum of the other rows)
+        float qr[3];
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            const float q0 = st.q[3 * c], q1 = st.q[3 * c + 1], q2 = st.q[3 * c + 2];
+            qr[c] = j == 0 ? q0 : (j == 1 ? q1 : (j == 2 ? q2 : -((q0 + q1) + q2)));
+        }
+        const float4 me = sel4(j, xp[0], xp[1], xp[2], xp[3]);
+        const int lj = sel4(j, l[0], l[1], l[2], l[3]);
+        const float wj = fabsf(me.w);
+        float2 lam = lams[i];
+        float dj[3] = {0.f, 0.f, 0.f};
+        bool ok = true;
+        if (fabsf(J) >= kDegenerateJ) {
+            float g1[3], g2[3];
+            float Cd = 0.f, Ch = 0.f, invC = 0.f, fac = 0.f;
+            if (WHICH != 1) {
+                const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
+                                  (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
+                invC = rsqrtf(ss);
+                Cd = ss * invC;
+            }
+            if (WHICH != 0) {
+                if (J >= 1.f) {
+                    Ch = -st.gam + logf(J);
+                    fac = __frcp_rn(J);
+                } else {
+                    const float dd = J - 1.f;
+                    Ch = -st.gam + dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f);
+                    fac = fmaf(dd, dd, 1.f - dd);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) {
+                g1[k] = invC * fmaf(F[k], qr[0], fmaf(F[3 + k], qr[1], F[6 + k] * qr[2]));
+                g2[k] = fac * fmaf(Fc[k], qr[0], fmaf(Fc[3 + k], qr[1], Fc[6 + k] * qr[2]));
+            }
+            if (WHICH == 2) {
+                float aa = wj * dot3(g1, g1), ab = wj * dot3(g1, g2), bb = wj * dot3(g2, g2);
+                aa += __shfl_xor_sync(gmask, aa, 1);
+                ab += __shfl_xor_sync(gmask, ab, 1);
+                bb += __shfl_xor_sync(gmask, bb, 1);
+                aa += __shfl_xor_sync(gmask, aa, 2);
+                ab += __shfl_xor_sync(gmask, ab, 2);
+                bb += __shfl_xor_sync(gmask, bb, 2);
+                const float L00 = st.atd + aa, L01 = ab, L11 = st.ath + bb;
+                const float r0 = fmaf(st.atd, lam.x, Cd), r1 = fmaf(st.ath, lam.y, Ch);
+                const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
+                const float dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
+                const float dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
+                ok = isfinite(dl0) && isfinite(dl1);
+                if (ok) {
+                    lam.x += dl0;
+                    lam.y += dl1;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) dj[k] = wj * fmaf(g1[k], dl0, g2[k] * dl1);
+                }
+            } else {
+                const float* g = WHICH == 0 ? g1 : g2;
+                const float at = WHICH == 0 ? st.atd : st.ath;
+                const float C = WHICH == 0 ? Cd : Ch;
+                float gg = wj * dot3(g, g);
+                gg += __shfl_xor_sync(gmask, gg, 1);
+                gg += __shfl_xor_sync(gmask, gg, 2);
+                const float lw = WHICH == 0 ? lam.x : lam.y;
+                const float dl = -fmaf(at, lw, C) / (at + gg);
+                ok = isfinite(dl);
+                if (ok) {
+                    if (WHICH == 0) lam.x += dl;
+                    else lam.y += dl;
+#pragma unroll
+                    for (int k = 0; k < 3; k++) dj[k] = wj * g[k] * dl;
+                }
+            }
+        } else {
+            // near-degenerate: every lane runs the FP64 projection and keeps its corner
+            Fp64Out o;
+            if (WHICH == 2) {
+                o = project_combined_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], lam.x, lam.y);
+                ok = isfinite(o.dl0) && isfinite(o.dl1);
+                if (ok) { lam.x += o.dl0; lam.y += o.dl1; }
+            } else {
+                o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], WHICH, WHICH == 0 ? lam.x : lam.y);
+                ok = isfinite(o.dl0);
+                if (ok) { if (WHICH == 0) lam.x += o.dl0; else lam.y += o.dl0; }
+            }
+#pragma unroll
+            for (int k = 0; k < 3; k++) dj[k] = sel4(j, o.d[k], o.d[3 + k], o.d[6 + k], o.d[9 + k]);
+            if (j == 0) atomicAdd(&flags->degenerate, 1ull);
+        }
+        if (ok) {
+            sv[lj][pl] = make_float4(me.x + dj[0], me.y + dj[1], me.z + dj[2], me.w);
+        } else if (j == 0) {
+            atomicAdd(&flags->nonfinite, 1ull);
+        }
+        if (j == 0) t.lam[slot] = lam;
+        __syncwarp(gmask);
+    }
+    if (j < nverts) x[my_v0] = sv[j][pl];
+    if (j + 4 < nverts) x[my_v1] = sv[j + 4][pl];
+}
+
 // Static collision projection of one contact slot: C = n.(u x1 + v x2 + w x3 - p),
 // skipped when C > 0, alpha = 0. Returns false when skipped.
 __device__ __forceinline__ bool contact_update(const ContactArrays& c, int slot, const float4 xs[3], float d[3][3],
@@ -1014,10 +1301,26 @@ void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, f
 }
 
 void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
-                            float4* x, bool first, int which, Flags* flags, int min_blocks) {
+                            float4* x, bool first, int which, Flags* flags, int min_blocks, int variant) {
     const int n = pend - pbegin;
     if (n <= 0) return;
     const int g = nblk(n, kPatchBlock);
+    if (variant == 0) {
+#define XG_PATCHR(F, W) go(k_project_patch_reg<F, W>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
+        if (which == 2) { if (first) XG_PATCHR(true, 2); else XG_PATCHR(false, 2); }
+        else if (which == 0) { if (first) XG_PATCHR(true, 0); else XG_PATCHR(false, 0); }
+        else { if (first) XG_PATCHR(true, 1); else XG_PATCHR(false, 1); }
+#undef XG_PATCHR
+        return;
+    }
+    if (variant == 2) {
+#define XG_PATCH4(F, W) go(k_project_patch_x4<F, W>, g, 4 * kPatchBlock, s, t, pa, pbegin, pend, x, flags)
+        if (which == 2) { if (first) XG_PATCH4(true, 2); else XG_PATCH4(false, 2); }
+        else if (which == 0) { if (first) XG_PATCH4(true, 0); else XG_PATCH4(false, 0); }
+        else { if (first) XG_PATCH4(true, 1); else XG_PATCH4(false, 1); }
+#undef XG_PATCH4
+        return;
+    }
 #define XG_PATCH(F, W, M) go(k_project_patch<F, W, M>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
 #define XG_PATCH_M(F, W) do { if (min_blocks == 8) XG_PATCH(F, W, 8); else XG_PATCH(F, W, 6); } while (0)
     if (which == 2) { if (first) XG_PATCH_M(true, 2); else XG_PATCH_M(false, 2); }

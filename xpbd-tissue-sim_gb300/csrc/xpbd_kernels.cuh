@@ -58,6 +58,10 @@ struct ContactArrays {
 constexpr int kMaxPatchTets = 5;
 constexpr int kMaxPatchVerts = 8;
 constexpr int kPatchBlock = 64;
+// Gauss-Seidel sweep kernels: 0 one lane per patch, static tet records
+// prefetched into registers; 1 one lane per patch, records staged in shared
+// memory by bulk copies; 2 four lanes per patch (one per tet corner), staged.
+constexpr int kGsVariants = 3;
 struct PatchArrays {
     const int4* meta;   // [P] x: first slot, y: ntets | nverts << 8, z/w: local vertex ids, 3 bits per
                         //     (tet i, corner j) at bit 12 i + 3 j of the 64-bit word (z low, w high)
@@ -100,7 +104,7 @@ void launch_gather_apply(const Launch& s, float4* x, const float4* dxt, const in
 void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, float4* vel, bool final_step,
                   float dt, bool write_vel);
 void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
-                            float4* x, bool first, int which, Flags* flags, int min_blocks);
+                            float4* x, bool first, int which, Flags* flags, int min_blocks, int variant);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);

@@ -58,7 +58,7 @@ class Params(C.Structure):
         ("num_iters", C.c_int32), ("solver_type", C.c_int32), ("constraint_type", C.c_int32),
         ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
         ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
-        ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32),
+        ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32), ("gs_variant", C.c_int32),
     ]
 
 
