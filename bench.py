@@ -357,8 +357,8 @@ def run_ours(args):
         extra["use_pdl"] = 0
     if args.min_blocks:
         extra["gs_min_blocks"] = args.min_blocks
-    if args.lanes:
-        extra["gs_variant"] = args.lanes
+    if args.variant is not None:
+        extra["gs_variant"] = args.variant
     s = W.make_solver(w, **extra)
     step_no = 0
 
@@ -510,7 +510,7 @@ def main():
     ap.add_argument("--patch-tets", type=int, default=None, help="Gauss-Seidel patch size (1 = per-tet colouring)")
     ap.add_argument("--no-pdl", action="store_true", help="disable programmatic dependent launch")
     ap.add_argument("--min-blocks", type=int, default=0, choices=[0, 6, 8], help="patch kernel blocks/SM target")
-    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2], help="Gauss-Seidel sweep kernel variant")
+    ap.add_argument("--variant", type=int, default=None, choices=[0, 1], help="Gauss-Seidel sweep kernel variant")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

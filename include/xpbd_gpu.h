@@ -97,8 +97,7 @@ typedef struct {
                                /* (8 caps registers at 128); 0 = 6                 */
     int32_t gs_variant;        /* sweep kernel: 0 one lane per patch, tet records  */
                                /* prefetched into registers; 1 one lane, records   */
-                               /* staged in shared memory by bulk (TMA) copies;    */
-                               /* 2 four lanes per patch (one per tet corner)      */
+                               /* staged in shared memory by bulk (TMA) copies     */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -255,6 +254,52 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_instances, xpbd_params
 /* the context's CUDA stream (a cudaStream_t), for callers that time or order
  * their own work against the solver's */
 int xpbd_get_stream(xpbd_ctx* ctx, void** stream);
+
+/* ---- Learned warm start (no counterpart in the reference) ----
+ * A per-tet network, 14 -> 64 -> 64 -> 64 -> 2 with SiLU, maps features taken
+ * right after position prediction -- F (9, column-major), alpha~_d lambda_d
+ * and alpha~_h lambda_h of the previous substep, log10(E)/5, nu, 1e3 dt
+ * (alpha~ = alpha / dt^2) -- to alpha~ lambda of this substep's solution. It
+ * runs on the tensor cores (BF16 operands, FP32 accumulation) and trains online
+ * with Adam on (features, solved multipliers) pairs recorded from the
+ * solver's own substeps.
+ * A warm start sets lambda_0 and moves the predicted positions by
+ * M^-1 grad C(x_pred)^T lambda_0; when that leaves a larger constraint residual
+ * than the plain start, ||r(x_warm, lambda_0)|| > ||r(x_pred, 0)||, the substep
+ * falls back on the device to (x_pred, lambda = 0). With a residual policy
+ * other than "never", record 0 of the history stays ||r(x_pred, 0)|| so
+ * relative residuals compare with the plain solver's. */
+#define XPBD_MLP_INPUTS 16    /* feature row: 14 features + 2 zero pads       */
+#define XPBD_MLP_PARAMS 9538  /* W1 64x16, b1, W2 64x64, b2, W3 64x64, b3,   */
+                              /* W4 2x64, b4; each W row-major (out x in)     */
+#define XPBD_WARM_NONE 0      /* lambda_0 = 0 (the reference's start)         */
+#define XPBD_WARM_PREVIOUS 1  /* lambda_0 = the previous substep's lambda     */
+#define XPBD_WARM_MLP 2       /* lambda_0 = the network's prediction          */
+/* He-normal initial parameters from seed; resets the Adam state */
+int xpbd_mlp_init(xpbd_ctx* ctx, uint64_t seed);
+int xpbd_mlp_set_params(xpbd_ctx* ctx, const float* params, int64_t n);  /* n = XPBD_MLP_PARAMS */
+int xpbd_mlp_get_params(xpbd_ctx* ctx, float* params, int64_t n);
+/* network output (n x 2) for host feature rows (n x XPBD_MLP_INPUTS, rounded
+ * to BF16 on upload) */
+int xpbd_mlp_forward(xpbd_ctx* ctx, const float* X, int64_t n, float* out);
+/* mean squared error over n rows and its gradient (XPBD_MLP_PARAMS floats,
+ * either output may be NULL); the gradient stays on the device for
+ * xpbd_mlp_adam_step(ctx, NULL, lr) */
+int xpbd_mlp_loss_grad(xpbd_ctx* ctx, const float* X, const float* Y, int64_t n, double* loss, float* grad);
+/* one Adam step (beta 0.9 / 0.999, eps 1e-8) with grad, or with the device
+ * gradient of the last loss evaluation when grad is NULL */
+int xpbd_mlp_adam_step(xpbd_ctx* ctx, const float* grad, float lr);
+/* on = 1: every substep keeps its features and solved alpha~ lambda (the
+ * training pairs of the last substep) */
+int xpbd_mlp_record(xpbd_ctx* ctx, int32_t on);
+/* the recorded pairs in tet order: X (T x XPBD_MLP_INPUTS), Y (T x 2); either may be NULL */
+int xpbd_mlp_get_samples(xpbd_ctx* ctx, float* X, float* Y);
+/* epochs of minibatch Adam over the recorded pairs (batch rows per step);
+ * *loss = mean squared error of the last epoch, taken before each step */
+int xpbd_mlp_train(xpbd_ctx* ctx, int32_t epochs, int32_t batch, float lr, double* loss);
+int xpbd_set_warm_start(xpbd_ctx* ctx, int32_t mode);
+/* warm starts kept / rejected by the residual test since creation */
+int xpbd_warm_start_stats(xpbd_ctx* ctx, int64_t* kept, int64_t* rejected);
 
 #ifdef __cplusplus
 }

@@ -69,8 +69,7 @@ def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, gpu=None, **kw):
 
 
 @pytest.mark.parametrize("solver,cap,var", [(G.SOLVER_JACOBI, 0, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 0),
-                                            (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1),
-                                            (G.SOLVER_GAUSS_SEIDEL, 5, 2)])
+                                            (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1)])
 def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap, var):
     """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise): 20 steps at the
     spec bound, then 100 steps within the FP32 band. Gauss-Seidel runs
@@ -137,7 +136,7 @@ def test_gs_sweep_order_is_patch_colouring(lib, cap):
 
 
 @pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
-                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
+                                        (G.SOLVER_GAUSS_SEIDEL, 1)])
 def test_separate_constraints_trajectory(lib, solver, var):
     X, tets, faces, x0 = _noisy_cube(4, seed=3)
     s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=8, solver_type=solver,
@@ -193,7 +192,7 @@ def test_gather_variant_is_deterministic_and_matches_atomic(lib):
 
 
 @pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
-                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
+                                        (G.SOLVER_GAUSS_SEIDEL, 1)])
 def test_graph_and_direct_launch_agree(lib, solver, var):
     w = W.cube(n=5)
     out = []

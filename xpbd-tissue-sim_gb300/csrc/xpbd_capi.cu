@@ -17,168 +17,12 @@
 #include <vector>
 
 #include "../../include/xpbd_gpu.h"
+#include "xpbd_ctx.cuh"
 #include "xpbd_kernels.cuh"
 
 using namespace xg;
 
 namespace {
-
-template <typename T>
-struct DevBuf {
-    T* p = nullptr;
-    size_t n = 0;
-    cudaError_t alloc(size_t count) {
-        n = count;
-        if (count == 0) return cudaSuccess;
-        return cudaMalloc((void**)&p, count * sizeof(T));
-    }
-    void release() {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-};
-
-struct Prof {
-    bool on = false;
-    std::vector<cudaEvent_t> pool;
-    std::vector<int> ids;  // kernel id per recorded pair
-    size_t used = 0;
-};
-
-}  // namespace
-
-struct xpbd_ctx {
-    xpbd_params prm{};
-    int V = 0, T = 0, F = 0;
-    int block = 256;
-    cudaStream_t stream = nullptr;
-    std::string err;
-    long long launches = 0;
-
-    // host mirrors
-    std::vector<double> inv_mass_h;     // V, positive
-    std::vector<uint8_t> fixed_h;       // V
-    std::vector<double> mass_h;         // V
-    std::vector<int> tet_of_slot;       // T
-    std::vector<int> tets_h, faces_h;   // 4T, 3F (original order)
-    std::vector<int> tet_colour;        // T, by original index
-    std::vector<int> fcol_off;          // face colour ranges over face_list
-    int n_tet_colours = 1, n_face_colours = 0;
-    std::vector<float> alpha_t_d, alpha_t_h;  // per slot, for energy
-
-    // device state
-    DevBuf<float4> x, prev, vel, dx, dxt;
-    DevBuf<int4> tet_idx;
-    DevBuf<float4> q0, q1, q2;
-    DevBuf<float2> lam;
-    DevBuf<int> perm, csr_off, csr_ent;
-    DevBuf<int4> faces;
-    DevBuf<int> face_list;
-    DevBuf<int4> patch_meta, patch_verts;
-    std::vector<int> pcol_off;           // patch colour ranges (Gauss-Seidel)
-    DevBuf<float4> c_bary, c_p, c_n;
-    DevBuf<float> c_lam;
-    int S = 4;
-    // instances (batched objects): offsets into the concatenated arrays
-    int n_inst = 1;
-    std::vector<int64_t> voff, toff, foff;
-    std::vector<float4> sphere_tab_h;  // [n_inst * S], radius < 0 = empty
-    DevBuf<float4> sphere_tab;
-    DevBuf<int> face_inst;
-    bool sphere_dirty = true;
-    int n_spheres_total = 0;
-    DevBuf<int> kin_idx;
-    DevBuf<float4> kin_rest;
-    int nkin = 0;
-    DevBuf<Flags> flags;
-    DevBuf<double> res_partial, res_rows, energy_partial;
-    DevBuf<float> rvec;
-    int res_stride = 0;   // doubles per residual row
-    bool have_rvec = false;
-    std::vector<int> api_slots;  // contacts added through the API per face
-
-    // pinned staging
-    float4* h_stage = nullptr;
-    double* h_rows = nullptr;
-    int h_rows_cap = 0;
-    int last_rows = 0;
-    bool rows_pending = false;
-
-    // host simulation clock (Simulation.cpp:197-276)
-    double time = 0, last_cd = 0;
-
-    // graphs: [write_vel]
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    long long graph_kernels[2] = {0, 0};  // kernels captured in each graph
-    bool graph_dirty = true;
-
-    Prof prof;
-
-    TetArrays tets() {
-        return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
-    }
-    Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
-    PatchArrays patches() const { return PatchArrays{patch_meta.p, patch_verts.p}; }
-    ContactArrays contacts() {
-        return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
-    }
-};
-
-namespace {
-
-int fail(xpbd_ctx* c, int code, const char* fmt, ...) {
-    if (c) {
-        char buf[512];
-        va_list ap;
-        va_start(ap, fmt);
-        vsnprintf(buf, sizeof buf, fmt, ap);
-        va_end(ap);
-        c->err = buf;
-    }
-    return code;
-}
-
-int cuda_check(xpbd_ctx* c, cudaError_t e, const char* what) {
-    if (e == cudaSuccess) return XPBD_OK;
-    return fail(c, XPBD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-}
-
-#define XPBD_CU(ctx, call)                                         \
-    do {                                                           \
-        int _st = cuda_check((ctx), (call), #call);                \
-        if (_st != XPBD_OK) return _st;                            \
-    } while (0)
-
-int after_launches(xpbd_ctx* c, const char* what) {
-    return cuda_check(c, cudaGetLastError(), what);
-}
-
-// ---- profiling brackets (only when prof.on) ----
-void prof_begin(xpbd_ctx* c, int id) {
-    if (!c->prof.on) return;
-    if (c->prof.used + 2 > c->prof.pool.size()) {
-        size_t old = c->prof.pool.size();
-        c->prof.pool.resize(std::max<size_t>(256, old * 2));
-        for (size_t i = old; i < c->prof.pool.size(); i++) cudaEventCreate(&c->prof.pool[i]);
-    }
-    cudaEventRecord(c->prof.pool[c->prof.used], c->stream);
-    c->prof.ids.push_back(id);
-}
-void prof_end(xpbd_ctx* c) {
-    if (!c->prof.on) return;
-    cudaEventRecord(c->prof.pool[c->prof.used + 1], c->stream);
-    c->prof.used += 2;
-}
-
-struct Scope {
-    xpbd_ctx* c;
-    Scope(xpbd_ctx* c_, int id) : c(c_) {
-        prof_begin(c, id);
-        c->launches++;
-    }
-    ~Scope() { prof_end(c); }
-};
 
 bool valid_params(const xpbd_params& p) {
     return p.dt > 0 && std::isfinite(p.dt) && std::isfinite(p.g_accel) && p.num_iters >= 0 &&
@@ -311,6 +155,52 @@ void exact_residual_row(xpbd_ctx* c, int row, bool with_vec) {
                     (float)(c->prm.dt * c->prm.dt));
 }
 
+// r(x, 0): the residual at the current positions with every multiplier 0
+void zero_lambda_residual_row(xpbd_ctx* c, int row) {
+    Scope s(c, K_RESIDUAL);
+    launch_residual(c->L(), c->block, c->tets(), c->T, c->x.p, c->prm.constraint_type == XPBD_CONSTRAINT_SEPARATE,
+                    c->perm.p, nullptr, sink(c, row, 0), nullptr, (float)(c->prm.dt * c->prm.dt), true);
+}
+
+// network features of every tet at the predicted positions
+void enqueue_features(xpbd_ctx* c) {
+    Scope sc(c, K_WARM);
+    launch_mlp_features(c->L(), c->tets(), c->x.p, c->mat.p, (float)(c->prm.dt * 1e3), 0, c->T, c->feat.p);
+}
+
+// Warm start of one substep (after prediction): lambda_0 from the network or
+// the previous substep, x += M^-1 grad C^T lambda_0, and the residual-triggered
+// fallback to (x_pred, lambda = 0) when ||r(x_warm, lambda_0)|| > ||r(x_pred, 0)||.
+void enqueue_warm_start(xpbd_ctx* c) {
+    cudaStream_t s = c->stream;
+    const bool mlp = c->warm_mode == XPBD_WARM_MLP;
+    const int r0 = c->prm.num_iters + 2;  // two scratch rows past the history
+    double* rows = c->res_partial.p + (size_t)r0 * c->res_stride;
+    cudaMemsetAsync(rows, 0, sizeof(double) * 2 * (size_t)c->res_stride, s);
+    if (mlp || c->record) enqueue_features(c);
+    if (mlp) {
+        Scope sc(c, K_MLP);
+        launch_mlp_forward(s, c->feat.p, c->T, c->net(), c->pred.p, nullptr, &c->flags.p->timeouts);
+    }
+    zero_lambda_residual_row(c, r0);
+    cudaMemcpyAsync(c->x_pred.p, c->x.p, sizeof(float4) * (size_t)c->V, cudaMemcpyDeviceToDevice, s);
+    {
+        Scope sc(c, K_WARM);
+        launch_warm_start(c->L(), c->tets(), c->T, mlp ? c->pred.p : nullptr, c->x.p, c->dx.p);
+    }
+    {
+        Scope sc(c, K_APPLY);
+        launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, false, (float)c->prm.dt, false);
+    }
+    exact_residual_row(c, r0 + 1, false);
+    {
+        Scope sc(c, K_REDUCE);
+        launch_reduce_rows(c->L(), rows, 2, c->res_stride, c->warm_rows.p);
+    }
+    Scope sc(c, K_WARM);
+    launch_warm_fallback(c->L(), c->warm_rows.p, c->x.p, c->x_pred.p, c->lam.p, c->V, c->T, c->warm_stats.p);
+}
+
 // ---- the substep body (XPBDMeshObject_::update, XPBDMeshObject.cpp:426-505) ----
 int enqueue_update(xpbd_ctx* c, bool write_vel) {
     const xpbd_params& p = c->prm;
@@ -327,18 +217,27 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         Scope sc(c, K_PREDICT);
         launch_predict(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
     }
-    if (track) {
+    const bool warm = c->warm_mode != XPBD_WARM_NONE;
+    if (track) cudaMemsetAsync(c->res_partial.p, 0, sizeof(double) * (size_t)c->res_stride * (iters + 1), s);
+    if (warm) {
+        // r(x_pred, 0) before the warm start moves anything
+        if (track && !every_iter) zero_lambda_residual_row(c, 0);
+        enqueue_warm_start(c);
+    } else {
+        // features read the previous substep's multipliers: before the reset
+        if (c->record) enqueue_features(c);
         // lambda <- 0 (XPBDSolver.hpp:71-77) before the r(x_pred, 0) evaluation
-        cudaMemsetAsync(c->lam.p, 0, sizeof(float2) * (size_t)c->T, s);
-        cudaMemsetAsync(c->res_partial.p, 0, sizeof(double) * (size_t)c->res_stride * (iters + 1), s);
+        if (track) cudaMemsetAsync(c->lam.p, 0, sizeof(float2) * (size_t)c->T, s);
     }
     const bool jacobi = p.solver_type == XPBD_SOLVER_JACOBI;
     const bool fuse_final = !track;
     if (jacobi) {
         const bool gather = p.jacobi_variant == XPBD_JACOBI_GATHER;
-        if (track && !every_iter) exact_residual_row(c, 0, false);
+        if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
-            const bool first = it == 0;
+            // a warm start keeps its multipliers: no iteration treats lambda as 0
+            const bool first = it == 0 && !warm;
+            const bool first_contact = it == 0;
             const ResidualSink rs = every_iter ? sink(c, it, 0) : no_sink();
             const bool last = it == iters - 1;
             if (gather) {
@@ -349,7 +248,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 }
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
-                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first);
+                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
                 Scope sc(c, K_GATHER);
                 launch_gather_apply(c->L(), c->x.p, c->dxt.p, c->csr_off.p, c->csr_ent.p, c->dx.p, c->V, c->prev.p,
@@ -362,14 +261,14 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 }
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
-                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first);
+                    launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
                 Scope sc(c, K_APPLY);
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
     } else {
-        if (track && !every_iter) exact_residual_row(c, 0, false);
+        if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
             const bool first = it == 0;
             if (every_iter) exact_residual_row(c, it, false);
@@ -378,7 +277,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 const int which = separate ? pass : 2;
                 // in the separate form the second pass (Hyd) of iteration 0
                 // must not re-zero the Dev multipliers updated by pass 0
-                const bool f = first && (!separate || pass == 0);
+                const bool f = first && !warm && (!separate || pass == 0);
                 for (int col = 0; col < c->n_tet_colours; col++) {
                     Scope sc(c, K_PROJECT_GS);
                     launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
@@ -393,6 +292,10 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 }
             }
         }
+    }
+    if (c->record) {
+        Scope sc(c, K_WARM);
+        launch_mlp_targets(c->L(), c->tets(), 0, c->T, c->target.p);
     }
     if (track) {
         exact_residual_row(c, iters, true);
@@ -410,9 +313,9 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
 }
 
 int prepare_update(xpbd_ctx* c) {
-    if (tracking(c)) {
-        // one extra row for on-demand residual queries
-        int st = ensure_residual_rows(c, c->prm.num_iters + 2);
+    if (tracking(c) || c->warm_mode != XPBD_WARM_NONE) {
+        // one extra row for on-demand residual queries, two for the warm start
+        int st = ensure_residual_rows(c, c->prm.num_iters + 4);
         if (st) return st;
     }
     return XPBD_OK;
@@ -457,6 +360,7 @@ int run_update(xpbd_ctx* c, bool write_vel) {
     }
     c->rows_pending = tracking(c);
     c->last_rows = c->prm.num_iters + 1;
+    if (c->record) c->recorded = true;
     if (tracking(c)) c->have_rvec = true;
     return after_launches(c, "update");
 }
@@ -508,6 +412,10 @@ void release(xpbd_ctx* c) {
     c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
+    c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
+    c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
+    c->x_pred.release(); c->warm_stats.release(); c->warm_rows.release(); c->mse.release();
+    c->cache_z.release(); c->cache_out.release(); c->cache_a.release();
     if (c->h_stage) cudaFreeHost(c->h_stage);
     if (c->h_rows) cudaFreeHost(c->h_rows);
     c->h_stage = nullptr;
@@ -646,6 +554,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     const double dt2 = p.dt * p.dt;
     std::vector<int4> hidx(T);
     std::vector<float4> h0(T), h1(T), h2(T);
+    std::vector<float2> hmat(T);
     c->alpha_t_d.resize(T);
     c->alpha_t_h.resize(T);
     for (int sidx = 0; sidx < T; sidx++) {
@@ -659,6 +568,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         h2[sidx] = make_float4((float)q[8], atd, ath, (float)gm[t]);
         c->alpha_t_d[sidx] = atd;
         c->alpha_t_h[sidx] = ath;
+        hmat[sidx] = make_float2((float)(std::log10(Ecat[t]) / 5.0), (float)nucat[t]);
     }
 
     // faces and their colouring (Gauss-Seidel contact order)
@@ -704,6 +614,10 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     XPBD_CU(c, c->lam.alloc(T));
     XPBD_CU(c, c->perm.alloc(T));
     XPBD_CU(c, c->flags.alloc(1));
+    XPBD_CU(c, c->mat.alloc(T));
+    XPBD_CU(c, c->warm_stats.alloc(2));
+    XPBD_CU(c, c->warm_rows.alloc(2));
+    XPBD_CU(c, c->mse.alloc(1));
     XPBD_CU(c, c->rvec.alloc(2 * (size_t)T));
     XPBD_CU(c, c->energy_partial.alloc(residual_blocks(T, c->block) + 1));
     XPBD_CU(c, cudaMallocHost((void**)&c->h_stage, sizeof(float4) * (size_t)std::max(V, 1)));
@@ -741,6 +655,8 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     XPBD_CU(c, cudaMemcpy(c->q1.p, h1.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->q2.p, h2.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->perm.p, c->tet_of_slot.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->mat.p, hmat.data(), sizeof(float2) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemset(c->warm_stats.p, 0, 2 * sizeof(unsigned long long)));
     XPBD_CU(c, cudaMemset(c->lam.p, 0, sizeof(float2) * T));
     XPBD_CU(c, cudaMemset(c->dx.p, 0, sizeof(float4) * V));
     XPBD_CU(c, cudaMemset(c->vel.p, 0, sizeof(float4) * V));
@@ -1260,7 +1176,8 @@ int xpbd_get_sweep_order(xpbd_ctx* c, int32_t* order) {
 
 static const char* kNames[K_COUNT] = {"predict",  "project_jacobi", "apply",    "project_gs",
                                       "contacts", "detect",         "finalize", "residual",
-                                      "reduce",   "kinematic",      "gather_apply", "velocity"};
+                                      "reduce",   "kinematic",      "gather_apply", "velocity",
+                                      "warm_start", "mlp"};
 
 const char* xpbd_kernel_name(int32_t id) { return (id >= 0 && id < K_COUNT) ? kNames[id] : "?"; }
 
@@ -1310,7 +1227,7 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
         for (int patch : {1, 2, 3, 5})
             for (int pdl : {0, 1})
-                for (int var_minb : {6, 16, 18, 26}) {  // variant x min blocks: (0,-) (1,6) (1,8) (2,-)
+                for (int var_minb : {6, 16, 18}) {  // variant x min blocks: (0,-) (1,6) (1,8)
                     xpbd_params q = base;
                     q.gs_patch_tets = patch;
                     q.use_pdl = pdl;

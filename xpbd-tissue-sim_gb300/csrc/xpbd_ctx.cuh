@@ -1,0 +1,210 @@
+// Private host-side state of one solver context (the opaque xpbd_ctx of
+// include/xpbd_gpu.h) and the error / profiling helpers shared by the C ABI
+// translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <string>
+#include <vector>
+
+#include "../../include/xpbd_gpu.h"
+#include "xpbd_kernels.cuh"
+
+namespace xg {
+
+template <typename T>
+struct DevBuf {
+    T* p = nullptr;
+    size_t n = 0;
+    cudaError_t alloc(size_t count) {
+        n = count;
+        if (count == 0) return cudaSuccess;
+        return cudaMalloc((void**)&p, count * sizeof(T));
+    }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct Prof {
+    bool on = false;
+    std::vector<cudaEvent_t> pool;
+    std::vector<int> ids;  // kernel id per recorded pair
+    size_t used = 0;
+};
+
+}  // namespace xg
+
+using xg::DevBuf;
+using xg::Flags;
+using xg::Launch;
+using xg::PatchArrays;
+using xg::Prof;
+using xg::TetArrays;
+using xg::ContactArrays;
+
+struct xpbd_ctx {
+    xpbd_params prm{};
+    int V = 0, T = 0, F = 0;
+    int block = 256;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    long long launches = 0;
+
+    // host mirrors
+    std::vector<double> inv_mass_h;     // V, positive
+    std::vector<uint8_t> fixed_h;       // V
+    std::vector<double> mass_h;         // V
+    std::vector<int> tet_of_slot;       // T
+    std::vector<int> tets_h, faces_h;   // 4T, 3F (original order)
+    std::vector<int> tet_colour;        // T, by original index
+    std::vector<int> fcol_off;          // face colour ranges over face_list
+    int n_tet_colours = 1, n_face_colours = 0;
+    std::vector<float> alpha_t_d, alpha_t_h;  // per slot, for energy
+
+    // device state
+    DevBuf<float4> x, prev, vel, dx, dxt;
+    DevBuf<int4> tet_idx;
+    DevBuf<float4> q0, q1, q2;
+    DevBuf<float2> lam;
+    DevBuf<int> perm, csr_off, csr_ent;
+    DevBuf<int4> faces;
+    DevBuf<int> face_list;
+    DevBuf<int4> patch_meta, patch_verts;
+    std::vector<int> pcol_off;           // patch colour ranges (Gauss-Seidel)
+    DevBuf<float4> c_bary, c_p, c_n;
+    DevBuf<float> c_lam;
+    int S = 4;
+    // instances (batched objects): offsets into the concatenated arrays
+    int n_inst = 1;
+    std::vector<int64_t> voff, toff, foff;
+    std::vector<float4> sphere_tab_h;  // [n_inst * S], radius < 0 = empty
+    DevBuf<float4> sphere_tab;
+    DevBuf<int> face_inst;
+    bool sphere_dirty = true;
+    int n_spheres_total = 0;
+    DevBuf<int> kin_idx;
+    DevBuf<float4> kin_rest;
+    int nkin = 0;
+    DevBuf<Flags> flags;
+    DevBuf<double> res_partial, res_rows, energy_partial;
+    DevBuf<float> rvec;
+    int res_stride = 0;   // doubles per residual row
+    bool have_rvec = false;
+    std::vector<int> api_slots;  // contacts added through the API per face
+
+    // pinned staging
+    float4* h_stage = nullptr;
+    double* h_rows = nullptr;
+    int h_rows_cap = 0;
+    int last_rows = 0;
+    bool rows_pending = false;
+
+    // host simulation clock (Simulation.cpp:197-276)
+    double time = 0, last_cd = 0;
+
+    // graphs: [write_vel]
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    long long graph_kernels[2] = {0, 0};  // kernels captured in each graph
+    bool graph_dirty = true;
+
+    Prof prof;
+
+    // learned warm start (MLP on the tensor cores) and its online training
+    int warm_mode = 0;                 // XPBD_WARM_*
+    bool record = false;               // keep (features, solved multipliers) of each substep
+    bool recorded = false;             // a substep has been recorded since record was set
+    bool mlp_ready = false;            // parameters initialised and packed
+    int adam_t = 0;                    // Adam steps taken
+    DevBuf<float> mlp_p, mlp_m, mlp_v, mlp_g, mlp_w4f;  // kMlpParams each (w4f: 128)
+    DevBuf<__nv_bfloat16> mlp_tiles;   // packed operand tiles W1|W2|W3|W4|W2t|W3t
+    DevBuf<float2> mat;                // per slot: log10(E)/5, nu
+    DevBuf<__nv_bfloat16> feat;        // [T][16] features of the last substep
+    DevBuf<float> pred, target;        // [T][2] network output, recorded targets
+    DevBuf<float4> x_pred;             // V: predicted positions (fallback restore)
+    DevBuf<unsigned long long> warm_stats;  // kept, rejected warm starts
+    DevBuf<double> warm_rows, mse;     // 2 residual sums; loss accumulator
+    int cache_rows = 0;                // training cache capacity (rows)
+    DevBuf<float> cache_z, cache_out;
+    DevBuf<__nv_bfloat16> cache_a;
+
+    xg::MlpNet net() {
+        __nv_bfloat16* b = mlp_tiles.p;
+        const int w1 = 64 * 16, w2 = 64 * 64, w4 = 16 * 64;
+        return xg::MlpNet{b,           b + w1,          b + w1 + w2, b + w1 + 2 * w2, b + w1 + 2 * w2 + w4,
+                          b + w1 + 3 * w2 + w4, mlp_p.p + xg::kOffB1, mlp_p.p + xg::kOffB2, mlp_p.p + xg::kOffB3,
+                          mlp_p.p + xg::kOffB4, mlp_w4f.p};
+    }
+
+    TetArrays tets() {
+        return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
+    }
+    Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
+    PatchArrays patches() const { return PatchArrays{patch_meta.p, patch_verts.p}; }
+    ContactArrays contacts() {
+        return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
+    }
+};
+
+namespace xg {
+
+inline int fail(xpbd_ctx* c, int code, const char* fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+inline int cuda_check(xpbd_ctx* c, cudaError_t e, const char* what) {
+    if (e == cudaSuccess) return XPBD_OK;
+    return fail(c, XPBD_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define XPBD_CU(ctx, call)                                         \
+    do {                                                           \
+        int _st = cuda_check((ctx), (call), #call);                \
+        if (_st != XPBD_OK) return _st;                            \
+    } while (0)
+
+inline int after_launches(xpbd_ctx* c, const char* what) {
+    return cuda_check(c, cudaGetLastError(), what);
+}
+
+// ---- profiling brackets (only when prof.on) ----
+inline void prof_begin(xpbd_ctx* c, int id) {
+    if (!c->prof.on) return;
+    if (c->prof.used + 2 > c->prof.pool.size()) {
+        size_t old = c->prof.pool.size();
+        c->prof.pool.resize(std::max<size_t>(256, old * 2));
+        for (size_t i = old; i < c->prof.pool.size(); i++) cudaEventCreate(&c->prof.pool[i]);
+    }
+    cudaEventRecord(c->prof.pool[c->prof.used], c->stream);
+    c->prof.ids.push_back(id);
+}
+inline void prof_end(xpbd_ctx* c) {
+    if (!c->prof.on) return;
+    cudaEventRecord(c->prof.pool[c->prof.used + 1], c->stream);
+    c->prof.used += 2;
+}
+
+struct Scope {
+    xpbd_ctx* c;
+    Scope(xpbd_ctx* c_, int id) : c(c_) {
+        prof_begin(c, id);
+        c->launches++;
+    }
+    ~Scope() { prof_end(c); }
+};
+
+}  // namespace xg

@@ -798,204 +798,6 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch_reg(TetArrays t, 
         if (k < nverts) x[vid[k]] = sv[k][tid];
 }
 
-// register-resident selection by a lane-dependent index (no local memory)
-template <typename T>
-__device__ __forceinline__ T sel4(int j, T a, T b, T c, T d) {
-    return j == 0 ? a : (j == 1 ? b : (j == 2 ? c : d));
-}
-
-// Four lanes per patch: lane j of a patch's group owns corner j of the tet
-// being projected. F, det F and ||F|| are computed by every lane; each lane
-// forms only its corner's gradients (corner 3 through the extended row
-// Q(3,c) = -sum_i Q(i,c)), the 2x2 system is summed over the group with two
-// xor shuffles, and each lane writes its own corner. The sequential order of
-// tets within a patch (and of patches within a colour) is that of the
-// one-lane kernel, so results differ only by FP32 summation order.
-template <bool FIRST, int WHICH>
-__global__ void __launch_bounds__(4 * kPatchBlock) k_project_patch_x4(TetArrays t, PatchArrays pa, int pbegin,
-                                                                     int pend, float4* __restrict__ x, Flags* flags) {
-    __shared__ __align__(128) float4 sq[3][kPatchBlock * kMaxPatchTets];
-    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
-    __shared__ __align__(8) unsigned long long bar;
-    __shared__ int s_first;
-    const int tid = threadIdx.x;
-    const int pl = tid >> 2;  // patch within the block
-    const int j = tid & 3;    // corner owned by this lane
-    const unsigned gmask = 0xFu << (threadIdx.x & 28);
-    const int p0 = pbegin + blockIdx.x * kPatchBlock;
-    const int p = p0 + pl;
-    const bool active = p < pend;
-    if (tid == 0) mbar_init(&bar, 1);
-    __syncthreads();
-    if (tid == 0) {
-        const int plast = min(p0 + kPatchBlock - 1, pend - 1);
-        const int4 m0 = __ldg(pa.meta + p0), m1 = __ldg(pa.meta + plast);
-        const int s0 = m0.x, s1 = m1.x + (m1.y & 0xff);
-        const unsigned bytes = (unsigned)(s1 - s0) * 16u;
-        s_first = s0;
-        mbar_arrive_expect_tx(&bar, 3u * bytes);
-        tma_load_1d(sq[0], t.q0 + s0, bytes, &bar);
-        tma_load_1d(sq[1], t.q1 + s0, bytes, &bar);
-        tma_load_1d(sq[2], t.q2 + s0, bytes, &bar);
-    }
-    int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
-    int ntets = 0, nverts = 0;
-    if (active) {
-        meta = __ldg(pa.meta + p);
-        va = __ldg(pa.verts + 2 * (size_t)p);
-        vb = __ldg(pa.verts + 2 * (size_t)p + 1);
-        ntets = meta.y & 0xff;
-        nverts = meta.y >> 8;
-    }
-    pdl_wait_then_release();
-    // lane j stages vertices j and j + 4; lane 0 holds the patch's multipliers
-    const int my_v0 = sel4(j, va.x, va.y, va.z, va.w), my_v1 = sel4(j, vb.x, vb.y, vb.z, vb.w);
-    if (j < nverts) sv[j][pl] = x[my_v0];
-    if (j + 4 < nverts) sv[j + 4][pl] = x[my_v1];
-    float2 lams[kMaxPatchTets];
-#pragma unroll
-    for (int i = 0; i < kMaxPatchTets; i++)
-        lams[i] = (!FIRST && j == 0 && i < ntets) ? t.lam[meta.x + i] : make_float2(0.f, 0.f);
-    __syncthreads();  // s_first and the staged vertices are visible
-    const bool staged = mbar_wait_bounded(&bar, 0, kWaitLimit);
-    if (!staged) {
-        if (tid == 0) {
-            atomicAdd(&flags->timeouts, 1ull);
-            mbar_wait_bounded(&bar, 0, kWaitLimit);
-        }
-        return;
-    }
-    if (!active) return;
-    const int base = meta.x - s_first;
-    const unsigned long long loc = (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
-#pragma unroll
-    for (int i = 0; i < kMaxPatchTets; i++) {
-        if (i >= ntets) break;
-        const int slot = meta.x + i;
-        TetState<float> st;
-        {
-            const float4 a = sq[0][base + i], b = sq[1][base + i], c = sq[2][base + i];
-            st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
-            st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
-            st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
-        }
-        float4 xp[4];
-        int l[4];
-#pragma unroll
-        for (int k = 0; k < 4; k++) {
-            l[k] = (int)((loc >> (12 * i + 3 * k)) & 7ull);
-            xp[k] = sv[l[k]][pl];
-            st.p[k][0] = xp[k].x; st.p[k][1] = xp[k].y; st.p[k][2] = xp[k].z;
-            st.w[k] = fabsf(xp[k].w);
-        }
-        float F[9];
-        tet_F(st, F);
-        float Fc[9];
-        Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-        Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-        Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
-        const float J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
-        // this lane's row of Q (corner 3: minus the sum of the other rows)
-        float qr[3];
-#pragma unroll
-        for (int c = 0; c < 3; c++) {
-            const float q0 = st.q[3 * c], q1 = st.q[3 * c + 1], q2 = st.q[3 * c + 2];
-            qr[c] = j == 0 ? q0 : (j == 1 ? q1 : (j == 2 ? q2 : -((q0 + q1) + q2)));
-        }
-        const float4 me = sel4(j, xp[0], xp[1], xp[2], xp[3]);
-        const int lj = sel4(j, l[0], l[1], l[2], l[3]);
-        const float wj = fabsf(me.w);
-        float2 lam = lams[i];
-        float dj[3] = {0.f, 0.f, 0.f};
-        bool ok = true;
-        if (fabsf(J) >= kDegenerateJ) {
-            float g1[3], g2[3];
-            float Cd = 0.f, Ch = 0.f, invC = 0.f, fac = 0.f;
-            if (WHICH != 1) {
-                const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
-                                  (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
-                invC = rsqrtf(ss);
-                Cd = ss * invC;
-            }
-            if (WHICH != 0) {
-                if (J >= 1.f) {
-                    Ch = -st.gam + logf(J);
-                    fac = __frcp_rn(J);
-                } else {
-                    const float dd = J - 1.f;
-                    Ch = -st.gam + dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f);
-                    fac = fmaf(dd, dd, 1.f - dd);
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < 3; k++) {
-                g1[k] = invC * fmaf(F[k], qr[0], fmaf(F[3 + k], qr[1], F[6 + k] * qr[2]));
-                g2[k] = fac * fmaf(Fc[k], qr[0], fmaf(Fc[3 + k], qr[1], Fc[6 + k] * qr[2]));
-            }
-            if (WHICH == 2) {
-                float aa = wj * dot3(g1, g1), ab = wj * dot3(g1, g2), bb = wj * dot3(g2, g2);
-                aa += __shfl_xor_sync(gmask, aa, 1);
-                ab += __shfl_xor_sync(gmask, ab, 1);
-                bb += __shfl_xor_sync(gmask, bb, 1);
-                aa += __shfl_xor_sync(gmask, aa, 2);
-                ab += __shfl_xor_sync(gmask, ab, 2);
-                bb += __shfl_xor_sync(gmask, bb, 2);
-                const float L00 = st.atd + aa, L01 = ab, L11 = st.ath + bb;
-                const float r0 = fmaf(st.atd, lam.x, Cd), r1 = fmaf(st.ath, lam.y, Ch);
-                const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
-                const float dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
-                const float dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
-                ok = isfinite(dl0) && isfinite(dl1);
-                if (ok) {
-                    lam.x += dl0;
-                    lam.y += dl1;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) dj[k] = wj * fmaf(g1[k], dl0, g2[k] * dl1);
-                }
-            } else {
-                const float* g = WHICH == 0 ? g1 : g2;
-                const float at = WHICH == 0 ? st.atd : st.ath;
-                const float C = WHICH == 0 ? Cd : Ch;
-                float gg = wj * dot3(g, g);
-                gg += __shfl_xor_sync(gmask, gg, 1);
-                gg += __shfl_xor_sync(gmask, gg, 2);
-                const float lw = WHICH == 0 ? lam.x : lam.y;
-                const float dl = -fmaf(at, lw, C) / (at + gg);
-                ok = isfinite(dl);
-                if (ok) {
-                    if (WHICH == 0) lam.x += dl;
-                    else lam.y += dl;
-#pragma unroll
-                    for (int k = 0; k < 3; k++) dj[k] = wj * g[k] * dl;
-                }
-            }
-        } else {
-            // near-degenerate: every lane runs the FP64 projection and keeps its corner
-            Fp64Out o;
-            if (WHICH == 2) {
-                o = project_combined_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], lam.x, lam.y);
-                ok = isfinite(o.dl0) && isfinite(o.dl1);
-                if (ok) { lam.x += o.dl0; lam.y += o.dl1; }
-            } else {
-                o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], WHICH, WHICH == 0 ? lam.x : lam.y);
-                ok = isfinite(o.dl0);
-                if (ok) { if (WHICH == 0) lam.x += o.dl0; else lam.y += o.dl0; }
-            }
-#pragma unroll
-            for (int k = 0; k < 3; k++) dj[k] = sel4(j, o.d[k], o.d[3 + k], o.d[6 + k], o.d[9 + k]);
-            if (j == 0) atomicAdd(&flags->degenerate, 1ull);
-        }
-        if (ok) {
-            sv[lj][pl] = make_float4(me.x + dj[0], me.y + dj[1], me.z + dj[2], me.w);
-        } else if (j == 0) {
-            atomicAdd(&flags->nonfinite, 1ull);
-        }
-        if (j == 0) t.lam[slot] = lam;
-        __syncwarp(gmask);
-    }
-    if (j < nverts) x[my_v0] = sv[j][pl];
-    if (j + 4 < nverts) x[my_v1] = sv[j + 4][pl];
-}
 
 // Static collision projection of one contact slot: C = n.(u x1 + v x2 + w x3 - p),
 // skipped when C > 0, alpha = 0. Returns false when skipped.
@@ -1174,7 +976,8 @@ __global__ void k_velocity(const float4* __restrict__ x, const float4* __restric
 // per-constraint residuals in the reference's order via the slot->tet map.
 __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const float4* __restrict__ x, bool separate,
                                                   const int* __restrict__ perm, float* __restrict__ rvec,
-                                                  ResidualSink res, double* __restrict__ energy_partial, float dt2) {
+                                                  ResidualSink res, double* __restrict__ energy_partial, float dt2,
+                                                  bool zero_lam) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     float rsq = 0.f, en = 0.f;
     int4 e;
@@ -1184,7 +987,7 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
     if (slot < T) {
         float4 xp[4];
         gather_tet(x, e, s, xp);
-        const float2 lam = t.lam[slot];
+        const float2 lam = zero_lam ? make_float2(0.f, 0.f) : t.lam[slot];
         float Cd, Ch, gd[9], gh[9], J;
         tet_eval(s, Cd, Ch, gd, gh, J);
         const float r0 = Cd + s.atd * lam.x, r1 = Ch + s.ath * lam.y;
@@ -1201,6 +1004,110 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
         __syncthreads();
         block_sum_store(en, energy_partial + blockIdx.x);
     }
+}
+
+// ---- learned warm start ----
+// Features of the tets in slots [s0, s0 + n) at the current (predicted)
+// positions: F (9, column-major), the previous multipliers scaled to
+// alpha_tilde * lambda (dimensionless), log10(E)/5, nu, dt * 1e3.
+__global__ void k_mlp_features(TetArrays t, const float4* __restrict__ x, const float2* __restrict__ mat, float dt_feat,
+                               int s0, int n, __nv_bfloat16* __restrict__ X) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    pdl_wait_then_release();
+    if (i >= n) return;
+    const int slot = s0 + i;
+    int4 e;
+    TetState<float> st;
+    load_tet_static(t, slot, e, st);
+    float4 xp[4];
+    gather_tet(x, e, st, xp);
+    float F[9];
+    tet_F(st, F);
+    const float2 lam = t.lam[slot];
+    const float2 m = mat[slot];
+    float f[16];
+#pragma unroll
+    for (int k = 0; k < 9; k++) f[k] = F[k];
+    f[9] = st.atd * lam.x;
+    f[10] = st.ath * lam.y;
+    f[11] = m.x;
+    f[12] = m.y;
+    f[13] = dt_feat;
+    f[14] = 0.f;
+    f[15] = 0.f;
+    __nv_bfloat162 h[8];
+#pragma unroll
+    for (int k = 0; k < 8; k++) h[k] = __floats2bfloat162_rn(f[2 * k], f[2 * k + 1]);
+    uint4* dst = reinterpret_cast<uint4*>(X + (size_t)i * 16);
+    dst[0] = reinterpret_cast<const uint4*>(h)[0];
+    dst[1] = reinterpret_cast<const uint4*>(h)[1];
+}
+
+// Training targets: the solved multipliers, scaled as the features.
+__global__ void k_mlp_targets(TetArrays t, int s0, int n, float* __restrict__ Y) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    pdl_wait_then_release();
+    if (i >= n) return;
+    const int slot = s0 + i;
+    const float4 c = __ldg(t.q2 + slot);
+    const float2 lam = t.lam[slot];
+    Y[2 * (size_t)i] = c.y * lam.x;
+    Y[2 * (size_t)i + 1] = c.z * lam.y;
+}
+
+// Warm start: lambda <- lambda0 and x += M^-1 grad C(x)^T lambda0 summed over
+// tets (into dx; applied by k_apply). lambda0 comes from the network output
+// (scaled, pred != nullptr) or from the multipliers already in place (the
+// previous step's, pred == nullptr).
+__global__ void k_warm_start(TetArrays t, int T, const float* __restrict__ pred, const float4* __restrict__ x,
+                             float4* __restrict__ dx) {
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    pdl_wait_then_release();
+    if (slot >= T) return;
+    int4 e;
+    TetState<float> st;
+    load_tet_static(t, slot, e, st);
+    float4 xp[4];
+    gather_tet(x, e, st, xp);
+    float2 lam;
+    if (pred) {
+        lam = make_float2(pred[2 * (size_t)slot] / st.atd, pred[2 * (size_t)slot + 1] / st.ath);
+        if (!(isfinite(lam.x) && isfinite(lam.y))) lam = make_float2(0.f, 0.f);
+        t.lam[slot] = lam;
+    } else {
+        lam = t.lam[slot];
+    }
+    float Cd, Ch, gd[9], gh[9], J;
+    tet_eval(st, Cd, Ch, gd, gh, J);
+    float d[4][3];
+#pragma unroll
+    for (int i = 0; i < 4; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float a = i < 3 ? gd[3 * i + k] : -gd[k] - gd[3 + k] - gd[6 + k];
+            const float b = i < 3 ? gh[3 * i + k] : -gh[k] - gh[3 + k] - gh[6 + k];
+            d[i][k] = st.w[i] * (a * lam.x + b * lam.y);
+        }
+    add_vec4(dx + e.x, d[0][0], d[0][1], d[0][2]);
+    add_vec4(dx + e.y, d[1][0], d[1][1], d[1][2]);
+    add_vec4(dx + e.z, d[2][0], d[2][1], d[2][2]);
+    add_vec4(dx + e.w, d[3][0], d[3][1], d[3][2]);
+}
+
+// Residual-triggered fallback: rows[0] = ||r(x_pred, 0)||^2, rows[1] =
+// ||r(x_warm, lambda0)||^2. When the warm start made the residual worse, the
+// predicted positions and lambda = 0 are restored. stats[0] counts kept warm
+// starts, stats[1] rejected ones.
+__global__ void k_warm_fallback(const double* __restrict__ rows, float4* __restrict__ x,
+                                const float4* __restrict__ x_pred, float2* __restrict__ lam, int V, int T,
+                                unsigned long long* __restrict__ stats) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    pdl_wait_then_release();
+    const bool reject = rows[1] > rows[0];
+    if (i == 0) atomicAdd(&stats[reject ? 1 : 0], 1ull);
+    if (!reject) return;
+    if (i < V) x[i] = x_pred[i];
+    if (i < T) lam[i] = make_float2(0.f, 0.f);
 }
 
 // One block per row: FP64 sum of `stride` partials, fixed order.
@@ -1313,14 +1220,6 @@ void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArra
 #undef XG_PATCHR
         return;
     }
-    if (variant == 2) {
-#define XG_PATCH4(F, W) go(k_project_patch_x4<F, W>, g, 4 * kPatchBlock, s, t, pa, pbegin, pend, x, flags)
-        if (which == 2) { if (first) XG_PATCH4(true, 2); else XG_PATCH4(false, 2); }
-        else if (which == 0) { if (first) XG_PATCH4(true, 0); else XG_PATCH4(false, 0); }
-        else { if (first) XG_PATCH4(true, 1); else XG_PATCH4(false, 1); }
-#undef XG_PATCH4
-        return;
-    }
 #define XG_PATCH(F, W, M) go(k_project_patch<F, W, M>, g, kPatchBlock, s, t, pa, pbegin, pend, x, flags)
 #define XG_PATCH_M(F, W) do { if (min_blocks == 8) XG_PATCH(F, W, 8); else XG_PATCH(F, W, 6); } while (0)
     if (which == 2) { if (first) XG_PATCH_M(true, 2); else XG_PATCH_M(false, 2); }
@@ -1361,9 +1260,29 @@ void launch_velocity(const Launch& s, const float4* x, const float4* prev, float
 }
 
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
-                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2) {
+                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2,
+                     bool zero_lam) {
     if (T <= 0) return;
-    go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2);
+    go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2, zero_lam);
+}
+
+void launch_mlp_features(const Launch& s, const TetArrays& t, const float4* x, const float2* mat, float dt_feat,
+                         int s0, int n, __nv_bfloat16* X) {
+    if (n > 0) go(k_mlp_features, nblk(n, 256), 256, s, t, x, mat, dt_feat, s0, n, X);
+}
+
+void launch_mlp_targets(const Launch& s, const TetArrays& t, int s0, int n, float* Y) {
+    if (n > 0) go(k_mlp_targets, nblk(n, 256), 256, s, t, s0, n, Y);
+}
+
+void launch_warm_start(const Launch& s, const TetArrays& t, int T, const float* pred, const float4* x, float4* dx) {
+    if (T > 0) go(k_warm_start, nblk(T, 256), 256, s, t, T, pred, x, dx);
+}
+
+void launch_warm_fallback(const Launch& s, const double* rows, float4* x, const float4* x_pred, float2* lam, int V,
+                          int T, unsigned long long* stats) {
+    const int n = V > T ? V : T;
+    go(k_warm_fallback, nblk(n, 256), 256, s, rows, x, x_pred, lam, V, T, stats);
 }
 
 void launch_reduce_rows(const Launch& s, const double* partial, int rows, int stride, double* out) {

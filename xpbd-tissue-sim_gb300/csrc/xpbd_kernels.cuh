@@ -14,6 +14,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
 namespace xg {
@@ -32,6 +33,8 @@ enum KernelId {
     K_KINEMATIC,
     K_GATHER,
     K_VELOCITY,
+    K_WARM,
+    K_MLP,
     K_COUNT
 };
 
@@ -61,7 +64,7 @@ constexpr int kPatchBlock = 64;
 // Gauss-Seidel sweep kernels: 0 one lane per patch, static tet records
 // prefetched into registers; 1 one lane per patch, records staged in shared
 // memory by bulk copies; 2 four lanes per patch (one per tet corner), staged.
-constexpr int kGsVariants = 3;
+constexpr int kGsVariants = 2;
 struct PatchArrays {
     const int4* meta;   // [P] x: first slot, y: ntets | nverts << 8, z/w: local vertex ids, 3 bits per
                         //     (tet i, corner j) at bit 12 i + 3 j of the 64-bit word (z low, w high)
@@ -91,6 +94,42 @@ struct Launch {
     bool pdl;
 };
 
+// ---- warm-start MLP (14 -> 64 -> 64 -> 64 -> 2, SiLU), BF16 tensor cores ----
+// Flat FP32 parameter vector: W_k row-major (out x in), then b_k.
+constexpr int kMlpIn = 16;  // 14 features, zero padded
+constexpr int kMlpHid = 64;
+constexpr int kOffW1 = 0;                    // 64 x 16
+constexpr int kOffB1 = kOffW1 + 64 * 16;     // 64
+constexpr int kOffW2 = kOffB1 + 64;          // 64 x 64
+constexpr int kOffB2 = kOffW2 + 64 * 64;     // 64
+constexpr int kOffW3 = kOffB2 + 64;          // 64 x 64
+constexpr int kOffB3 = kOffW3 + 64 * 64;     // 64
+constexpr int kOffW4 = kOffB3 + 64;          // 2 x 64
+constexpr int kOffB4 = kOffW4 + 2 * 64;      // 2
+constexpr int kMlpParams = kOffB4 + 2;
+
+struct MlpNet {
+    __nv_bfloat16 *w1, *w2, *w3, *w4, *w2t, *w3t;  // packed K-major operand tiles
+    const float *b1, *b2, *b3, *b4;                // into the FP32 parameter vector
+    float* w4f;                                    // BF16-rounded W4 as FP32 (2 x 64), backward pass
+};
+
+struct MlpCache {
+    float* z[3];            // pre-activations of the hidden layers, [n][64]
+    __nv_bfloat16* a[3];    // their BF16 activations, [n][64]
+};
+
+cudaError_t mlp_prepare_kernels();
+int mlp_forward_smem();
+int mlp_backward_smem();
+void launch_mlp_pack(cudaStream_t s, const float* params, const MlpNet& net);
+void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16* X, int n, const MlpNet& net, float* out,
+                        const MlpCache* cache, unsigned long long* err);
+void launch_mlp_backward(cudaStream_t s, const __nv_bfloat16* X, const float* Y, int n, const MlpNet& net,
+                         const MlpCache& cache, const float* out, float* grad, unsigned long long* err);
+void launch_mse(cudaStream_t s, const float* out, const float* Y, int n, double* acc);
+void launch_adam(cudaStream_t s, float* p, const float* g, float* m, float* v, int n, float lr, int step);
+
 // ---- launchers (all asynchronous on L.s) ----
 void launch_predict(const Launch& s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz);
 void launch_kinematic(const Launch& s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
@@ -113,7 +152,14 @@ void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, con
 void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);
 void launch_velocity(const Launch& s, const float4* x, const float4* prev, float4* vel, int V, float dt);
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
-                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2);
+                     const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2,
+                     bool zero_lam = false);
+void launch_mlp_features(const Launch& s, const TetArrays& t, const float4* x, const float2* mat, float dt_feat,
+                         int s0, int n, __nv_bfloat16* X);
+void launch_mlp_targets(const Launch& s, const TetArrays& t, int s0, int n, float* Y);
+void launch_warm_start(const Launch& s, const TetArrays& t, int T, const float* pred, const float4* x, float4* dx);
+void launch_warm_fallback(const Launch& s, const double* rows, float4* x, const float4* x_pred, float2* lam, int V,
+                          int T, unsigned long long* stats);
 void launch_reduce_rows(const Launch& s, const double* partial, int rows, int stride, double* out);
 int residual_blocks(int T, int block);
 

@@ -29,6 +29,8 @@ SOLVER_GAUSS_SEIDEL, SOLVER_JACOBI = 0, 1
 CONSTRAINT_COMBINED, CONSTRAINT_SEPARATE = 0, 1
 RESIDUAL_NEVER, RESIDUAL_EVERY_SUBSTEP, RESIDUAL_EVERY_ITERATION = 0, 1, 2
 JACOBI_ATOMIC, JACOBI_GATHER = 0, 1
+WARM_NONE, WARM_PREVIOUS, WARM_MLP = 0, 1, 2
+MLP_INPUTS, MLP_PARAMS = 16, 9538
 
 # YAML `solver-type` strings (include/config/simobject/XPBDMeshObjectConfig.hpp:26-34)
 # plus the GPU names; "Parallel-Jacobi" aliases the GPU Jacobi solver.
@@ -140,6 +142,17 @@ def load(path: str | None = None):
         "xpbd_instance_offsets": ([P, P, P, P], C.c_int),
         "xpbd_set_instance_spheres": ([P, I32, I32, P, P], C.c_int),
         "xpbd_autotune": ([P, I32, P, I32, P, I32], C.c_int),
+        "xpbd_mlp_init": ([P, C.c_uint64], C.c_int),
+        "xpbd_mlp_set_params": ([P, P, I64], C.c_int),
+        "xpbd_mlp_get_params": ([P, P, I64], C.c_int),
+        "xpbd_mlp_forward": ([P, P, I64, P], C.c_int),
+        "xpbd_mlp_loss_grad": ([P, P, P, I64, P, P], C.c_int),
+        "xpbd_mlp_adam_step": ([P, P, C.c_float], C.c_int),
+        "xpbd_mlp_record": ([P, I32], C.c_int),
+        "xpbd_mlp_get_samples": ([P, P, P], C.c_int),
+        "xpbd_mlp_train": ([P, I32, I32, C.c_float, P], C.c_int),
+        "xpbd_set_warm_start": ([P, I32], C.c_int),
+        "xpbd_warm_start_stats": ([P, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -438,3 +451,56 @@ class XPBDSolver:
         n = C.c_int64()
         self._ck(self.L.xpbd_launch_count(self.h, C.byref(n)))
         return n.value
+
+    # ---- learned warm start ----
+    def mlp_init(self, seed: int = 0):
+        self._ck(self.L.xpbd_mlp_init(self.h, int(seed)))
+
+    def mlp_params(self) -> np.ndarray:
+        p = np.zeros(MLP_PARAMS, np.float32)
+        self._ck(self.L.xpbd_mlp_get_params(self.h, _p(p), MLP_PARAMS))
+        return p
+
+    def set_mlp_params(self, p):
+        p = np.ascontiguousarray(p, np.float32)
+        self._ck(self.L.xpbd_mlp_set_params(self.h, _p(p), p.size))
+
+    def mlp_forward(self, X) -> np.ndarray:
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, MLP_INPUTS)
+        out = np.zeros((X.shape[0], 2), np.float32)
+        self._ck(self.L.xpbd_mlp_forward(self.h, _p(X), X.shape[0], _p(out)))
+        return out
+
+    def mlp_loss_grad(self, X, Y):
+        X = np.ascontiguousarray(X, np.float32).reshape(-1, MLP_INPUTS)
+        Y = np.ascontiguousarray(Y, np.float32).reshape(-1, 2)
+        loss = C.c_double()
+        g = np.zeros(MLP_PARAMS, np.float32)
+        self._ck(self.L.xpbd_mlp_loss_grad(self.h, _p(X), _p(Y), X.shape[0], C.byref(loss), _p(g)))
+        return loss.value, g
+
+    def mlp_adam_step(self, lr: float = 1e-3, grad=None):
+        g = None if grad is None else np.ascontiguousarray(grad, np.float32)
+        self._ck(self.L.xpbd_mlp_adam_step(self.h, None if g is None else _p(g), float(lr)))
+
+    def mlp_record(self, on: bool = True):
+        self._ck(self.L.xpbd_mlp_record(self.h, 1 if on else 0))
+
+    def mlp_samples(self):
+        X = np.zeros((self.T, MLP_INPUTS), np.float32)
+        Y = np.zeros((self.T, 2), np.float32)
+        self._ck(self.L.xpbd_mlp_get_samples(self.h, _p(X), _p(Y)))
+        return X, Y
+
+    def mlp_train(self, epochs: int = 1, batch: int = 65536, lr: float = 1e-3) -> float:
+        loss = C.c_double()
+        self._ck(self.L.xpbd_mlp_train(self.h, int(epochs), int(batch), float(lr), C.byref(loss)))
+        return loss.value
+
+    def set_warm_start(self, mode: int):
+        self._ck(self.L.xpbd_set_warm_start(self.h, int(mode)))
+
+    def warm_start_stats(self):
+        k, r = C.c_int64(), C.c_int64()
+        self._ck(self.L.xpbd_warm_start_stats(self.h, C.byref(k), C.byref(r)))
+        return k.value, r.value
