@@ -301,6 +301,20 @@ int xpbd_set_warm_start(xpbd_ctx* ctx, int32_t mode);
 /* warm starts kept / rejected by the residual test since creation */
 int xpbd_warm_start_stats(xpbd_ctx* ctx, int64_t* kept, int64_t* rejected);
 
+/* ---- Residual without allocation (no counterpart in the reference) ----
+ * ||r(x, lambda)||_2 at the current state, the abs_norm of xpbd_residual, for
+ * callers that must not allocate device or pinned host memory: a real-time
+ * control or haptics thread, where cudaMalloc / cudaFree may synchronise the
+ * device and take unbounded time. xpbd_residual grows context buffers on
+ * demand; this call instead uses a fixed 128 KiB scratch array inside the
+ * library, one per device, and so handles at most 16384 x block tets
+ * (4,194,304 at the default block of 256): larger meshes get
+ * XPBD_ERR_CAPACITY. The first call on each device resolves the scratch's
+ * address (cudaGetSymbolAddress) with that device current: make that first
+ * call before any stream capture. All contexts on a device share the scratch,
+ * so calls that overlap in time race: serialise them. */
+int xpbd_residual_noalloc(xpbd_ctx* ctx, double* abs_norm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -153,6 +153,7 @@ def load(path: str | None = None):
         "xpbd_mlp_train": ([P, I32, I32, C.c_float, P], C.c_int),
         "xpbd_set_warm_start": ([P, I32], C.c_int),
         "xpbd_warm_start_stats": ([P, P, P], C.c_int),
+        "xpbd_residual_noalloc": ([P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -499,6 +500,12 @@ class XPBDSolver:
 
     def set_warm_start(self, mode: int):
         self._ck(self.L.xpbd_set_warm_start(self.h, int(mode)))
+
+    def residual_noalloc(self) -> float:
+        """||r|| at the current state through the non-allocating entry point."""
+        v = C.c_double()
+        self._ck(self.L.xpbd_residual_noalloc(self.h, C.byref(v)))
+        return v.value
 
     def warm_start_stats(self):
         k, r = C.c_int64(), C.c_int64()
