@@ -496,13 +496,145 @@ def run_ours(args):
     return 0
 
 
+def run_learned(args):
+    """The block mesh with the learned warm start (per-tet MLP on the tensor
+    cores). Online training on seeded loading paths: episodes of `episode`
+    steps from rest in which the top face is moved 1 cm along a seeded
+    direction; after each step one epoch of minibatch Adam (batch 65,536) over
+    the step's recorded (features, solved alpha~ lambda) pairs. Evaluation on a
+    held-out path: relative residual after 5/10/30 iterations, plain start vs
+    learned start (with the residual-triggered fallback), the iterations each
+    needs to reach 1e-3 (FP64 residual before every iteration), and the wall
+    time per substep to get there: timed per-iteration cost x iterations + the
+    timed cost of the warm start itself."""
+    import numpy as np
+    import torch
+
+    import workloads as W
+    import xpbd_gb300 as G
+    torch.cuda.set_device(env_int("LOCAL_RANK", 0))
+    w = W.block()
+    ep = args.episode
+    rng = np.random.default_rng(1234)
+
+    def path(seed):
+        r = np.random.default_rng(seed)
+        d = r.standard_normal(3)
+        d[2] = abs(d[2]) + 0.5
+        return 0.01 * d / np.linalg.norm(d)
+
+    def run_episode(s, d, steps, after=None):
+        s.set_positions(w.X)
+        s.set_velocities(np.zeros_like(w.X))
+        out = []
+        for k in range(1, steps + 1):
+            s.set_kinematic_offset(d * min(k / ep, 1.0))
+            s.step(1)
+            out.append(after(s) if after else None)
+        return out
+
+    # ---- online training ----
+    s = W.make_solver(w)
+    s.mlp_init(0)
+    s.mlp_record(True)
+    n_ep = max(1, args.train_steps // ep)
+    t0 = time.perf_counter()
+    losses = []
+    for e in range(n_ep):
+        d = path(int(rng.integers(1 << 30)))
+        losses += run_episode(s, d, ep, after=lambda t: t.mlp_train(epochs=1, batch=65536, lr=1e-3))
+    s.synchronize()
+    train_s = time.perf_counter() - t0
+    params = s.mlp_params()
+    s.close()
+
+    # ---- evaluation on a held-out path ----
+    d_eval = path(999_999)
+    n_eval = min(args.steps, ep)
+    eval_res = {}
+    for name, mode in (("plain", G.WARM_NONE), ("learned", G.WARM_MLP)):
+        t = W.make_solver(w, residual_policy=G.RESIDUAL_EVERY_ITERATION, num_iters=200)
+        t.set_mlp_params(params)
+        t.set_warm_start(mode)
+        hists = run_episode(t, d_eval, n_eval, after=lambda u: u.residual_history())
+        rel = np.array([h / h[0] for h in hists])
+        first = [int(np.nonzero(r <= 1e-3)[0][0]) if (r <= 1e-3).any() else None for r in rel]
+        ok = [f for f in first if f is not None]
+        eval_res[name] = {
+            "rel_residual_after": {str(k): float(np.mean(rel[:, k])) for k in (5, 10, 30)},
+            "iters_to_1e-3_mean": float(np.mean(ok)) if ok else None,
+            "steps_reaching_1e-3": len(ok), "steps": n_eval,
+            "warm_starts_kept_rejected": list(t.warm_start_stats()),
+        }
+        t.close()
+
+    # ---- timed production steps (no residual tracking, graphs) ----
+    timing = {}
+    for name, mode in (("plain", G.WARM_NONE), ("learned", G.WARM_MLP)):
+        t = W.make_solver(w)
+        t.set_mlp_params(params)
+        t.set_warm_start(mode)
+        run_episode(t, d_eval, 3)
+        t.synchronize()
+        st = torch.cuda.ExternalStream(t.stream_handle())
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        for k in range(args.steps):
+            t.set_kinematic_offset(d_eval * min((k + 4) / ep, 1.0))
+            evs[k][0].record(st)
+            t.step(1)
+            evs[k][1].record(st)
+        torch.cuda.synchronize()
+        prof = t.profile_steps(3)
+        timing[name] = {"ms_per_step": sum(a.elapsed_time(b) for a, b in evs) / args.steps,
+                        "kernels_ms_per_step": {k: v[0] * v[1] / 3 for k, v in prof.items()},
+                        "mlp_ms": prof.get("mlp", (0.0, 0))[0]}
+        t.close()
+    ms_plain = timing["plain"]["ms_per_step"]
+    ms_iter = ms_plain / w.iters  # sweeps dominate; predict/finalize are < 1 %
+    warm_ms = timing["learned"]["ms_per_step"] - ms_plain
+    wall = {}
+    for name, extra_ms in (("plain", 0.0), ("learned", warm_ms)):
+        it = eval_res[name]["iters_to_1e-3_mean"]
+        wall[name] = None if it is None else extra_ms + it * ms_iter
+    mlp_ms = timing["learned"]["mlp_ms"]
+    flop = 18_432 * w.T
+    peak = None
+    try:
+        with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")) as f:
+            peak = json.load(f).get("bf16_tflops")
+    except (OSError, ValueError):
+        pass
+    achieved = flop / (mlp_ms * 1e-3) / 1e12 if mlp_ms > 0 else None
+    line = {
+        "metric": METRIC, "value": (1e3 / wall["learned"]) if wall["learned"] else None,
+        "unit": "substeps/s at 1e-3 rel. residual", "n_gpus": 1, "steps": args.steps, "warmup": 3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 (MLP bf16/f32)",
+        "data": "synthetic",
+        "config": {"workload": f"learned: {describe(w)['workload']}, per-tet E log-uniform [1e3,1e5]", "episode": ep,
+                   "train_steps": n_ep * ep, "eval_steps": n_eval, "mlp": "14-64-64-64-2 SiLU, BF16 tcgen05"},
+        "plain_substeps_per_s_at_1e-3": (1e3 / wall["plain"]) if wall["plain"] else None,
+        "ms_per_substep_at_1e-3": wall, "speedup_at_1e-3": (wall["plain"] / wall["learned"])
+        if wall["plain"] and wall["learned"] else None,
+        "evaluation": eval_res, "timing": timing, "warm_start_overhead_ms": warm_ms,
+        "training": {"seconds": train_s, "loss_first": losses[0], "loss_last": losses[-1],
+                     "loss_last10_mean": float(np.mean(losses[-10:]))},
+        "roofline_mlp": {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": (achieved / peak) if achieved and peak else None,
+                         "flop_per_launch": flop, "avg_launch_ms": mlp_ms},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="block", choices=["block", "beam", "cube", "batched"])
+    ap.add_argument("--workload", default="block", choices=["block", "beam", "cube", "batched", "learned"])
+    ap.add_argument("--train-steps", type=int, default=200, help="learned: solver steps of online training")
+    ap.add_argument("--episode", type=int, default=50, help="learned: steps per loading path")
     ap.add_argument("--autotune", action="store_true", help="batched: pick launch parameters with the autotuner")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--quick", action="store_true", help="timed steps only (no e2e/roofline/CPU legs)")
@@ -518,6 +650,8 @@ def main():
         return run_reference(args)
     if args.workload == "batched":
         return run_batched(args)
+    if args.workload == "learned":
+        return run_learned(args)
     return run_ours(args)
 
 

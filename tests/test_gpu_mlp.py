@@ -194,12 +194,14 @@ def test_previous_lambda_warm_start_matches_fp64_oracle(lib, solver):
     o.close()
 
 
-def test_rejected_warm_starts_reproduce_the_plain_solver(lib):
+@pytest.mark.parametrize("policy", [G.RESIDUAL_NEVER, G.RESIDUAL_EVERY_SUBSTEP, G.RESIDUAL_EVERY_ITERATION])
+def test_rejected_warm_starts_reproduce_the_plain_solver(lib, policy):
     """A network whose prediction is rejected on every substep leaves the
-    trajectory bit-identical to the plain start."""
+    trajectory bit-identical to the plain start, and the residual history
+    (record 0 = ||r(x_pred, 0)||) identical too."""
     w = W.cube(6, seed=3)
-    plain = W.make_solver(w, num_iters=8)
-    warm = W.make_solver(w, num_iters=8)
+    plain = W.make_solver(w, num_iters=8, residual_policy=policy)
+    warm = W.make_solver(w, num_iters=8, residual_policy=policy)
     p = M.init_params(0)
     p[7] = np.array([50.0, -50.0], np.float32)  # alpha~ lambda_0 far off: rejected
     warm.set_mlp_params(M.flatten(p))
@@ -209,6 +211,8 @@ def test_rejected_warm_starts_reproduce_the_plain_solver(lib):
     kept, rejected = warm.warm_start_stats()
     assert (kept, rejected) == (0, 15)
     np.testing.assert_array_equal(plain.positions(), warm.positions())
+    if policy != G.RESIDUAL_NEVER:
+        np.testing.assert_array_equal(plain.residual_history(), warm.residual_history())
     plain.close()
     warm.close()
 

@@ -221,7 +221,9 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     if (track) cudaMemsetAsync(c->res_partial.p, 0, sizeof(double) * (size_t)c->res_stride * (iters + 1), s);
     if (warm) {
         // r(x_pred, 0) before the warm start moves anything
-        if (track && !every_iter) zero_lambda_residual_row(c, 0);
+        // (record 0 of the history, also under the every-iteration policy, so
+        // relative residuals share the plain start's denominator)
+        if (track) zero_lambda_residual_row(c, 0);
         enqueue_warm_start(c);
     } else {
         // features read the previous substep's multipliers: before the reset
@@ -238,7 +240,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
             // a warm start keeps its multipliers: no iteration treats lambda as 0
             const bool first = it == 0 && !warm;
             const bool first_contact = it == 0;
-            const ResidualSink rs = every_iter ? sink(c, it, 0) : no_sink();
+            const ResidualSink rs = every_iter && !(warm && it == 0) ? sink(c, it, 0) : no_sink();
             const bool last = it == iters - 1;
             if (gather) {
                 {
@@ -271,7 +273,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
             const bool first = it == 0;
-            if (every_iter) exact_residual_row(c, it, false);
+            if (every_iter && !(warm && it == 0)) exact_residual_row(c, it, false);
             const int passes = separate ? 2 : 1;
             for (int pass = 0; pass < passes; pass++) {
                 const int which = separate ? pass : 2;
