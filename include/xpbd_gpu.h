@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 1
+#define XPBD_ABI_VERSION 2
 
 /* status codes */
 #define XPBD_OK 0
@@ -98,6 +98,10 @@ typedef struct {
     int32_t gs_variant;        /* sweep kernel: 0 one lane per patch, tet records  */
                                /* prefetched into registers; 1 one lane, records   */
                                /* staged in shared memory by bulk (TMA) copies     */
+    int32_t num_local_collision_iters; /* num-local-collision-iters: passes    */
+                               /* after the global solve over every contact    */
+                               /* and the tets touching a vertex of a contact  */
+                               /* projected with lambda != 0; 0 = off          */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -234,6 +238,12 @@ int xpbd_get_tet_colours(xpbd_ctx* ctx, int32_t* colour_of_tet);
  * colour by colour, patch by patch, tets of a patch in index order. The FP64
  * oracle replays this order for parity. */
 int xpbd_get_sweep_order(xpbd_ctx* ctx, int32_t* order);
+/* The order of the Gauss-Seidel local collision passes: T tet indices, colour
+ * by colour (a greedy per-tet colouring in tet index order), ascending tet
+ * index within a colour; colour_offsets (n_colours + 1 entries, may be NULL)
+ * delimit the colours. XPBD_ERR_STATE without faces or local passes. */
+int xpbd_get_local_order(xpbd_ctx* ctx, int32_t* order, int32_t* colour_offsets, int32_t max_colours,
+                         int32_t* n_colours);
 
 /* Per-kernel timing with CUDA events on the context's stream over n substeps
  * (no graphs). Fills up to max_k entries: average milliseconds per launch and

@@ -234,6 +234,25 @@ class Oracle:
         if self.L.xo_set_order(C.c_void_p(self.h), len(order), _p(order)) != 0:
             raise ValueError("not a permutation of the tets")
 
+    def set_local_iterations(self, iters, order=None):
+        """num-local-collision-iters; `order` (a tet permutation) is the tet
+        order of the coloured local passes."""
+        if order is None:
+            st = self.L.xo_set_local(C.c_void_p(self.h), int(iters), 0, None)
+        else:
+            order = np.ascontiguousarray(order, np.int32)
+            st = self.L.xo_set_local(C.c_void_p(self.h), int(iters), len(order), _p(order))
+        if st != 0:
+            raise ValueError("bad local iteration settings")
+
+    def local_tets(self):
+        """Tets gathered for the local collision passes, duplicates included."""
+        n = self.L.xo_local_tets(C.c_void_p(self.h), None)
+        out = np.zeros(n, np.int32)
+        if n:
+            self.L.xo_local_tets(C.c_void_p(self.h), _p(out))
+        return out
+
     def tet_order(self):
         n = self.L.xo_tet_order(C.c_void_p(self.h), None)
         out = np.zeros(n, np.int32)

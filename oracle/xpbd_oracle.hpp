@@ -462,6 +462,10 @@ struct Object {
     std::vector<int> tet_order;      // tets in colour order
     std::vector<int> face_colour;    // F
     int n_face_colours = 0;
+    // local collision iterations (num-local-collision-iters) and, for
+    // COLOURED_GS, the order of their tet passes
+    int num_local_iter = 0;
+    std::vector<int> local_order;
     // spheres
     std::vector<R> sph_c, sph_r;
     // kinematic vertex group
@@ -637,6 +641,76 @@ struct Object {
         }
     }
 
+    // _gatherProjectorsForLocalCollisionIterations (XPBDMeshObject.cpp:764-825):
+    // for every contact projected with lambda != 0, for each of its three
+    // vertices, every element attached to that vertex in ascending element
+    // order (TetMesh.cpp:88-96) -- duplicates kept, as the reference lists them
+    std::vector<int> local_tet_list() const {
+        std::vector<std::vector<int>> attached(V);
+        for (long long t = 0; t < T; t++)
+            for (int i = 0; i < 4; i++) attached[tets[4 * t + i]].push_back((int)t);
+        std::vector<int> out;
+        for (const auto& ct : contacts)
+            if (ct.lambda != 0)
+                for (int i = 0; i < 3; i++)
+                    for (int t : attached[ct.v[i]]) out.push_back(t);
+        return out;
+    }
+
+    // Local collision iterations (XPBDMeshObject.cpp:472-505): passes over the
+    // gathered projectors without re-initialising lambda, elastic projectors
+    // before collision projectors (type order of the projector lists).
+    //   GAUSS_SEIDEL: the reference's list order, duplicates included;
+    //   COLOURED_GS : each listed tet once per pass, in local_order;
+    //   JACOBI      : each listed tet once per pass, every projection from the
+    //                 same x, updates summed with the contacts'.
+    void local_iterations() {
+        if (num_local_iter <= 0 || contacts.empty()) return;
+        const std::vector<int> list = local_tet_list();
+        std::vector<char> mark(T, 0);
+        for (int t : list) mark[t] = 1;
+        R dx[12];
+        for (int it = 0; it < num_local_iter; it++) {
+            if (solver == GAUSS_SEIDEL) {
+                if (ckind == COMBINED) {
+                    for (int t : list) { project_tet_combined(t, dx); add_tet(t, dx); }
+                } else {
+                    for (int t : list) { project_tet_single(t, 0, dx); add_tet(t, dx); }
+                    for (int t : list) { project_tet_single(t, 1, dx); add_tet(t, dx); }
+                }
+                for (auto& ct : contacts)
+                    if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            } else if (solver == COLOURED_GS) {
+                for (int pass = 0; pass < (ckind == COMBINED ? 1 : 2); pass++)
+                    for (int t : local_order) {
+                        if (!mark[t]) continue;
+                        if (ckind == COMBINED) project_tet_combined(t, dx);
+                        else project_tet_single(t, pass, dx);
+                        add_tet(t, dx);
+                    }
+                for (int k = 0; k < n_face_colours; k++)
+                    for (auto& ct : contacts)
+                        if (face_colour[ct.face] == k)
+                            if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            } else {
+                std::vector<R> acc(3 * V, 0);
+                for (long long t = 0; t < T; t++) {
+                    if (!mark[t]) continue;
+                    const int* e = &tets[4 * t];
+                    for (int pass = 0; pass < (ckind == COMBINED ? 1 : 2); pass++) {
+                        if (ckind == COMBINED) project_tet_combined(t, dx);
+                        else project_tet_single(t, pass, dx);
+                        for (int i = 0; i < 4; i++) for (int k = 0; k < 3; k++) acc[3 * e[i] + k] += dx[3 * i + k];
+                    }
+                }
+                for (auto& ct : contacts)
+                    if (project_contact_i(ct, dx))
+                        for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
+                for (long long i = 0; i < 3 * V; i++) x[i] += acc[i];
+            }
+        }
+    }
+
     // Warm-started update: the multipliers start at lam0 (2 per tet, dev/hyd)
     // and the positions take the matching correction x += M^-1 grad C(x)^T lam0
     // (summed over tets at the predicted positions) before the sweeps; the
@@ -679,6 +753,7 @@ struct Object {
             iterate();
         }
         if (record_residual) res_history.push_back(residual_norm());
+        local_iterations();
         for (long long i = 0; i < V; i++)
             if (fixed[i])
                 for (int k = 0; k < 3; k++) x[3 * i + k] = prev[3 * i + k];
@@ -704,6 +779,7 @@ struct Object {
             iterate();
         }
         if (record_residual) res_history.push_back(residual_norm());
+        local_iterations();
         // fixed vertices back to previous position (XPBDMeshObject.cpp:497-503)
         for (long long i = 0; i < V; i++)
             if (fixed[i])

@@ -232,6 +232,29 @@ double xo_strain_energy(void* p) {
 }
 // replace the coloured Gauss-Seidel order (a permutation of the tets), e.g.
 // with the sweep order the GPU library reports
+// num-local-collision-iters and (optional, n == T) the tet order of the
+// coloured local passes
+int xo_set_local(void* p, int iters, int n, const int* order) {
+    return with((Handle*)p, [&](auto& o) {
+        if (iters < 0 || (n && n != (int)o.T)) return 1;
+        o.num_local_iter = iters;
+        if (n) o.local_order.assign(order, order + n);
+        if (o.face_colour.size() != (size_t)o.F || (o.F && o.n_face_colours == 0))
+            o.n_face_colours = o.F ? xo::greedy_colour(o.F, 3, o.faces.data(), o.V, o.face_colour.data()) : 0;
+        return 0;
+    });
+}
+
+// the tets the reference gathers for local collision passes (with duplicates);
+// returns the count, writes them when out != NULL
+int xo_local_tets(void* p, int* out) {
+    return with((Handle*)p, [&](auto& o) {
+        const std::vector<int> l = o.local_tet_list();
+        if (out) std::copy(l.begin(), l.end(), out);
+        return (int)l.size();
+    });
+}
+
 int xo_set_order(void* p, int n, const int* order) {
     return with((Handle*)p, [&](auto& o) {
         if (n != (int)o.T) return 1;

@@ -35,7 +35,8 @@ bool valid_params(const xpbd_params& p) {
            (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
            p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
            (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8) &&
-           p.gs_variant >= 0 && p.gs_variant < kGsVariants;
+           p.gs_variant >= 0 && p.gs_variant < kGsVariants && p.num_local_collision_iters >= 0 &&
+           p.num_local_collision_iters <= 1000;
 }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
@@ -201,6 +202,52 @@ void enqueue_warm_start(xpbd_ctx* c) {
     launch_warm_fallback(c->L(), c->warm_rows.p, c->x.p, c->x_pred.p, c->lam.p, c->V, c->T, c->warm_stats.p);
 }
 
+// Local collision iterations after the global solve
+// (XPBDMeshObject_::_projectConstraints, XPBDMeshObject.cpp:472-505, with
+// _gatherProjectorsForLocalCollisionIterations, :764-825): every contact plus
+// the tets attached to a vertex of a contact projected with lambda != 0, for
+// num_local_collision_iters passes without re-initialising lambda, elastic
+// projectors before collision projectors (the projector type order). A tet
+// the reference lists once per incident contact vertex is projected once per
+// pass here, in per-tet colour order (Gauss-Seidel) or from the same x
+// (Jacobi).
+void enqueue_local_collision_iters(xpbd_ctx* c) {
+    const xpbd_params& p = c->prm;
+    const bool separate = p.constraint_type == XPBD_CONSTRAINT_SEPARATE;
+    const ContactArrays ca = c->contacts();
+    cudaMemsetAsync(c->vmask.p, 0, (size_t)c->V, c->stream);
+    {
+        Scope sc(c, K_LOCAL);
+        launch_mark_local(c->L(), ca, c->tets(), c->T, c->vmask.p, c->tmask.p);
+    }
+    const int ncol = (int)c->lcol_off.size() - 1;
+    for (int it = 0; it < p.num_local_collision_iters; it++) {
+        if (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
+            for (int pass = 0; pass < (separate ? 2 : 1); pass++)
+                for (int col = 0; col < ncol; col++) {
+                    Scope sc(c, K_PROJECT_GS);
+                    launch_project_local_gs(c->L(), c->tets(), c->local_slots.p, c->lcol_off[col], c->lcol_off[col + 1],
+                                            c->tmask.p, c->x.p, separate ? pass : 2, c->flags.p);
+                }
+            for (int fc = 0; fc < c->n_face_colours; fc++) {
+                Scope sc(c, K_CONTACT);
+                launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, false);
+            }
+        } else {
+            {
+                Scope sc(c, K_PROJECT_JACOBI);
+                launch_project_local_jacobi(c->L(), c->tets(), c->T, c->tmask.p, c->x.p, c->dx.p, separate, c->flags.p);
+            }
+            {
+                Scope sc(c, K_CONTACT);
+                launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, false);
+            }
+            Scope sc(c, K_APPLY);
+            launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, false, (float)p.dt, false);
+        }
+    }
+}
+
 // ---- the substep body (XPBDMeshObject_::update, XPBDMeshObject.cpp:426-505) ----
 int enqueue_update(xpbd_ctx* c, bool write_vel) {
     const xpbd_params& p = c->prm;
@@ -232,7 +279,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         if (track) cudaMemsetAsync(c->lam.p, 0, sizeof(float2) * (size_t)c->T, s);
     }
     const bool jacobi = p.solver_type == XPBD_SOLVER_JACOBI;
-    const bool fuse_final = !track;
+    const bool local = have_faces && p.num_local_collision_iters > 0 && c->local_slots.p;
+    const bool fuse_final = !track && !local;
     if (jacobi) {
         const bool gather = p.jacobi_variant == XPBD_JACOBI_GATHER;
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
@@ -307,6 +355,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         }
         cudaMemcpyAsync(c->h_rows, c->res_rows.p, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, s);
     }
+    if (local) enqueue_local_collision_iters(c);
     if (!jacobi || !fuse_final || iters == 0) {
         Scope sc(c, K_FINALIZE);
         launch_finalize(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
@@ -413,6 +462,7 @@ void release(xpbd_ctx* c) {
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
     c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
+    c->local_slots.release(); c->vmask.release(); c->tmask.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
     c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
@@ -587,6 +637,27 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     }
     c->api_slots.assign(F, 0);
 
+    // local collision iterations: a per-tet greedy colouring in tet index
+    // order; the local order lists the slots colour by colour, ascending tet
+    // index within a colour
+    std::vector<int> lslots;
+    if (F && p.num_local_collision_iters > 0) {
+        std::vector<int> tcol(T), slot_of(T);
+        const int nc = greedy_colour(T, 4, c->tets_h.data(), V, tcol.data());
+        c->lcol_off.assign(nc + 1, 0);
+        for (int t = 0; t < T; t++) c->lcol_off[tcol[t] + 1]++;
+        for (int k = 0; k < nc; k++) c->lcol_off[k + 1] += c->lcol_off[k];
+        for (int s = 0; s < T; s++) slot_of[c->tet_of_slot[s]] = s;
+        std::vector<int> fill(c->lcol_off.begin(), c->lcol_off.end() - 1);
+        lslots.resize(T);
+        c->local_tets_h.resize(T);
+        for (int t = 0; t < T; t++) {
+            const int j = fill[tcol[t]]++;
+            lslots[j] = slot_of[t];
+            c->local_tets_h[j] = t;
+        }
+    }
+
     // CSR vertex -> (slot, local vertex) for the gather variant
     std::vector<int> off(V + 1, 0), ent(4 * (size_t)T);
     if (p.solver_type == XPBD_SOLVER_JACOBI && p.jacobi_variant == XPBD_JACOBI_GATHER) {
@@ -638,6 +709,12 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, cudaMemset(c->c_lam.p, 0, sizeof(float) * ns));
         XPBD_CU(c, cudaMemcpy(c->faces.p, hf.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
         XPBD_CU(c, cudaMemcpy(c->face_list.p, flist.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+    }
+    if (!lslots.empty()) {
+        XPBD_CU(c, c->local_slots.alloc(T));
+        XPBD_CU(c, c->vmask.alloc(V));
+        XPBD_CU(c, c->tmask.alloc(T));
+        XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     }
     if (!pmeta.empty()) {
         XPBD_CU(c, c->patch_meta.alloc(pmeta.size()));
@@ -708,6 +785,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->gs_patch_tets = 0;
     p->gs_min_blocks = 0;
     p->gs_variant = 0;
+    p->num_local_collision_iters = 0;
     return XPBD_OK;
 }
 
@@ -1176,10 +1254,25 @@ int xpbd_get_sweep_order(xpbd_ctx* c, int32_t* order) {
     return XPBD_OK;
 }
 
+int xpbd_get_local_order(xpbd_ctx* c, int32_t* order, int32_t* colour_offsets, int32_t max_colours,
+                         int32_t* n_colours) {
+    if (!c || !order || !n_colours) return XPBD_ERR_INVALID;
+    if (c->local_tets_h.empty())
+        return fail(c, XPBD_ERR_STATE, "no local collision iterations (needs faces and num_local_collision_iters > 0)");
+    const int nc = (int)c->lcol_off.size() - 1;
+    *n_colours = nc;
+    std::copy(c->local_tets_h.begin(), c->local_tets_h.end(), order);
+    if (colour_offsets) {
+        if (max_colours < nc + 1) return fail(c, XPBD_ERR_CAPACITY, "need %d colour offsets", nc + 1);
+        std::copy(c->lcol_off.begin(), c->lcol_off.end(), colour_offsets);
+    }
+    return XPBD_OK;
+}
+
 static const char* kNames[K_COUNT] = {"predict",  "project_jacobi", "apply",    "project_gs",
                                       "contacts", "detect",         "finalize", "residual",
                                       "reduce",   "kinematic",      "gather_apply", "velocity",
-                                      "warm_start", "mlp"};
+                                      "warm_start", "mlp", "local_mark"};
 
 const char* xpbd_kernel_name(int32_t id) { return (id >= 0 && id < K_COUNT) ? kNames[id] : "?"; }
 

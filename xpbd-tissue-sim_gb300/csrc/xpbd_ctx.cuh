@@ -78,6 +78,11 @@ struct xpbd_ctx {
     DevBuf<int> face_list;
     DevBuf<int4> patch_meta, patch_verts;
     std::vector<int> pcol_off;           // patch colour ranges (Gauss-Seidel)
+    // local collision iterations: slots in per-tet colour order, masks
+    std::vector<int> lcol_off;           // colour ranges over local_slots
+    std::vector<int> local_tets_h;       // the same order as tet indices
+    DevBuf<int> local_slots;
+    DevBuf<unsigned char> vmask, tmask;
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;

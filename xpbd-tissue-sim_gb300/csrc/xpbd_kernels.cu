@@ -1006,6 +1006,101 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
     }
 }
 
+// ---- local collision iterations (XPBDMeshObject.cpp:472-505, 764-825) ----
+// Vertices of every contact that was projected (lambda != 0) in the global
+// solve; vmask must be cleared first.
+__global__ void k_mark_contact_verts(ContactArrays c, unsigned char* __restrict__ vmask) {
+    pdl_wait_then_release();
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= c.S * c.F) return;
+    if (c.bary[slot].w == 0.f || c.lam[slot] == 0.f) return;
+    const int4 fv = c.faces[slot % c.F];
+    vmask[fv.x] = 1;
+    vmask[fv.y] = 1;
+    vmask[fv.z] = 1;
+}
+
+// Tets attached to a marked vertex (TetMesh::vertexAttachedElements)
+__global__ void k_mark_tets(const int4* __restrict__ idx, int T, const unsigned char* __restrict__ vmask,
+                            unsigned char* __restrict__ tmask) {
+    pdl_wait_then_release();
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= T) return;
+    const int4 e = __ldg(idx + slot);
+    tmask[slot] = vmask[e.x] | vmask[e.y] | vmask[e.z] | vmask[e.w];
+}
+
+// Gauss-Seidel over the marked tets of one colour of the local order
+// (order[i] = slot), in place; which: 2 combined, 0 Dev, 1 Hyd.
+__global__ void k_project_local_gs(TetArrays t, const int* __restrict__ order, int begin, int end,
+                                   const unsigned char* __restrict__ tmask, float4* __restrict__ x, int which,
+                                   Flags* flags) {
+    pdl_wait_then_release();
+    const int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    const int slot = __ldg(order + i);
+    if (!tmask[slot]) return;
+    int4 e;
+    TetState<float> s;
+    load_tet_static(t, slot, e, s);
+    float4 xp[4];
+    gather_tet(x, e, s, xp);
+    float2 lam = t.lam[slot];
+    float d[4][3];
+    bool ok;
+    if (which == 2) {
+        float rsq;
+        ok = project_one<false>(s, t, slot, xp, lam, d, rsq, flags);
+    } else {
+        float J, r, dl;
+        const float lw = which == 0 ? lam.x : lam.y;
+        tet_project_single(s, which, lw, r, dl, d, J);
+        if (fabsf(J) < kDegenerateJ) {
+            const Fp64Out o = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], which, lw);
+            dl = o.dl0;
+#pragma unroll
+            for (int a = 0; a < 4; a++)
+#pragma unroll
+                for (int k = 0; k < 3; k++) d[a][k] = o.d[3 * a + k];
+            atomicAdd(&flags->degenerate, 1ull);
+        }
+        ok = isfinite(dl);
+        if (!ok) atomicAdd(&flags->nonfinite, 1ull);
+        else if (which == 0) lam.x += dl;
+        else lam.y += dl;
+    }
+    if (ok) {
+        const int v[4] = {e.x, e.y, e.z, e.w};
+#pragma unroll
+        for (int j = 0; j < 4; j++)
+            x[v[j]] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
+    }
+    t.lam[slot] = lam;
+}
+
+// Jacobi over the marked tets: updates from the same x summed into dx
+template <bool SEPARATE>
+__global__ void k_project_local_jacobi(TetArrays t, int T, const unsigned char* __restrict__ tmask,
+                                       const float4* __restrict__ x, float4* __restrict__ dx, Flags* flags) {
+    pdl_wait_then_release();
+    const int slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= T || !tmask[slot]) return;
+    int4 e;
+    TetState<float> s;
+    load_tet_static(t, slot, e, s);
+    float4 xp[4];
+    gather_tet(x, e, s, xp);
+    float2 lam = t.lam[slot];
+    float d[4][3], rsq;
+    if (project_one<SEPARATE>(s, t, slot, xp, lam, d, rsq, flags)) {
+        add_vec4(dx + e.x, d[0][0], d[0][1], d[0][2]);
+        add_vec4(dx + e.y, d[1][0], d[1][1], d[1][2]);
+        add_vec4(dx + e.z, d[2][0], d[2][1], d[2][2]);
+        add_vec4(dx + e.w, d[3][0], d[3][1], d[3][2]);
+    }
+    t.lam[slot] = lam;
+}
+
 // ---- learned warm start ----
 // Features of the tets in slots [s0, s0 + n) at the current (predicted)
 // positions: F (9, column-major), the previous multipliers scaled to
@@ -1264,6 +1359,25 @@ void launch_residual(const Launch& s, int block, const TetArrays& t, int T, cons
                      bool zero_lam) {
     if (T <= 0) return;
     go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2, zero_lam);
+}
+
+void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,
+                       unsigned char* tmask) {
+    const int n = c.S * c.F;
+    if (n > 0) go(k_mark_contact_verts, nblk(n, 256), 256, s, c, vmask);
+    if (T > 0) go(k_mark_tets, nblk(T, 256), 256, s, t.idx, T, (const unsigned char*)vmask, tmask);
+}
+
+void launch_project_local_gs(const Launch& s, const TetArrays& t, const int* order, int begin, int end,
+                             const unsigned char* tmask, float4* x, int which, Flags* flags) {
+    if (end > begin) go(k_project_local_gs, nblk(end - begin, 128), 128, s, t, order, begin, end, tmask, x, which, flags);
+}
+
+void launch_project_local_jacobi(const Launch& s, const TetArrays& t, int T, const unsigned char* tmask,
+                                 const float4* x, float4* dx, bool separate, Flags* flags) {
+    if (T <= 0) return;
+    if (separate) go(k_project_local_jacobi<true>, nblk(T, 256), 256, s, t, T, tmask, x, dx, flags);
+    else go(k_project_local_jacobi<false>, nblk(T, 256), 256, s, t, T, tmask, x, dx, flags);
 }
 
 void launch_mlp_features(const Launch& s, const TetArrays& t, const float4* x, const float2* mat, float dt_feat,

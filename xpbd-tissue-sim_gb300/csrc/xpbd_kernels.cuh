@@ -35,6 +35,7 @@ enum KernelId {
     K_VELOCITY,
     K_WARM,
     K_MLP,
+    K_LOCAL,
     K_COUNT
 };
 
@@ -154,6 +155,12 @@ void launch_velocity(const Launch& s, const float4* x, const float4* prev, float
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
                      const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2,
                      bool zero_lam = false);
+void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,
+                       unsigned char* tmask);
+void launch_project_local_gs(const Launch& s, const TetArrays& t, const int* order, int begin, int end,
+                             const unsigned char* tmask, float4* x, int which, Flags* flags);
+void launch_project_local_jacobi(const Launch& s, const TetArrays& t, int T, const unsigned char* tmask,
+                                 const float4* x, float4* dx, bool separate, Flags* flags);
 void launch_mlp_features(const Launch& s, const TetArrays& t, const float4* x, const float2* mat, float dt_feat,
                          int s0, int n, __nv_bfloat16* X);
 void launch_mlp_targets(const Launch& s, const TetArrays& t, int s0, int n, float* Y);

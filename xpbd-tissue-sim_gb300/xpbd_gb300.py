@@ -61,6 +61,7 @@ class Params(C.Structure):
         ("residual_policy", C.c_int32), ("jacobi_variant", C.c_int32), ("block_size", C.c_int32),
         ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
         ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32), ("gs_variant", C.c_int32),
+        ("num_local_collision_iters", C.c_int32),
     ]
 
 
@@ -154,6 +155,7 @@ def load(path: str | None = None):
         "xpbd_set_warm_start": ([P, I32], C.c_int),
         "xpbd_warm_start_stats": ([P, P, P], C.c_int),
         "xpbd_residual_noalloc": ([P, P], C.c_int),
+        "xpbd_get_local_order": ([P, P, P, I32, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -500,6 +502,14 @@ class XPBDSolver:
 
     def set_warm_start(self, mode: int):
         self._ck(self.L.xpbd_set_warm_start(self.h, int(mode)))
+
+    def local_order(self):
+        """(tet order, colour offsets) of the Gauss-Seidel local collision passes."""
+        order = np.zeros(self.T, np.int32)
+        off = np.zeros(1025, np.int32)
+        n = C.c_int32()
+        self._ck(self.L.xpbd_get_local_order(self.h, _p(order), _p(off), off.size, C.byref(n)))
+        return order, off[: n.value + 1].copy()
 
     def residual_noalloc(self) -> float:
         """||r|| at the current state through the non-allocating entry point."""
