@@ -12,6 +12,7 @@
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstdint>
 
 #include "xpbd_kernels.cuh"
@@ -111,7 +112,7 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, float* v) {
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
 }
 
-__device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z)); }
+__device__ __forceinline__ float silu_f(float z) { return __fdividef(z, 1.f + __expf(-z)); }
 __device__ __forceinline__ float dsilu_f(float z) {
     const float s = 1.f / (1.f + __expf(-z));
     return s * (1.f + z * (1.f - s));
@@ -152,99 +153,137 @@ constexpr int kW4Bytes = kOutPad * kHid * 2;   // 16 x 64
 constexpr int kA0Bytes = kRows * kIn * 2;      // 128 x 16
 constexpr int kABytes = kRows * kHid * 2;      // 128 x 64
 
-// ---- forward: one 128-tet tile per CTA ----
-// Smem: W1 | W2 | W3 | W4 | A0 | A  (+ barrier, tmem address)
+// ---- forward: persistent CTAs, one 128-tet tile at a time ----
+// Smem: W1 | W2 | W3 | W4 | A0 | A  (+ biases, barrier, tmem address). The
+// weights and biases are staged once per CTA; each tile's input rows are
+// loaded into registers while the previous tile is computed. Eight warps:
+// warp w reads tensor-memory lanes 32 (w % 4) .. +31 (its rows) and runs the
+// epilogue of hidden columns 32 (w / 4) .. +31.
 constexpr int kFwdSmem = kW1Bytes + 2 * kW2Bytes + kW4Bytes + kA0Bytes + kABytes;
+constexpr int kFwdThreads = 2 * kRows;
 
 template <bool TRAIN>
-__global__ void __launch_bounds__(kRows) k_mlp_forward(const __nv_bfloat16* __restrict__ X, int n, MlpNet net,
+__global__ void __launch_bounds__(kFwdThreads) k_mlp_forward(const __nv_bfloat16* __restrict__ X, int n, MlpNet net,
                                                        float* __restrict__ out, MlpCache cache,
                                                        unsigned long long* __restrict__ err) {
     extern __shared__ __align__(128) char smem[];
     __shared__ __align__(8) unsigned long long bar;
     __shared__ unsigned s_tmem;
+    __shared__ __align__(16) float s_b[3 * kHid + 2];
     char* W1 = smem;
     char* W2 = W1 + kW1Bytes;
     char* W3 = W2 + kW2Bytes;
     char* W4 = W3 + kW2Bytes;
     char* A0 = W4 + kW4Bytes;
     char* A = A0 + kA0Bytes;
-    const int t = threadIdx.x, warp = t >> 5;
-    const int row = blockIdx.x * kRows + t;
-    const bool live = row < n;
+    const int warp = threadIdx.x >> 5;
+    const int t = (warp & 3) * 32 + (threadIdx.x & 31);  // row within the tile
+    const int half = warp >> 2;                           // hidden columns 32 half .. +31
+    const int ntiles = (n + kRows - 1) / kRows;
     copy_smem(W1, (const char*)net.w1, kW1Bytes);
     copy_smem(W2, (const char*)net.w2, kW2Bytes);
     copy_smem(W3, (const char*)net.w3, kW2Bytes);
     copy_smem(W4, (const char*)net.w4, kW4Bytes);
-    {
-        uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-        if (live) {
-            a = __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * kIn));
-            b = __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * kIn + 8));
-        }
-        *reinterpret_cast<uint4*>(A0 + kmaj_off(t, 0, kIn)) = a;
-        *reinterpret_cast<uint4*>(A0 + kmaj_off(t, 8, kIn)) = b;
+    for (int i = threadIdx.x; i < kHid; i += blockDim.x) {
+        s_b[i] = __ldg(net.b1 + i);
+        s_b[kHid + i] = __ldg(net.b2 + i);
+        s_b[2 * kHid + i] = __ldg(net.b3 + i);
     }
-    if (t == 0) bar_init(&bar);
+    if (threadIdx.x < 2) s_b[3 * kHid + threadIdx.x] = __ldg(net.b4 + threadIdx.x);
+    if (threadIdx.x == 0) bar_init(&bar);
     if (warp == 0) tmem_alloc(&s_tmem, 64);
-    async_smem_fence();
     tc_before();
     __syncthreads();
     tc_after();
     const unsigned tmem = s_tmem;
-    const unsigned my_lane = tmem + ((unsigned)(32 * warp) << 16);
+    const unsigned my_lane = tmem + ((unsigned)(32 * (warp & 3)) << 16);
+    unsigned phase = 0;
     bool ok = true;
-#pragma unroll
-    for (int layer = 0; layer < 4; layer++) {
-        const int K = layer == 0 ? kIn : kHid;
-        const int N = layer == 3 ? kOutPad : kHid;
-        const char* Wl = layer == 0 ? W1 : (layer == 1 ? W2 : (layer == 2 ? W3 : W4));
-        const float* bl = layer == 0 ? net.b1 : (layer == 1 ? net.b2 : net.b3);
-        if (t == 0) {
-            mma_tile(tmem, layer == 0 ? A0 : A, Wl, K, N, false);
-            umma_commit(&bar);
+    // this thread's input row of the first tile
+    uint4 xa = make_uint4(0, 0, 0, 0), xb = make_uint4(0, 0, 0, 0);
+    {
+        const int row = blockIdx.x * kRows + t;
+        if (half == 0 && blockIdx.x < ntiles && row < n) {
+            xa = __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * kIn));
+            xb = __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * kIn + 8));
         }
-        // every thread polls; the block agrees on the outcome
-        ok = __syncthreads_and(bar_wait(&bar, layer & 1)) != 0;
-        tc_after();
-        if (!ok) break;
-        if (layer < 3) {
-#pragma unroll
-            for (int c = 0; c < kHid; c += 16) {
-                float v[16];
-                tmem_ld16(my_lane + c, v);
-                float a[16];
-#pragma unroll
-                for (int i = 0; i < 16; i++) {
-                    const float z = v[i] + __ldg(bl + c + i);
-                    a[i] = silu_f(z);
-                    if (TRAIN && live) cache.z[layer][(size_t)row * kHid + c + i] = z;
-                }
-                st_row8(A, t, c, kHid, a);
-                st_row8(A, t, c + 8, kHid, a + 8);
-                if (TRAIN && live) {
-                    // the BF16 activation the next layer consumes
-                    *reinterpret_cast<uint4*>(cache.a[layer] + (size_t)row * kHid + c) =
-                        *reinterpret_cast<const uint4*>(A + kmaj_off(t, c, kHid));
-                    *reinterpret_cast<uint4*>(cache.a[layer] + (size_t)row * kHid + c + 8) =
-                        *reinterpret_cast<const uint4*>(A + kmaj_off(t, c + 8, kHid));
-                }
+    }
+    for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int row = tile * kRows + t;
+        const bool live = row < n;
+        if (half == 0) {
+            *reinterpret_cast<uint4*>(A0 + kmaj_off(t, 0, kIn)) = xa;
+            *reinterpret_cast<uint4*>(A0 + kmaj_off(t, 8, kIn)) = xb;
+        }
+        // next tile's row: in flight while this tile is computed
+        {
+            const int nrow = (tile + gridDim.x) * kRows + t;
+            xa = make_uint4(0, 0, 0, 0);
+            xb = make_uint4(0, 0, 0, 0);
+            if (half == 0 && tile + (int)gridDim.x < ntiles && nrow < n) {
+                xa = __ldg(reinterpret_cast<const uint4*>(X + (size_t)nrow * kIn));
+                xb = __ldg(reinterpret_cast<const uint4*>(X + (size_t)nrow * kIn + 8));
             }
-            async_smem_fence();
-            tc_before();
-            __syncthreads();
+        }
+        async_smem_fence();
+        tc_before();
+        __syncthreads();
+        tc_after();
+#pragma unroll
+        for (int layer = 0; layer < 4; layer++) {
+            const int K = layer == 0 ? kIn : kHid;
+            const int N = layer == 3 ? kOutPad : kHid;
+            const char* Wl = layer == 0 ? W1 : (layer == 1 ? W2 : (layer == 2 ? W3 : W4));
+            if (threadIdx.x == 0) {
+                mma_tile(tmem, layer == 0 ? A0 : A, Wl, K, N, false);
+                umma_commit(&bar);
+            }
+            // every thread polls; the block agrees on the outcome
+            ok = __syncthreads_and(bar_wait(&bar, phase)) != 0;
+            phase ^= 1u;
             tc_after();
-        } else {
-            float v[16];
-            tmem_ld16(my_lane, v);
-            if (live) {
-                out[2 * (size_t)row] = v[0] + __ldg(net.b4);
-                out[2 * (size_t)row + 1] = v[1] + __ldg(net.b4 + 1);
+            if (!ok) break;
+            if (layer < 3) {
+                const float* bl = s_b + layer * kHid;
+#pragma unroll
+                for (int c = 32 * half; c < 32 * half + 32; c += 16) {
+                    float v[16];
+                    tmem_ld16(my_lane + c, v);
+                    float a[16];
+#pragma unroll
+                    for (int i = 0; i < 16; i++) {
+                        const float z = v[i] + bl[c + i];
+                        a[i] = silu_f(z);
+                        if (TRAIN && live) cache.z[layer][(size_t)row * kHid + c + i] = z;
+                    }
+                    st_row8(A, t, c, kHid, a);
+                    st_row8(A, t, c + 8, kHid, a + 8);
+                    if (TRAIN && live) {
+                        // the BF16 activation the next layer consumes
+                        *reinterpret_cast<uint4*>(cache.a[layer] + (size_t)row * kHid + c) =
+                            *reinterpret_cast<const uint4*>(A + kmaj_off(t, c, kHid));
+                        *reinterpret_cast<uint4*>(cache.a[layer] + (size_t)row * kHid + c + 8) =
+                            *reinterpret_cast<const uint4*>(A + kmaj_off(t, c + 8, kHid));
+                    }
+                }
+                async_smem_fence();
+                tc_before();
+                __syncthreads();
+                tc_after();
+            } else if (half == 0) {
+                float v[16];
+                tmem_ld16(my_lane, v);
+                if (live) {
+                    *reinterpret_cast<float2*>(out + 2 * (size_t)row) =
+                        make_float2(v[0] + s_b[3 * kHid], v[1] + s_b[3 * kHid + 1]);
+                }
+                // the next tile's first MMA overwrites these columns
+                tc_before();
             }
         }
     }
     if (!ok) {
-        if (t == 0) atomicAdd(err, 1ull);
+        if (threadIdx.x == 0) atomicAdd(err, 1ull);
         // let any MMA still in flight land before the tensor memory is freed
         bar_wait(&bar, 0);
         bar_wait(&bar, 1);
@@ -471,10 +510,19 @@ void launch_mlp_pack(cudaStream_t s, const float* params, const MlpNet& net) {
 void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16* X, int n, const MlpNet& net, float* out,
                         const MlpCache* cache, unsigned long long* err) {
     if (n <= 0) return;
+    // persistent: at most 4 CTAs per SM (smem allows 5), weights staged once each
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 148;
+    }
+    const int grid = std::min(nb(n, kRows), 4 * sms);
     if (cache)
-        k_mlp_forward<true><<<nb(n, kRows), kRows, kFwdSmem, s>>>(X, n, net, out, *cache, err);
+        k_mlp_forward<true><<<grid, kFwdThreads, kFwdSmem, s>>>(X, n, net, out, *cache, err);
     else
-        k_mlp_forward<false><<<nb(n, kRows), kRows, kFwdSmem, s>>>(X, n, net, out, MlpCache{}, err);
+        k_mlp_forward<false><<<grid, kFwdThreads, kFwdSmem, s>>>(X, n, net, out, MlpCache{}, err);
 }
 
 void launch_mlp_backward(cudaStream_t s, const __nv_bfloat16* X, const float* Y, int n, const MlpNet& net,
