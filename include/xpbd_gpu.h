@@ -214,9 +214,9 @@ int xpbd_residual(xpbd_ctx* ctx, double* abs_norm, double* rel);
  * [dev_0, hyd_0, dev_1, ...]; separate: all dev, then all hyd). */
 int xpbd_get_constraint_residual(xpbd_ctx* ctx, double* r, int64_t n);
 /* Per-iteration ||r|| of the last update when residual_policy is
- * EVERY_ITERATION: n = num_iters + 1 values (before each sweep, after the last).
- * Jacobi values are exact state residuals; Gauss-Seidel values are sweep
- * residuals (each tet evaluated when it is projected) except the last. */
+ * EVERY_ITERATION: num_iters + 1 exact state residuals (before each sweep,
+ * after the last); EVERY_SUBSTEP: 2 values (||r(x_pred, 0)||, the final one).
+ * Writes at most max_n values; *n_out = the number written. */
 int xpbd_residual_history(xpbd_ctx* ctx, double* out, int32_t max_n, int32_t* n_out);
 /* Lagrange multipliers, T x 2 (dev, hyd) in tet order. */
 int xpbd_get_lambda(xpbd_ctx* ctx, double* lam);

@@ -414,3 +414,16 @@ def test_beam_full_size_with_sphere(lib):
     assert np.isfinite(x).all()
     np.testing.assert_allclose(x[w.fixed], w.X[w.fixed], atol=1e-7)
     s.close()
+
+
+def test_residual_history_follows_set_num_iters(lib):
+    X, tets, faces, x0 = _noisy_cube(3, seed=8)
+    s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=4, residual_policy=G.RESIDUAL_EVERY_ITERATION)
+    s.set_positions(x0)
+    s.step(1)
+    assert len(s.residual_history()) == 5
+    s.set_num_iters(40)
+    s.step(1)
+    h = s.residual_history()
+    assert len(h) == 41 and np.all(np.isfinite(h)) and h[-1] < h[0]
+    s.close()

@@ -1150,11 +1150,11 @@ int xpbd_residual_history(xpbd_ctx* c, double* out, int32_t max_n, int32_t* n_ou
         // only r(x_pred, 0) and the final residual are evaluated
         if (max_n > 0) out[0] = std::sqrt(c->h_rows[0]);
         if (max_n > 1) out[1] = std::sqrt(c->h_rows[n - 1]);
-        *n_out = 2;
+        *n_out = std::min(2, max_n);
         return XPBD_OK;
     }
     for (int i = 0; i < n && i < max_n; i++) out[i] = std::sqrt(c->h_rows[i]);
-    *n_out = n;
+    *n_out = std::min(n, max_n);
     return XPBD_OK;
 }
 

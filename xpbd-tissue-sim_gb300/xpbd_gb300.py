@@ -339,6 +339,7 @@ class XPBDSolver:
 
     def set_num_iters(self, n):
         self._ck(self.L.xpbd_set_num_iters(self.h, int(n)))
+        self.params.num_iters = int(n)
 
     # ---- collisions ----
     def set_spheres(self, centers, radii, instance=0):
