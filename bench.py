@@ -144,14 +144,17 @@ def measured_peaks():
 
 
 def profiled_traffic(kernel, workload_name):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
-    p = os.path.join(ROOT, "profiles", "roofline_traffic.json")
+    """DRAM bytes per launch of `kernel` from the committed ncu figures
+    (profiles/roofline_traffic.txt: `workload/kernel bytes summary` lines)."""
+    p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
-        d = json.load(f)
-    e = d.get(f"{workload_name}/{kernel}")
-    return None if e is None else e.get("dram_bytes_per_launch")
+        for line in f:
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#") and parts[0] == f"{workload_name}/{kernel}":
+                return float(parts[1])
+    return None
 
 
 def algorithmic_bytes(w, kernel):
