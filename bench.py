@@ -645,7 +645,7 @@ def main():
     ap.add_argument("--patch-tets", type=int, default=None, help="Gauss-Seidel patch size (1 = per-tet colouring)")
     ap.add_argument("--no-pdl", action="store_true", help="disable programmatic dependent launch")
     ap.add_argument("--min-blocks", type=int, default=0, choices=[0, 6, 8], help="patch kernel blocks/SM target")
-    ap.add_argument("--variant", type=int, default=None, choices=[0, 1], help="Gauss-Seidel sweep kernel variant")
+    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3], help="Gauss-Seidel sweep kernel variant")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

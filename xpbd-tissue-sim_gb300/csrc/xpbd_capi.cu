@@ -35,7 +35,7 @@ bool valid_params(const xpbd_params& p) {
            (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
            p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
            (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8) &&
-           p.gs_variant >= 0 && p.gs_variant < kGsVariants && p.num_local_collision_iters >= 0 &&
+           p.gs_variant >= 0 && p.gs_variant <= 3 && p.num_local_collision_iters >= 0 &&
            p.num_local_collision_iters <= 1000;
 }
 
@@ -317,6 +317,13 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
+    } else if (!separate && !every_iter && !have_faces && p.gs_variant >= 2 && c->ntasks > 0) {
+        // every iteration and colour in one cooperative launch
+        if (track && !warm) exact_residual_row(c, 0, false);
+        cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
+        Scope sc(c, K_PROJECT_GS);
+        launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
+                              c->flow_grid, p.gs_variant == 3);
     } else {
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
@@ -332,7 +339,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_PROJECT_GS);
                     launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
                                            c->x.p, f, which, c->flags.p, c->prm.gs_min_blocks ? c->prm.gs_min_blocks : 6,
-                                           c->prm.gs_variant);
+                                           c->prm.gs_variant == 2 ? 0 : (c->prm.gs_variant == 3 ? 1 : c->prm.gs_variant));
                 }
             }
             if (have_faces) {
@@ -463,6 +470,7 @@ void release(xpbd_ctx* c) {
     c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->local_slots.release(); c->vmask.release(); c->tmask.release();
+    c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
     c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
@@ -474,6 +482,78 @@ void release(xpbd_ctx* c) {
     c->h_rows = nullptr;
     if (c->stream) cudaStreamDestroy(c->stream);
     c->stream = nullptr;
+}
+
+// Dataflow tasks: runs of up to kTaskPatches consecutive patches of one colour
+// (tasks therefore in colour order), and for each task the tasks sharing a
+// vertex with it, flagged when theirs is the higher colour.
+int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vector<int4>& pverts) {
+    const int P = (int)pmeta.size(), V = c->V;
+    std::vector<int4> tasks;
+    std::vector<int> tcol, task_of(P);
+    for (int col = 0; col < c->n_tet_colours; col++)
+        for (int q = c->pcol_off[col]; q < c->pcol_off[col + 1]; q += kTaskPatches) {
+            const int n = std::min(kTaskPatches, c->pcol_off[col + 1] - q);
+            int slots = 0;
+            for (int k = 0; k < n; k++) {
+                task_of[q + k] = (int)tasks.size();
+                // the task's tets form one contiguous slot range (bulk-copied whole)
+                if (pmeta[q + k].x != pmeta[q].x + slots)
+                    return fail(c, XPBD_ERR_STATE, "dataflow: patch %d does not continue its task's slots", q + k);
+                slots += pmeta[q + k].y & 0xff;
+            }
+            tasks.push_back(make_int4(q, n, pmeta[q].x, slots));
+            tcol.push_back(col);
+        }
+    const int NT = (int)tasks.size();
+    auto pv = [&](int q, int k) {
+        const int4& a = pverts[2 * (size_t)q + (k >> 2)];
+        const int kk = k & 3;
+        return kk == 0 ? a.x : (kk == 1 ? a.y : (kk == 2 ? a.z : a.w));
+    };
+    // vertex -> tasks (CSR, deduplicated)
+    std::vector<int> voff(V + 1, 0);
+    for (int q = 0; q < P; q++)
+        for (int k = 0; k < (pmeta[q].y >> 8); k++) voff[pv(q, k) + 1]++;
+    for (int v = 0; v < V; v++) voff[v + 1] += voff[v];
+    std::vector<int> vt(voff[V]), fill(voff.begin(), voff.end() - 1);
+    for (int q = 0; q < P; q++)
+        for (int k = 0; k < (pmeta[q].y >> 8); k++) vt[fill[pv(q, k)]++] = task_of[q];
+    // per-task dependency lists
+    std::vector<int> doff(NT + 1, 0), dep;
+    std::vector<int> scratch;
+    for (int j = 0; j < NT; j++) {
+        scratch.clear();
+        for (int q = tasks[j].x; q < tasks[j].x + tasks[j].y; q++)
+            for (int k = 0; k < (pmeta[q].y >> 8); k++) {
+                const int v = pv(q, k);
+                for (int e = voff[v]; e < voff[v + 1]; e++)
+                    if (vt[e] != j) scratch.push_back(vt[e]);
+            }
+        std::sort(scratch.begin(), scratch.end());
+        scratch.erase(std::unique(scratch.begin(), scratch.end()), scratch.end());
+        for (int d : scratch) {
+            if (tcol[d] == tcol[j]) return fail(c, XPBD_ERR_STATE, "dataflow: tasks %d and %d share a colour and a vertex", j, d);
+            dep.push_back((d << 1) | (tcol[d] > tcol[j] ? 1 : 0));
+        }
+        doff[j + 1] = (int)dep.size();
+    }
+    const int per_sm = sweep_dataflow_blocks_per_sm(c->prm.gs_variant == 3);
+    int dev = 0, sms = 0;
+    XPBD_CU(c, cudaGetDevice(&dev));
+    XPBD_CU(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    if (per_sm <= 0 || sms <= 0) return fail(c, XPBD_ERR_CUDA, "dataflow sweep: no co-resident blocks");
+    c->ntasks = NT;
+    c->flow_grid = per_sm * sms;
+    XPBD_CU(c, c->flow_tasks.alloc(NT));
+    XPBD_CU(c, c->flow_dep_off.alloc(NT + 1));
+    XPBD_CU(c, c->flow_dep.alloc(std::max<size_t>(dep.size(), 1)));
+    XPBD_CU(c, c->flow_epoch.alloc(NT + 1));
+    XPBD_CU(c, cudaMemcpy(c->flow_tasks.p, tasks.data(), sizeof(int4) * NT, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NT + 1), cudaMemcpyHostToDevice));
+    if (!dep.empty()) XPBD_CU(c, cudaMemcpy(c->flow_dep.p, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NT + 1)));
+    return XPBD_OK;
 }
 
 int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
@@ -715,6 +795,10 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, c->vmask.alloc(V));
         XPBD_CU(c, c->tmask.alloc(T));
         XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
+    }
+    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2) {
+        int st = build_flow_tasks(c, pmeta, pverts);
+        if (st) return st;
     }
     if (!pmeta.empty()) {
         XPBD_CU(c, c->patch_meta.alloc(pmeta.size()));

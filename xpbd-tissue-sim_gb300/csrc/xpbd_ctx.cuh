@@ -83,6 +83,11 @@ struct xpbd_ctx {
     std::vector<int> local_tets_h;       // the same order as tet indices
     DevBuf<int> local_slots;
     DevBuf<unsigned char> vmask, tmask;
+    // dataflow Gauss-Seidel (sweep variant 2): tasks, dependencies, epochs
+    int ntasks = 0, flow_grid = 0;
+    DevBuf<int4> flow_tasks;
+    DevBuf<int> flow_dep_off, flow_dep;
+    DevBuf<unsigned> flow_epoch;  // ntasks epochs + the abort flag
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -147,6 +152,9 @@ struct xpbd_ctx {
                           mlp_p.p + xg::kOffB4, mlp_w4f.p};
     }
 
+    xg::TaskArrays tasks() {
+        return xg::TaskArrays{flow_tasks.p, flow_dep_off.p, flow_dep.p, flow_epoch.p, flow_epoch.p + ntasks, ntasks};
+    }
     TetArrays tets() {
         return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
     }

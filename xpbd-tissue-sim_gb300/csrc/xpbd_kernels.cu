@@ -337,6 +337,13 @@ __device__ __forceinline__ void load_tet_static(const TetArrays& t, int slot, in
     s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
 }
 
+// A vertex moved by a projection's update. The adds are not contracted with
+// the update's last multiply, so every Gauss-Seidel kernel variant rounds the
+// same way and their results agree bit for bit.
+__device__ __forceinline__ float4 moved(const float4& p, const float* d) {
+    return make_float4(__fadd_rn(p.x, d[0]), __fadd_rn(p.y, d[1]), __fadd_rn(p.z, d[2]), p.w);
+}
+
 __device__ __forceinline__ void gather_tet(const float4* __restrict__ x, const int4& e, TetState<float>& s,
                                            float4 xp[4]) {
     xp[0] = x[e.x]; xp[1] = x[e.y]; xp[2] = x[e.z]; xp[3] = x[e.w];
@@ -701,7 +708,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t
         if (ok) {
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                sv[l[j]][tid] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
+                sv[l[j]][tid] = moved(xp[j], d[j]);
         }
         t.lam[slot] = lam;
     }
@@ -789,7 +796,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch_reg(TetArrays t, 
         if (ok) {
 #pragma unroll
             for (int j = 0; j < 4; j++)
-                sv[l[j]][tid] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
+                sv[l[j]][tid] = moved(xp[j], d[j]);
         }
         t.lam[slot] = lam;
     }
@@ -1006,6 +1013,252 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
     }
 }
 
+// ---- dataflow Gauss-Seidel: all iterations and colours in one cooperative launch ----
+constexpr unsigned kFlowLimit = 1u << 21;  // polls of one dependency before giving up
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// One warp per task, the warp's tasks in (iteration, colour, index) order. The
+// smallest unfinished task always has its dependencies done and its warp at
+// it (all blocks are co-resident), so the waits end; each is bounded anyway,
+// and a wait that gives up sets abort_flag so that every other waiter leaves.
+// The projections, their order and their arithmetic are those of
+// k_project_patch_reg, so results equal the colour-by-colour launches.
+template <bool FIRST_ZERO>
+__global__ void __launch_bounds__(kPatchBlock) k_sweep_dataflow(TetArrays t, PatchArrays pa, TaskArrays ta, int iters,
+                                                            float4* __restrict__ x, Flags* flags) {
+    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    pdl_wait_then_release();
+    for (int it = 0; it < iters; it++) {
+        for (int j = gw; j < ta.ntasks; j += nw) {
+            const int4 tk = __ldg(ta.task + j);
+            const int p = tk.x + lane;
+            const bool active = lane < tk.y;
+            // static data first: it does not depend on other tasks
+            int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
+            TetState<float> st[kMaxPatchTets];
+            int ntets = 0, nverts = 0;
+            if (active) {
+                meta = __ldg(pa.meta + p);
+                va = __ldg(pa.verts + 2 * (size_t)p);
+                vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+                ntets = meta.y & 0xff;
+                nverts = meta.y >> 8;
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++) {
+                    if (i < ntets) {
+                        int4 dummy;
+                        load_tet_static(t, meta.x + i, dummy, st[i]);
+                    }
+                }
+            }
+            // dependencies: lower colours at it + 1, higher colours at it
+            bool ok = true;
+            const int d1 = __ldg(ta.dep_off + j + 1);
+            for (int d = __ldg(ta.dep_off + j) + lane; d < d1 && ok; d += 32) {
+                const int e = __ldg(ta.dep + d);
+                const unsigned need = (e & 1) ? (unsigned)it : (unsigned)it + 1u;
+                const unsigned* f = ta.epoch + (e >> 1);
+                unsigned n = 0;
+                while (ld_acquire_u32(f) < need) {
+                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) {
+                    atomicExch(ta.abort_flag, 1u);
+                    atomicAdd(&flags->timeouts, 1ull);
+                }
+                return;
+            }
+            __syncwarp();
+            if (active) {
+                const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+                float2 lams[kMaxPatchTets];
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++)
+                    lams[i] = (!(FIRST_ZERO && it == 0) && i < ntets) ? __ldcg(t.lam + meta.x + i)
+                                                                      : make_float2(0.f, 0.f);
+                // positions other warps wrote: read past L1
+#pragma unroll
+                for (int k = 0; k < kMaxPatchVerts; k++)
+                    if (k < nverts) sv[k][tid] = __ldcg(x + vid[k]);
+                const unsigned long long loc =
+                    (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++) {
+                    if (i >= ntets) break;
+                    const int slot = meta.x + i;
+                    int l[4];
+                    float4 xp[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+                        xp[q] = sv[l[q]][tid];
+                        st[i].p[q][0] = xp[q].x; st[i].p[q][1] = xp[q].y; st[i].p[q][2] = xp[q].z;
+                        st[i].w[q] = fabsf(xp[q].w);
+                    }
+                    float2 lam = lams[i];
+                    float d[4][3], rsq;
+                    if (project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags)) {
+#pragma unroll
+                        for (int q = 0; q < 4; q++)
+                            sv[l[q]][tid] = moved(xp[q], d[q]);
+                    }
+                    t.lam[slot] = lam;
+                }
+#pragma unroll
+                for (int k = 0; k < kMaxPatchVerts; k++)
+                    if (k < nverts) x[vid[k]] = sv[k][tid];
+            }
+            // every lane's stores are ordered before the warp's release
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_release_u32(ta.epoch + j, (unsigned)it + 1u);
+        }
+    }
+}
+
+// Dataflow sweep with the task's static tet records staged in shared memory:
+// lane 0 issues three bulk copies (q0, q1, q2 over the task's contiguous slot
+// range) before the dependency wait; each warp owns its staging buffer and
+// mbarrier. Same projections, order and arithmetic as k_sweep_dataflow.
+constexpr int kFlowWarps = kPatchBlock / 32;
+constexpr int kTaskSlots = kTaskPatches * kMaxPatchTets;
+
+template <bool FIRST_ZERO>
+__global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArrays t, PatchArrays pa, TaskArrays ta,
+                                                                         int iters, float4* __restrict__ x,
+                                                                         Flags* flags) {
+    __shared__ __align__(128) float4 sq[kFlowWarps][3][kTaskSlots];
+    __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
+    __shared__ __align__(8) unsigned long long bar[kFlowWarps];
+    const int tid = threadIdx.x, lane = tid & 31, wib = tid >> 5;
+    const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (lane == 0) mbar_init(&bar[wib], 1);
+    __syncwarp();
+    unsigned phase = 0;
+    pdl_wait_then_release();
+    for (int it = 0; it < iters; it++) {
+        for (int j = gw; j < ta.ntasks; j += nw) {
+            const int4 tk = __ldg(ta.task + j);
+            if (lane == 0) {
+                // the previous task's reads of sq are done (syncwarp below)
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const unsigned bytes = (unsigned)tk.w * 16u;
+                mbar_arrive_expect_tx(&bar[wib], 3u * bytes);
+                tma_load_1d(sq[wib][0], t.q0 + tk.z, bytes, &bar[wib]);
+                tma_load_1d(sq[wib][1], t.q1 + tk.z, bytes, &bar[wib]);
+                tma_load_1d(sq[wib][2], t.q2 + tk.z, bytes, &bar[wib]);
+            }
+            const int p = tk.x + lane;
+            const bool active = lane < tk.y;
+            int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
+            int ntets = 0, nverts = 0;
+            if (active) {
+                meta = __ldg(pa.meta + p);
+                va = __ldg(pa.verts + 2 * (size_t)p);
+                vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+                ntets = meta.y & 0xff;
+                nverts = meta.y >> 8;
+            }
+            bool ok = true;
+            const int d1 = __ldg(ta.dep_off + j + 1);
+            for (int d = __ldg(ta.dep_off + j) + lane; d < d1 && ok; d += 32) {
+                const int e = __ldg(ta.dep + d);
+                const unsigned need = (e & 1) ? (unsigned)it : (unsigned)it + 1u;
+                const unsigned* f = ta.epoch + (e >> 1);
+                unsigned n = 0;
+                while (ld_acquire_u32(f) < need) {
+                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(32);
+                }
+            }
+            ok = __all_sync(0xffffffffu, ok) != 0;
+            const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+            float2 lams[kMaxPatchTets];
+            if (ok && active) {
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++)
+                    lams[i] = (!(FIRST_ZERO && it == 0) && i < ntets) ? __ldcg(t.lam + meta.x + i)
+                                                                      : make_float2(0.f, 0.f);
+#pragma unroll
+                for (int k = 0; k < kMaxPatchVerts; k++)
+                    if (k < nverts) sv[k][tid] = __ldcg(x + vid[k]);
+            }
+            // the copies land (or not) whatever happened above
+            const bool staged = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[wib], phase, kWaitLimit)) != 0;
+            phase ^= 1u;
+            if (!ok || !staged) {
+                if (lane == 0) {
+                    atomicExch(ta.abort_flag, 1u);
+                    atomicAdd(&flags->timeouts, 1ull);
+                    if (!staged) mbar_wait_bounded(&bar[wib], phase ^ 1u, kWaitLimit);
+                }
+                __syncwarp();
+                return;
+            }
+            if (active) {
+                const int base = meta.x - tk.z;
+                const unsigned long long loc =
+                    (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++) {
+                    if (i >= ntets) break;
+                    const int slot = meta.x + i;
+                    TetState<float> st;
+                    {
+                        const float4 a = sq[wib][0][base + i], b = sq[wib][1][base + i], c = sq[wib][2][base + i];
+                        st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
+                        st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
+                        st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
+                    }
+                    int l[4];
+                    float4 xp[4];
+#pragma unroll
+                    for (int q = 0; q < 4; q++) {
+                        l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+                        xp[q] = sv[l[q]][tid];
+                        st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+                        st.w[q] = fabsf(xp[q].w);
+                    }
+                    float2 lam = lams[i];
+                    float d[4][3], rsq;
+                    if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
+#pragma unroll
+                        for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
+                    }
+                    t.lam[slot] = lam;
+                }
+#pragma unroll
+                for (int k = 0; k < kMaxPatchVerts; k++)
+                    if (k < nverts) x[vid[k]] = sv[k][tid];
+            }
+            __threadfence();
+            __syncwarp();
+            if (lane == 0) st_release_u32(ta.epoch + j, (unsigned)it + 1u);
+        }
+    }
+}
+
 // ---- local collision iterations (XPBDMeshObject.cpp:472-505, 764-825) ----
 // Vertices of every contact that was projected (lambda != 0) in the global
 // solve; vmask must be cleared first.
@@ -1073,7 +1326,7 @@ __global__ void k_project_local_gs(TetArrays t, const int* __restrict__ order, i
         const int v[4] = {e.x, e.y, e.z, e.w};
 #pragma unroll
         for (int j = 0; j < 4; j++)
-            x[v[j]] = make_float4(xp[j].x + d[j][0], xp[j].y + d[j][1], xp[j].z + d[j][2], xp[j].w);
+            x[v[j]] = moved(xp[j], d[j]);
     }
     t.lam[slot] = lam;
 }
@@ -1359,6 +1612,41 @@ void launch_residual(const Launch& s, int block, const TetArrays& t, int T, cons
                      bool zero_lam) {
     if (T <= 0) return;
     go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2, zero_lam);
+}
+
+int sweep_dataflow_blocks_per_sm(bool staged) {
+    int n = 0, m = 0;
+    cudaError_t e;
+    if (staged) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow_staged<true>, kPatchBlock, 0);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow_staged<false>, kPatchBlock, 0);
+    } else {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true>, kPatchBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false>, kPatchBlock, 0);
+    }
+    if (e != cudaSuccess) return 0;
+    return n < m ? n : m;
+}
+
+cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const PatchArrays& pa, const TaskArrays& ta,
+                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged) {
+    if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kPatchBlock);
+    cfg.stream = s.s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (staged) {
+        if (first_zero) return cudaLaunchKernelEx(&cfg, k_sweep_dataflow_staged<true>, t, pa, ta, iters, x, flags);
+        return cudaLaunchKernelEx(&cfg, k_sweep_dataflow_staged<false>, t, pa, ta, iters, x, flags);
+    }
+    if (first_zero) return cudaLaunchKernelEx(&cfg, k_sweep_dataflow<true>, t, pa, ta, iters, x, flags);
+    return cudaLaunchKernelEx(&cfg, k_sweep_dataflow<false>, t, pa, ta, iters, x, flags);
 }
 
 void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,

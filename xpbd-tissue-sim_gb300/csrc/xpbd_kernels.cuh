@@ -74,6 +74,22 @@ struct PatchArrays {
 
 constexpr int kMaxSpheres = 16;  // sphere slots per instance
 
+// Dataflow Gauss-Seidel (sweep variant 2): every iteration and colour in one
+// cooperative launch. A task is up to 32 consecutive patches of one colour,
+// run by one warp; a task waits until every task sharing a vertex with it has
+// reached the right iteration (lower colours: this one, higher colours: the
+// previous one), which is exactly the order of the colour-by-colour launches.
+constexpr int kTaskPatches = 32;
+struct TaskArrays {
+    const int4* task;     // [ntasks] first patch, patch count, first slot, slot count;
+                          // tasks in colour order
+    const int* dep_off;   // [ntasks + 1] CSR into dep
+    const int* dep;       // (task << 1) | 1 when that task has the higher colour
+    unsigned* epoch;      // [ntasks] iterations completed; zeroed before each launch
+    unsigned* abort_flag; // set when a wait gives up; every waiter then leaves
+    int ntasks;
+};
+
 struct Flags {
     unsigned long long nonfinite;
     unsigned long long degenerate;
@@ -145,6 +161,12 @@ void launch_apply(const Launch& s, float4* x, float4* dx, int V, float4* prev, f
                   float dt, bool write_vel);
 void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArrays& pa, int pbegin, int pend,
                             float4* x, bool first, int which, Flags* flags, int min_blocks, int variant);
+// returns the launch's status (cooperative launches can be refused)
+// staged = true: the task's static tet records arrive in shared memory by bulk
+// copies issued before the dependency wait (fewer registers, more warps)
+cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const PatchArrays& pa, const TaskArrays& ta,
+                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged);
+int sweep_dataflow_blocks_per_sm(bool staged);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);
