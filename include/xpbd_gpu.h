@@ -103,7 +103,7 @@ typedef struct {
                                /* dependency counters (combined constraints, no    */
                                /* faces, no per-iteration residual; else as 0);    */
                                /* 3 dataflow with records staged by bulk copies    */
-                               /* (else as 1)                                      */
+                               /* (else as 1); default 2                           */
     int32_t num_local_collision_iters; /* num-local-collision-iters: passes    */
                                /* after the global solve over every contact    */
                                /* and the tets touching a vertex of a contact  */

@@ -323,7 +323,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
         Scope sc(c, K_PROJECT_GS);
         launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
-                              c->flow_grid, p.gs_variant == 3);
+                              c->flow_grid, p.gs_variant == 3, p.gs_min_blocks);
     } else {
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
@@ -538,7 +538,7 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         }
         doff[j + 1] = (int)dep.size();
     }
-    const int per_sm = sweep_dataflow_blocks_per_sm(c->prm.gs_variant == 3);
+    const int per_sm = sweep_dataflow_blocks_per_sm(c->prm.gs_variant == 3, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
     XPBD_CU(c, cudaGetDevice(&dev));
     XPBD_CU(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -796,7 +796,8 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, c->tmask.alloc(T));
         XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     }
-    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2) {
+    // (faces allow contacts, which the dataflow sweep leaves to the launches)
+    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2 && F == 0) {
         int st = build_flow_tasks(c, pmeta, pverts);
         if (st) return st;
     }
@@ -868,7 +869,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->use_pdl = 1;
     p->gs_patch_tets = 0;
     p->gs_min_blocks = 0;
-    p->gs_variant = 0;
+    p->gs_variant = 2;
     p->num_local_collision_iters = 0;
     return XPBD_OK;
 }
@@ -1406,7 +1407,8 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
         for (int patch : {1, 2, 3, 5})
             for (int pdl : {0, 1})
-                for (int var_minb : {6, 16, 18}) {  // variant x min blocks: (0,-) (1,6) (1,8)
+                // variant x min blocks: (0,-) (1,6) (1,8) (2,uncapped) (3,-)
+                for (int var_minb : {6, 16, 18, 20, 30}) {
                     xpbd_params q = base;
                     q.gs_patch_tets = patch;
                     q.use_pdl = pdl;

@@ -1031,9 +1031,9 @@ __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
 // and a wait that gives up sets abort_flag so that every other waiter leaves.
 // The projections, their order and their arithmetic are those of
 // k_project_patch_reg, so results equal the colour-by-colour launches.
-template <bool FIRST_ZERO>
-__global__ void __launch_bounds__(kPatchBlock) k_sweep_dataflow(TetArrays t, PatchArrays pa, TaskArrays ta, int iters,
-                                                            float4* __restrict__ x, Flags* flags) {
+template <bool FIRST_ZERO, int MINB>
+__global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays t, PatchArrays pa, TaskArrays ta,
+                                                                  int iters, float4* __restrict__ x, Flags* flags) {
     __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
     const int tid = threadIdx.x, lane = tid & 31;
     const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
@@ -1046,7 +1046,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_sweep_dataflow(TetArrays t, Pat
             const bool active = lane < tk.y;
             // static data first: it does not depend on other tasks
             int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
-            TetState<float> st[kMaxPatchTets];
+            float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
             int ntets = 0, nverts = 0;
             if (active) {
                 meta = __ldg(pa.meta + p);
@@ -1057,8 +1057,9 @@ __global__ void __launch_bounds__(kPatchBlock) k_sweep_dataflow(TetArrays t, Pat
 #pragma unroll
                 for (int i = 0; i < kMaxPatchTets; i++) {
                     if (i < ntets) {
-                        int4 dummy;
-                        load_tet_static(t, meta.x + i, dummy, st[i]);
+                        r0[i] = __ldg(t.q0 + meta.x + i);
+                        r1[i] = __ldg(t.q1 + meta.x + i);
+                        r2[i] = __ldg(t.q2 + meta.x + i);
                     }
                 }
             }
@@ -1103,18 +1104,22 @@ __global__ void __launch_bounds__(kPatchBlock) k_sweep_dataflow(TetArrays t, Pat
                 for (int i = 0; i < kMaxPatchTets; i++) {
                     if (i >= ntets) break;
                     const int slot = meta.x + i;
+                    TetState<float> st;
+                    st.q[0] = r0[i].x; st.q[1] = r0[i].y; st.q[2] = r0[i].z; st.q[3] = r0[i].w;
+                    st.q[4] = r1[i].x; st.q[5] = r1[i].y; st.q[6] = r1[i].z; st.q[7] = r1[i].w;
+                    st.q[8] = r2[i].x; st.atd = r2[i].y; st.ath = r2[i].z; st.gam = r2[i].w;
                     int l[4];
                     float4 xp[4];
 #pragma unroll
                     for (int q = 0; q < 4; q++) {
                         l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
                         xp[q] = sv[l[q]][tid];
-                        st[i].p[q][0] = xp[q].x; st[i].p[q][1] = xp[q].y; st[i].p[q][2] = xp[q].z;
-                        st[i].w[q] = fabsf(xp[q].w);
+                        st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+                        st.w[q] = fabsf(xp[q].w);
                     }
                     float2 lam = lams[i];
                     float d[4][3], rsq;
-                    if (project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags)) {
+                    if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
                         for (int q = 0; q < 4; q++)
                             sv[l[q]][tid] = moved(xp[q], d[q]);
@@ -1614,23 +1619,30 @@ void launch_residual(const Launch& s, int block, const TetArrays& t, int T, cons
     go(k_residual, nblk(T, block), block, s, t, T, x, separate, perm, rvec, res, energy_partial, dt2, zero_lam);
 }
 
-int sweep_dataflow_blocks_per_sm(bool staged) {
+int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks) {
     int n = 0, m = 0;
     cudaError_t e;
     if (staged) {
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow_staged<true>, kPatchBlock, 0);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow_staged<false>, kPatchBlock, 0);
+    } else if (min_blocks == 8) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 8>, kPatchBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 8>, kPatchBlock, 0);
+    } else if (min_blocks == 6) {
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 6>, kPatchBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 6>, kPatchBlock, 0);
     } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true>, kPatchBlock, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false>, kPatchBlock, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 1>, kPatchBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 1>, kPatchBlock, 0);
     }
     if (e != cudaSuccess) return 0;
     return n < m ? n : m;
 }
 
 cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const PatchArrays& pa, const TaskArrays& ta,
-                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged) {
+                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged,
+                                  int min_blocks) {
     if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
@@ -1645,8 +1657,12 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
         if (first_zero) return cudaLaunchKernelEx(&cfg, k_sweep_dataflow_staged<true>, t, pa, ta, iters, x, flags);
         return cudaLaunchKernelEx(&cfg, k_sweep_dataflow_staged<false>, t, pa, ta, iters, x, flags);
     }
-    if (first_zero) return cudaLaunchKernelEx(&cfg, k_sweep_dataflow<true>, t, pa, ta, iters, x, flags);
-    return cudaLaunchKernelEx(&cfg, k_sweep_dataflow<false>, t, pa, ta, iters, x, flags);
+#define XG_FLOW(F, M) return cudaLaunchKernelEx(&cfg, k_sweep_dataflow<F, M>, t, pa, ta, iters, x, flags)
+    if (min_blocks == 8) { if (first_zero) XG_FLOW(true, 8); else XG_FLOW(false, 8); }
+    if (min_blocks == 6) { if (first_zero) XG_FLOW(true, 6); else XG_FLOW(false, 6); }
+    if (first_zero) XG_FLOW(true, 1);
+    XG_FLOW(false, 1);
+#undef XG_FLOW
 }
 
 void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,

@@ -165,8 +165,10 @@ void launch_project_patches(const Launch& s, const TetArrays& t, const PatchArra
 // staged = true: the task's static tet records arrive in shared memory by bulk
 // copies issued before the dependency wait (fewer registers, more warps)
 cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const PatchArrays& pa, const TaskArrays& ta,
-                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged);
-int sweep_dataflow_blocks_per_sm(bool staged);
+                                  int iters, bool first_zero, float4* x, Flags* flags, int grid, bool staged,
+                                  int min_blocks);
+// min_blocks (variant 2): 0 = no register cap, 6 or 8 blocks per SM
+int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);
