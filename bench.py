@@ -143,16 +143,17 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel, workload_name):
+def profiled_traffic(kernel, workload_name, variant):
     """DRAM bytes per launch of `kernel` from the committed ncu figures
-    (profiles/roofline_traffic.txt: `workload/kernel bytes summary` lines)."""
+    (profiles/roofline_traffic.txt: `workload/kernel/v<variant> bytes summary`
+    lines; a launch is one colour for variants 0/1, one substep for 2/3)."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         for line in f:
             parts = line.split()
-            if len(parts) >= 2 and not line.startswith("#") and parts[0] == f"{workload_name}/{kernel}":
+            if len(parts) >= 2 and not line.startswith("#") and parts[0] == f"{workload_name}/{kernel}/v{variant}":
                 return float(parts[1])
     return None
 
@@ -444,7 +445,7 @@ def run_ours(args):
     if sweep_bytes is not None:
         per_launch = sweep_bytes / (nl_step / w.iters) if dom == "project_gs" else sweep_bytes
         achieved = per_launch / (ms_launch * 1e-3) / 1e9
-        traffic = profiled_traffic(dom, w.name)
+        traffic = profiled_traffic(dom, w.name, s.params.gs_variant)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                     "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": ms_launch,

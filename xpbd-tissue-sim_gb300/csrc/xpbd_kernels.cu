@@ -1024,11 +1024,16 @@ __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
 __device__ __forceinline__ void st_release_u32(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
 
 // One warp per task, the warp's tasks in (iteration, colour, index) order. The
 // smallest unfinished task always has its dependencies done and its warp at
 // it (all blocks are co-resident), so the waits end; each is bounded anyway,
 // and a wait that gives up sets abort_flag so that every other waiter leaves.
+// A task's epoch counts lane releases (32 per iteration): every lane's
+// red.release orders its own position and multiplier stores before it.
 // The projections, their order and their arithmetic are those of
 // k_project_patch_reg, so results equal the colour-by-colour launches.
 template <bool FIRST_ZERO, int MINB>
@@ -1068,7 +1073,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
             const int d1 = __ldg(ta.dep_off + j + 1);
             for (int d = __ldg(ta.dep_off + j) + lane; d < d1 && ok; d += 32) {
                 const int e = __ldg(ta.dep + d);
-                const unsigned need = (e & 1) ? (unsigned)it : (unsigned)it + 1u;
+                const unsigned need = 32u * ((e & 1) ? (unsigned)it : (unsigned)it + 1u);
                 const unsigned* f = ta.epoch + (e >> 1);
                 unsigned n = 0;
                 while (ld_acquire_u32(f) < need) {
@@ -1130,10 +1135,9 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
                 for (int k = 0; k < kMaxPatchVerts; k++)
                     if (k < nverts) x[vid[k]] = sv[k][tid];
             }
-            // every lane's stores are ordered before the warp's release
-            __threadfence();
-            __syncwarp();
-            if (lane == 0) st_release_u32(ta.epoch + j, (unsigned)it + 1u);
+            // each lane releases its own stores: the task's epoch counts lanes,
+            // 32 per completed iteration
+            red_release_add_u32(ta.epoch + j, 1u);
         }
     }
 }

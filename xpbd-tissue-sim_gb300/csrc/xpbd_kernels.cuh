@@ -85,7 +85,8 @@ struct TaskArrays {
                           // tasks in colour order
     const int* dep_off;   // [ntasks + 1] CSR into dep
     const int* dep;       // (task << 1) | 1 when that task has the higher colour
-    unsigned* epoch;      // [ntasks] iterations completed; zeroed before each launch
+    unsigned* epoch;      // [ntasks] progress (variant 2: 32 lane releases per iteration,
+                          // variant 3: iterations); zeroed before each launch
     unsigned* abort_flag; // set when a wait gives up; every waiter then leaves
     int ntasks;
 };
