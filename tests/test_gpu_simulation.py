@@ -1,0 +1,110 @@
+"""The YAML-configured Simulation loop on the GPU: equal to driving the
+solver by hand with the same placed mesh and parameters, and to the FP64
+oracle."""
+import numpy as np
+import pytest
+
+import msh
+import oracle as O
+import simulation as S
+import xpbd_gb300 as G
+
+pytestmark = pytest.mark.gpu
+
+SCENE = """
+name: "Scene"
+visualization: "None"
+sim-mode: "AFAP"
+time-step: 1e-3
+collision-rate: 100
+end-time: {end}
+g-accel: 9.81
+materials:
+  - name: "Soft"
+    density: 1000
+    E: 3e3
+    nu: 0.45
+  - name: "Stiff"
+    density: 1200
+    E: 3e4
+    nu: 0.4
+objects:
+  - name: "Cube"
+    type: "XPBDMeshObject"
+    filename: "cube.msh"
+    materials: ["Soft", "Stiff"]
+    {classes}
+    max-size: 0.5
+    position: [0.1, 0, 0.5]
+    rotation: [0, 0, 30]
+    collisions: {coll}
+    num-solver-iters: 6
+    solver-type: "{solver}"
+  - name: "Ball"
+    type: "RigidSphere"
+    radius: 0.2
+    position: [0.1, 0, 0.93]
+    fixed: true
+    collisions: true
+"""
+
+
+def _scene(tmp_path, end=0.04, coll="true", solver="Gauss-Seidel", classes=None):
+    X, tets, faces = G.grid_mesh(4, 4, 4, 0.25)
+    msh.write_msh(str(tmp_path / "cube.msh"), X, tets, faces)
+    cl = ""
+    if classes is not None:
+        (tmp_path / "classes.txt").write_text("\n".join(str(int(c)) for c in classes) + "\n")
+        cl = 'element-classes-filename: "classes.txt"'
+    cfg = tmp_path / "scene.yaml"
+    cfg.write_text(SCENE.format(end=end, coll=coll, solver=solver, classes=cl))
+    return str(cfg), X, tets, faces
+
+
+@pytest.mark.parametrize("solver", ["Gauss-Seidel", "Jacobi"])
+def test_simulation_equals_the_solver_driven_by_hand(lib, tmp_path, solver):
+    cfg, X, tets, faces = _scene(tmp_path, solver=solver)
+    with S.Simulation(cfg) as sim:
+        sim.setup()
+        n = sim.update()
+        assert n == 40 and abs(sim.time - 0.04) < 1e-12
+        got = sim.objects["Cube"].positions()
+    Xp = msh.place(X, faces, (0.1, 0, 0.5), (0, 0, 30), 0.5, None)
+    T = tets.shape[0]
+    s = G.XPBDSolver(Xp, tets, faces, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0), dt=1e-3,
+                     collision_rate=100, num_iters=6, solver_type=G.SOLVER_TYPES[solver])
+    s.set_spheres([[0.1, 0, 0.93]], [0.2])
+    s.step(40)
+    np.testing.assert_array_equal(got, s.positions())
+    assert len(s.collisions()) > 0  # the sphere reaches the top face
+    s.close()
+
+
+def test_element_classes_pick_materials(lib, tmp_path):
+    X, tets, faces = G.grid_mesh(4, 4, 4, 0.25)
+    classes = (np.arange(tets.shape[0]) % 3 == 0).astype(int)
+    cfg, _, _, _ = _scene(tmp_path, coll="false", classes=classes)
+    with S.Simulation(cfg) as sim:
+        sim.setup()
+        o = sim.objects["Cube"]
+        np.testing.assert_array_equal(o.E, np.where(classes == 1, 3e4, 3e3))
+        np.testing.assert_array_equal(o.rho, np.where(classes == 1, 1200.0, 1000.0))
+        sim.update()
+        got = o.positions()
+    Xp = msh.place(X, faces, (0.1, 0, 0.5), (0, 0, 30), 0.5, None)
+    ref = O.Oracle(Xp, tets, faces, np.where(classes == 1, 3e4, 3e3), np.where(classes == 1, 0.4, 0.45),
+                   np.where(classes == 1, 1200.0, 1000.0), dt=1e-3, g=9.81, num_iter=6, solver=O.COLOURED_GS)
+    order_solver = G.XPBDSolver(Xp, tets, None, 3e3, 0.45, 1000.0, num_iters=6)
+    ref.set_order(order_solver.sweep_order())
+    order_solver.close()
+    ref.time_steps(40)
+    err = np.abs(got - ref.positions()).max()
+    assert err <= 1e-4 * 0.5, err
+    ref.close()
+
+
+def test_unprovided_objects_fail_loudly(lib, tmp_path):
+    cfg, _, _, _ = _scene(tmp_path)
+    text = open(cfg).read().replace("fixed: true", "fixed: false")
+    with pytest.raises(NotImplementedError):
+        S.Simulation(text, base_dir=str(tmp_path)).setup()
