@@ -61,8 +61,10 @@ def _scene(tmp_path, end=0.04, coll="true", solver="Gauss-Seidel", classes=None)
     return str(cfg), X, tets, faces
 
 
-@pytest.mark.parametrize("solver", ["Gauss-Seidel", "Jacobi"])
-def test_simulation_equals_the_solver_driven_by_hand(lib, tmp_path, solver):
+def test_simulation_equals_the_solver_driven_by_hand(lib, tmp_path):
+    """Gauss-Seidel is bit-reproducible, so the configured loop must equal the
+    hand-driven solver exactly (the plain-sum Jacobi's float atomics are not)."""
+    solver = "Gauss-Seidel"
     cfg, X, tets, faces = _scene(tmp_path, solver=solver)
     with S.Simulation(cfg) as sim:
         sim.setup()
@@ -76,8 +78,13 @@ def test_simulation_equals_the_solver_driven_by_hand(lib, tmp_path, solver):
     s.set_spheres([[0.1, 0, 0.93]], [0.2])
     s.step(40)
     np.testing.assert_array_equal(got, s.positions())
-    assert len(s.collisions()) > 0  # the sphere reaches the top face
+    # the sphere, 2 cm into the top face at the start, changed the motion
+    free = G.XPBDSolver(Xp, tets, None, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0), dt=1e-3,
+                        num_iters=6)
+    free.step(40)
+    assert np.abs(free.positions() - got).max() > 1e-3
     s.close()
+    free.close()
 
 
 def test_element_classes_pick_materials(lib, tmp_path):
