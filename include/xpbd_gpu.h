@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 2
+#define XPBD_ABI_VERSION 3
 
 /* status codes */
 #define XPBD_OK 0
@@ -108,6 +108,12 @@ typedef struct {
                                /* after the global solve over every contact    */
                                /* and the tets touching a vertex of a contact  */
                                /* projected with lambda != 0; 0 = off          */
+    int32_t first_order;       /* 1: FirstOrderXPBDMeshObject -- alpha~ = alpha/dt, */
+                               /* vertex damping B as the constraint inertia,   */
+                               /* x_z += -g m dt / B as the inertial move       */
+    int32_t adjust_damping_to_material; /* adjust-damping-to-material          */
+    double damping_multiplier; /* damping-multiplier: B = V_vertex * this       */
+                               /* (* E_v / (1 + nu_v) when adjusted); default 1 */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,

@@ -234,6 +234,12 @@ class Oracle:
         if self.L.xo_set_order(C.c_void_p(self.h), len(order), _p(order)) != 0:
             raise ValueError("not a permutation of the tets")
 
+    def set_first_order(self, damping_multiplier=1.0, adjust=False):
+        """FirstOrderXPBDMeshObject: alpha~ = alpha/dt, vertex damping as inertia."""
+        E = np.ascontiguousarray(np.broadcast_to(self._E, (self.T,)), np.float64)
+        nu = np.ascontiguousarray(np.broadcast_to(self._nu, (self.T,)), np.float64)
+        self.L.xo_set_first_order(C.c_void_p(self.h), C.c_double(damping_multiplier), int(adjust), _p(E), _p(nu))
+
     def set_local_iterations(self, iters, order=None):
         """num-local-collision-iters; `order` (a tet permutation) is the tet
         order of the coloured local passes."""

@@ -511,6 +511,45 @@ struct Object {
         face_colour.assign(F, 0);
     }
 
+    // 1st-order XPBD (FirstOrderXPBDMeshObject): alpha~ = alpha/dt and the
+    // vertex damping B as the constraint inertia (XPBDMeshObject.cpp:333-348,
+    // XPBDMeshObjectBase.hpp:131-137), with the vertex E and nu averaged over
+    // the attached elements (:321-329). E and nu are per tet.
+    bool first_order = false;
+    std::vector<R> damping;  // B per vertex
+    void set_first_order(double multiplier, bool adjust, const double* E, const double* nu) {
+        first_order = true;
+        std::vector<R> vvol(V, 0), vE(V, 0), vnu(V, 0);
+        std::vector<int> natt(V, 0);
+        for (long long t = 0; t < T; t++)
+            for (int k = 0; k < 4; k++) natt[tets[4 * t + k]]++;
+        for (long long t = 0; t < T; t++)
+            for (int k = 0; k < 4; k++) {
+                const int v = tets[4 * t + k];
+                vvol[v] += vol[t] / R(4.0);
+                vE[v] += (R)E[t] / natt[v];
+                vnu[v] += (R)nu[t] / natt[v];
+            }
+        damping.assign(V, 0);
+        for (long long i = 0; i < V; i++) {
+            damping[i] = adjust ? vvol[i] * (R)multiplier * vE[i] / (1 + vnu[i]) : vvol[i] * (R)multiplier;
+            inv_mass[i] = R(1.0) / damping[i];
+        }
+    }
+    R adt() const { return first_order ? dt : dt * dt; }
+
+    // _movePositionsInertially (XPBDMeshObject.cpp:446-470)
+    void move_inertially() {
+        for (long long i = 0; i < V; i++) {
+            if (first_order) {
+                x[3 * i + 2] += -g * mass[i] * dt / damping[i];
+            } else {
+                for (int k = 0; k < 3; k++) x[3 * i + k] += dt * vel[3 * i + k];
+                x[3 * i + 2] += -g * dt * dt;
+            }
+        }
+    }
+
     void use_colouring() {
         std::vector<int> col(T);
         int nc = greedy_colour(T, 4, tets.data(), V, col.data());
@@ -521,8 +560,8 @@ struct Object {
         n_face_colours = F ? greedy_colour(F, 3, faces.data(), V, face_colour.data()) : 0;
     }
 
-    R at_d(long long t) const { return alpha_d[t] / (dt * dt); }
-    R at_h(long long t) const { return alpha_h[t] / (dt * dt); }
+    R at_d(long long t) const { return alpha_d[t] / adt(); }
+    R at_h(long long t) const { return alpha_h[t] / adt(); }
 
     void project_tet_combined(long long t, R* dx) {
         const int* e = &tets[4 * t];
@@ -562,11 +601,11 @@ struct Object {
             compute_F(&x[3 * e[0]], &x[3 * e[1]], &x[3 * e[2]], &x[3 * e[3]], &Q[9 * t], F_);
             R Cd = dev_C(F_), Ch = hyd_C(F_, gamma[t]);
             if (ckind == COMBINED) {
-                r[2 * t] = Cd + alpha_d[t] / (dt * dt) * lam[2 * t];
-                r[2 * t + 1] = Ch + alpha_h[t] / (dt * dt) * lam[2 * t + 1];
+                r[2 * t] = Cd + alpha_d[t] / adt() * lam[2 * t];
+                r[2 * t + 1] = Ch + alpha_h[t] / adt() * lam[2 * t + 1];
             } else {  // separate: all Dev residuals, then all Hyd residuals
-                r[t] = Cd + alpha_d[t] / (dt * dt) * lam[2 * t];
-                r[T + t] = Ch + alpha_h[t] / (dt * dt) * lam[2 * t + 1];
+                r[t] = Cd + alpha_d[t] / adt() * lam[2 * t];
+                r[T + t] = Ch + alpha_h[t] / adt() * lam[2 * t + 1];
             }
         }
     }
@@ -719,10 +758,7 @@ struct Object {
     // initialisation is restored. Returns true when the warm start was kept.
     bool update_warm(const std::vector<R>& lam0, bool record_residual, bool fallback) {
         prev = x;
-        for (long long i = 0; i < V; i++) {
-            for (int k = 0; k < 3; k++) x[3 * i + k] += dt * vel[3 * i + k];
-            x[3 * i + 2] += -g * dt * dt;
-        }
+        move_inertially();
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;
         const double r_plain = residual_norm();
@@ -765,11 +801,7 @@ struct Object {
     // iteration and after the last one.
     void update(bool record_residual = false) {
         prev = x;
-        // _movePositionsInertially, 2nd order (XPBDMeshObject.cpp:446-470)
-        for (long long i = 0; i < V; i++) {
-            for (int k = 0; k < 3; k++) x[3 * i + k] += dt * vel[3 * i + k];
-            x[3 * i + 2] += -g * dt * dt;
-        }
+        move_inertially();
         // XPBDSolver::solve: lambda <- 0, num_iter sweeps (XPBDSolver.hpp:66-97)
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;

@@ -255,6 +255,14 @@ int xo_local_tets(void* p, int* out) {
     });
 }
 
+// 1st-order XPBD with the given damping multiplier (E, nu per tet)
+void xo_set_first_order(void* p, double multiplier, int adjust, const double* E, const double* nu) {
+    with((Handle*)p, [&](auto& o) {
+        o.set_first_order(multiplier, adjust != 0, E, nu);
+        return 0;
+    });
+}
+
 int xo_set_order(void* p, int n, const int* order) {
     return with((Handle*)p, [&](auto& o) {
         if (n != (int)o.T) return 1;

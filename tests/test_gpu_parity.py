@@ -505,3 +505,28 @@ def test_dataflow_sweep_full_block(lib, var):
         s.close()
     np.testing.assert_array_equal(out[0], out[2])
     assert np.abs(out[0] - out[1]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("solver,adjust", [(G.SOLVER_GAUSS_SEIDEL, 0), (G.SOLVER_JACOBI, 0),
+                                           (G.SOLVER_GAUSS_SEIDEL, 1)])
+def test_first_order_trajectory_matches_fp64_oracle(lib, solver, adjust):
+    """FirstOrderXPBDMeshObject: alpha~ = alpha/dt, vertex damping as the
+    constraint inertia, gravity as -g m dt / B per step; bottom fixed, 60
+    steps against the FP64 oracle (GPU sweep order replayed)."""
+    X, tets, faces, x0 = _noisy_cube(5, seed=11)
+    mult = 2e4 if not adjust else 2.0
+    s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=8, solver_type=solver, first_order=1,
+                     damping_multiplier=mult, adjust_damping_to_material=adjust)
+    o32, o64 = _oracle_pair(X, tets, faces, 3e3, 0.45, 1000.0, solver, 8, gpu=s)
+    fixed = X[:, 2] == 0
+    s.set_positions(x0); s.fix_vertices(fixed)
+    for o in (o32, o64):
+        o.set_first_order(mult, adjust=bool(adjust))
+        o.set_positions(x0); o.set_fixed(fixed)
+    s.step(60); o32.time_steps(60); o64.time_steps(60)
+    band = np.abs(o32.positions() - o64.positions()).max()
+    err = np.abs(s.positions() - o64.positions()).max()
+    assert err <= max(1e-4 * _extent(X), 3 * band), (err, band)
+    # the body moved (gravity acts through the damping)
+    assert np.abs(s.positions() - x0).max() > 1e-4
+    s.close()

@@ -115,3 +115,23 @@ def test_unprovided_objects_fail_loudly(lib, tmp_path):
     text = open(cfg).read().replace("fixed: true", "fixed: false")
     with pytest.raises(NotImplementedError):
         S.Simulation(text, base_dir=str(tmp_path)).setup()
+
+
+def test_first_order_object_from_config(lib, tmp_path):
+    cfg, X, tets, faces = _scene(tmp_path, coll="false")
+    text = open(cfg).read().replace('type: "XPBDMeshObject"',
+                                    'type: "FirstOrderXPBDMeshObject"\n    damping-multiplier: 5e3')
+    with S.Simulation(text, base_dir=str(tmp_path)) as sim:
+        sim.setup()
+        sim.update()
+        got = sim.objects["Cube"].positions()
+    Xp = msh.place(X, faces, (0.1, 0, 0.5), (0, 0, 30), 0.5, None)
+    T = tets.shape[0]
+    s = G.XPBDSolver(Xp, tets, None, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0), dt=1e-3, num_iters=6,
+                     first_order=1, damping_multiplier=5e3)
+    s.step(40)
+    np.testing.assert_array_equal(got, s.positions())
+    # unconstrained 1st-order body: a rigid drift of -g rho dt / multiplier per step
+    np.testing.assert_allclose(got - Xp, np.broadcast_to([0, 0, -40 * 9.81 * 1000 * 1e-3 / 5e3], Xp.shape),
+                               atol=2e-6)
+    s.close()

@@ -232,3 +232,32 @@ def test_greedy_colouring_is_valid_and_ordered(oracle_mod):
         assert len(np.unique(v)) == len(v)
     # greedy: each tet's colour is the smallest not used by earlier neighbours
     assert col[0] == 0
+
+
+def test_first_order_free_body_translates_at_g_rho_dt_over_multiplier():
+    """1st-order XPBD (FirstOrderXPBDMeshObject): with B = V_vertex * multiplier
+    every vertex has m / B = rho / multiplier, so an unconstrained body at rest
+    moves rigidly by -g rho dt / multiplier per step and stays undeformed
+    (XPBDMeshObject.cpp:333-348, 449-456)."""
+    import xpbd_gb300 as G
+    X, tets, faces = G.grid_mesh(3, 3, 3, 0.1)
+    for solver in (O.GAUSS_SEIDEL, O.JACOBI):
+        o = O.Oracle(X, tets, faces, 3e3, 0.45, 1000.0, dt=1e-3, g=9.81, num_iter=5, solver=solver)
+        o.set_first_order(5e4)
+        o.time_steps(10)
+        d = o.positions() - X
+        assert np.abs(d[:, :2]).max() < 1e-12
+        np.testing.assert_allclose(d[:, 2], -10 * 9.81 * 1000.0 * 1e-3 / 5e4, rtol=1e-9)
+        o.close()
+
+
+def test_first_order_damping_adjusted_to_material():
+    """adjust-damping-to-material: B = V_vertex * multiplier * E_v / (1 + nu_v)."""
+    import xpbd_gb300 as G
+    X, tets, faces = G.grid_mesh(2, 2, 2, 0.1)
+    o = O.Oracle(X, tets, faces, 2e3, 0.25, 1000.0, dt=1e-3, g=9.81, num_iter=3)
+    o.set_first_order(10.0, adjust=True)
+    o.time_steps(4)
+    d = o.positions() - X
+    np.testing.assert_allclose(d[:, 2], -4 * 9.81 * 1000.0 * 1e-3 / (10.0 * 2e3 / 1.25), rtol=1e-9)
+    o.close()

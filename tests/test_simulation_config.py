@@ -108,6 +108,9 @@ def test_config_objects_and_errors():
         S.SimulationConfig.from_node({"objects": [{"type": "Teapot"}]})
     with pytest.raises(NotImplementedError):
         S.SimulationConfig.from_node({"objects": [{"type": "RigidBox"}]})
+    fo = S.SimulationConfig.from_node({"objects": [{"type": "FirstOrderXPBDMeshObject", "damping-multiplier": 5e4}]})
+    assert fo.objects[0].first_order and fo.objects[0].damping_multiplier == 5e4
+    assert not fo.objects[0].adjust_damping_to_material
     with pytest.raises(ValueError):
         S.XPBDMeshObjectConfig.from_node({"solver-type": "Conjugate"})
 

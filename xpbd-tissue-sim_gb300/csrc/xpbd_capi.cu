@@ -36,7 +36,9 @@ bool valid_params(const xpbd_params& p) {
            p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
            (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8) &&
            p.gs_variant >= 0 && p.gs_variant <= 3 && p.num_local_collision_iters >= 0 &&
-           p.num_local_collision_iters <= 1000;
+           p.num_local_collision_iters <= 1000 && (p.first_order == 0 || p.first_order == 1) &&
+           (p.adjust_damping_to_material == 0 || p.adjust_damping_to_material == 1) &&
+           (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier)));
 }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
@@ -262,7 +264,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     const bool have_faces = c->F > 0;
     {
         Scope sc(c, K_PREDICT);
-        launch_predict(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
+        if (p.first_order) launch_predict_first_order(c->L(), c->x.p, c->prev.p, c->gdz.p, c->V);
+        else launch_predict(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
     }
     const bool warm = c->warm_mode != XPBD_WARM_NONE;
     if (track) cudaMemsetAsync(c->res_partial.p, 0, sizeof(double) * (size_t)c->res_stride * (iters + 1), s);
@@ -469,7 +472,7 @@ void release(xpbd_ctx* c) {
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
     c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
-    c->local_slots.release(); c->vmask.release(); c->tmask.release();
+    c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
@@ -606,6 +609,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     const double* X = Xcat.data();
     std::vector<double> Q(9 * (size_t)T), ad(T), ah(T), gm(T);
     c->mass_h.assign(V, 0.0);
+    std::vector<double> vvol(V, 0.0);  // vertex volumes (1st-order damping)
     for (int t = 0; t < T; t++) {
         const int* e = &c->tets_h[4 * (size_t)t];
         double D[9];
@@ -638,12 +642,38 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         gm[t] = mu / la;
         const double em = vol * rho;
         for (int k = 0; k < 4; k++) c->mass_h[e[k]] += em / 4.0;
+        for (int k = 0; k < 4; k++) vvol[e[k]] += vol / 4.0;
     }
     c->inv_mass_h.assign(V, 0.0);
     for (int i = 0; i < V; i++) {
         if (!(c->mass_h[i] > 0))
             return fail(c, XPBD_ERR_INVALID, "vertex %d belongs to no tet (zero mass)", i);
         c->inv_mass_h[i] = 1.0 / c->mass_h[i];
+    }
+    if (p.first_order) {
+        // per-vertex damping B is the constraint inertia of 1st-order XPBD
+        // (XPBDMeshObject.cpp:333-348, XPBDMeshObjectBase.hpp:131-137); the
+        // vertex E and nu average the attached elements' (:321-329)
+        std::vector<double> vE(V, 0.0), vnu(V, 0.0);
+        std::vector<int> natt(V, 0);
+        for (int t = 0; t < T; t++)
+            for (int k = 0; k < 4; k++) natt[c->tets_h[4 * (size_t)t + k]]++;
+        for (int t = 0; t < T; t++)
+            for (int k = 0; k < 4; k++) {
+                const int v = c->tets_h[4 * (size_t)t + k];
+                vE[v] += Ecat[t] / natt[v];
+                vnu[v] += nucat[t] / natt[v];
+            }
+        std::vector<float> gdz(V);
+        for (int i = 0; i < V; i++) {
+            const double B = p.adjust_damping_to_material ? vvol[i] * p.damping_multiplier * vE[i] / (1 + vnu[i])
+                                                          : vvol[i] * p.damping_multiplier;
+            c->inv_mass_h[i] = 1.0 / B;
+            // _movePositionsInertially, 1st order (XPBDMeshObject.cpp:449-456)
+            gdz[i] = (float)(-p.g_accel * c->mass_h[i] * p.dt / B);
+        }
+        XPBD_CU(c, c->gdz.alloc(V));
+        XPBD_CU(c, cudaMemcpy(c->gdz.p, gdz.data(), sizeof(float) * V, cudaMemcpyHostToDevice));
     }
     c->fixed_h.assign(V, 0);
 
@@ -683,7 +713,9 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         for (int t = 0; t < T; t++) c->tet_of_slot[t] = t;
         c->n_tet_colours = 1;
     }
-    const double dt2 = p.dt * p.dt;
+    // alpha~ = alpha / dt^2 (2nd order) or alpha / dt (1st order,
+    // CombinedNeohookeanConstraintProjector.cpp:35, ConstraintProjector.hpp:133-140)
+    const double dt2 = p.first_order ? p.dt : p.dt * p.dt;
     std::vector<int4> hidx(T);
     std::vector<float4> h0(T), h1(T), h2(T);
     std::vector<float2> hmat(T);
@@ -871,6 +903,9 @@ int xpbd_default_params(xpbd_params* p) {
     p->gs_min_blocks = 0;
     p->gs_variant = 2;
     p->num_local_collision_iters = 0;
+    p->first_order = 0;
+    p->adjust_damping_to_material = 0;
+    p->damping_multiplier = 1.0;
     return XPBD_OK;
 }
 

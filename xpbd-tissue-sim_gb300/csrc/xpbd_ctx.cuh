@@ -83,6 +83,7 @@ struct xpbd_ctx {
     std::vector<int> local_tets_h;       // the same order as tet indices
     DevBuf<int> local_slots;
     DevBuf<unsigned char> vmask, tmask;
+    DevBuf<float> gdz;                   // 1st order: per-vertex inertial z move
     // dataflow Gauss-Seidel (sweep variant 2): tasks, dependencies, epochs
     int ntasks = 0, flow_grid = 0;
     DevBuf<int4> flow_tasks;

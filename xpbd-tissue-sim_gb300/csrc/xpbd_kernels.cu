@@ -478,6 +478,18 @@ __global__ void k_predict(float4* __restrict__ x, float4* __restrict__ prev, con
     x[i] = make_float4(p.x + dt * v.x, p.y + dt * v.y, (p.z + dt * v.z) + dz, p.w);
 }
 
+// 1st-order inertial move: no velocity term, gravity scaled by m / B per
+// vertex (XPBDMeshObject.cpp:449-456)
+__global__ void k_predict_first_order(float4* __restrict__ x, float4* __restrict__ prev, const float* __restrict__ gdz,
+                                      int V) {
+    pdl_wait_then_release();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float4 p = x[i];
+    prev[i] = p;
+    x[i] = make_float4(p.x, p.y, p.z + __ldg(gdz + i), p.w);
+}
+
 __global__ void k_kinematic(float4* __restrict__ x, const int* __restrict__ idx, const float4* __restrict__ rest,
                             int n, float ox, float oy, float oz) {
     pdl_wait_then_release();
@@ -1504,6 +1516,10 @@ void go(void (*kernel)(KArgs...), int grid, int block, const Launch& L, Args&&..
 }  // namespace
 
 int residual_blocks(int T, int block) { return nblk(T, block); }
+
+void launch_predict_first_order(const Launch& s, float4* x, float4* prev, const float* gdz, int V) {
+    if (V > 0) go(k_predict_first_order, nblk(V, 256), 256, s, x, prev, gdz, V);
+}
 
 void launch_predict(const Launch& s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz) {
     if (V > 0) go(k_predict, nblk(V, 256), 256, s, x, prev, vel, V, dt, dz);

@@ -149,6 +149,7 @@ void launch_mse(cudaStream_t s, const float* out, const float* Y, int n, double*
 void launch_adam(cudaStream_t s, float* p, const float* g, float* m, float* v, int n, float lr, int step);
 
 // ---- launchers (all asynchronous on L.s) ----
+void launch_predict_first_order(const Launch& s, float4* x, float4* prev, const float* gdz, int V);
 void launch_predict(const Launch& s, float4* x, float4* prev, const float4* vel, int V, float dt, float dz);
 void launch_kinematic(const Launch& s, float4* x, const int* idx, const float4* rest, int n, float ox, float oy,
                       float oz);

@@ -6,6 +6,7 @@ Configs (defaults as in the reference's config classes):
   ObjectConfig            include/config/simobject/ObjectConfig.hpp:28-62
   MeshObjectConfig        include/config/simobject/MeshObjectConfig.hpp:15-54
   XPBDMeshObjectConfig    include/config/simobject/XPBDMeshObjectConfig.hpp:62-125
+  FirstOrderXPBDMeshObjectConfig  FirstOrderXPBDMeshObjectConfig.hpp:21-59
   RigidSphereConfig       include/config/simobject/RigidPrimitiveConfigs.hpp:26-44,
                           RigidObjectConfig.hpp:18-41
 
@@ -25,10 +26,9 @@ Rigid spheres with `collisions: true` collide with every XPBD object that has
 between steps (move_sphere). The reference only builds graphics for
 `visualization`; there is no graphics here and the key is read and ignored.
 
-Not provided (each raises NotImplementedError naming the key): first-order
-objects (`FirstOrderXPBDMeshObject`), non-fixed rigid bodies (two-way
-coupling), rigid boxes, cylinders and meshes, self-collisions and the Virtuoso
-robot objects.
+Not provided (each raises NotImplementedError naming the key): non-fixed
+rigid bodies (two-way coupling), rigid boxes, cylinders and meshes,
+self-collisions and the Virtuoso robot objects.
 """
 from __future__ import annotations
 
@@ -104,9 +104,12 @@ class XPBDMeshObjectConfig:
     solver_type: int = G.SOLVER_GAUSS_SEIDEL
     constraint_type: int = G.CONSTRAINT_COMBINED
     residual_policy: int = G.RESIDUAL_NEVER
+    first_order: bool = False
+    damping_multiplier: float = 1.0
+    adjust_damping_to_material: bool = False
 
     @classmethod
-    def from_node(cls, n):
+    def from_node(cls, n, first_order=False):
         c = cls(name=str(_get(n, "name", "")), collisions=bool(_get(n, "collisions", False)),
                 graphics_only=bool(_get(n, "graphics-only", False)),
                 position=_vec3(n, "position", [0, 0, 0]), velocity=_vec3(n, "velocity", [0, 0, 0]),
@@ -119,6 +122,10 @@ class XPBDMeshObjectConfig:
                 solver_type=_options(n, "solver-type", SOLVER_TYPES, "Gauss-Seidel"),
                 constraint_type=_options(n, "constraint-type", CONSTRAINT_TYPES, "Stable-Neohookean-Combined"),
                 residual_policy=_options(n, "residual-policy", RESIDUAL_POLICIES, "Never"))
+        if first_order:
+            c.first_order = True
+            c.damping_multiplier = float(_get(n, "damping-multiplier", 1.0))
+            c.adjust_damping_to_material = bool(_get(n, "adjust-damping-to-material", False))
         if _get(n, "max-size", None) is not None:
             c.max_size = float(n["max-size"])
         if _get(n, "size", None) is not None:
@@ -178,10 +185,11 @@ class SimulationConfig:
                 raise ValueError("Type of object is needed!")
             if t == "XPBDMeshObject":
                 c.objects.append(XPBDMeshObjectConfig.from_node(on))
+            elif t == "FirstOrderXPBDMeshObject":
+                c.objects.append(XPBDMeshObjectConfig.from_node(on, first_order=True))
             elif t == "RigidSphere":
                 c.objects.append(RigidSphereConfig.from_node(on))
-            elif t in ("FirstOrderXPBDMeshObject", "RigidMeshObject", "RigidBox", "RigidCylinder", "VirtuosoArm",
-                       "VirtuosoRobot"):
+            elif t in ("RigidMeshObject", "RigidBox", "RigidCylinder", "VirtuosoArm", "VirtuosoRobot"):
                 raise NotImplementedError(f"object type {t!r} is not provided by the GB300 solver")
             else:
                 raise ValueError(f"Unknown type of object! {t!r} is not a type of simulation object.")
@@ -240,7 +248,9 @@ class XPBDObject:
                                    dt=sc.time_step, g_accel=sc.g_accel, collision_rate=sc.collision_rate,
                                    num_iters=cfg.num_solver_iters, solver_type=cfg.solver_type,
                                    constraint_type=cfg.constraint_type, residual_policy=cfg.residual_policy,
-                                   num_local_collision_iters=cfg.num_local_collision_iters)
+                                   num_local_collision_iters=cfg.num_local_collision_iters,
+                                   first_order=int(cfg.first_order), damping_multiplier=cfg.damping_multiplier,
+                                   adjust_damping_to_material=int(cfg.adjust_damping_to_material))
         if np.any(cfg.velocity != 0):
             self.solver.set_velocities(np.broadcast_to(cfg.velocity, self.X.shape))
 

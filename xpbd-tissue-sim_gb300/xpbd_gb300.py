@@ -62,6 +62,7 @@ class Params(C.Structure):
         ("max_contacts_per_face", C.c_int32), ("use_graphs", C.c_int32), ("use_pdl", C.c_int32),
         ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32), ("gs_variant", C.c_int32),
         ("num_local_collision_iters", C.c_int32),
+        ("first_order", C.c_int32), ("adjust_damping_to_material", C.c_int32), ("damping_multiplier", C.c_double),
     ]
 
 
