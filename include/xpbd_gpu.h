@@ -191,6 +191,25 @@ int xpbd_set_spheres(xpbd_ctx* ctx, int32_t n, const double* centers3n, const do
 /* the same for one instance of a batch (xpbd_set_spheres addresses instance 0) */
 int xpbd_set_instance_spheres(xpbd_ctx* ctx, int32_t instance, int32_t n, const double* centers3n,
                               const double* radii);
+/* Fixed rigid primitives as SDFs: spheres, boxes and cylinders
+ * (SphereSDF / BoxSDF / CylinderSDF, src/geometry/*SDF.cpp) at a position with
+ * an orientation quaternion (x, y, z, w), as RigidSphere / RigidBox /
+ * RigidCylinder hold them (RigidObject::globalToBody, RigidObject.cpp:94-97).
+ * dims: sphere (radius, -, -), box (full size x, y, z), cylinder (radius,
+ * height, -). Slot k of the contact table belongs to primitive k; at most
+ * max_contacts_per_face primitives. The sphere setters above fill the same
+ * table. */
+#define XPBD_SDF_SPHERE 0
+#define XPBD_SDF_BOX 1
+#define XPBD_SDF_CYLINDER 2
+int xpbd_set_sdfs(xpbd_ctx* ctx, int32_t n, const int32_t* kind, const double* pos3n, const double* quat4n,
+                  const double* dims3n);
+int xpbd_set_instance_sdfs(xpbd_ctx* ctx, int32_t instance, int32_t n, const int32_t* kind, const double* pos3n,
+                           const double* quat4n, const double* dims3n);
+/* SDF value and gradient of one primitive at n points on the device
+ * (out: n x (sdf, gx, gy, gz)); a test and tooling hook, no context needed */
+int xpbd_sdf_eval(int32_t kind, const double* pos3, const double* quat4, const double* dims3, int64_t n,
+                  const double* pts3n, double* out4n);
 
 /* clearCollisionConstraints (XPBDMeshObject.cpp:233-251). */
 int xpbd_clear_collisions(xpbd_ctx* ctx);

@@ -167,6 +167,15 @@ class Oracle:
         r = np.ascontiguousarray(radii, np.float64).reshape(-1)
         self.L.xo_set_spheres(C.c_void_p(self.h), len(r), _p(c), _p(r))
 
+    def set_prims(self, kinds, positions, quats, dims):
+        """Fixed SDF primitives: kinds 0 sphere, 1 box, 2 cylinder; quats (x, y, z, w)."""
+        k = np.ascontiguousarray(kinds, np.int32).reshape(-1)
+        n = k.size
+        p = np.ascontiguousarray(positions, np.float64).reshape(n, 3)
+        q = np.ascontiguousarray(quats, np.float64).reshape(n, 4)
+        d = np.ascontiguousarray(dims, np.float64).reshape(n, 3)
+        self.L.xo_set_prims(C.c_void_p(self.h), n, _p(k), _p(p), _p(q), _p(d))
+
     def detect(self):
         return self.L.xo_detect(C.c_void_p(self.h))
 
@@ -265,6 +274,20 @@ class Oracle:
         if n:
             self.L.xo_tet_order(C.c_void_p(self.h), _p(out))
         return out
+
+
+PRIM_SPHERE, PRIM_BOX, PRIM_CYLINDER = 0, 1, 2
+
+
+def prim_eval(kind, position, quat, dims, x, precision=64):
+    """(sdf, gx, gy, gz) of one SDF primitive at point x."""
+    out = np.zeros(4)
+    pos = np.ascontiguousarray(position, np.float64)
+    q = np.ascontiguousarray(quat, np.float64)
+    d = np.ascontiguousarray(dims, np.float64)
+    xx = np.ascontiguousarray(x, np.float64)
+    lib().xo_prim_eval(int(precision), int(kind), _p(pos), _p(q), _p(d), _p(xx), _p(out))
+    return out
 
 
 def read_msh41(path_or_text: str):

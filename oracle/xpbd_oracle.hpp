@@ -324,16 +324,114 @@ inline void sphere_grad(const R* x, const R* c, R* g) {
     }
 }
 
+// Static SDF primitive of a fixed rigid object: sphere (d = radius),
+// box (d = full size), cylinder (d = radius, height), at position p with
+// orientation quaternion q = (x, y, z, w) (include/simobject/RigidPrimitives.hpp).
+enum { PRIM_SPHERE = 0, PRIM_BOX = 1, PRIM_CYLINDER = 2 };
+template <typename R>
+struct Prim {
+    int kind = PRIM_SPHERE;
+    R p[3] = {0, 0, 0};
+    R q[4] = {0, 0, 0, 1};
+    R d[3] = {0, 0, 0};
+};
+
+// GeometryUtils::rotateVectorByQuat / inverseQuat (src/utils/GeometryUtils.cpp:92-102)
+template <typename R>
+inline void quat_rotate(const R* v, const R* q, R* out) {
+    const R ud = q[0] * v[0] + q[1] * v[1] + q[2] * v[2];
+    const R s = 2 * q[3] * q[3] - 1;
+    const R cx = q[1] * v[2] - q[2] * v[1], cy = q[2] * v[0] - q[0] * v[2], cz = q[0] * v[1] - q[1] * v[0];
+    out[0] = 2 * ud * q[0] + s * v[0] + 2 * q[3] * cx;
+    out[1] = 2 * ud * q[1] + s * v[1] + 2 * q[3] * cy;
+    out[2] = 2 * ud * q[2] + s * v[2] + 2 * q[3] * cz;
+}
+// RigidObject::globalToBody (src/simobject/RigidObject.cpp:94-97)
+template <typename R>
+inline void to_body(const Prim<R>& pr, const R* x, R* out) {
+    const R n2 = pr.q[0] * pr.q[0] + pr.q[1] * pr.q[1] + pr.q[2] * pr.q[2] + pr.q[3] * pr.q[3];
+    const R qi[4] = {-pr.q[0] / n2, -pr.q[1] / n2, -pr.q[2] / n2, pr.q[3] / n2};
+    const R v[3] = {x[0] - pr.p[0], x[1] - pr.p[1], x[2] - pr.p[2]};
+    quat_rotate(v, qi, out);
+}
+// Eigen's normalized(): unchanged when the norm is zero
+template <typename R>
+inline void normalize3(R* v) {
+    const R n2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
+    if (n2 > R(0)) {
+        const R n = std::sqrt(n2);
+        v[0] /= n; v[1] /= n; v[2] /= n;
+    }
+}
+
+// BoxSDF::evaluate / CylinderSDF::evaluate (src/geometry/BoxSDF.cpp,
+// CylinderSDF.cpp); spheres as sphere_sdf
+template <typename R>
+inline R prim_sdf(const Prim<R>& pr, const R* x) {
+    if (pr.kind == PRIM_SPHERE) return sphere_sdf(x, pr.p, pr.d[0]);
+    R b[3];
+    to_body(pr, x, b);
+    if (pr.kind == PRIM_BOX) {
+        R qv[3], o = 0;
+        for (int k = 0; k < 3; k++) {
+            qv[k] = std::abs(b[k]) - R(0.5) * pr.d[k];
+            const R m = std::max(qv[k], R(0));
+            o += m * m;
+        }
+        return std::sqrt(o) + std::min(std::max({qv[0], qv[1], qv[2]}), R(0));
+    }
+    const R xy = std::sqrt(b[0] * b[0] + b[1] * b[1]) - pr.d[0];
+    const R z = std::abs(b[2]) - R(0.5) * pr.d[1];
+    const R ox = std::max(xy, R(0)), oz = std::max(z, R(0));
+    return std::sqrt(ox * ox + oz * oz) + std::min(std::max(xy, z), R(0));
+}
+
+template <typename R>
+inline void prim_grad(const Prim<R>& pr, const R* x, R* g) {
+    if (pr.kind == PRIM_SPHERE) {
+        sphere_grad(x, pr.p, g);
+        return;
+    }
+    R b[3], go[3], gi[3];
+    to_body(pr, x, b);
+    if (pr.kind == PRIM_BOX) {
+        R qv[3];
+        for (int k = 0; k < 3; k++) qv[k] = std::abs(b[k]) - pr.d[k] / R(2.0);
+        const R md = std::min(std::max({qv[0], qv[1], qv[2]}), R(0));
+        for (int k = 0; k < 3; k++) {
+            const R sg = b[k] > 0 ? R(1) : R(-1);
+            go[k] = sg * std::max(qv[k], R(0));
+            gi[k] = sg * (qv[k] == md ? R(1) : R(0));
+        }
+        normalize3(go);
+    } else {
+        const R xy = std::sqrt(b[0] * b[0] + b[1] * b[1]) - pr.d[0];
+        const R z = std::abs(b[2]) - R(0.5) * pr.d[1];
+        const R ox = std::max(xy, R(0)), oz = std::max(z, R(0));
+        const R in = std::min(std::max(xy, z), R(0));
+        go[0] = b[0] * (ox > 0 ? R(1) : R(0));
+        go[1] = b[1] * (ox > 0 ? R(1) : R(0));
+        go[2] = b[2] * (oz > 0 ? R(1) : R(0));
+        gi[0] = b[0] * (in == xy ? R(1) : R(0));
+        gi[1] = b[1] * (in == xy ? R(1) : R(0));
+        gi[2] = b[2] * (in == z ? R(1) : R(0));
+        normalize3(go);
+        normalize3(gi);
+    }
+    const R sum[3] = {go[0] + gi[0], go[1] + gi[1], go[2] + gi[2]};
+    quat_rotate(sum, pr.q, g);
+}
+
 // CollisionScene::_frankWolfe (src/collision/CollisionScene.cpp:253-283)
 template <typename R>
-inline void frank_wolfe(const R* c, R r, const R* p1, const R* p2, const R* p3, R* x) {
-    R d1 = sphere_sdf(p1, c, r), d2 = sphere_sdf(p2, c, r), d3 = sphere_sdf(p3, c, r);
+inline void frank_wolfe(const Prim<R>& pr, const R* p1, const R* p2, const R* p3, R* x) {
+    R d1 = prim_sdf(pr, p1), d2 = prim_sdf(pr, p2), d3 = prim_sdf(pr, p3);
     const R* s0 = (d1 <= d2 && d1 <= d3) ? p1 : ((d2 <= d1 && d2 <= d3) ? p2 : p3);
     x[0] = s0[0]; x[1] = s0[1]; x[2] = s0[2];
     for (int i = 0; i < 32; i++) {
         R alpha = R(2.0) / R(i + 3);
         R g[3];
-        sphere_grad(x, c, g);
+        prim_grad(pr, x, g);
         R sg1 = p1[0] * g[0] + p1[1] * g[1] + p1[2] * g[2];
         R sg2 = p2[0] * g[0] + p2[1] * g[1] + p2[2] * g[2];
         R sg3 = p3[0] * g[0] + p3[1] * g[1] + p3[2] * g[2];
@@ -355,11 +453,11 @@ inline void barycentric(const R* p, const R* a, const R* b, const R* c, R* u, R*
     *u = 1 - *v - *w;
 }
 
-// One face against one sphere: centroid cull, Frank-Wolfe, threshold,
+// One face against one SDF primitive: centroid cull, Frank-Wolfe, threshold,
 // barycentrics, surface point (CollisionScene.cpp:171-214). Returns true and
 // fills the contact when the face is in contact.
 template <typename R>
-inline bool collide_face_sphere(const R* p1, const R* p2, const R* p3, const R* c, R r, Contact<R>* out) {
+inline bool collide_face(const R* p1, const R* p2, const R* p3, const Prim<R>& pr, Contact<R>* out) {
     auto sq = [](const R* a, const R* b) {
         R d0 = b[0] - a[0], d1 = b[1] - a[1], d2 = b[2] - a[2];
         return d0 * d0 + d1 * d1 + d2 * d2;
@@ -368,15 +466,15 @@ inline bool collide_face_sphere(const R* p1, const R* p2, const R* p3, const R* 
     R max_edge = std::max({e12, e13, e23});
     R cen[3];
     for (int k = 0; k < 3; k++) cen[k] = (p1[k] + p2[k] + p3[k]) / R(3);
-    R cd = sphere_sdf(cen, c, r);
+    R cd = prim_sdf(pr, cen);
     if (cd * cd > max_edge) return false;
     R x[3];
-    frank_wolfe(c, r, p1, p2, p3, x);
-    const double distance = (double)sphere_sdf(x, c, r);
+    frank_wolfe(pr, p1, p2, p3, x);
+    const double distance = (double)prim_sdf(pr, x);
     if (!(distance <= 1e-4)) return false;
     barycentric(x, p1, p2, p3, &out->u, &out->v_, &out->w);
     R g[3];
-    sphere_grad(x, c, g);
+    prim_grad(pr, x, g);
     for (int k = 0; k < 3; k++) {
         out->p[k] = (R)(x[k] - g[k] * distance);
         out->n[k] = g[k];
@@ -467,7 +565,7 @@ struct Object {
     int num_local_iter = 0;
     std::vector<int> local_order;
     // spheres
-    std::vector<R> sph_c, sph_r;
+    std::vector<Prim<R>> prims;   // static SDF primitives (fixed rigid bodies)
     // kinematic vertex group
     std::vector<int> kin_idx;
     std::vector<R> kin_rest;
@@ -828,12 +926,12 @@ struct Object {
     // (XPBDMeshObject.cpp:233-251; CollisionScene.cpp:32-51,171-214).
     void detect() {
         contacts.clear();
-        long long S = (long long)sph_r.size();
+        long long S = (long long)prims.size();
         for (long long s = 0; s < S; s++)
             for (long long f = 0; f < F; f++) {
                 const int* fv = &faces[3 * f];
                 Contact<R> ct;
-                if (collide_face_sphere(&x[3 * fv[0]], &x[3 * fv[1]], &x[3 * fv[2]], &sph_c[3 * s], sph_r[s], &ct)) {
+                if (collide_face(&x[3 * fv[0]], &x[3 * fv[1]], &x[3 * fv[2]], prims[s], &ct)) {
                     ct.sphere = (int)s;
                     ct.face = (int)f;
                     ct.v[0] = fv[0]; ct.v[1] = fv[1]; ct.v[2] = fv[2];

@@ -115,11 +115,49 @@ void xo_set_lambda(void* p, const double* lam) {
 void xo_set_spheres(void* p, int n, const double* c, const double* r) {
     with((Handle*)p, [&](auto& o) {
         using R = typename std::decay_t<decltype(o.x)>::value_type;
-        o.sph_c.assign(3 * n, 0); o.sph_r.assign(n, 0);
-        for (int i = 0; i < 3 * n; i++) o.sph_c[i] = (R)c[i];
-        for (int i = 0; i < n; i++) o.sph_r[i] = (R)r[i];
+        o.prims.assign(n, xo::Prim<R>{});
+        for (int i = 0; i < n; i++) {
+            o.prims[i].kind = xo::PRIM_SPHERE;
+            for (int k = 0; k < 3; k++) o.prims[i].p[k] = (R)c[3 * i + k];
+            o.prims[i].d[0] = (R)r[i];
+        }
         return 0;
     });
+}
+
+// SDF primitives: kind[n] (0 sphere, 1 box, 2 cylinder), pos 3n, quat 4n
+// (x, y, z, w), dims 3n (radius | full size | radius, height)
+void xo_set_prims(void* p, int n, const int* kind, const double* pos, const double* quat, const double* dims) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        o.prims.assign(n, xo::Prim<R>{});
+        for (int i = 0; i < n; i++) {
+            o.prims[i].kind = kind[i];
+            for (int k = 0; k < 3; k++) o.prims[i].p[k] = (R)pos[3 * i + k];
+            for (int k = 0; k < 4; k++) o.prims[i].q[k] = (R)quat[4 * i + k];
+            for (int k = 0; k < 3; k++) o.prims[i].d[k] = (R)dims[3 * i + k];
+        }
+        return 0;
+    });
+}
+
+// one SDF value and gradient (test hook): out = (sdf, gx, gy, gz)
+void xo_prim_eval(int precision, int kind, const double* pos, const double* quat, const double* dims,
+                  const double* x, double* out) {
+    auto run = [&](auto zero) {
+        using R = decltype(zero);
+        xo::Prim<R> pr;
+        pr.kind = kind;
+        for (int k = 0; k < 3; k++) { pr.p[k] = (R)pos[k]; pr.d[k] = (R)dims[k]; }
+        for (int k = 0; k < 4; k++) pr.q[k] = (R)quat[k];
+        const R xx[3] = {(R)x[0], (R)x[1], (R)x[2]};
+        R g[3];
+        out[0] = (double)xo::prim_sdf(pr, xx);
+        xo::prim_grad(pr, xx, g);
+        for (int k = 0; k < 3; k++) out[1 + k] = (double)g[k];
+    };
+    if (precision == 32) run(0.0f);
+    else run(0.0);
 }
 
 // kinematic vertices are fixed vertices driven to rest + offset

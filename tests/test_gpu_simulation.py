@@ -135,3 +135,39 @@ def test_first_order_object_from_config(lib, tmp_path):
     np.testing.assert_allclose(got - Xp, np.broadcast_to([0, 0, -40 * 9.81 * 1000 * 1e-3 / 5e3], Xp.shape),
                                atol=2e-6)
     s.close()
+
+
+def test_fixed_box_and_cylinder_from_config(lib, tmp_path):
+    """RigidBox / RigidCylinder objects become SDFs with the reference's
+    orientation convention; the configured loop equals the hand-driven solver."""
+    cfg, X, tets, faces = _scene(tmp_path)
+    text = open(cfg).read().replace('''  - name: "Ball"
+    type: "RigidSphere"
+    radius: 0.2
+    position: [0.1, 0, 0.93]''', '''  - name: "Slab"
+    type: "RigidBox"
+    size: [0.6, 0.6, 0.1]
+    rotation: [0, 0, 20]
+    position: [0.1, 0, 0.79]
+    fixed: true
+    collisions: true
+  - name: "Post"
+    type: "RigidCylinder"
+    radius: 0.1
+    height: 0.4
+    rotation: [90, 0, 0]
+    position: [0.1, 0, 0.2]''')
+    with S.Simulation(text, base_dir=str(tmp_path)) as sim:
+        sim.setup()
+        assert set(sim.rigids) == {"Slab", "Post"}
+        sim.update()
+        got = sim.objects["Cube"].positions()
+    Xp = msh.place(X, faces, (0.1, 0, 0.5), (0, 0, 30), 0.5, None)
+    T = tets.shape[0]
+    s = G.XPBDSolver(Xp, tets, faces, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0), dt=1e-3,
+                     collision_rate=100, num_iters=6)
+    s.set_sdfs([G.SDF_BOX, G.SDF_CYLINDER], [[0.1, 0, 0.79], [0.1, 0, 0.2]],
+               [S.eul_xyz_to_quat([0, 0, 20]), S.eul_xyz_to_quat([90, 0, 0])], [[0.6, 0.6, 0.1], [0.1, 0.4, 0]])
+    s.step(40)
+    np.testing.assert_array_equal(got, s.positions())
+    s.close()

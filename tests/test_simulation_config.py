@@ -107,7 +107,11 @@ def test_config_objects_and_errors():
     with pytest.raises(ValueError):
         S.SimulationConfig.from_node({"objects": [{"type": "Teapot"}]})
     with pytest.raises(NotImplementedError):
-        S.SimulationConfig.from_node({"objects": [{"type": "RigidBox"}]})
+        S.SimulationConfig.from_node({"objects": [{"type": "RigidMeshObject"}]})
+    boxes = S.SimulationConfig.from_node({"objects": [{"type": "RigidBox", "size": [1, 2, 3], "fixed": True},
+                                                      {"type": "RigidCylinder", "radius": 0.5}]})
+    assert np.allclose(boxes.objects[0].size, [1, 2, 3]) and boxes.objects[0].fixed
+    assert boxes.objects[1].radius == 0.5 and boxes.objects[1].height == 1.0
     fo = S.SimulationConfig.from_node({"objects": [{"type": "FirstOrderXPBDMeshObject", "damping-multiplier": 5e4}]})
     assert fo.objects[0].first_order and fo.objects[0].damping_multiplier == 5e4
     assert not fo.objects[0].adjust_damping_to_material
@@ -161,3 +165,12 @@ def test_element_classes_file(tmp_path):
     p = tmp_path / "classes.txt"
     p.write_text("0\n1\n1\n0\nend\n2\n")
     np.testing.assert_array_equal(S.read_element_classes(str(p)), [0, 1, 1, 0])
+
+
+def test_euler_quaternion_matches_the_rotation_matrix():
+    for deg in ([0, 0, 0], [30, 0, 0], [10, 20, 30], [-45, 60, 170]):
+        x, y, z, w = S.eul_xyz_to_quat(deg)
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)],
+                      [2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)],
+                      [2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)]])
+        np.testing.assert_allclose(R, msh.rotation_xyz(deg), atol=1e-12)

@@ -601,7 +601,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         }
         for (int64_t f = 0; f < m.num_faces; f++) finst[fo + f] = k;
     }
-    c->sphere_tab_h.assign((size_t)n_inst * c->S, make_float4(0.f, 0.f, 0.f, -1.f));
+    c->sphere_tab_h.assign(3 * (size_t)n_inst * c->S, make_float4(0.f, 0.f, 0.f, -1.f));
 
     // rest shape, compliance, lumped mass (ElementConstraint.hpp:23-51;
     // HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
@@ -1104,13 +1104,83 @@ int xpbd_set_instance_spheres(xpbd_ctx* c, int32_t inst, int32_t n, const double
         if (!(rad[i] >= 0) || !std::isfinite(ctr[3 * i]) || !std::isfinite(ctr[3 * i + 1]) ||
             !std::isfinite(ctr[3 * i + 2]))
             return fail(c, XPBD_ERR_INVALID, "sphere %d has a bad centre or radius", i);
-    float4* row = &c->sphere_tab_h[(size_t)inst * c->S];
-    for (int k = 0; k < c->S; k++)
-        row[k] = k < n ? make_float4((float)ctr[3 * k], (float)ctr[3 * k + 1], (float)ctr[3 * k + 2], (float)rad[k])
-                       : make_float4(0.f, 0.f, 0.f, -1.f);
+    std::vector<int32_t> kind(n, XPBD_SDF_SPHERE);
+    std::vector<double> quat(4 * (size_t)n, 0.0), dims(3 * (size_t)n, 0.0);
+    for (int i = 0; i < n; i++) {
+        quat[4 * i + 3] = 1.0;
+        dims[3 * i] = rad[i];
+    }
+    return xpbd_set_instance_sdfs(c, inst, n, kind.data(), ctr, quat.data(), dims.data());
+}
+
+int xpbd_set_instance_sdfs(xpbd_ctx* c, int32_t inst, int32_t n, const int32_t* kind, const double* pos,
+                           const double* quat, const double* dims) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (inst < 0 || inst >= c->n_inst) return fail(c, XPBD_ERR_INVALID, "instance %d out of range", inst);
+    if (n < 0 || n > kMaxSpheres || (n > 0 && (!kind || !pos || !quat || !dims)))
+        return fail(c, XPBD_ERR_INVALID, "SDF count %d outside [0,%d]", n, kMaxSpheres);
+    if (n > c->S) return fail(c, XPBD_ERR_CAPACITY, "%d SDFs exceed %d contact slots per face", n, c->S);
+    for (int i = 0; i < n; i++) {
+        bool ok = kind[i] >= XPBD_SDF_SPHERE && kind[i] <= XPBD_SDF_CYLINDER;
+        for (int k = 0; k < 3; k++) ok = ok && std::isfinite(pos[3 * i + k]) && dims[3 * i + k] >= 0;
+        double qn = 0;
+        for (int k = 0; k < 4; k++) qn += quat[4 * i + k] * quat[4 * i + k];
+        ok = ok && qn > 0 && std::isfinite(qn);
+        if (!ok) return fail(c, XPBD_ERR_INVALID, "SDF %d has a bad kind, position, orientation or size", i);
+    }
+    float4* row = &c->sphere_tab_h[3 * (size_t)inst * c->S];
+    for (int k = 0; k < c->S; k++) {
+        if (k < n) {
+            row[3 * k] = make_float4((float)pos[3 * k], (float)pos[3 * k + 1], (float)pos[3 * k + 2], (float)kind[k]);
+            row[3 * k + 1] = make_float4((float)quat[4 * k], (float)quat[4 * k + 1], (float)quat[4 * k + 2],
+                                         (float)quat[4 * k + 3]);
+            row[3 * k + 2] = make_float4((float)dims[3 * k], (float)dims[3 * k + 1], (float)dims[3 * k + 2], 0.f);
+        } else {
+            row[3 * k] = make_float4(0.f, 0.f, 0.f, -1.f);
+            row[3 * k + 1] = make_float4(0.f, 0.f, 0.f, 1.f);
+            row[3 * k + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    }
     c->n_spheres_total = 0;
-    for (const float4& e : c->sphere_tab_h) c->n_spheres_total += e.w >= 0.f ? 1 : 0;
+    for (size_t e = 0; e < c->sphere_tab_h.size(); e += 3) c->n_spheres_total += c->sphere_tab_h[e].w >= 0.f ? 1 : 0;
     c->sphere_dirty = true;
+    return XPBD_OK;
+}
+
+int xpbd_set_sdfs(xpbd_ctx* c, int32_t n, const int32_t* kind, const double* pos, const double* quat,
+                  const double* dims) {
+    return xpbd_set_instance_sdfs(c, 0, n, kind, pos, quat, dims);
+}
+
+int xpbd_sdf_eval(int32_t kind, const double* pos, const double* quat, const double* dims, int64_t n,
+                  const double* pts, double* out) {
+    if (!pos || !quat || !dims || n < 0 || (n > 0 && (!pts || !out)) || kind < XPBD_SDF_SPHERE ||
+        kind > XPBD_SDF_CYLINDER)
+        return XPBD_ERR_INVALID;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return XPBD_ERR_NO_DEVICE;
+    }
+    std::vector<float4> h(3 + 2 * (size_t)n);
+    h[0] = make_float4((float)pos[0], (float)pos[1], (float)pos[2], (float)kind);
+    h[1] = make_float4((float)quat[0], (float)quat[1], (float)quat[2], (float)quat[3]);
+    h[2] = make_float4((float)dims[0], (float)dims[1], (float)dims[2], 0.f);
+    for (int64_t i = 0; i < n; i++) h[3 + i] = make_float4((float)pts[3 * i], (float)pts[3 * i + 1], (float)pts[3 * i + 2], 0.f);
+    float4* d = nullptr;
+    if (cudaMalloc((void**)&d, sizeof(float4) * h.size()) != cudaSuccess) return XPBD_ERR_CUDA;
+    cudaError_t e = cudaMemcpy(d, h.data(), sizeof(float4) * (3 + n), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        launch_prim_eval(0, d, d + 3, (int)n, d + 3 + n);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(h.data() + 3 + n, d + 3 + n, sizeof(float4) * n, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return XPBD_ERR_CUDA;
+    for (int64_t i = 0; i < n; i++) {
+        const float4 r = h[3 + n + i];
+        out[4 * i] = r.x; out[4 * i + 1] = r.y; out[4 * i + 2] = r.z; out[4 * i + 3] = r.w;
+    }
     return XPBD_OK;
 }
 

@@ -95,7 +95,7 @@ struct xpbd_ctx {
     // instances (batched objects): offsets into the concatenated arrays
     int n_inst = 1;
     std::vector<int64_t> voff, toff, foff;
-    std::vector<float4> sphere_tab_h;  // [n_inst * S], radius < 0 = empty
+    std::vector<float4> sphere_tab_h;  // [n_inst * S] SDF primitives, 3 float4 each (kind < 0 = empty)
     DevBuf<float4> sphere_tab;
     DevBuf<int> face_inst;
     bool sphere_dirty = true;

@@ -895,23 +895,116 @@ __global__ void k_contacts_gs(ContactArrays c, const int* __restrict__ face_list
 }
 
 // ---- collision detection (one thread per (sphere slot, face)) ----
-__device__ __forceinline__ float sdf_sphere(float px, float py, float pz, float4 sph) {
-    const float a = px - sph.x, b = py - sph.y, c = pz - sph.z;
-    return sqrtf(a * a + b * b + c * c) - sph.w;
+// SDF primitive of a fixed rigid object, three float4 per table entry:
+// a = (position, kind: 0 sphere, 1 box, 2 cylinder, < 0 empty),
+// q = orientation quaternion (x, y, z, w), d = radius | full size | (radius, height).
+struct Prim {
+    float4 a, q, d;
+};
+
+__device__ __forceinline__ Prim load_prim(const float4* __restrict__ table, size_t e) {
+    return Prim{table[3 * e], table[3 * e + 1], table[3 * e + 2]};
 }
-__device__ __forceinline__ void grad_sphere(float px, float py, float pz, float4 sph, float g[3]) {
-    const float a = px - sph.x, b = py - sph.y, c = pz - sph.z;
-    const float n2 = a * a + b * b + c * c;
+
+// GeometryUtils::rotateVectorByQuat (src/utils/GeometryUtils.cpp:92-97)
+__device__ __forceinline__ void quat_rotate(const float v[3], float qx, float qy, float qz, float qw, float o[3]) {
+    const float ud = qx * v[0] + qy * v[1] + qz * v[2];
+    const float s = 2.f * qw * qw - 1.f;
+    const float cx = qy * v[2] - qz * v[1], cy = qz * v[0] - qx * v[2], cz = qx * v[1] - qy * v[0];
+    o[0] = 2.f * ud * qx + s * v[0] + 2.f * qw * cx;
+    o[1] = 2.f * ud * qy + s * v[1] + 2.f * qw * cy;
+    o[2] = 2.f * ud * qz + s * v[2] + 2.f * qw * cz;
+}
+
+// RigidObject::globalToBody (src/simobject/RigidObject.cpp:94-97)
+__device__ __forceinline__ void to_body(const Prim& P, float px, float py, float pz, float b[3]) {
+    const float n2 = P.q.x * P.q.x + P.q.y * P.q.y + P.q.z * P.q.z + P.q.w * P.q.w;
+    const float v[3] = {px - P.a.x, py - P.a.y, pz - P.a.z};
+    quat_rotate(v, -P.q.x / n2, -P.q.y / n2, -P.q.z / n2, P.q.w / n2, b);
+}
+
+__device__ __forceinline__ void normalize3(float v[3]) {
+    const float n2 = v[0] * v[0] + v[1] * v[1] + v[2] * v[2];
     if (n2 > 0.f) {
         const float n = sqrtf(n2);
-        g[0] = a / n; g[1] = b / n; g[2] = c / n;
-    } else {
-        g[0] = a; g[1] = b; g[2] = c;
+        v[0] /= n; v[1] /= n; v[2] /= n;
     }
 }
 
-// Sphere table: table[instance * S + slot] = (centre, radius); radius < 0
-// marks an empty slot. face_inst maps a surface face to its instance.
+// SphereSDF / BoxSDF / CylinderSDF::evaluate (src/geometry/*SDF.cpp)
+__device__ __forceinline__ float sdf_prim(float px, float py, float pz, const Prim& P) {
+    if (P.a.w == 0.f) {
+        const float a = px - P.a.x, b = py - P.a.y, c = pz - P.a.z;
+        return sqrtf(a * a + b * b + c * c) - P.d.x;
+    }
+    float b[3];
+    to_body(P, px, py, pz, b);
+    if (P.a.w == 1.f) {
+        const float q0 = fabsf(b[0]) - 0.5f * P.d.x, q1 = fabsf(b[1]) - 0.5f * P.d.y, q2 = fabsf(b[2]) - 0.5f * P.d.z;
+        const float m0 = fmaxf(q0, 0.f), m1 = fmaxf(q1, 0.f), m2 = fmaxf(q2, 0.f);
+        return sqrtf(m0 * m0 + m1 * m1 + m2 * m2) + fminf(fmaxf(fmaxf(q0, q1), q2), 0.f);
+    }
+    const float xy = sqrtf(b[0] * b[0] + b[1] * b[1]) - P.d.x;
+    const float z = fabsf(b[2]) - 0.5f * P.d.y;
+    const float ox = fmaxf(xy, 0.f), oz = fmaxf(z, 0.f);
+    return sqrtf(ox * ox + oz * oz) + fminf(fmaxf(xy, z), 0.f);
+}
+
+// ...::gradient; a zero vector stays zero when normalised (Eigen)
+__device__ __forceinline__ void grad_prim(float px, float py, float pz, const Prim& P, float g[3]) {
+    if (P.a.w == 0.f) {
+        const float a = px - P.a.x, b = py - P.a.y, c = pz - P.a.z;
+        const float n2 = a * a + b * b + c * c;
+        if (n2 > 0.f) {
+            const float n = sqrtf(n2);
+            g[0] = a / n; g[1] = b / n; g[2] = c / n;
+        } else {
+            g[0] = a; g[1] = b; g[2] = c;
+        }
+        return;
+    }
+    float b[3], go[3], gi[3];
+    to_body(P, px, py, pz, b);
+    if (P.a.w == 1.f) {
+        const float dd[3] = {P.d.x, P.d.y, P.d.z};
+        float q[3];
+#pragma unroll
+        for (int k = 0; k < 3; k++) q[k] = fabsf(b[k]) - dd[k] / 2.f;
+        const float md = fminf(fmaxf(fmaxf(q[0], q[1]), q[2]), 0.f);
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            const float sg = b[k] > 0.f ? 1.f : -1.f;
+            go[k] = sg * fmaxf(q[k], 0.f);
+            gi[k] = sg * (q[k] == md ? 1.f : 0.f);
+        }
+        normalize3(go);
+    } else {
+        const float xy = sqrtf(b[0] * b[0] + b[1] * b[1]) - P.d.x;
+        const float z = fabsf(b[2]) - 0.5f * P.d.y;
+        const float in = fminf(fmaxf(xy, z), 0.f);
+        const float fo = fmaxf(xy, 0.f) > 0.f ? 1.f : 0.f, fz = fmaxf(z, 0.f) > 0.f ? 1.f : 0.f;
+        go[0] = b[0] * fo; go[1] = b[1] * fo; go[2] = b[2] * fz;
+        const float ix = in == xy ? 1.f : 0.f, iz = in == z ? 1.f : 0.f;
+        gi[0] = b[0] * ix; gi[1] = b[1] * ix; gi[2] = b[2] * iz;
+        normalize3(go);
+        normalize3(gi);
+    }
+    const float sum[3] = {go[0] + gi[0], go[1] + gi[1], go[2] + gi[2]};
+    quat_rotate(sum, P.q.x, P.q.y, P.q.z, P.q.w, g);
+}
+
+// one primitive's SDF value and gradient at points (test hook)
+__global__ void k_prim_eval(const float4* __restrict__ prim, const float4* __restrict__ pts, int n,
+                            float4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const Prim P = load_prim(prim, 0);
+    const float4 p = pts[i];
+    float g[3];
+    grad_prim(p.x, p.y, p.z, P, g);
+    out[i] = make_float4(sdf_prim(p.x, p.y, p.z, P), g[0], g[1], g[2]);
+}
+
 __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const float4* __restrict__ table,
                          const int* __restrict__ face_inst) {
     pdl_wait_then_release();
@@ -919,8 +1012,8 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const fl
     if (slot >= c.S * c.F) return;
     const int s = slot / c.F, f = slot - s * c.F;
     float4 bary = make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 S = table[(size_t)face_inst[f] * c.S + s];
-    if (S.w >= 0.f) {
+    const Prim S = load_prim(table, (size_t)face_inst[f] * c.S + s);
+    if (S.a.w >= 0.f) {
         const int4 fv = c.faces[f];
         const float4 q1 = x[fv.x], q2 = x[fv.y], q3 = x[fv.z];
         const float p1[3] = {q1.x, q1.y, q1.z}, p2[3] = {q2.x, q2.y, q2.z}, p3[3] = {q3.x, q3.y, q3.z};
@@ -929,19 +1022,19 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const fl
             return d0 * d0 + d1 * d1 + d2 * d2;
         };
         const float me = fmaxf(fmaxf(sq(p1, p2), sq(p1, p3)), sq(p2, p3));
-        const float cd = sdf_sphere((p1[0] + p2[0] + p3[0]) / 3.f, (p1[1] + p2[1] + p3[1]) / 3.f,
+        const float cd = sdf_prim((p1[0] + p2[0] + p3[0]) / 3.f, (p1[1] + p2[1] + p3[1]) / 3.f,
                                     (p1[2] + p2[2] + p3[2]) / 3.f, S);
         if (!(cd * cd > me)) {
             // Frank-Wolfe over the triangle, 32 iterations, from the vertex of
             // smallest SDF (CollisionScene.cpp:253-283)
-            const float d1 = sdf_sphere(p1[0], p1[1], p1[2], S), d2 = sdf_sphere(p2[0], p2[1], p2[2], S),
-                        d3 = sdf_sphere(p3[0], p3[1], p3[2], S);
+            const float d1 = sdf_prim(p1[0], p1[1], p1[2], S), d2 = sdf_prim(p2[0], p2[1], p2[2], S),
+                        d3 = sdf_prim(p3[0], p3[1], p3[2], S);
             const float* s0 = (d1 <= d2 && d1 <= d3) ? p1 : ((d2 <= d1 && d2 <= d3) ? p2 : p3);
             float xx[3] = {s0[0], s0[1], s0[2]};
             for (int i = 0; i < 32; i++) {
                 const float alpha = 2.0f / (float)(i + 3);
                 float g[3];
-                grad_sphere(xx[0], xx[1], xx[2], S, g);
+                grad_prim(xx[0], xx[1], xx[2], S, g);
                 const float sg1 = p1[0] * g[0] + p1[1] * g[1] + p1[2] * g[2];
                 const float sg2 = p2[0] * g[0] + p2[1] * g[1] + p2[2] * g[2];
                 const float sg3 = p3[0] * g[0] + p3[1] * g[1] + p3[2] * g[2];
@@ -949,7 +1042,7 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const fl
 #pragma unroll
                 for (int k = 0; k < 3; k++) xx[k] = xx[k] + alpha * (sv[k] - xx[k]);
             }
-            const float dist = sdf_sphere(xx[0], xx[1], xx[2], S);
+            const float dist = sdf_prim(xx[0], xx[1], xx[2], S);
             if ((double)dist <= 1e-4) {
                 // barycentrics (GeometryUtils.cpp:6-23)
                 float v0[3], v1[3], v2[3];
@@ -962,7 +1055,7 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const fl
                 const float bw = (d00 * d21 - d01 * d20) / den;
                 const float bu = 1.f - bv - bw;
                 float g[3];
-                grad_sphere(xx[0], xx[1], xx[2], S, g);
+                grad_prim(xx[0], xx[1], xx[2], S, g);
                 bary = make_float4(bu, bv, bw, 1.f);
                 c.p[slot] = make_float4(xx[0] - g[0] * dist, xx[1] - g[1] * dist, xx[2] - g[2] * dist, 0.f);
                 c.n[slot] = make_float4(g[0], g[1], g[2], 0.f);
@@ -1615,6 +1708,10 @@ void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face
     if (n <= 0) return;
     if (first) go(k_contacts_gs<true>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
     else go(k_contacts_gs<false>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
+}
+
+void launch_prim_eval(cudaStream_t s, const float4* prim, const float4* pts, int n, float4* out) {
+    if (n > 0) k_prim_eval<<<nblk(n, 128), 128, 0, s>>>(prim, pts, n, out);
 }
 
 void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const float4* sphere_table,

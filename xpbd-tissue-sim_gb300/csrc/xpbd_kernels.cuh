@@ -174,6 +174,9 @@ int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
                         bool first);
+// prim: one 3-float4 primitive entry; out[i] = (sdf, gradient) at pts[i]
+void launch_prim_eval(cudaStream_t s, const float4* prim, const float4* pts, int n, float4* out);
+// sphere_table: 3 float4 per (instance, slot) primitive entry
 void launch_detect(const Launch& s, const ContactArrays& c, const float4* x, const float4* sphere_table,
                    const int* face_inst);
 void launch_finalize(const Launch& s, float4* x, const float4* prev, float4* vel, int V, float dt, bool write_vel);

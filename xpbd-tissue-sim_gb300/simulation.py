@@ -7,7 +7,8 @@ Configs (defaults as in the reference's config classes):
   MeshObjectConfig        include/config/simobject/MeshObjectConfig.hpp:15-54
   XPBDMeshObjectConfig    include/config/simobject/XPBDMeshObjectConfig.hpp:62-125
   FirstOrderXPBDMeshObjectConfig  FirstOrderXPBDMeshObjectConfig.hpp:21-59
-  RigidSphereConfig       include/config/simobject/RigidPrimitiveConfigs.hpp:26-44,
+  RigidSphereConfig, RigidBoxConfig, RigidCylinderConfig
+                          include/config/simobject/RigidPrimitiveConfigs.hpp:26-115,
                           RigidObjectConfig.hpp:18-41
 
 Simulation mirrors src/simulation/Simulation.cpp:
@@ -21,14 +22,15 @@ Simulation mirrors src/simulation/Simulation.cpp:
                runs collision detection on the shared cadence, the update and
                the velocity update
 
-Rigid spheres with `collisions: true` collide with every XPBD object that has
-`collisions: true`; a sphere is a static SDF in the solver and can be moved
-between steps (move_sphere). The reference only builds graphics for
+Fixed rigid spheres, boxes and cylinders with `collisions: true` collide with
+every XPBD object that has `collisions: true`: each is a static SDF in the
+solver (orientation from `rotation`, RigidObject.cpp:14) and can be moved
+between steps (move_rigid). The reference only builds graphics for
 `visualization`; there is no graphics here and the key is read and ignored.
 
 Not provided (each raises NotImplementedError naming the key): non-fixed
-rigid bodies (two-way coupling), rigid boxes, cylinders and meshes,
-self-collisions and the Virtuoso robot objects.
+rigid bodies (two-way coupling), rigid meshes, self-collisions and the
+Virtuoso robot objects.
 """
 from __future__ import annotations
 
@@ -143,6 +145,7 @@ class RigidSphereConfig:
     radius: float = 1.0
     density: float = 1000.0
     fixed: bool = False
+    rotation: np.ndarray = field(default_factory=lambda: np.zeros(3))
 
     @classmethod
     def from_node(cls, n):
@@ -150,7 +153,37 @@ class RigidSphereConfig:
                    graphics_only=bool(_get(n, "graphics-only", False)),
                    position=_vec3(n, "position", [0, 0, 0]), velocity=_vec3(n, "velocity", [0, 0, 0]),
                    radius=float(_get(n, "radius", 1.0)), density=float(_get(n, "density", 1000.0)),
-                   fixed=bool(_get(n, "fixed", False)))
+                   fixed=bool(_get(n, "fixed", False)), rotation=_vec3(n, "rotation", [0, 0, 0]))
+
+
+@dataclass
+class RigidBoxConfig(RigidSphereConfig):
+    size: np.ndarray = field(default_factory=lambda: np.ones(3))
+
+    @classmethod
+    def from_node(cls, n):
+        b = RigidSphereConfig.from_node(n)
+        return cls(**{**b.__dict__, "size": _vec3(n, "size", [1, 1, 1])})
+
+
+@dataclass
+class RigidCylinderConfig(RigidSphereConfig):
+    height: float = 1.0
+
+    @classmethod
+    def from_node(cls, n):
+        b = RigidSphereConfig.from_node(n)
+        return cls(**{**b.__dict__, "height": float(_get(n, "height", 1.0))})
+
+
+def eul_xyz_to_quat(deg):
+    """Quaternion (x, y, z, w) of the rotation about x, then y, then z by the
+    given angles in degrees (the reference's eulXYZ2Quat convention,
+    src/utils/GeometryUtils.cpp:104-112)."""
+    hx, hy, hz = (0.5 * np.radians(a) for a in deg)
+    cx, sx, cy, sy, cz, sz = np.cos(hx), np.sin(hx), np.cos(hy), np.sin(hy), np.cos(hz), np.sin(hz)
+    return np.array([sx * cy * cz - cx * sy * sz, cx * sy * cz + sx * cy * sz, cx * cy * sz - sx * sy * cz,
+                     cx * cy * cz + sx * sy * sz])
 
 
 SIM_MODES = {"Visualization": "Visualization", "AFAP": "AFAP", "Frame-by-frame": "Frame-by-frame"}
@@ -189,7 +222,11 @@ class SimulationConfig:
                 c.objects.append(XPBDMeshObjectConfig.from_node(on, first_order=True))
             elif t == "RigidSphere":
                 c.objects.append(RigidSphereConfig.from_node(on))
-            elif t in ("RigidMeshObject", "RigidBox", "RigidCylinder", "VirtuosoArm", "VirtuosoRobot"):
+            elif t == "RigidBox":
+                c.objects.append(RigidBoxConfig.from_node(on))
+            elif t == "RigidCylinder":
+                c.objects.append(RigidCylinderConfig.from_node(on))
+            elif t in ("RigidMeshObject", "VirtuosoArm", "VirtuosoRobot"):
                 raise NotImplementedError(f"object type {t!r} is not provided by the GB300 solver")
             else:
                 raise ValueError(f"Unknown type of object! {t!r} is not a type of simulation object.")
@@ -262,10 +299,13 @@ class XPBDObject:
 
 
 @dataclass
-class Sphere:
+class Rigid:
+    """A fixed rigid primitive: kind (G.SDF_*), pose, dimensions."""
     name: str
-    centre: np.ndarray
-    radius: float
+    kind: int
+    position: np.ndarray
+    quat: np.ndarray
+    dims: np.ndarray
     collisions: bool
 
 
@@ -278,7 +318,7 @@ class Simulation:
             self.base_dir = base_dir or d
         self.time = 0.0
         self.objects: dict[str, XPBDObject] = {}
-        self.spheres: dict[str, Sphere] = {}
+        self.rigids: dict[str, Rigid] = {}
         self._setup = False
 
     def material(self, name: str) -> ElasticMaterialConfig:
@@ -295,23 +335,35 @@ class Simulation:
                 continue
             if isinstance(oc, RigidSphereConfig):
                 if not oc.fixed:
-                    raise NotImplementedError(f"rigid sphere {oc.name!r}: non-fixed rigid bodies (two-way "
+                    raise NotImplementedError(f"rigid object {oc.name!r}: non-fixed rigid bodies (two-way "
                                               "coupling) are not provided; set `fixed: true`")
-                self.spheres[oc.name] = Sphere(oc.name, oc.position.copy(), oc.radius, oc.collisions)
+                if isinstance(oc, RigidBoxConfig):
+                    kind, dims = G.SDF_BOX, np.asarray(oc.size, np.float64)
+                elif isinstance(oc, RigidCylinderConfig):
+                    kind, dims = G.SDF_CYLINDER, np.array([oc.radius, oc.height, 0.0])
+                else:
+                    kind, dims = G.SDF_SPHERE, np.array([oc.radius, 0.0, 0.0])
+                rot = getattr(oc, "rotation", np.zeros(3))
+                self.rigids[oc.name] = Rigid(oc.name, kind, oc.position.copy(), eul_xyz_to_quat(rot), dims,
+                                             oc.collisions)
             else:
                 self.objects[oc.name] = XPBDObject(oc, self)
-        self._push_spheres()
+        self._push_rigids()
 
-    def _push_spheres(self):
-        live = [s for s in self.spheres.values() if s.collisions]
+    def _push_rigids(self):
+        live = [r for r in self.rigids.values() if r.collisions]
         for o in self.objects.values():
             if o.cfg.collisions and live:
-                o.solver.set_spheres(np.array([s.centre for s in live]), [s.radius for s in live])
+                o.solver.set_sdfs([r.kind for r in live], [r.position for r in live], [r.quat for r in live],
+                                  [r.dims for r in live])
 
-    def move_sphere(self, name: str, centre):
-        """Kinematic sphere motion between steps (the fixed sphere's new pose)."""
-        self.spheres[name].centre = np.asarray(centre, np.float64)
-        self._push_spheres()
+    def move_rigid(self, name: str, position, rotation_deg=None):
+        """Kinematic motion of a fixed rigid object between steps."""
+        r = self.rigids[name]
+        r.position = np.asarray(position, np.float64)
+        if rotation_deg is not None:
+            r.quat = eul_xyz_to_quat(rotation_deg)
+        self._push_rigids()
 
     def time_step(self):
         for o in self.objects.values():

@@ -30,6 +30,7 @@ CONSTRAINT_COMBINED, CONSTRAINT_SEPARATE = 0, 1
 RESIDUAL_NEVER, RESIDUAL_EVERY_SUBSTEP, RESIDUAL_EVERY_ITERATION = 0, 1, 2
 JACOBI_ATOMIC, JACOBI_GATHER = 0, 1
 WARM_NONE, WARM_PREVIOUS, WARM_MLP = 0, 1, 2
+SDF_SPHERE, SDF_BOX, SDF_CYLINDER = 0, 1, 2
 MLP_INPUTS, MLP_PARAMS = 16, 9538
 
 # YAML `solver-type` strings (include/config/simobject/XPBDMeshObjectConfig.hpp:26-34)
@@ -157,6 +158,9 @@ def load(path: str | None = None):
         "xpbd_warm_start_stats": ([P, P, P], C.c_int),
         "xpbd_residual_noalloc": ([P, P], C.c_int),
         "xpbd_get_local_order": ([P, P, P, I32, P], C.c_int),
+        "xpbd_set_sdfs": ([P, I32, P, P, P, P], C.c_int),
+        "xpbd_set_instance_sdfs": ([P, I32, I32, P, P, P, P], C.c_int),
+        "xpbd_sdf_eval": ([I32, P, P, P, I64, P, P], C.c_int),
     }
     for name, (args, res) in sig.items():
         fn = getattr(L, name)
@@ -348,6 +352,16 @@ class XPBDSolver:
         r = np.ascontiguousarray(radii, np.float64).reshape(-1)
         self._ck(self.L.xpbd_set_instance_spheres(self.h, int(instance), len(r), _p(c), _p(r)))
 
+    def set_sdfs(self, kinds, positions, quats, dims, instance=0):
+        """Fixed rigid primitives (SDF_SPHERE / SDF_BOX / SDF_CYLINDER) with
+        orientation quaternions (x, y, z, w)."""
+        k = np.ascontiguousarray(kinds, np.int32).reshape(-1)
+        n = k.size
+        p = np.ascontiguousarray(positions, np.float64).reshape(n, 3)
+        q = np.ascontiguousarray(quats, np.float64).reshape(n, 4)
+        d = np.ascontiguousarray(dims, np.float64).reshape(n, 3)
+        self._ck(self.L.xpbd_set_instance_sdfs(self.h, int(instance), n, _p(k), _p(p), _p(q), _p(d)))
+
     def instance_offsets(self):
         """(vertex, tet, face) offsets of each instance, n + 1 entries each."""
         n = self.n_instances + 1
@@ -523,3 +537,17 @@ class XPBDSolver:
         k, r = C.c_int64(), C.c_int64()
         self._ck(self.L.xpbd_warm_start_stats(self.h, C.byref(k), C.byref(r)))
         return k.value, r.value
+
+
+def sdf_eval(kind, position, quat, dims, points) -> np.ndarray:
+    """(n, 4): SDF value and gradient of one primitive at points, on the GPU."""
+    L = load()
+    pos = np.ascontiguousarray(position, np.float64)
+    q = np.ascontiguousarray(quat, np.float64)
+    d = np.ascontiguousarray(dims, np.float64)
+    pts = np.ascontiguousarray(points, np.float64).reshape(-1, 3)
+    out = np.zeros((pts.shape[0], 4))
+    st = L.xpbd_sdf_eval(int(kind), _p(pos), _p(q), _p(d), pts.shape[0], _p(pts), _p(out))
+    if st != XPBD_OK:
+        raise XPBDError(st, "sdf_eval failed")
+    return out
