@@ -223,6 +223,19 @@ int xpbd_add_static_collision(xpbd_ctx* ctx, int32_t face, double u, double v, d
  * *n_out receives the count; at most max_rows rows are written. */
 int xpbd_get_collisions(xpbd_ctx* ctx, int32_t max_rows, double* rows, int32_t* n_out);
 
+/* Attachment constraints (AttachmentConstraint, include/solver/constraint/
+ * AttachmentConstraint.hpp; XPBDMeshObject_::addAttachmentConstraint /
+ * clearAttachmentConstraints, XPBDMeshObject.cpp:254-275): C = |x_v - (point +
+ * offset)|, alpha = 0, projected after the contacts of every iteration (the
+ * projector type order). The point can move between steps (a grasping tool);
+ * the offset is fixed. Attachments do not enter the residual. The reference's
+ * update writes 3 of its 4 coordinate slots and applies the fourth stale slot;
+ * here only the vertex's 3 coordinates change. */
+int xpbd_add_attachment(xpbd_ctx* ctx, int32_t vertex, const double* point3, const double* offset3, int32_t* id);
+int xpbd_set_attachment_point(xpbd_ctx* ctx, int32_t id, const double* point3);
+int xpbd_clear_attachments(xpbd_ctx* ctx);
+int xpbd_num_attachments(xpbd_ctx* ctx, int32_t* n);
+
 /* XPBDMeshObject_::update (XPBDMeshObject.cpp:426-505): prev <- x, inertial
  * move, solve (lambda <- 0, num_iters sweeps), fixed reset. Asynchronous. */
 int xpbd_update(xpbd_ctx* ctx);

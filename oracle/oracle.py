@@ -167,6 +167,14 @@ class Oracle:
         r = np.ascontiguousarray(radii, np.float64).reshape(-1)
         self.L.xo_set_spheres(C.c_void_p(self.h), len(r), _p(c), _p(r))
 
+    def add_attachment(self, vertex, target):
+        t = np.ascontiguousarray(target, np.float64)
+        self.L.xo_add_attachment(C.c_void_p(self.h), int(vertex), _p(t))
+
+    def set_attachment_target(self, attachment, target):
+        t = np.ascontiguousarray(target, np.float64)
+        self.L.xo_set_attachment_target(C.c_void_p(self.h), int(attachment), _p(t))
+
     def set_prims(self, kinds, positions, quats, dims):
         """Fixed SDF primitives: kinds 0 sphere, 1 box, 2 cylinder; quats (x, y, z, w)."""
         k = np.ascontiguousarray(kinds, np.int32).reshape(-1)

@@ -551,6 +551,33 @@ struct Object {
     std::vector<R> Q, vol, alpha_d, alpha_h, gamma;  // 9T, T, T, T, T
     std::vector<R> lam;              // 2T: [2t]=dev, [2t+1]=hyd
     std::vector<Contact<R>> contacts;
+    // attachment constraints: vertex, target (attach point + offset), lambda
+    struct Attachment {
+        int v;
+        R t[3];
+        R lambda;
+    };
+    std::vector<Attachment> attachments;
+    // AttachmentConstraint::evaluateWithGradient (AttachmentConstraint.hpp:70-90)
+    // projected by ConstraintProjector::project with alpha = 0
+    // (ConstraintProjector.hpp:111-172); dx receives the vertex's 3 updates
+    bool project_attachment(Attachment& at, R* dx) const {
+        const R* xv = &x[3 * at.v];
+        R a = xv[0] - at.t[0], b = xv[1] - at.t[1], c = xv[2] - at.t[2];
+        R dist = std::sqrt(a * a + b * b + c * c);
+        R g[3];
+        if (dist < R(1e-12)) {
+            g[0] = g[1] = g[2] = R(1e-12);
+        } else {
+            g[0] = a / dist; g[1] = b / dist; g[2] = c / dist;
+        }
+        const R w = inv_mass[at.v];
+        const R L = w * (g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        const R dl = -dist / L;
+        at.lambda += dl;
+        for (int k = 0; k < 3; k++) dx[k] = w * g[k] * dl;
+        return true;
+    }
     R dt = R(1e-3), g = R(9.81);
     double dt_host = 1e-3;           // the host loop's time step, always double
     int num_iter = 1;
@@ -744,6 +771,10 @@ struct Object {
             }
             for (auto& ct : contacts)
                 if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            for (auto& at : attachments) {
+                project_attachment(at, dx);
+                for (int k = 0; k < 3; k++) x[3 * at.v + k] += dx[k];
+            }
         } else if (solver == COLOURED_GS) {
             if (ckind == COMBINED) {
                 for (int t : tet_order) { project_tet_combined(t, dx); add_tet(t, dx); }
@@ -757,6 +788,11 @@ struct Object {
                 for (auto& ct : contacts)
                     if (face_colour[ct.face] == k)
                         if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            // attachments in insertion order (the GPU's colours keep it per vertex)
+            for (auto& at : attachments) {
+                project_attachment(at, dx);
+                for (int k = 0; k < 3; k++) x[3 * at.v + k] += dx[k];
+            }
         } else {  // Jacobi: every projection reads the same x; updates summed, no averaging
             std::vector<R> acc(3 * V, 0);
             for (long long t = 0; t < T; t++) {
@@ -774,6 +810,10 @@ struct Object {
             for (auto& ct : contacts)
                 if (project_contact_i(ct, dx))
                     for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
+            for (auto& at : attachments) {
+                project_attachment(at, dx);
+                for (int k = 0; k < 3; k++) acc[3 * at.v + k] += dx[k];
+            }
             for (long long i = 0; i < 3 * V; i++) x[i] += acc[i];
         }
     }
@@ -859,6 +899,7 @@ struct Object {
         move_inertially();
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;
+        for (auto& at : attachments) at.lambda = 0;
         const double r_plain = residual_norm();
         const std::vector<R> x_pred = x;
         std::vector<R> acc(3 * V, 0);
@@ -903,6 +944,7 @@ struct Object {
         // XPBDSolver::solve: lambda <- 0, num_iter sweeps (XPBDSolver.hpp:66-97)
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;
+        for (auto& at : attachments) at.lambda = 0;
         res_history.clear();
         for (int it = 0; it < num_iter; it++) {
             if (record_residual) res_history.push_back(residual_norm());

@@ -301,6 +301,26 @@ void xo_set_first_order(void* p, double multiplier, int adjust, const double* E,
     });
 }
 
+// attachment constraint on vertex v with target point (attach point + offset)
+void xo_add_attachment(void* p, int v, const double* target3) {
+    with((Handle*)p, [&](auto& o) {
+        using A = typename std::decay_t<decltype(o.attachments)>::value_type;
+        A a;
+        a.v = v;
+        for (int k = 0; k < 3; k++) a.t[k] = target3[k];
+        a.lambda = 0;
+        o.attachments.push_back(a);
+        return 0;
+    });
+}
+
+void xo_set_attachment_target(void* p, int id, const double* target3) {
+    with((Handle*)p, [&](auto& o) {
+        for (int k = 0; k < 3; k++) o.attachments[id].t[k] = target3[k];
+        return 0;
+    });
+}
+
 int xo_set_order(void* p, int n, const int* order) {
     return with((Handle*)p, [&](auto& o) {
         if (n != (int)o.T) return 1;

@@ -530,3 +530,40 @@ def test_first_order_trajectory_matches_fp64_oracle(lib, solver, adjust):
     # the body moved (gravity acts through the damping)
     assert np.abs(s.positions() - x0).max() > 1e-4
     s.close()
+
+
+@pytest.mark.parametrize("solver", [G.SOLVER_GAUSS_SEIDEL, G.SOLVER_JACOBI])
+def test_attachments_match_fp64_oracle(lib, solver):
+    """Grasping-style attachments: two top vertices attached (one with an
+    offset) to points that rise 1 mm per step; bottom fixed; 30 steps."""
+    X, tets, faces, x0 = _noisy_cube(4, seed=21, noise=1e-3)
+    E = 3e3 if solver == G.SOLVER_GAUSS_SEIDEL else 1e3
+    s = G.XPBDSolver(X, tets, None, E, 0.4, 1000.0, num_iters=8, solver_type=solver)
+    o = O.Oracle(X, tets, faces, E, 0.4, 1000.0, num_iter=8,
+                 solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS)
+    if solver == G.SOLVER_GAUSS_SEIDEL:
+        o.set_order(s.sweep_order())
+    fixed = X[:, 2] == 0
+    s.set_positions(x0); s.fix_vertices(fixed)
+    o.set_positions(x0); o.set_fixed(fixed)
+    top = np.nonzero(X[:, 2] == X[:, 2].max())[0]
+    v1, v2 = int(top[0]), int(top[-1])
+    off = np.array([0.0, 0.0, 0.002])
+    a1 = s.add_attachment(v1, X[v1])
+    a2 = s.add_attachment(v2, X[v2] - off, off)
+    o.add_attachment(v1, X[v1])
+    o.add_attachment(v2, X[v2])
+    for k in range(30):
+        lift = np.array([0, 0, 1e-3 * (k + 1)])
+        s.set_attachment_point(a1, X[v1] + lift)
+        s.set_attachment_point(a2, X[v2] - off + lift)
+        o.set_attachment_target(0, X[v1] + lift)
+        o.set_attachment_target(1, X[v2] + lift)
+        s.update(); s.velocity_update()
+        o.update(); o.velocity_update()
+    err = np.abs(s.positions() - o.positions()).max()
+    assert err <= 1e-4 * _extent(X), err
+    # the attached vertices followed their points
+    assert s.positions()[v1, 2] > X[v1, 2] + 0.02
+    s.close()
+    o.close()

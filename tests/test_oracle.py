@@ -261,3 +261,17 @@ def test_first_order_damping_adjusted_to_material():
     d = o.positions() - X
     np.testing.assert_allclose(d[:, 2], -4 * 9.81 * 1000.0 * 1e-3 / (10.0 * 2e3 / 1.25), rtol=1e-9)
     o.close()
+
+
+def test_attachment_puts_its_vertex_on_the_target():
+    """alpha = 0 and |grad C| = 1: one scalar projection moves the vertex by
+    -(x - target); projected last in an iteration, it ends on the target."""
+    import xpbd_gb300 as G
+    X, tets, faces = G.grid_mesh(2, 2, 2, 0.1)
+    o = O.Oracle(X, tets, faces, 3e3, 0.45, 1000.0, dt=1e-3, g=0.0, num_iter=1)
+    v = int(np.argmax(X[:, 2] + X[:, 0]))
+    target = X[v] + np.array([0.01, -0.02, 0.03])
+    o.add_attachment(v, target)
+    o.update()
+    np.testing.assert_allclose(o.positions()[v], target, atol=1e-12)
+    o.close()

@@ -14,6 +14,7 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/xpbd_gpu.h"
@@ -303,6 +304,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
+                if (!c->att_v.empty()) {
+                    Scope sc(c, K_CONTACT);
+                    launch_attach_jacobi(c->L(), c->d_att_v.p, c->d_att_target.p, c->d_att_lam.p,
+                                         (int)c->att_v.size(), c->x.p, c->dx.p, first_contact);
+                }
                 Scope sc(c, K_GATHER);
                 launch_gather_apply(c->L(), c->x.p, c->dxt.p, c->csr_off.p, c->csr_ent.p, c->dx.p, c->V, c->prev.p,
                                     c->vel.p, last && fuse_final, dt, write_vel);
@@ -316,11 +322,16 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
+                if (!c->att_v.empty()) {
+                    Scope sc(c, K_CONTACT);
+                    launch_attach_jacobi(c->L(), c->d_att_v.p, c->d_att_target.p, c->d_att_lam.p,
+                                         (int)c->att_v.size(), c->x.p, c->dx.p, first_contact);
+                }
                 Scope sc(c, K_APPLY);
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
-    } else if (!separate && !every_iter && !have_faces && p.gs_variant >= 2 && c->ntasks > 0) {
+    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() && p.gs_variant >= 2 && c->ntasks > 0) {
         // every iteration and colour in one cooperative launch
         if (track && !warm) exact_residual_row(c, 0, false);
         cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
@@ -351,6 +362,12 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
                 }
             }
+            // attachments last: the projector type order (XPBDTypedefs.hpp:55-56)
+            for (int ac = 0; ac + 1 < (int)c->att_col_off.size(); ac++) {
+                Scope sc(c, K_CONTACT);
+                launch_attach_gs(c->L(), c->d_att_v.p, c->d_att_target.p, c->d_att_lam.p, c->d_att_order.p,
+                                 c->att_col_off[ac], c->att_col_off[ac + 1], c->x.p, first);
+            }
         }
     }
     if (c->record) {
@@ -373,7 +390,61 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     return XPBD_OK;
 }
 
+// device copies of the attachments: structure (vertices, colours) when
+// attachments were added or cleared, targets whenever an attach point moved
+int sync_attachments(xpbd_ctx* c) {
+    const int n = (int)c->att_v.size();
+    if (c->att_struct_dirty) {
+        XPBD_CU(c, cudaStreamSynchronize(c->stream));
+        if ((size_t)n > c->d_att_v.n) {
+            const size_t cap = std::max<size_t>(64, 2 * (size_t)n);
+            c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
+            XPBD_CU(c, c->d_att_v.alloc(cap));
+            XPBD_CU(c, c->d_att_order.alloc(cap));
+            XPBD_CU(c, c->d_att_target.alloc(cap));
+            XPBD_CU(c, c->d_att_lam.alloc(cap));
+        }
+        // greedy colouring by vertex, in insertion order: attachments on one
+        // vertex keep their order across colours
+        std::vector<int> col(n);
+        std::unordered_map<int, int> seen;
+        int ncol = 0;
+        for (int a = 0; a < n; a++) {
+            col[a] = seen[c->att_v[a]]++;
+            ncol = std::max(ncol, col[a] + 1);
+        }
+        c->att_col_off.assign(n ? ncol + 1 : 0, 0);
+        for (int a = 0; a < n; a++) c->att_col_off[col[a] + 1]++;
+        for (int k = 0; k < ncol; k++) c->att_col_off[k + 1] += c->att_col_off[k];
+        c->att_order.assign(n, 0);
+        std::vector<int> fill(c->att_col_off.begin(), c->att_col_off.end() - (n ? 1 : 0));
+        for (int a = 0; a < n; a++) c->att_order[fill[col[a]]++] = a;
+        if (n) {
+            XPBD_CU(c, cudaMemcpy(c->d_att_v.p, c->att_v.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+            XPBD_CU(c, cudaMemcpy(c->d_att_order.p, c->att_order.data(), sizeof(int) * n, cudaMemcpyHostToDevice));
+            XPBD_CU(c, cudaMemset(c->d_att_lam.p, 0, sizeof(float) * n));
+        }
+        c->att_struct_dirty = false;
+        c->att_target_dirty = true;
+        c->graph_dirty = true;
+    }
+    if (c->att_target_dirty && n) {
+        std::vector<float4> tg(n);
+        for (int a = 0; a < n; a++)
+            tg[a] = make_float4((float)(c->att_point[3 * a] + c->att_offset[3 * a]),
+                                (float)(c->att_point[3 * a + 1] + c->att_offset[3 * a + 1]),
+                                (float)(c->att_point[3 * a + 2] + c->att_offset[3 * a + 2]), 0.f);
+        // pageable source: staged before the call returns, ordered on the stream
+        XPBD_CU(c, cudaMemcpyAsync(c->d_att_target.p, tg.data(), sizeof(float4) * n, cudaMemcpyHostToDevice,
+                                   c->stream));
+    }
+    c->att_target_dirty = false;
+    return XPBD_OK;
+}
+
 int prepare_update(xpbd_ctx* c) {
+    int ast = sync_attachments(c);
+    if (ast) return ast;
     if (tracking(c) || c->warm_mode != XPBD_WARM_NONE) {
         // one extra row for on-demand residual queries, two for the warm start
         int st = ensure_residual_rows(c, c->prm.num_iters + 4);
@@ -473,6 +544,7 @@ void release(xpbd_ctx* c) {
     c->sphere_tab.release(); c->face_inst.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
+    c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
@@ -1246,6 +1318,48 @@ int xpbd_add_static_collision(xpbd_ctx* c, int32_t face, double u, double v, dou
     XPBD_CU(c, cudaMemcpy(c->c_lam.p + slot, &z, sizeof z, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->c_bary.p + slot, &b, sizeof b, cudaMemcpyHostToDevice));
     c->api_slots[face] = s + 1;
+    return XPBD_OK;
+}
+
+int xpbd_add_attachment(xpbd_ctx* c, int32_t vertex, const double* point3, const double* offset3, int32_t* id) {
+    if (!c || !point3) return XPBD_ERR_INVALID;
+    if (vertex < 0 || vertex >= c->V) return fail(c, XPBD_ERR_INVALID, "vertex %d out of range", vertex);
+    for (int k = 0; k < 3; k++)
+        if (!std::isfinite(point3[k]) || (offset3 && !std::isfinite(offset3[k])))
+            return fail(c, XPBD_ERR_INVALID, "attachment point or offset is not finite");
+    c->att_v.push_back(vertex);
+    for (int k = 0; k < 3; k++) {
+        c->att_point.push_back(point3[k]);
+        c->att_offset.push_back(offset3 ? offset3[k] : 0.0);
+    }
+    if (id) *id = (int32_t)c->att_v.size() - 1;
+    c->att_struct_dirty = true;
+    return XPBD_OK;
+}
+
+int xpbd_set_attachment_point(xpbd_ctx* c, int32_t id, const double* point3) {
+    if (!c || !point3) return XPBD_ERR_INVALID;
+    if (id < 0 || id >= (int)c->att_v.size()) return fail(c, XPBD_ERR_INVALID, "attachment %d does not exist", id);
+    for (int k = 0; k < 3; k++) {
+        if (!std::isfinite(point3[k])) return fail(c, XPBD_ERR_INVALID, "attachment point is not finite");
+        c->att_point[3 * id + k] = point3[k];
+    }
+    c->att_target_dirty = true;
+    return XPBD_OK;
+}
+
+int xpbd_clear_attachments(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (!c->att_v.empty()) c->att_struct_dirty = true;
+    c->att_v.clear();
+    c->att_point.clear();
+    c->att_offset.clear();
+    return XPBD_OK;
+}
+
+int xpbd_num_attachments(xpbd_ctx* c, int32_t* n) {
+    if (!c || !n) return XPBD_ERR_INVALID;
+    *n = (int32_t)c->att_v.size();
     return XPBD_OK;
 }
 

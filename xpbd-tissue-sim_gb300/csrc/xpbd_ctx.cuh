@@ -84,6 +84,15 @@ struct xpbd_ctx {
     DevBuf<int> local_slots;
     DevBuf<unsigned char> vmask, tmask;
     DevBuf<float> gdz;                   // 1st order: per-vertex inertial z move
+    // attachment constraints: vertex, attach point + offset (host, double),
+    // the device copies, and a colouring so no colour repeats a vertex
+    std::vector<int> att_v;
+    std::vector<double> att_point, att_offset;  // 3 per attachment
+    std::vector<int> att_order, att_col_off;
+    bool att_struct_dirty = false, att_target_dirty = false;
+    DevBuf<int> d_att_v, d_att_order;
+    DevBuf<float4> d_att_target;
+    DevBuf<float> d_att_lam;
     // dataflow Gauss-Seidel (sweep variant 2): tasks, dependencies, epochs
     int ntasks = 0, flow_grid = 0;
     DevBuf<int4> flow_tasks;

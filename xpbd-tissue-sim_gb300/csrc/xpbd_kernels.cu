@@ -1373,6 +1373,68 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
     }
 }
 
+// ---- attachment constraints (AttachmentConstraint.hpp:15-100) ----
+// C = |x - target|, grad C = (x - target) / C (1e-12 per component when C <
+// 1e-12), alpha = 0, an equality constraint projected by the scalar rule of
+// ConstraintProjector::project (ConstraintProjector.hpp:111-172).
+__device__ __forceinline__ void attach_update(const float4 xv, const float4 tg, float lam, float& dlam, float d[3]) {
+    const float a = xv.x - tg.x, b = xv.y - tg.y, c = xv.z - tg.z;
+    const float dist = sqrtf(a * a + b * b + c * c);
+    float g0, g1, g2;
+    if (dist < 1e-12f) {
+        g0 = g1 = g2 = 1e-12f;
+    } else {
+        g0 = a / dist; g1 = b / dist; g2 = c / dist;
+    }
+    const float w = fabsf(xv.w);
+    const float L = w * (g0 * g0 + g1 * g1 + g2 * g2);
+    dlam = -dist / L;
+    d[0] = w * g0 * dlam;
+    d[1] = w * g1 * dlam;
+    d[2] = w * g2 * dlam;
+    (void)lam;  // alpha~ = 0: lambda does not enter the update
+}
+
+// Gauss-Seidel: one colour of attachments (no two share a vertex), in place
+__global__ void k_attach_gs(const int* __restrict__ vert, const float4* __restrict__ target,
+                            float* __restrict__ lam, const int* __restrict__ order, int begin, int end,
+                            float4* __restrict__ x, bool first) {
+    pdl_wait_then_release();
+    const int i = begin + blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= end) return;
+    const int a = order[i];
+    const int v = vert[a];
+    const float4 xv = x[v];
+    float l = first ? 0.f : lam[a];
+    float dl, d[3];
+    attach_update(xv, target[a], l, dl, d);
+    if (isfinite(dl)) {
+        lam[a] = l + dl;
+        x[v] = moved(xv, d);
+    } else {
+        lam[a] = l;
+    }
+}
+
+// Jacobi: every attachment from the same x, updates summed into dx
+__global__ void k_attach_jacobi(const int* __restrict__ vert, const float4* __restrict__ target,
+                                float* __restrict__ lam, int n, const float4* __restrict__ x,
+                                float4* __restrict__ dx, bool first) {
+    pdl_wait_then_release();
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    if (a >= n) return;
+    const int v = vert[a];
+    float l = first ? 0.f : lam[a];
+    float dl, d[3];
+    attach_update(x[v], target[a], l, dl, d);
+    if (isfinite(dl)) {
+        lam[a] = l + dl;
+        add_vec4(dx + v, d[0], d[1], d[2]);
+    } else {
+        lam[a] = l;
+    }
+}
+
 // ---- local collision iterations (XPBDMeshObject.cpp:472-505, 764-825) ----
 // Vertices of every contact that was projected (lambda != 0) in the global
 // solve; vmask must be cleared first.
@@ -1780,6 +1842,16 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
     if (first_zero) XG_FLOW(true, 1);
     XG_FLOW(false, 1);
 #undef XG_FLOW
+}
+
+void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
+                      int end, float4* x, bool first) {
+    if (end > begin) go(k_attach_gs, nblk(end - begin, 128), 128, s, vert, target, lam, order, begin, end, x, first);
+}
+
+void launch_attach_jacobi(const Launch& s, const int* vert, const float4* target, float* lam, int n, const float4* x,
+                          float4* dx, bool first) {
+    if (n > 0) go(k_attach_jacobi, nblk(n, 128), 128, s, vert, target, lam, n, x, dx, first);
 }
 
 void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,

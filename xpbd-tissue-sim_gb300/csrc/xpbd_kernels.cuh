@@ -184,6 +184,10 @@ void launch_velocity(const Launch& s, const float4* x, const float4* prev, float
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
                      const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2,
                      bool zero_lam = false);
+void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
+                      int end, float4* x, bool first);
+void launch_attach_jacobi(const Launch& s, const int* vert, const float4* target, float* lam, int n, const float4* x,
+                          float4* dx, bool first);
 void launch_mark_local(const Launch& s, const ContactArrays& c, const TetArrays& t, int T, unsigned char* vmask,
                        unsigned char* tmask);
 void launch_project_local_gs(const Launch& s, const TetArrays& t, const int* order, int begin, int end,

@@ -159,6 +159,10 @@ def load(path: str | None = None):
         "xpbd_residual_noalloc": ([P, P], C.c_int),
         "xpbd_get_local_order": ([P, P, P, I32, P], C.c_int),
         "xpbd_set_sdfs": ([P, I32, P, P, P, P], C.c_int),
+        "xpbd_add_attachment": ([P, I32, P, P, P], C.c_int),
+        "xpbd_set_attachment_point": ([P, I32, P], C.c_int),
+        "xpbd_clear_attachments": ([P], C.c_int),
+        "xpbd_num_attachments": ([P, P], C.c_int),
         "xpbd_set_instance_sdfs": ([P, I32, I32, P, P, P, P], C.c_int),
         "xpbd_sdf_eval": ([I32, P, P, P, I64, P, P], C.c_int),
     }
@@ -361,6 +365,20 @@ class XPBDSolver:
         q = np.ascontiguousarray(quats, np.float64).reshape(n, 4)
         d = np.ascontiguousarray(dims, np.float64).reshape(n, 3)
         self._ck(self.L.xpbd_set_instance_sdfs(self.h, int(instance), n, _p(k), _p(p), _p(q), _p(d)))
+
+    def add_attachment(self, vertex, point, offset=(0.0, 0.0, 0.0)) -> int:
+        p = np.ascontiguousarray(point, np.float64)
+        o = np.ascontiguousarray(offset, np.float64)
+        i = C.c_int32()
+        self._ck(self.L.xpbd_add_attachment(self.h, int(vertex), _p(p), _p(o), C.byref(i)))
+        return i.value
+
+    def set_attachment_point(self, attachment, point):
+        p = np.ascontiguousarray(point, np.float64)
+        self._ck(self.L.xpbd_set_attachment_point(self.h, int(attachment), _p(p)))
+
+    def clear_attachments(self):
+        self._ck(self.L.xpbd_clear_attachments(self.h))
 
     def instance_offsets(self):
         """(vertex, tet, face) offsets of each instance, n + 1 entries each."""
