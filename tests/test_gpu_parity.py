@@ -533,28 +533,35 @@ def test_first_order_trajectory_matches_fp64_oracle(lib, solver, adjust):
 
 
 @pytest.mark.parametrize("solver", [G.SOLVER_GAUSS_SEIDEL, G.SOLVER_JACOBI])
-def test_attachments_match_fp64_oracle(lib, solver):
-    """Grasping-style attachments: two top vertices attached (one with an
-    offset) to points that rise 1 mm per step; bottom fixed; 30 steps."""
+def test_attachments_match_fp32_oracle(lib, solver):
+    """Grasping-style attachments: two top vertices attached (one through an
+    offset) to points that rise 0.1 mm per step; bottom fixed; 15 steps.
+    Compared with the FP32 oracle: below |x - target| = 1e-12 the reference's
+    gradient falls back to (1e-12, 1e-12, 1e-12), which turns a rounding-level
+    distance into a jump of -C / 3e-12 per coordinate. FP64 runs reach that
+    branch after a vertex has been snapped onto its target (distances of
+    1e-13 .. 1e-15); FP32 distances between coordinates away from 0 never fall
+    below it except at exactly 0, where the update is 0 -- so the FP64
+    trajectory is not a usable reference here."""
     X, tets, faces, x0 = _noisy_cube(4, seed=21, noise=1e-3)
-    E = 3e3 if solver == G.SOLVER_GAUSS_SEIDEL else 1e3
-    s = G.XPBDSolver(X, tets, None, E, 0.4, 1000.0, num_iters=8, solver_type=solver)
-    o = O.Oracle(X, tets, faces, E, 0.4, 1000.0, num_iter=8,
+    s = G.XPBDSolver(X, tets, None, 3e4, 0.4, 1000.0, num_iters=8, solver_type=solver)
+    o = O.Oracle(X, tets, faces, 3e4, 0.4, 1000.0, num_iter=8, precision=32,
                  solver=O.JACOBI if solver == G.SOLVER_JACOBI else O.COLOURED_GS)
     if solver == G.SOLVER_GAUSS_SEIDEL:
         o.set_order(s.sweep_order())
     fixed = X[:, 2] == 0
     s.set_positions(x0); s.fix_vertices(fixed)
     o.set_positions(x0); o.set_fixed(fixed)
-    top = np.nonzero(X[:, 2] == X[:, 2].max())[0]
+    # top vertices away from the coordinate planes (no sub-1e-12 float spacing)
+    top = np.nonzero((X[:, 2] == X[:, 2].max()) & (X[:, 0] >= 0.25) & (X[:, 1] >= 0.25))[0]
     v1, v2 = int(top[0]), int(top[-1])
     off = np.array([0.0, 0.0, 0.002])
     a1 = s.add_attachment(v1, X[v1])
     a2 = s.add_attachment(v2, X[v2] - off, off)
     o.add_attachment(v1, X[v1])
     o.add_attachment(v2, X[v2])
-    for k in range(30):
-        lift = np.array([0, 0, 1e-3 * (k + 1)])
+    for k in range(15):
+        lift = np.array([0, 0, 1e-4 * (k + 1)])
         s.set_attachment_point(a1, X[v1] + lift)
         s.set_attachment_point(a2, X[v2] - off + lift)
         o.set_attachment_target(0, X[v1] + lift)
@@ -562,8 +569,8 @@ def test_attachments_match_fp64_oracle(lib, solver):
         s.update(); s.velocity_update()
         o.update(); o.velocity_update()
     err = np.abs(s.positions() - o.positions()).max()
-    assert err <= 1e-4 * _extent(X), err
-    # the attached vertices followed their points
-    assert s.positions()[v1, 2] > X[v1, 2] + 0.02
+    assert err <= 1e-5 * _extent(X), err
+    # the attached vertex ends on its point (within Jacobi's summed updates)
+    np.testing.assert_allclose(s.positions()[v1], X[v1] + [0, 0, 1.5e-3], atol=1e-6)
     s.close()
     o.close()
