@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 3
+#define XPBD_ABI_VERSION 4
 
 /* status codes */
 #define XPBD_OK 0
@@ -206,6 +206,24 @@ int xpbd_set_sdfs(xpbd_ctx* ctx, int32_t n, const int32_t* kind, const double* p
                   const double* dims3n);
 int xpbd_set_instance_sdfs(xpbd_ctx* ctx, int32_t instance, int32_t n, const int32_t* kind, const double* pos3n,
                            const double* quat4n, const double* dims3n);
+/* Free rigid bodies: SDF slot `slot` of `instance` becomes a RigidObject
+ * with fixed: false (src/simobject/RigidObject.cpp) -- mass, diagonal inertia
+ * (RigidPrimitives.cpp formulas are the caller's), velocity and angular
+ * velocity; the pose is the one last given to xpbd_set_instance_sdfs (double).
+ * Detection then makes its contacts RigidDeformableCollisionConstraints
+ * (CollisionScene.cpp:204-210), projected after the static contacts by
+ * RigidBodyConstraintProjector (RigidBodyConstraintProjector.hpp:97-158): the
+ * multiplier from the deformable weights alone, the body moved by
+ * PositionalRigidBodyXPBDHelper::update (RigidBodyConstraint.hpp), all
+ * contacts in slot order by one device thread (each moves the body the next
+ * one reads). Each xpbd_step then runs RigidObject::update (gravity, the
+ * Euler step of the angular velocity, normalised orientation) and
+ * velocityUpdate after the deformable update. Setting SDFs for an instance
+ * drops its free bodies. State: FP64 on the device. Needs surface faces. */
+int xpbd_set_rigid_body(xpbd_ctx* ctx, int32_t instance, int32_t slot, double mass, const double* inertia3,
+                        const double* velocity3, const double* angular_velocity3);
+/* state13 = position[3], orientation (x, y, z, w)[4], velocity[3], angular velocity[3] */
+int xpbd_get_rigid_body(xpbd_ctx* ctx, int32_t instance, int32_t slot, double* state13);
 /* SDF value and gradient of one primitive at n points on the device
  * (out: n x (sdf, gx, gy, gz)); a test and tooling hook, no context needed */
 int xpbd_sdf_eval(int32_t kind, const double* pos3, const double* quat4, const double* dims3, int64_t n,

@@ -184,6 +184,18 @@ class Oracle:
         d = np.ascontiguousarray(dims, np.float64).reshape(n, 3)
         self.L.xo_set_prims(C.c_void_p(self.h), n, _p(k), _p(p), _p(q), _p(d))
 
+    def set_rigid_body(self, prim, position, quat, mass, inertia, velocity=(0, 0, 0), angular_velocity=(0, 0, 0)):
+        """Primitive `prim` (after set_prims) becomes a free rigid body."""
+        a = [np.ascontiguousarray(v, np.float64) for v in (position, quat, inertia, velocity, angular_velocity)]
+        self.L.xo_set_rigid_body(C.c_void_p(self.h), int(prim), _p(a[0]), _p(a[1]), C.c_double(mass), _p(a[2]),
+                                 _p(a[3]), _p(a[4]))
+
+    def rigid_body(self, prim):
+        """(position, quaternion (x, y, z, w), velocity, angular velocity)."""
+        out = np.zeros(13)
+        self.L.xo_get_rigid_body(C.c_void_p(self.h), int(prim), _p(out))
+        return out[:3], out[3:7], out[7:10], out[10:13]
+
     def detect(self):
         return self.L.xo_detect(C.c_void_p(self.h))
 

@@ -303,6 +303,7 @@ struct Contact {
     R p[3];        // surface point
     R n[3];        // normal
     R lambda;
+    bool dynamic = false;  // against a free rigid body (RigidDeformableCollisionConstraint)
 };
 
 // SphereSDF::evaluate / gradient (src/geometry/SphereSDF.cpp:16-26). Eigen's
@@ -509,6 +510,129 @@ inline bool project_contact(const R* x1, const R* x2, const R* x3, const R* wv, 
 }
 
 // ---------------------------------------------------------------------------
+// Free rigid bodies (RigidObject with fixed: false) and two-way coupling.
+// The rigid state is double, as the reference's Real, for either precision
+// of the deformable object.
+// ---------------------------------------------------------------------------
+// GeometryUtils::quatMult (src/utils/GeometryUtils.cpp:81-90), (x, y, z, w)
+inline void quat_mult(const double* a, const double* b, double* r) {
+    r[0] = a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1];
+    r[1] = a[3] * b[1] + a[1] * b[3] + a[2] * b[0] - a[0] * b[2];
+    r[2] = a[3] * b[2] + a[2] * b[3] + a[0] * b[1] - a[1] * b[0];
+    r[3] = a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2];
+}
+// GeometryUtils::inverseQuat (src/utils/GeometryUtils.cpp:99-102)
+inline void quat_inverse(const double* q, double* r) {
+    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
+    r[0] = -q[0] / n2; r[1] = -q[1] / n2; r[2] = -q[2] / n2; r[3] = q[3] / n2;
+}
+inline void cross3(const double* a, const double* b, double* r) {
+    r[0] = a[1] * b[2] - a[2] * b[1];
+    r[1] = a[2] * b[0] - a[0] * b[2];
+    r[2] = a[0] * b[1] - a[1] * b[0];
+}
+
+// RigidObject (src/simobject/RigidObject.cpp) with a diagonal inertia (the
+// primitives' _I, src/simobject/RigidPrimitives.cpp).
+struct RigidBody {
+    int kind = PRIM_SPHERE;
+    double d[3] = {0, 0, 0};
+    double p[3] = {0, 0, 0}, q[4] = {0, 0, 0, 1}, v[3] = {0, 0, 0}, w[3] = {0, 0, 0};
+    double p_prev[3] = {0, 0, 0}, q_prev[4] = {0, 0, 0, 1};
+    double m = 1, I[3] = {1, 1, 1}, I_inv[3] = {1, 1, 1};
+
+    Prim<double> prim() const {
+        Prim<double> pr;
+        pr.kind = kind;
+        for (int k = 0; k < 3; k++) { pr.p[k] = p[k]; pr.d[k] = d[k]; }
+        for (int k = 0; k < 4; k++) pr.q[k] = q[k];
+        return pr;
+    }
+
+    // RigidObject::update (RigidObject.cpp:41-60): gravity on v and p, the
+    // body-frame Euler step of w (no external torque), q += dt/2 [w,0] q, normalised
+    void update(double dt, double g) {
+        const double f[3] = {0.0, 0.0, -m * g};
+        for (int k = 0; k < 3; k++) v[k] = v[k] + dt * f[k] / m;
+        for (int k = 0; k < 3; k++) p[k] = p[k] + dt * v[k];
+        double qi[4], wb[3], Iw[3], c[3];
+        quat_inverse(q, qi);
+        quat_rotate(w, qi, wb);
+        for (int k = 0; k < 3; k++) Iw[k] = I[k] * wb[k];
+        cross3(wb, Iw, c);
+        for (int k = 0; k < 3; k++) wb[k] = wb[k] + dt * I_inv[k] * (0.0 - c[k]);
+        quat_rotate(wb, q, w);
+        const double w4[4] = {w[0], w[1], w[2], 0.0};
+        double dq[4];
+        quat_mult(w4, q, dq);
+        for (int k = 0; k < 4; k++) q[k] = q[k] + 0.5 * dt * dq[k];
+        const double n = std::sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+        for (int k = 0; k < 4; k++) q[k] /= n;
+    }
+
+    // RigidObject::velocityUpdate (RigidObject.cpp:62-77)
+    void velocity_update(double dt) {
+        for (int k = 0; k < 3; k++) v[k] = (p[k] - p_prev[k]) / dt;
+        double qi[4], dq[4];
+        quat_inverse(q_prev, qi);
+        quat_mult(q, qi, dq);
+        for (int k = 0; k < 3; k++) w[k] = 2 / dt * dq[k];
+        if (dq[3] < 0)
+            for (int k = 0; k < 3; k++) w[k] = -w[k];
+        for (int k = 0; k < 3; k++) p_prev[k] = p[k];
+        for (int k = 0; k < 4; k++) q_prev[k] = q[k];
+    }
+
+    // PositionalRigidBodyXPBDHelper::update (RigidBodyConstraint.hpp) for a
+    // contact at global point pt with direction -n: position and orientation
+    // increments from the body's current pose
+    void contact_delta(double dlam, const double* pt, const double* n, double* dp, double* dq) const {
+        const double dir[3] = {-n[0], -n[1], -n[2]};
+        double qi[4], rb[3], nb[3], t[3], c[3], wb[3], ws[3];
+        quat_inverse(q, qi);
+        const double rel[3] = {pt[0] - p[0], pt[1] - p[1], pt[2] - p[2]};
+        quat_rotate(rel, qi, rb);
+        quat_rotate(dir, qi, nb);
+        for (int k = 0; k < 3; k++) dp[k] = dlam * dir[k] / m;
+        for (int k = 0; k < 3; k++) t[k] = dlam * nb[k];
+        cross3(rb, t, c);
+        for (int k = 0; k < 3; k++) wb[k] = 0.5 * I_inv[k] * c[k];
+        quat_rotate(wb, q, ws);
+        const double w4[4] = {ws[0], ws[1], ws[2], 0.0};
+        quat_mult(w4, q, dq);
+    }
+};
+
+// RigidDeformableCollisionConstraint (RigidDeformableCollisionConstraint.cpp:23-55)
+// projected by RigidBodyConstraintProjector::project
+// (RigidBodyConstraintProjector.hpp:97-158): C = the body's SDF at the
+// contact's barycentric point (current pose), gradient (u n, v n, w n),
+// inequality skip when C > 0, alpha = 0; the multiplier update uses only the
+// deformable weights. Deformable arithmetic in double; dx receives the 9
+// vertex updates. Returns false when skipped.
+template <typename R>
+inline bool project_rigid_contact(const R* x1, const R* x2, const R* x3, const R* wv, Contact<R>& ct,
+                                  const RigidBody& rb, double* dx, double* dlam_out) {
+    const double b[3] = {(double)ct.u, (double)ct.v_, (double)ct.w};
+    double a[3];
+    for (int k = 0; k < 3; k++) a[k] = b[0] * (double)x1[k] + b[1] * (double)x2[k] + b[2] * (double)x3[k];
+    const double C = prim_sdf(rb.prim(), a);
+    if (C > 0) return false;
+    const double n[3] = {(double)ct.n[0], (double)ct.n[1], (double)ct.n[2]};
+    double L = 0;
+    for (int i = 0; i < 3; i++) {
+        const double gx = b[i] * n[0], gy = b[i] * n[1], gz = b[i] * n[2];
+        L += (double)wv[i] * (gx * gx + gy * gy + gz * gz);
+    }
+    const double dl = -C / L;
+    ct.lambda = (R)((double)ct.lambda + dl);
+    for (int i = 0; i < 3; i++)
+        for (int k = 0; k < 3; k++) dx[3 * i + k] = (double)wv[i] * (b[i] * n[k]) * dl;
+    *dlam_out = dl;
+    return true;
+}
+
+// ---------------------------------------------------------------------------
 // Greedy tet colouring used by the coloured Gauss-Seidel order. Tets are
 // visited in index order; each takes the smallest colour not used by any tet
 // already coloured that shares a vertex. Surface faces use the same rule.
@@ -592,7 +716,56 @@ struct Object {
     int num_local_iter = 0;
     std::vector<int> local_order;
     // spheres
-    std::vector<Prim<R>> prims;   // static SDF primitives (fixed rigid bodies)
+    std::vector<Prim<R>> prims;   // SDF primitives (fixed rigid bodies, and free ones' current poses)
+    std::vector<int> prim_body;   // per primitive: index into bodies, -1 when fixed
+    std::vector<RigidBody> bodies;
+    bool is_dynamic(int s) const { return s < (int)prim_body.size() && prim_body[s] >= 0; }
+    // the detection pose of free bodies: their current state in R
+    void sync_prims() {
+        for (size_t s = 0; s < prim_body.size(); s++)
+            if (prim_body[s] >= 0) {
+                const RigidBody& b = bodies[prim_body[s]];
+                for (int k = 0; k < 3; k++) prims[s].p[k] = (R)b.p[k];
+                for (int k = 0; k < 4; k++) prims[s].q[k] = (R)b.q[k];
+            }
+    }
+    // Rigid contacts, after the static ones (projector type order,
+    // include/common/XPBDTypedefs.hpp:55-56), in detection order. Gauss-Seidel
+    // applies each update at once; Jacobi reads one state, sums the vertex
+    // updates into acc and the body increments, applied after the pass
+    // (XPBDGaussSeidelSolver.hpp:61-95, XPBDJacobiSolver.hpp:79-114).
+    void project_rigid_contacts(std::vector<R>* acc) {
+        std::vector<double> dps(3 * bodies.size(), 0.0), dqs(4 * bodies.size(), 0.0);
+        for (auto& ct : contacts) {
+            if (!ct.dynamic) continue;
+            RigidBody& rb = bodies[prim_body[ct.sphere]];
+            R wv[3] = {inv_mass[ct.v[0]], inv_mass[ct.v[1]], inv_mass[ct.v[2]]};
+            double dx[9], dl;
+            if (!project_rigid_contact(&x[3 * ct.v[0]], &x[3 * ct.v[1]], &x[3 * ct.v[2]], wv, ct, rb, dx, &dl))
+                continue;
+            double pt[3] = {(double)ct.p[0], (double)ct.p[1], (double)ct.p[2]};
+            double nn[3] = {(double)ct.n[0], (double)ct.n[1], (double)ct.n[2]};
+            double dp[3], dq[4];
+            rb.contact_delta(dl, pt, nn, dp, dq);
+            if (acc) {
+                for (int i = 0; i < 3; i++)
+                    for (int k = 0; k < 3; k++) (*acc)[3 * ct.v[i] + k] += (R)dx[3 * i + k];
+                const size_t bi = (size_t)prim_body[ct.sphere];
+                for (int k = 0; k < 3; k++) dps[3 * bi + k] += dp[k];
+                for (int k = 0; k < 4; k++) dqs[4 * bi + k] += dq[k];
+            } else {
+                for (int i = 0; i < 3; i++)
+                    for (int k = 0; k < 3; k++) x[3 * ct.v[i] + k] = (R)((double)x[3 * ct.v[i] + k] + dx[3 * i + k]);
+                for (int k = 0; k < 3; k++) rb.p[k] = rb.p[k] + dp[k];
+                for (int k = 0; k < 4; k++) rb.q[k] = rb.q[k] + dq[k];
+            }
+        }
+        if (acc)
+            for (size_t bi = 0; bi < bodies.size(); bi++) {
+                for (int k = 0; k < 3; k++) bodies[bi].p[k] += dps[3 * bi + k];
+                for (int k = 0; k < 4; k++) bodies[bi].q[k] += dqs[4 * bi + k];
+            }
+    }
     // kinematic vertex group
     std::vector<int> kin_idx;
     std::vector<R> kin_rest;
@@ -770,7 +943,8 @@ struct Object {
                 for (long long t = 0; t < T; t++) { project_tet_single(t, 1, dx); add_tet(t, dx); }
             }
             for (auto& ct : contacts)
-                if (project_contact_i(ct, dx)) add_contact(ct, dx);
+                if (!ct.dynamic && project_contact_i(ct, dx)) add_contact(ct, dx);
+            project_rigid_contacts(nullptr);
             for (auto& at : attachments) {
                 project_attachment(at, dx);
                 for (int k = 0; k < 3; k++) x[3 * at.v + k] += dx[k];
@@ -786,8 +960,9 @@ struct Object {
             // ascending sphere within a face
             for (int k = 0; k < n_face_colours; k++)
                 for (auto& ct : contacts)
-                    if (face_colour[ct.face] == k)
+                    if (face_colour[ct.face] == k && !ct.dynamic)
                         if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            project_rigid_contacts(nullptr);
             // attachments in insertion order (the GPU's colours keep it per vertex)
             for (auto& at : attachments) {
                 project_attachment(at, dx);
@@ -808,8 +983,9 @@ struct Object {
                 }
             }
             for (auto& ct : contacts)
-                if (project_contact_i(ct, dx))
+                if (!ct.dynamic && project_contact_i(ct, dx))
                     for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
+            project_rigid_contacts(&acc);
             for (auto& at : attachments) {
                 project_attachment(at, dx);
                 for (int k = 0; k < 3; k++) acc[3 * at.v + k] += dx[k];
@@ -828,7 +1004,7 @@ struct Object {
             for (int i = 0; i < 4; i++) attached[tets[4 * t + i]].push_back((int)t);
         std::vector<int> out;
         for (const auto& ct : contacts)
-            if (ct.lambda != 0)
+            if (ct.lambda != 0 && !ct.dynamic)
                 for (int i = 0; i < 3; i++)
                     for (int t : attached[ct.v[i]]) out.push_back(t);
         return out;
@@ -842,7 +1018,10 @@ struct Object {
     //   JACOBI      : each listed tet once per pass, every projection from the
     //                 same x, updates summed with the contacts'.
     void local_iterations() {
-        if (num_local_iter <= 0 || contacts.empty()) return;
+        if (num_local_iter <= 0) return;
+        bool any_static = false;
+        for (const auto& ct : contacts) any_static |= !ct.dynamic;
+        if (!any_static) return;
         const std::vector<int> list = local_tet_list();
         std::vector<char> mark(T, 0);
         for (int t : list) mark[t] = 1;
@@ -856,7 +1035,7 @@ struct Object {
                     for (int t : list) { project_tet_single(t, 1, dx); add_tet(t, dx); }
                 }
                 for (auto& ct : contacts)
-                    if (project_contact_i(ct, dx)) add_contact(ct, dx);
+                    if (!ct.dynamic && project_contact_i(ct, dx)) add_contact(ct, dx);
             } else if (solver == COLOURED_GS) {
                 for (int pass = 0; pass < (ckind == COMBINED ? 1 : 2); pass++)
                     for (int t : local_order) {
@@ -867,7 +1046,7 @@ struct Object {
                     }
                 for (int k = 0; k < n_face_colours; k++)
                     for (auto& ct : contacts)
-                        if (face_colour[ct.face] == k)
+                        if (face_colour[ct.face] == k && !ct.dynamic)
                             if (project_contact_i(ct, dx)) add_contact(ct, dx);
             } else {
                 std::vector<R> acc(3 * V, 0);
@@ -881,7 +1060,7 @@ struct Object {
                     }
                 }
                 for (auto& ct : contacts)
-                    if (project_contact_i(ct, dx))
+                    if (!ct.dynamic && project_contact_i(ct, dx))
                         for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
                 for (long long i = 0; i < 3 * V; i++) x[i] += acc[i];
             }
@@ -968,6 +1147,7 @@ struct Object {
     // (XPBDMeshObject.cpp:233-251; CollisionScene.cpp:32-51,171-214).
     void detect() {
         contacts.clear();
+        sync_prims();
         long long S = (long long)prims.size();
         for (long long s = 0; s < S; s++)
             for (long long f = 0; f < F; f++) {
@@ -977,6 +1157,7 @@ struct Object {
                     ct.sphere = (int)s;
                     ct.face = (int)f;
                     ct.v[0] = fv[0]; ct.v[1] = fv[1]; ct.v[2] = fv[2];
+                    ct.dynamic = is_dynamic((int)s);
                     contacts.push_back(ct);
                 }
             }
@@ -988,12 +1169,18 @@ struct Object {
     }
 
     // Simulation::_timeStep for this object (Simulation.cpp:197-276):
-    // collision detection on the strict cadence test, update, velocity, time.
+    // collision detection on the strict cadence test, update, the free rigid
+    // bodies' update, velocities, time.
     void time_step(bool record_residual = false) {
         bool cd = (time - last_cd > cd_interval);
         if (cd) detect();
         update(record_residual);
+        // the rigid objects update after the XPBD objects, then every object's
+        // velocity update runs (Simulation.cpp:245-255; object type order,
+        // include/common/SimulationTypeDefs.hpp)
+        for (auto& b : bodies) b.update(dt_host, (double)g);
         velocity_update();
+        for (auto& b : bodies) b.velocity_update(dt_host);
         if (time - last_cd > cd_interval) last_cd = time;
         time += dt_host;
     }

@@ -137,6 +137,48 @@ void xo_set_prims(void* p, int n, const int* kind, const double* pos, const doub
             for (int k = 0; k < 4; k++) o.prims[i].q[k] = (R)quat[4 * i + k];
             for (int k = 0; k < 3; k++) o.prims[i].d[k] = (R)dims[3 * i + k];
         }
+        o.prim_body.assign(n, -1);
+        o.bodies.clear();
+        return 0;
+    });
+}
+
+// primitive `prim` becomes a free rigid body with the given pose (double),
+// mass, diagonal inertia, velocity and angular velocity
+void xo_set_rigid_body(void* p, int prim, const double* pos3, const double* quat4, double mass,
+                       const double* inertia3, const double* vel3, const double* omega3) {
+    with((Handle*)p, [&](auto& o) {
+        xo::RigidBody b;
+        b.kind = o.prims[prim].kind;
+        for (int k = 0; k < 3; k++) {
+            b.d[k] = (double)o.prims[prim].d[k];
+            b.p[k] = b.p_prev[k] = pos3[k];
+            b.v[k] = vel3[k];
+            b.w[k] = omega3[k];
+            b.I[k] = inertia3[k];
+            b.I_inv[k] = 1.0 / inertia3[k];
+        }
+        for (int k = 0; k < 4; k++) b.q[k] = b.q_prev[k] = quat4[k];
+        b.m = mass;
+        if (o.prim_body[prim] >= 0) {
+            o.bodies[o.prim_body[prim]] = b;
+        } else {
+            o.prim_body[prim] = (int)o.bodies.size();
+            o.bodies.push_back(b);
+        }
+        o.sync_prims();
+        return 0;
+    });
+}
+
+// out = p[3], q[4], v[3], w[3] of primitive `prim`'s rigid body
+void xo_get_rigid_body(void* p, int prim, double* out) {
+    with((Handle*)p, [&](auto& o) {
+        const xo::RigidBody& b = o.bodies[o.prim_body[prim]];
+        for (int k = 0; k < 3; k++) out[k] = b.p[k];
+        for (int k = 0; k < 4; k++) out[3 + k] = b.q[k];
+        for (int k = 0; k < 3; k++) out[7 + k] = b.v[k];
+        for (int k = 0; k < 3; k++) out[10 + k] = b.w[k];
         return 0;
     });
 }

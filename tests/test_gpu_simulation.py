@@ -112,9 +112,16 @@ def test_element_classes_pick_materials(lib, tmp_path):
 
 def test_unprovided_objects_fail_loudly(lib, tmp_path):
     cfg, _, _, _ = _scene(tmp_path)
-    text = open(cfg).read().replace("fixed: true", "fixed: false")
+    text = open(cfg).read()
+    # self-collisions
     with pytest.raises(NotImplementedError):
-        S.Simulation(text, base_dir=str(tmp_path)).setup()
+        S.Simulation(text.replace("num-solver-iters: 6", "num-solver-iters: 6\n    self-collisions: true"),
+                     base_dir=str(tmp_path)).setup()
+    # a free body colliding with two XPBD objects
+    second = text[text.index('  - name: "Cube"'):text.index('  - name: "Ball"')].replace('"Cube"', '"Cube2"')
+    two = text.replace("fixed: true", "fixed: false").replace('  - name: "Ball"', second + '  - name: "Ball"')
+    with pytest.raises(NotImplementedError):
+        S.Simulation(two, base_dir=str(tmp_path)).setup()
 
 
 def test_first_order_object_from_config(lib, tmp_path):
@@ -167,7 +174,7 @@ def test_fixed_box_and_cylinder_from_config(lib, tmp_path):
     s = G.XPBDSolver(Xp, tets, faces, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0), dt=1e-3,
                      collision_rate=100, num_iters=6)
     s.set_sdfs([G.SDF_BOX, G.SDF_CYLINDER], [[0.1, 0, 0.79], [0.1, 0, 0.2]],
-               [S.eul_xyz_to_quat([0, 0, 20]), S.eul_xyz_to_quat([90, 0, 0])], [[0.6, 0.6, 0.1], [0.1, 0.4, 0]])
+               [S.rigid_quat([0, 0, 20]), S.rigid_quat([90, 0, 0])], [[0.6, 0.6, 0.1], [0.1, 0.4, 0]])
     s.step(40)
     np.testing.assert_array_equal(got, s.positions())
     s.close()

@@ -304,6 +304,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
+                if (c->nbodies) {
+                    Scope sc(c, K_CONTACT);
+                    launch_rigid_contacts(c->L(), ca, c->rc_list.p, c->rc_count.p, c->sphere_tab.p, c->face_inst.p,
+                                          c->rb.p, c->nbodies, c->x.p, c->dx.p, true, first_contact, c->flags.p);
+                }
                 if (!c->att_v.empty()) {
                     Scope sc(c, K_CONTACT);
                     launch_attach_jacobi(c->L(), c->d_att_v.p, c->d_att_target.p, c->d_att_lam.p,
@@ -321,6 +326,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
+                }
+                if (c->nbodies) {
+                    Scope sc(c, K_CONTACT);
+                    launch_rigid_contacts(c->L(), ca, c->rc_list.p, c->rc_count.p, c->sphere_tab.p, c->face_inst.p,
+                                          c->rb.p, c->nbodies, c->x.p, c->dx.p, true, first_contact, c->flags.p);
                 }
                 if (!c->att_v.empty()) {
                     Scope sc(c, K_CONTACT);
@@ -362,6 +372,12 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
                 }
             }
+            // rigid-body contacts after the static ones (projector type order)
+            if (c->nbodies) {
+                Scope sc(c, K_CONTACT);
+                launch_rigid_contacts(c->L(), ca, c->rc_list.p, c->rc_count.p, c->sphere_tab.p, c->face_inst.p,
+                                      c->rb.p, c->nbodies, c->x.p, nullptr, false, first, c->flags.p);
+            }
             // attachments last: the projector type order (XPBDTypedefs.hpp:55-56)
             for (int ac = 0; ac + 1 < (int)c->att_col_off.size(); ac++) {
                 Scope sc(c, K_CONTACT);
@@ -386,6 +402,16 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     if (!jacobi || !fuse_final || iters == 0) {
         Scope sc(c, K_FINALIZE);
         launch_finalize(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
+    }
+    if (c->nbodies) {
+        // the rigid objects update after the XPBD objects (Simulation.cpp:245-255,
+        // object type order of include/common/SimulationTypeDefs.hpp)
+        Scope sc(c, K_FINALIZE);
+        launch_rigid_update(c->L(), c->rb.p, c->nbodies, p.dt, p.g_accel);
+    }
+    if (c->nbodies && write_vel) {
+        Scope sc(c, K_VELOCITY);
+        launch_rigid_velocity(c->L(), c->rb.p, c->nbodies, p.dt);
     }
     return XPBD_OK;
 }
@@ -497,6 +523,36 @@ int run_update(xpbd_ctx* c, bool write_vel) {
     return after_launches(c, "update");
 }
 
+// ---- free rigid bodies ----
+// device records -> body_h (the device state is the current one once steps ran)
+int pull_bodies(xpbd_ctx* c) {
+    c->body_h.resize((size_t)c->nbodies * kRigidRec);
+    if (!c->nbodies) return XPBD_OK;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    XPBD_CU(c, cudaMemcpy(c->body_h.data(), c->rb.p, sizeof(double) * c->body_h.size(), cudaMemcpyDeviceToHost));
+    return XPBD_OK;
+}
+
+// body_h -> device records, and every table entry's body mark (d.w = index + 1)
+int push_bodies(xpbd_ctx* c) {
+    c->nbodies = (int)(c->body_h.size() / kRigidRec);
+    for (size_t e = 0; e < c->sphere_tab_h.size(); e += 3) c->sphere_tab_h[e + 2].w = 0.f;
+    for (int i = 0; i < c->nbodies; i++) {
+        const size_t e = (size_t)c->body_h[(size_t)i * kRigidRec + RB_ENTRY];
+        c->sphere_tab_h[3 * e + 2].w = (float)(i + 1);
+    }
+    if (c->nbodies)
+        XPBD_CU(c, cudaMemcpyAsync(c->rb.p, c->body_h.data(), sizeof(double) * c->body_h.size(),
+                                   cudaMemcpyHostToDevice, c->stream));
+    // the rigid contacts found so far may name bodies that moved or ended:
+    // none is projected before the next detection
+    if (c->rc_count.p) XPBD_CU(c, cudaMemsetAsync(c->rc_count.p, 0, sizeof(int), c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    c->sphere_dirty = true;
+    c->graph_dirty = true;  // the body count is baked into captured launches
+    return XPBD_OK;
+}
+
 int detect(xpbd_ctx* c) {
     if (c->F == 0) return XPBD_OK;
     if (c->sphere_dirty) {
@@ -506,9 +562,18 @@ int detect(xpbd_ctx* c) {
                                    cudaMemcpyHostToDevice, c->stream));
         c->sphere_dirty = false;
     }
+    if (c->nbodies) {
+        // free bodies are detected at their current poses
+        Scope sc(c, K_DETECT);
+        launch_rigid_sync_table(c->L(), c->rb.p, c->nbodies, c->sphere_tab.p);
+    }
     {
         Scope sc(c, K_DETECT);
         launch_detect(c->L(), c->contacts(), c->x.p, c->sphere_tab.p, c->face_inst.p);
+    }
+    if (c->nbodies) {
+        Scope sc(c, K_DETECT);
+        launch_rigid_compact(c->L(), c->contacts(), c->rc_list.p, c->rc_count.p);
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
     return after_launches(c, "detect");
@@ -542,6 +607,7 @@ void release(xpbd_ctx* c) {
     c->c_bary.release(); c->c_p.release(); c->c_n.release(); c->c_lam.release();
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
     c->sphere_tab.release(); c->face_inst.release();
+    c->rb.release(); c->rc_list.release(); c->rc_count.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
@@ -674,6 +740,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         for (int64_t f = 0; f < m.num_faces; f++) finst[fo + f] = k;
     }
     c->sphere_tab_h.assign(3 * (size_t)n_inst * c->S, make_float4(0.f, 0.f, 0.f, -1.f));
+    c->sdf_pose_h.assign(10 * (size_t)n_inst * c->S, 0.0);
 
     // rest shape, compliance, lumped mass (ElementConstraint.hpp:23-51;
     // HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
@@ -893,6 +960,10 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, cudaMemset(c->c_lam.p, 0, sizeof(float) * ns));
         XPBD_CU(c, cudaMemcpy(c->faces.p, hf.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
         XPBD_CU(c, cudaMemcpy(c->face_list.p, flist.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+        XPBD_CU(c, c->rb.alloc((size_t)kRigidRec * n_inst * c->S));
+        XPBD_CU(c, c->rc_list.alloc(ns));
+        XPBD_CU(c, c->rc_count.alloc(1));
+        XPBD_CU(c, cudaMemset(c->rc_count.p, 0, sizeof(int)));
     }
     if (!lslots.empty()) {
         XPBD_CU(c, c->local_slots.alloc(T));
@@ -1200,6 +1271,21 @@ int xpbd_set_instance_sdfs(xpbd_ctx* c, int32_t inst, int32_t n, const int32_t* 
         ok = ok && qn > 0 && std::isfinite(qn);
         if (!ok) return fail(c, XPBD_ERR_INVALID, "SDF %d has a bad kind, position, orientation or size", i);
     }
+    // free bodies of this instance end here (the caller marks them again)
+    if (c->nbodies) {
+        int st = pull_bodies(c);
+        if (st) return st;
+        std::vector<double> keep;
+        for (int i = 0; i < c->nbodies; i++) {
+            const double* r = &c->body_h[(size_t)i * kRigidRec];
+            if ((int)r[RB_ENTRY] / c->S != inst) keep.insert(keep.end(), r, r + kRigidRec);
+        }
+        c->body_h.swap(keep);
+    }
+    double* pose = &c->sdf_pose_h[10 * (size_t)inst * c->S];
+    for (int k = 0; k < c->S; k++)
+        for (int j = 0; j < 10; j++)
+            pose[10 * k + j] = k >= n ? 0.0 : (j < 3 ? pos[3 * k + j] : (j < 7 ? quat[4 * k + j - 3] : dims[3 * k + j - 7]));
     float4* row = &c->sphere_tab_h[3 * (size_t)inst * c->S];
     for (int k = 0; k < c->S; k++) {
         if (k < n) {
@@ -1216,12 +1302,69 @@ int xpbd_set_instance_sdfs(xpbd_ctx* c, int32_t inst, int32_t n, const int32_t* 
     c->n_spheres_total = 0;
     for (size_t e = 0; e < c->sphere_tab_h.size(); e += 3) c->n_spheres_total += c->sphere_tab_h[e].w >= 0.f ? 1 : 0;
     c->sphere_dirty = true;
-    return XPBD_OK;
+    return push_bodies(c);
 }
 
 int xpbd_set_sdfs(xpbd_ctx* c, int32_t n, const int32_t* kind, const double* pos, const double* quat,
                   const double* dims) {
     return xpbd_set_instance_sdfs(c, 0, n, kind, pos, quat, dims);
+}
+
+int xpbd_set_rigid_body(xpbd_ctx* c, int32_t inst, int32_t slot, double mass, const double* inertia3,
+                        const double* vel3, const double* omega3) {
+    if (!c || !inertia3 || !vel3 || !omega3) return XPBD_ERR_INVALID;
+    if (!c->F) return fail(c, XPBD_ERR_STATE, "free rigid bodies need the surface faces (collisions)");
+    if (inst < 0 || inst >= c->n_inst || slot < 0 || slot >= c->S)
+        return fail(c, XPBD_ERR_INVALID, "instance %d / SDF slot %d out of range", inst, slot);
+    const size_t e = (size_t)inst * c->S + slot;
+    if (c->sphere_tab_h[3 * e].w < 0.f) return fail(c, XPBD_ERR_STATE, "SDF slot %d of instance %d is empty", slot, inst);
+    bool ok = mass > 0 && std::isfinite(mass);
+    for (int k = 0; k < 3; k++)
+        ok = ok && inertia3[k] > 0 && std::isfinite(inertia3[k]) && std::isfinite(vel3[k]) && std::isfinite(omega3[k]);
+    if (!ok) return fail(c, XPBD_ERR_INVALID, "rigid body: bad mass, inertia or velocity");
+    int st = pull_bodies(c);
+    if (st) return st;
+    std::vector<double> r(kRigidRec, 0.0);
+    const double* pose = &c->sdf_pose_h[10 * e];
+    for (int k = 0; k < 3; k++) {
+        r[RB_P + k] = r[RB_PP + k] = pose[k];
+        r[RB_V + k] = vel3[k];
+        r[RB_W + k] = omega3[k];
+        r[RB_I + k] = inertia3[k];
+        r[RB_II + k] = 1.0 / inertia3[k];
+        r[RB_D + k] = pose[7 + k];
+    }
+    for (int k = 0; k < 4; k++) r[RB_Q + k] = r[RB_QP + k] = pose[3 + k];
+    r[RB_M] = mass;
+    r[RB_KIND] = (double)c->sphere_tab_h[3 * e].w;
+    r[RB_ENTRY] = (double)e;
+    bool replaced = false;
+    for (int i = 0; i < c->nbodies && !replaced; i++)
+        if ((size_t)c->body_h[(size_t)i * kRigidRec + RB_ENTRY] == e) {
+            std::copy(r.begin(), r.end(), c->body_h.begin() + (size_t)i * kRigidRec);
+            replaced = true;
+        }
+    if (!replaced) c->body_h.insert(c->body_h.end(), r.begin(), r.end());
+    return push_bodies(c);
+}
+
+int xpbd_get_rigid_body(xpbd_ctx* c, int32_t inst, int32_t slot, double* state13) {
+    if (!c || !state13) return XPBD_ERR_INVALID;
+    if (inst < 0 || inst >= c->n_inst || slot < 0 || slot >= c->S)
+        return fail(c, XPBD_ERR_INVALID, "instance %d / SDF slot %d out of range", inst, slot);
+    int st = pull_bodies(c);
+    if (st) return st;
+    const size_t e = (size_t)inst * c->S + slot;
+    for (int i = 0; i < c->nbodies; i++) {
+        const double* r = &c->body_h[(size_t)i * kRigidRec];
+        if ((size_t)r[RB_ENTRY] != e) continue;
+        std::copy(r + RB_P, r + RB_P + 3, state13);
+        std::copy(r + RB_Q, r + RB_Q + 4, state13 + 3);
+        std::copy(r + RB_V, r + RB_V + 3, state13 + 7);
+        std::copy(r + RB_W, r + RB_W + 3, state13 + 10);
+        return XPBD_OK;
+    }
+    return fail(c, XPBD_ERR_STATE, "SDF slot %d of instance %d is not a free rigid body", slot, inst);
 }
 
 int xpbd_sdf_eval(int32_t kind, const double* pos, const double* quat, const double* dims, int64_t n,
@@ -1279,6 +1422,7 @@ int xpbd_clear_collisions(xpbd_ctx* c) {
     if (c->F) {
         XPBD_CU(c, cudaMemsetAsync(c->c_bary.p, 0, sizeof(float4) * (size_t)c->S * c->F, c->stream));
         XPBD_CU(c, cudaMemsetAsync(c->c_lam.p, 0, sizeof(float) * (size_t)c->S * c->F, c->stream));
+        XPBD_CU(c, cudaMemsetAsync(c->rc_count.p, 0, sizeof(int), c->stream));
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), 0);
     return XPBD_OK;
@@ -1402,6 +1546,10 @@ int xpbd_velocity_update(xpbd_ctx* c) {
     {
         Scope sc(c, K_VELOCITY);
         launch_velocity(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, (float)c->prm.dt);
+    }
+    if (c->nbodies) {
+        Scope sc(c, K_VELOCITY);
+        launch_rigid_velocity(c->L(), c->rb.p, c->nbodies, c->prm.dt);
     }
     return after_launches(c, "velocity update");
 }

@@ -106,6 +106,12 @@ struct xpbd_ctx {
     std::vector<int64_t> voff, toff, foff;
     std::vector<float4> sphere_tab_h;  // [n_inst * S] SDF primitives, 3 float4 each (kind < 0 = empty)
     DevBuf<float4> sphere_tab;
+    std::vector<double> sdf_pose_h;    // [n_inst * S] * 10: position, quaternion, dims as given (double)
+    // free rigid bodies (two-way coupling): FP64 records (xg::kRigidRec each)
+    int nbodies = 0;
+    std::vector<double> body_h;        // host copy, current after pull_bodies
+    DevBuf<double> rb;                 // capacity n_inst * S records
+    DevBuf<int> rc_list, rc_count;     // rigid contacts in slot order, their count
     DevBuf<int> face_inst;
     bool sphere_dirty = true;
     int n_spheres_total = 0;

@@ -74,6 +74,26 @@ struct PatchArrays {
 
 constexpr int kMaxSpheres = 16;  // sphere slots per instance
 
+// Free rigid bodies (RigidObject with fixed: false), one FP64 record each.
+// Their SDF table entries carry body index + 1 in d.w (0: fixed), and their
+// contacts are marked active = 2 by the detection.
+constexpr int kRigidRec = 40;
+enum RigidField {
+    RB_P = 0,      // position [3]
+    RB_Q = 3,      // orientation (x, y, z, w) [4]
+    RB_V = 7,      // velocity [3]
+    RB_W = 10,     // angular velocity [3]
+    RB_PP = 13,    // position at the last velocity update [3]
+    RB_QP = 16,    // orientation at the last velocity update [4]
+    RB_M = 20,     // mass
+    RB_I = 21,     // diagonal inertia [3]
+    RB_II = 24,    // its inverse [3]
+    RB_KIND = 27,  // SDF kind (0 sphere, 1 box, 2 cylinder)
+    RB_D = 28,     // SDF dimensions [3]
+    RB_ACC = 31,   // Jacobi sums of position [3] and orientation [4] increments
+    RB_ENTRY = 38  // SDF table entry (instance * S + slot)
+};
+
 // Dataflow Gauss-Seidel (sweep variant 2): every iteration and colour in one
 // cooperative launch. A task is up to 32 consecutive patches of one colour,
 // run by one warp; a task waits until every task sharing a vertex with it has
@@ -184,6 +204,16 @@ void launch_velocity(const Launch& s, const float4* x, const float4* prev, float
 void launch_residual(const Launch& s, int block, const TetArrays& t, int T, const float4* x, bool separate,
                      const int* perm, float* rvec, ResidualSink res, double* energy_partial, float dt2,
                      bool zero_lam = false);
+// free rigid bodies: table entries from the bodies' poses; the ordered list of
+// rigid contacts; their projection (Gauss-Seidel in list order, or Jacobi from
+// one state with summed increments); RigidObject::update and velocityUpdate
+void launch_rigid_sync_table(const Launch& s, const double* rb, int nb, float4* table);
+void launch_rigid_compact(const Launch& s, const ContactArrays& c, int* list, int* count);
+void launch_rigid_contacts(const Launch& s, const ContactArrays& c, const int* list, const int* count,
+                           const float4* table, const int* face_inst, double* rb, int nb, float4* x, float4* dx,
+                           bool jacobi, bool first, Flags* flags);
+void launch_rigid_update(const Launch& s, double* rb, int nb, double dt, double g);
+void launch_rigid_velocity(const Launch& s, double* rb, int nb, double dt);
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
                       int end, float4* x, bool first);
 void launch_attach_jacobi(const Launch& s, const int* vert, const float4* target, float* lam, int n, const float4* x,

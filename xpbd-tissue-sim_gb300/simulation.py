@@ -22,15 +22,21 @@ Simulation mirrors src/simulation/Simulation.cpp:
                runs collision detection on the shared cadence, the update and
                the velocity update
 
-Fixed rigid spheres, boxes and cylinders with `collisions: true` collide with
-every XPBD object that has `collisions: true`: each is a static SDF in the
-solver (orientation from `rotation`, RigidObject.cpp:14) and can be moved
-between steps (move_rigid). The reference only builds graphics for
+Rigid spheres, boxes and cylinders with `collisions: true` collide with
+every XPBD object that has `collisions: true`, as SDFs in the solver
+(orientation from `rotation`, RigidObject.cpp:12-14, whose degrees-to-radians
+factor is 3.1415/180). Fixed ones are static and can be moved between steps
+(move_rigid). Free ones (`fixed: false`) are the solver's rigid bodies: mass
+and inertia from `density` and the dimensions (RigidPrimitives.cpp), the
+initial `velocity` and `angular-velocity`, two-way coupling with the XPBD
+object in the solve, gravity and the angular Euler step after it
+(RigidObject.cpp:41-77). A free body without collisions only falls; it is
+integrated here on the host. The reference only builds graphics for
 `visualization`; there is no graphics here and the key is read and ignored.
 
-Not provided (each raises NotImplementedError naming the key): non-fixed
-rigid bodies (two-way coupling), rigid meshes, self-collisions and the
-Virtuoso robot objects.
+Not provided (each raises NotImplementedError naming the key): a free rigid
+body colliding with more than one XPBD object, rigid meshes, self-collisions
+and the Virtuoso robot objects.
 """
 from __future__ import annotations
 
@@ -146,6 +152,7 @@ class RigidSphereConfig:
     density: float = 1000.0
     fixed: bool = False
     rotation: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    angular_velocity: np.ndarray = field(default_factory=lambda: np.zeros(3))
 
     @classmethod
     def from_node(cls, n):
@@ -153,7 +160,14 @@ class RigidSphereConfig:
                    graphics_only=bool(_get(n, "graphics-only", False)),
                    position=_vec3(n, "position", [0, 0, 0]), velocity=_vec3(n, "velocity", [0, 0, 0]),
                    radius=float(_get(n, "radius", 1.0)), density=float(_get(n, "density", 1000.0)),
-                   fixed=bool(_get(n, "fixed", False)), rotation=_vec3(n, "rotation", [0, 0, 0]))
+                   fixed=bool(_get(n, "fixed", False)), rotation=_vec3(n, "rotation", [0, 0, 0]),
+                   angular_velocity=_vec3(n, "angular-velocity", [0, 0, 0]))
+
+    def mass_inertia(self):
+        """RigidSphere's mass and diagonal inertia (RigidPrimitives.cpp:9-20, pi as 3.1415)."""
+        m = 4.0 / 3.0 * 3.1415 * self.radius * self.radius * self.radius * self.density
+        i = 2.0 / 5.0 * m * self.radius * self.radius
+        return m, np.array([i, i, i])
 
 
 @dataclass
@@ -165,6 +179,13 @@ class RigidBoxConfig(RigidSphereConfig):
         b = RigidSphereConfig.from_node(n)
         return cls(**{**b.__dict__, "size": _vec3(n, "size", [1, 1, 1])})
 
+    def mass_inertia(self):
+        """RigidBox (RigidPrimitives.cpp:39-48)."""
+        sx, sy, sz = self.size
+        m = sx * sy * sz * self.density
+        return m, np.array([1.0 / 12.0 * m * (sy * sy + sz * sz), 1.0 / 12.0 * m * (sx * sx + sz * sz),
+                            1.0 / 12.0 * m * (sx * sx + sy * sy)])
+
 
 @dataclass
 class RigidCylinderConfig(RigidSphereConfig):
@@ -175,15 +196,71 @@ class RigidCylinderConfig(RigidSphereConfig):
         b = RigidSphereConfig.from_node(n)
         return cls(**{**b.__dict__, "height": float(_get(n, "height", 1.0))})
 
+    def mass_inertia(self):
+        """RigidCylinder (RigidPrimitives.cpp:86-94)."""
+        r, h = self.radius, self.height
+        m = 3.1415 * r * r * h * self.density
+        return m, np.array([1.0 / 12.0 * m * (3 * r * r + h * h), 1.0 / 12.0 * m * (3 * r * r + h * h),
+                            1.0 / 2.0 * m * r * r])
 
-def eul_xyz_to_quat(deg):
+
+def eul_xyz_to_quat(deg, rad_per_deg=np.pi / 180.0):
     """Quaternion (x, y, z, w) of the rotation about x, then y, then z by the
     given angles in degrees (the reference's eulXYZ2Quat convention,
     src/utils/GeometryUtils.cpp:104-112)."""
-    hx, hy, hz = (0.5 * np.radians(a) for a in deg)
+    hx, hy, hz = (0.5 * a * rad_per_deg for a in deg)
     cx, sx, cy, sy, cz, sz = np.cos(hx), np.sin(hx), np.cos(hy), np.sin(hy), np.cos(hz), np.sin(hz)
     return np.array([sx * cy * cz - cx * sy * sz, cx * sy * cz + sx * cy * sz, cx * cy * sz - sx * sy * cz,
                      cx * cy * cz + sx * sy * sz])
+
+
+def rigid_quat(deg):
+    """A rigid object's initial orientation: its `rotation` in degrees turned
+    to radians with the reference's factor 3.1415/180 (RigidObject.cpp:12-14)."""
+    return eul_xyz_to_quat(deg, 3.1415 / 180.0)
+
+
+class FreeBody:
+    """RigidObject::update / velocityUpdate (RigidObject.cpp:41-77) for a free
+    body that collides with nothing, on the host; the solver runs the same
+    steps on the device for free bodies that collide."""
+
+    def __init__(self, p, q, v, w, m, inertia):
+        self.p, self.q = np.array(p, float), np.array(q, float)
+        self.v, self.w = np.array(v, float), np.array(w, float)
+        self.p_prev, self.q_prev = self.p.copy(), self.q.copy()
+        self.m, self.I = float(m), np.asarray(inertia, float)
+
+    @staticmethod
+    def _mult(a, b):
+        return np.array([a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1],
+                         a[3] * b[1] + a[1] * b[3] + a[2] * b[0] - a[0] * b[2],
+                         a[3] * b[2] + a[2] * b[3] + a[0] * b[1] - a[1] * b[0],
+                         a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2]])
+
+    @staticmethod
+    def _rot(v, q):
+        u = q[:3]
+        return 2 * u.dot(v) * u + (2 * q[3] * q[3] - 1) * v + 2 * q[3] * np.cross(u, v)
+
+    @staticmethod
+    def _inv(q):
+        return np.array([-q[0], -q[1], -q[2], q[3]]) / q.dot(q)
+
+    def update(self, dt, g):
+        self.v = self.v + dt * np.array([0.0, 0.0, -self.m * g]) / self.m
+        self.p = self.p + dt * self.v
+        wb = self._rot(self.w, self._inv(self.q))
+        wb = wb + dt * (1.0 / self.I) * (0.0 - np.cross(wb, self.I * wb))
+        self.w = self._rot(wb, self.q)
+        self.q = self.q + 0.5 * dt * self._mult(np.append(self.w, 0.0), self.q)
+        self.q = self.q / np.linalg.norm(self.q)
+
+    def velocity_update(self, dt):
+        self.v = (self.p - self.p_prev) / dt
+        dq = self._mult(self.q, self._inv(self.q_prev))
+        self.w = 2 / dt * dq[:3] * (-1.0 if dq[3] < 0 else 1.0)
+        self.p_prev, self.q_prev = self.p.copy(), self.q.copy()
 
 
 SIM_MODES = {"Visualization": "Visualization", "AFAP": "AFAP", "Frame-by-frame": "Frame-by-frame"}
@@ -300,13 +377,21 @@ class XPBDObject:
 
 @dataclass
 class Rigid:
-    """A fixed rigid primitive: kind (G.SDF_*), pose, dimensions."""
+    """A rigid primitive: kind (G.SDF_*), pose, dimensions; free bodies also
+    carry mass, inertia and their initial velocities (the solver, or a
+    FreeBody when it collides with nothing, holds the live state)."""
     name: str
     kind: int
     position: np.ndarray
     quat: np.ndarray
     dims: np.ndarray
     collisions: bool
+    fixed: bool = True
+    mass: float = 0.0
+    inertia: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    velocity: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    angular_velocity: np.ndarray = field(default_factory=lambda: np.zeros(3))
+    host_body: FreeBody | None = None
 
 
 class Simulation:
@@ -334,9 +419,6 @@ class Simulation:
             if oc.graphics_only:
                 continue
             if isinstance(oc, RigidSphereConfig):
-                if not oc.fixed:
-                    raise NotImplementedError(f"rigid object {oc.name!r}: non-fixed rigid bodies (two-way "
-                                              "coupling) are not provided; set `fixed: true`")
                 if isinstance(oc, RigidBoxConfig):
                     kind, dims = G.SDF_BOX, np.asarray(oc.size, np.float64)
                 elif isinstance(oc, RigidCylinderConfig):
@@ -344,30 +426,68 @@ class Simulation:
                 else:
                     kind, dims = G.SDF_SPHERE, np.array([oc.radius, 0.0, 0.0])
                 rot = getattr(oc, "rotation", np.zeros(3))
-                self.rigids[oc.name] = Rigid(oc.name, kind, oc.position.copy(), eul_xyz_to_quat(rot), dims,
-                                             oc.collisions)
+                r = Rigid(oc.name, kind, oc.position.copy(), rigid_quat(rot), dims, oc.collisions, oc.fixed)
+                if not oc.fixed:
+                    r.mass, r.inertia = oc.mass_inertia()
+                    r.velocity, r.angular_velocity = oc.velocity.copy(), oc.angular_velocity.copy()
+                    if not oc.collisions:
+                        r.host_body = FreeBody(r.position, r.quat, r.velocity, r.angular_velocity, r.mass, r.inertia)
+                self.rigids[oc.name] = r
             else:
                 self.objects[oc.name] = XPBDObject(oc, self)
+        colliding = [o for o in self.objects.values() if o.cfg.collisions]
+        if len(colliding) > 1 and any(not r.fixed and r.collisions for r in self.rigids.values()):
+            raise NotImplementedError("a free rigid body colliding with more than one XPBD object is not provided")
+        self._pushed = False
         self._push_rigids()
 
     def _push_rigids(self):
         live = [r for r in self.rigids.values() if r.collisions]
         for o in self.objects.values():
             if o.cfg.collisions and live:
+                if self._pushed:
+                    # setting the SDFs drops the free bodies: carry their live state over
+                    for slot, r in enumerate(live):
+                        if not r.fixed:
+                            r.position, r.quat, r.velocity, r.angular_velocity = o.solver.rigid_body(slot)
                 o.solver.set_sdfs([r.kind for r in live], [r.position for r in live], [r.quat for r in live],
                                   [r.dims for r in live])
+                for slot, r in enumerate(live):
+                    if not r.fixed:
+                        o.solver.set_rigid_body(slot, r.mass, r.inertia, r.velocity, r.angular_velocity)
+        self._pushed = True
 
     def move_rigid(self, name: str, position, rotation_deg=None):
         """Kinematic motion of a fixed rigid object between steps."""
         r = self.rigids[name]
+        if not r.fixed:
+            raise ValueError(f"rigid object {name!r} is free: the solver moves it")
         r.position = np.asarray(position, np.float64)
         if rotation_deg is not None:
-            r.quat = eul_xyz_to_quat(rotation_deg)
+            r.quat = rigid_quat(rotation_deg)
         self._push_rigids()
+
+    def rigid_state(self, name: str):
+        """(position, orientation (x, y, z, w), velocity, angular velocity) of a rigid object."""
+        r = self.rigids[name]
+        if r.host_body is not None:
+            b = r.host_body
+            return b.p.copy(), b.q.copy(), b.v.copy(), b.w.copy()
+        if not r.fixed:
+            live = [x for x in self.rigids.values() if x.collisions]
+            for o in self.objects.values():
+                if o.cfg.collisions:
+                    return o.solver.rigid_body(live.index(r))
+        return r.position.copy(), r.quat.copy(), np.zeros(3), np.zeros(3)
 
     def time_step(self):
         for o in self.objects.values():
             o.solver.step(1)
+        # free bodies that collide with nothing: RigidObject::update, velocityUpdate
+        for r in self.rigids.values():
+            if r.host_body is not None:
+                r.host_body.update(self.config.time_step, self.config.g_accel)
+                r.host_body.velocity_update(self.config.time_step)
         self.time += self.config.time_step
 
     def update(self, max_steps: int | None = None):

@@ -139,6 +139,8 @@ def load(path: str | None = None):
         "xpbd_profile_steps": ([P, I32, I32, P, P], C.c_int),
         "xpbd_kernel_name": ([I32], C.c_char_p),
         "xpbd_launch_count": ([P, P], C.c_int),
+        "xpbd_set_rigid_body": ([P, C.c_int32, C.c_int32, C.c_double, P, P, P], C.c_int),
+        "xpbd_get_rigid_body": ([P, C.c_int32, C.c_int32, P], C.c_int),
         "xpbd_get_stream": ([P, P], C.c_int),
         "xpbd_create_batch": ([P, I32, P, P], C.c_int),
         "xpbd_num_instances": ([P, P], C.c_int),
@@ -483,6 +485,18 @@ class XPBDSolver:
         h = C.c_void_p()
         self._ck(self.L.xpbd_get_stream(self.h, C.byref(h)))
         return h.value or 0
+
+    def set_rigid_body(self, slot, mass, inertia, velocity=(0, 0, 0), angular_velocity=(0, 0, 0), instance=0):
+        """SDF slot `slot` becomes a free rigid body (two-way coupling)."""
+        a = [np.ascontiguousarray(v, np.float64).reshape(3) for v in (inertia, velocity, angular_velocity)]
+        self._ck(self.L.xpbd_set_rigid_body(self.h, int(instance), int(slot), float(mass), _p(a[0]), _p(a[1]),
+                                            _p(a[2])))
+
+    def rigid_body(self, slot, instance=0):
+        """(position, orientation (x, y, z, w), velocity, angular velocity) of a free body."""
+        out = np.zeros(13)
+        self._ck(self.L.xpbd_get_rigid_body(self.h, int(instance), int(slot), _p(out)))
+        return out[:3], out[3:7], out[7:10], out[10:13]
 
     def launch_count(self) -> int:
         n = C.c_int64()
