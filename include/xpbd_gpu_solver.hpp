@@ -135,6 +135,16 @@ class GPUXPBDSolver {
         check(xpbd_add_static_collision(ctx_, face, u, v, w, surface_point, normal));
     }
     void clearCollisionConstraints() { check(xpbd_clear_collisions(ctx_)); }
+    // a free rigid body in SDF slot `slot` (RigidObject with fixed: false); its
+    // contacts are the reference's RigidDeformableCollisionConstraints, created
+    // by the device detection (addRigidDeformableCollisionConstraint has no
+    // host-side counterpart)
+    void setRigidBody(int slot, double mass, const double* inertia3, const double* velocity3,
+                      const double* angular_velocity3) {
+        check(xpbd_set_rigid_body(ctx_, 0, slot, mass, inertia3, velocity3, angular_velocity3));
+    }
+    // position[3], orientation (x, y, z, w)[4], velocity[3], angular velocity[3]
+    void rigidBodyState(int slot, double* state13) { check(xpbd_get_rigid_body(ctx_, 0, slot, state13)); }
 
     xpbd_ctx* context() { return ctx_; }
 
