@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 4
+#define XPBD_ABI_VERSION 5
 
 /* status codes */
 #define XPBD_OK 0
@@ -114,6 +114,12 @@ typedef struct {
     int32_t adjust_damping_to_material; /* adjust-damping-to-material          */
     double damping_multiplier; /* damping-multiplier: B = V_vertex * this       */
                                /* (* E_v / (1 + nu_v) when adjusted); default 1 */
+    int32_t self_collisions;   /* self-collisions (XPBDMeshObjectConfig.hpp:66):  */
+                               /* each detection tests every surface vertex for   */
+                               /* a tet it is inside (selfCollisionCheck,        */
+                               /* XPBDMeshObject.cpp:719-762) and adds a          */
+                               /* DeformableDeformableCollisionConstraint with    */
+                               /* the closest rest-surface face; needs faces     */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -228,6 +234,12 @@ int xpbd_get_rigid_body(xpbd_ctx* ctx, int32_t instance, int32_t slot, double* s
  * (out: n x (sdf, gx, gy, gz)); a test and tooling hook, no context needed */
 int xpbd_sdf_eval(int32_t kind, const double* pos3, const double* quat4, const double* dims3, int64_t n,
                   const double* pts3n, double* out4n);
+
+/* The self contacts of the last detection (no counterpart in the reference's
+ * API; its constraint list holds them): rows of (surface vertex, face; face -1
+ * when the tet it is in was degenerate) into vf2n, their multipliers into
+ * lam (may be NULL); n_out = the count. */
+int xpbd_get_self_contacts(xpbd_ctx* ctx, int32_t max_rows, int32_t* vf2n, double* lam, int32_t* n_out);
 
 /* clearCollisionConstraints (XPBDMeshObject.cpp:233-251). */
 int xpbd_clear_collisions(xpbd_ctx* ctx);

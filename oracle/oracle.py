@@ -196,6 +196,24 @@ class Oracle:
         self.L.xo_get_rigid_body(C.c_void_p(self.h), int(prim), _p(out))
         return out[:3], out[3:7], out[7:10], out[10:13]
 
+    def enable_self_collisions(self):
+        self.L.xo_enable_self_collisions(C.c_void_p(self.h))
+
+    def self_contacts(self):
+        """rows of (surface vertex, surface face, lambda) found by the last detection."""
+        n = self.L.xo_num_self_contacts(C.c_void_p(self.h))
+        out = np.zeros((n, 3))
+        if n:
+            self.L.xo_get_self_contacts(C.c_void_p(self.h), _p(out))
+        return out
+
+    def self_contact_eval(self, v, f):
+        """C and its 12-entry gradient for vertex v against face f at the current positions."""
+        g = np.zeros(12)
+        self.L.xo_self_contact_eval.restype = C.c_double
+        c = self.L.xo_self_contact_eval(C.c_void_p(self.h), int(v), int(f), _p(g))
+        return c, g
+
     def detect(self):
         return self.L.xo_detect(C.c_void_p(self.h))
 

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <limits>
 #include <string>
 #include <vector>
 
@@ -633,6 +634,107 @@ inline bool project_rigid_contact(const R* x1, const R* x2, const R* x3, const R
 }
 
 // ---------------------------------------------------------------------------
+// Self-collisions: XPBDMeshObject_::selfCollisionCheck (XPBDMeshObject.cpp:719-762)
+// with Embree's queries restated, and DeformableDeformableCollisionConstraint.
+// ---------------------------------------------------------------------------
+// EmbreeTetMeshGeometry::isPointInTetrahedron (EmbreeTetMeshGeometry.cpp:20-47):
+// p is inside when it lies on the same side of each face as the opposite
+// vertex (or on the face), all in float
+inline bool same_side_f(const float* p, const float* a, const float* b, const float* c, const float* d) {
+    const float ab0 = b[0] - a[0], ab1 = b[1] - a[1], ab2 = b[2] - a[2];
+    const float ac0 = c[0] - a[0], ac1 = c[1] - a[1], ac2 = c[2] - a[2];
+    const float n0 = ab1 * ac2 - ab2 * ac1, n1 = ab2 * ac0 - ab0 * ac2, n2 = ab0 * ac1 - ab1 * ac0;
+    const float sp = n0 * (p[0] - a[0]) + n1 * (p[1] - a[1]) + n2 * (p[2] - a[2]);
+    const float sd = n0 * (d[0] - a[0]) + n1 * (d[1] - a[1]) + n2 * (d[2] - a[2]);
+    return sp * sd >= 0;
+}
+inline bool point_in_tet_f(const float* p, const float* v0, const float* v1, const float* v2, const float* v3) {
+    return same_side_f(p, v0, v1, v2, v3) && same_side_f(p, v0, v1, v3, v2) && same_side_f(p, v0, v2, v3, v1) &&
+           same_side_f(p, v1, v2, v3, v0);
+}
+
+// Distance from p to the triangle (a, b, c), in float: the closest point by
+// the Voronoi-region walk of Ericson, Real-Time Collision Detection, 5.1.5
+// (the method of EmbreeMeshGeometry::_closestPointTriangle)
+inline float point_triangle_distance_f(const float* p, const float* a, const float* b, const float* c) {
+    auto dot = [](const float* u, const float* v) { return u[0] * v[0] + u[1] * v[1] + u[2] * v[2]; };
+    const float ab[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const float ac[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    const float ap[3] = {p[0] - a[0], p[1] - a[1], p[2] - a[2]};
+    float o[3];
+    const float d1 = dot(ab, ap), d2 = dot(ac, ap);
+    const float bp[3] = {p[0] - b[0], p[1] - b[1], p[2] - b[2]};
+    const float d3 = dot(ab, bp), d4 = dot(ac, bp);
+    const float cp[3] = {p[0] - c[0], p[1] - c[1], p[2] - c[2]};
+    const float d5 = dot(ab, cp), d6 = dot(ac, cp);
+    if (d1 <= 0.f && d2 <= 0.f) {
+        o[0] = a[0]; o[1] = a[1]; o[2] = a[2];
+    } else if (d3 >= 0.f && d4 <= d3) {
+        o[0] = b[0]; o[1] = b[1]; o[2] = b[2];
+    } else if (d6 >= 0.f && d5 <= d6) {
+        o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
+    } else {
+        const float vc = d1 * d4 - d3 * d2, vb = d5 * d2 - d1 * d6, va = d3 * d6 - d5 * d4;
+        if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+            const float v = d1 / (d1 - d3);
+            for (int k = 0; k < 3; k++) o[k] = a[k] + v * ab[k];
+        } else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+            const float v = d2 / (d2 - d6);
+            for (int k = 0; k < 3; k++) o[k] = a[k] + v * ac[k];
+        } else if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+            const float v = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+            for (int k = 0; k < 3; k++) o[k] = b[k] + v * (c[k] - b[k]);
+        } else {
+            const float den = 1.f / (va + vb + vc);
+            const float v = vb * den, w = vc * den;
+            for (int k = 0; k < 3; k++) o[k] = a[k] + v * ab[k] + w * ac[k];
+        }
+    }
+    const float e0 = p[0] - o[0], e1 = p[1] - o[1], e2 = p[2] - o[2];
+    return std::sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+}
+
+// DeformableDeformableCollisionConstraint (DeformableDeformableCollisionConstraint.cpp):
+// q against the face plane through p1, p2, p3, C = (q - p1).a/|a| + 1e-5 with
+// a = (p2 - p1) x (p3 - p1), and its gradient as the reference writes it
+// (the third face vertex's term uses q - p2); g = (q, p1, p2, p3) x 3
+template <typename R>
+inline R self_contact_eval(const R* q, const R* p1, const R* p2, const R* p3, R* g) {
+    const R e1[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+    const R e2[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
+    const R a[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    const R an = std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
+    const R u1[3] = {q[0] - p1[0], q[1] - p1[1], q[2] - p1[2]};
+    const R u2[3] = {q[0] - p2[0], q[1] - p2[1], q[2] - p2[2]};
+    const R C = (u1[0] * a[0] + u1[1] * a[1] + u1[2] * a[2]) / an + R(1e-5);
+    // M = I/|a| - a a^T/|a|^3 (symmetric); u^T M [v]x = (M u) x v
+    const R an3 = an * an * an;
+    auto Mu = [&](const R* u, R* r) {
+        const R ad = a[0] * u[0] + a[1] * u[1] + a[2] * u[2];
+        for (int k = 0; k < 3; k++) r[k] = u[k] / an - a[k] * ad / an3;
+    };
+    auto cross = [](const R* x, const R* y, R* r) {
+        r[0] = x[1] * y[2] - x[2] * y[1];
+        r[1] = x[2] * y[0] - x[0] * y[2];
+        r[2] = x[0] * y[1] - x[1] * y[0];
+    };
+    R r1[3], r2[3], t[3];
+    Mu(u1, r1);
+    Mu(u2, r2);
+    for (int k = 0; k < 3; k++) g[k] = a[k] / an;
+    const R d32[3] = {p3[0] - p2[0], p3[1] - p2[1], p3[2] - p2[2]};
+    cross(r1, d32, t);
+    for (int k = 0; k < 3; k++) g[3 + k] = -a[k] / an + t[k];
+    const R d13[3] = {p1[0] - p3[0], p1[1] - p3[1], p1[2] - p3[2]};
+    cross(r1, d13, t);
+    for (int k = 0; k < 3; k++) g[6 + k] = t[k];
+    const R d21[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
+    cross(r2, d21, t);
+    for (int k = 0; k < 3; k++) g[9 + k] = t[k];
+    return C;
+}
+
+// ---------------------------------------------------------------------------
 // Greedy tet colouring used by the coloured Gauss-Seidel order. Tets are
 // visited in index order; each takes the smallest colour not used by any tet
 // already coloured that shares a vertex. Surface faces use the same rule.
@@ -719,6 +821,18 @@ struct Object {
     std::vector<Prim<R>> prims;   // SDF primitives (fixed rigid bodies, and free ones' current poses)
     std::vector<int> prim_body;   // per primitive: index into bodies, -1 when fixed
     std::vector<RigidBody> bodies;
+    // self-collisions (self-collisions: true): surface vertex against surface face
+    bool self_collisions = false;
+    std::vector<double> X0;        // rest positions, double (DeformableMeshSDF::_initial_vertices)
+    std::vector<double> Q64;       // Dm^-1 per tet in double (TetMesh::_element_inv_undeformed_basis)
+    std::vector<int> surface_verts;  // vertices of the surface faces, ascending
+    struct SelfContact {
+        int v, f;
+        R lambda;
+    };
+    std::vector<SelfContact> self_contacts;
+    // DeformableDeformableCollisionConstraint's compliance (its Constraint(..., 1e-8))
+    static constexpr double kSelfAlpha = 1e-8;
     bool is_dynamic(int s) const { return s < (int)prim_body.size() && prim_body[s] >= 0; }
     // the detection pose of free bodies: their current state in R
     void sync_prims() {
@@ -729,6 +843,99 @@ struct Object {
                 for (int k = 0; k < 4; k++) prims[s].q[k] = (R)b.q[k];
             }
     }
+    void enable_self_collisions() {
+        self_collisions = true;
+        std::vector<char> on(V, 0);
+        for (long long i = 0; i < 3 * F; i++) on[faces[i]] = 1;
+        surface_verts.clear();
+        for (long long v = 0; v < V; v++)
+            if (on[v]) surface_verts.push_back((int)v);
+    }
+
+    // selfCollisionCheck (XPBDMeshObject.cpp:719-762): for each surface vertex,
+    // the lowest-index tet that holds it without having it as a vertex
+    // (EmbreeScene::tetMeshSelfCollisionQuery, a std::set ordered by index, on
+    // float copies of the positions); then
+    // DeformableMeshSDF::closestSurfaceFaceToPointInTet (DeformableMeshSDF.cpp:68-82):
+    // the point mapped back to rest space through that tet, and the surface face
+    // closest to it in the rest shape (in float; of equally close faces the
+    // lowest index -- Embree's traversal order decides in the reference)
+    void detect_self() {
+        self_contacts.clear();
+        std::vector<float> xf(3 * V), X0f(3 * V);
+        for (long long i = 0; i < 3 * V; i++) {
+            xf[i] = (float)x[i];
+            X0f[i] = (float)X0[i];
+        }
+        for (int v : surface_verts) {
+            int hit = -1;
+            for (long long t = 0; t < T && hit < 0; t++) {
+                const int* e = &tets[4 * t];
+                if (e[0] == v || e[1] == v || e[2] == v || e[3] == v) continue;
+                if (point_in_tet_f(&xf[3 * v], &xf[3 * e[0]], &xf[3 * e[1]], &xf[3 * e[2]], &xf[3 * e[3]]))
+                    hit = (int)t;
+            }
+            if (hit < 0) continue;
+            const int* e = &tets[4 * hit];
+            double xd[5][3];
+            const int ids[5] = {e[0], e[1], e[2], e[3], v};
+            for (int i = 0; i < 5; i++)
+                for (int k = 0; k < 3; k++) xd[i][k] = (double)x[3 * ids[i] + k];
+            double Fm[9], Fi[9];
+            compute_F(xd[0], xd[1], xd[2], xd[3], &Q64[9 * hit], Fm);
+            if (std::abs(det3(Fm)) < 1e-8) continue;
+            inv3(Fm, Fi);
+            const double rel[3] = {xd[4][0] - xd[3][0], xd[4][1] - xd[3][1], xd[4][2] - xd[3][2]};
+            float pm[3];
+            for (int r = 0; r < 3; r++)
+                pm[r] = (float)(Fi[r] * rel[0] + Fi[3 + r] * rel[1] + Fi[6 + r] * rel[2] + X0[3 * e[3] + r]);
+            int best = -1;
+            float bd = std::numeric_limits<float>::infinity();
+            for (long long f = 0; f < F; f++) {
+                const int* fv = &faces[3 * f];
+                const float d = point_triangle_distance_f(pm, &X0f[3 * fv[0]], &X0f[3 * fv[1]], &X0f[3 * fv[2]]);
+                if (d < bd) {
+                    bd = d;
+                    best = (int)f;
+                }
+            }
+            if (best >= 0) self_contacts.push_back(SelfContact{v, best, R(0)});
+        }
+    }
+
+    // ConstraintProjector::project (ConstraintProjector.hpp:111-172) for one
+    // self contact: inequality skip when C > 0, alpha = 1e-8; dx gets the 12
+    // updates (q, p1, p2, p3). Returns false when skipped.
+    bool project_self_i(SelfContact& sc, R* dx) {
+        const int* fv = &faces[3 * sc.f];
+        const int ids[4] = {sc.v, fv[0], fv[1], fv[2]};
+        R g[12];
+        const R C = self_contact_eval(&x[3 * ids[0]], &x[3 * ids[1]], &x[3 * ids[2]], &x[3 * ids[3]], g);
+        if (C > 0) return false;
+        const R at = (R)kSelfAlpha / adt();
+        R L = at;
+        for (int i = 0; i < 4; i++)
+            L += inv_mass[ids[i]] * (g[3 * i] * g[3 * i] + g[3 * i + 1] * g[3 * i + 1] + g[3 * i + 2] * g[3 * i + 2]);
+        const R dl = (-C - at * sc.lambda) / L;
+        sc.lambda += dl;
+        for (int i = 0; i < 4; i++)
+            for (int k = 0; k < 3; k++) dx[3 * i + k] = inv_mass[ids[i]] * g[3 * i + k] * dl;
+        return true;
+    }
+    void project_self_contacts(std::vector<R>* acc) {
+        R dx[12];
+        for (auto& sc : self_contacts) {
+            if (!project_self_i(sc, dx)) continue;
+            const int* fv = &faces[3 * sc.f];
+            const int ids[4] = {sc.v, fv[0], fv[1], fv[2]};
+            for (int i = 0; i < 4; i++)
+                for (int k = 0; k < 3; k++) {
+                    if (acc) (*acc)[3 * ids[i] + k] += dx[3 * i + k];
+                    else x[3 * ids[i] + k] += dx[3 * i + k];
+                }
+        }
+    }
+
     // Rigid contacts, after the static ones (projector type order,
     // include/common/XPBDTypedefs.hpp:55-56), in detection order. Gauss-Seidel
     // applies each update at once; Jacobi reads one state, sums the vertex
@@ -782,6 +989,13 @@ struct Object {
         V = V_; T = T_; F = F_;
         x.assign(3 * V, 0);
         for (long long i = 0; i < 3 * V; i++) x[i] = (R)X[i];
+        X0.assign(X, X + 3 * V);
+        Q64.assign(9 * T_, 0.0);
+        for (long long t = 0; t < T_; t++) {
+            const int* e = tets_ + 4 * t;
+            double v_e;
+            rest_shape(&X0[3 * e[0]], &X0[3 * e[1]], &X0[3 * e[2]], &X0[3 * e[3]], &Q64[9 * t], &v_e);
+        }
         prev = x;
         vel.assign(3 * V, 0);
         tets.assign(tets_, tets_ + 4 * T);
@@ -944,6 +1158,7 @@ struct Object {
             }
             for (auto& ct : contacts)
                 if (!ct.dynamic && project_contact_i(ct, dx)) add_contact(ct, dx);
+            project_self_contacts(nullptr);
             project_rigid_contacts(nullptr);
             for (auto& at : attachments) {
                 project_attachment(at, dx);
@@ -962,6 +1177,7 @@ struct Object {
                 for (auto& ct : contacts)
                     if (face_colour[ct.face] == k && !ct.dynamic)
                         if (project_contact_i(ct, dx)) add_contact(ct, dx);
+            project_self_contacts(nullptr);
             project_rigid_contacts(nullptr);
             // attachments in insertion order (the GPU's colours keep it per vertex)
             for (auto& at : attachments) {
@@ -985,6 +1201,7 @@ struct Object {
             for (auto& ct : contacts)
                 if (!ct.dynamic && project_contact_i(ct, dx))
                     for (int i = 0; i < 3; i++) for (int k = 0; k < 3; k++) acc[3 * ct.v[i] + k] += dx[3 * i + k];
+            project_self_contacts(&acc);
             project_rigid_contacts(&acc);
             for (auto& at : attachments) {
                 project_attachment(at, dx);
@@ -1079,6 +1296,7 @@ struct Object {
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;
         for (auto& at : attachments) at.lambda = 0;
+        for (auto& sc : self_contacts) sc.lambda = 0;
         const double r_plain = residual_norm();
         const std::vector<R> x_pred = x;
         std::vector<R> acc(3 * V, 0);
@@ -1124,6 +1342,7 @@ struct Object {
         std::fill(lam.begin(), lam.end(), R(0));
         for (auto& ct : contacts) ct.lambda = 0;
         for (auto& at : attachments) at.lambda = 0;
+        for (auto& sc : self_contacts) sc.lambda = 0;
         res_history.clear();
         for (int it = 0; it < num_iter; it++) {
             if (record_residual) res_history.push_back(residual_norm());
@@ -1161,6 +1380,8 @@ struct Object {
                     contacts.push_back(ct);
                 }
             }
+        // self-collision tests run after the object pairs (CollisionScene.cpp:44-50)
+        if (self_collisions) detect_self();
     }
 
     void set_kinematic_offset(const R* off) {

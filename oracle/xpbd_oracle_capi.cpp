@@ -143,6 +143,42 @@ void xo_set_prims(void* p, int n, const int* kind, const double* pos, const doub
     });
 }
 
+// self-collisions on (XPBDMeshObjectConfig self-collisions)
+void xo_enable_self_collisions(void* p) {
+    with((Handle*)p, [&](auto& o) {
+        o.enable_self_collisions();
+        return 0;
+    });
+}
+
+int xo_num_self_contacts(void* p) {
+    return with((Handle*)p, [&](auto& o) { return (int)o.self_contacts.size(); });
+}
+
+// rows of (vertex, face, lambda)
+void xo_get_self_contacts(void* p, double* rows) {
+    with((Handle*)p, [&](auto& o) {
+        for (size_t i = 0; i < o.self_contacts.size(); i++) {
+            rows[3 * i] = o.self_contacts[i].v;
+            rows[3 * i + 1] = o.self_contacts[i].f;
+            rows[3 * i + 2] = (double)o.self_contacts[i].lambda;
+        }
+        return 0;
+    });
+}
+
+// C and gradient (12) of one self contact at the object's current positions
+double xo_self_contact_eval(void* p, int v, int f, double* g12) {
+    return with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        const int* fv = &o.faces[3 * f];
+        R g[12];
+        const R C = xo::self_contact_eval(&o.x[3 * v], &o.x[3 * fv[0]], &o.x[3 * fv[1]], &o.x[3 * fv[2]], g);
+        for (int i = 0; i < 12; i++) g12[i] = (double)g[i];
+        return (double)C;
+    });
+}
+
 // primitive `prim` becomes a free rigid body with the given pose (double),
 // mass, diagonal inertia, velocity and angular velocity
 void xo_set_rigid_body(void* p, int prim, const double* pos3, const double* quat4, double mass,

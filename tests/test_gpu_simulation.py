@@ -113,10 +113,6 @@ def test_element_classes_pick_materials(lib, tmp_path):
 def test_unprovided_objects_fail_loudly(lib, tmp_path):
     cfg, _, _, _ = _scene(tmp_path)
     text = open(cfg).read()
-    # self-collisions
-    with pytest.raises(NotImplementedError):
-        S.Simulation(text.replace("num-solver-iters: 6", "num-solver-iters: 6\n    self-collisions: true"),
-                     base_dir=str(tmp_path)).setup()
     # a free body colliding with two XPBD objects
     second = text[text.index('  - name: "Cube"'):text.index('  - name: "Ball"')].replace('"Cube"', '"Cube2"')
     two = text.replace("fixed: true", "fixed: false").replace('  - name: "Ball"', second + '  - name: "Ball"')

@@ -39,7 +39,8 @@ bool valid_params(const xpbd_params& p) {
            p.gs_variant >= 0 && p.gs_variant <= 3 && p.num_local_collision_iters >= 0 &&
            p.num_local_collision_iters <= 1000 && (p.first_order == 0 || p.first_order == 1) &&
            (p.adjust_damping_to_material == 0 || p.adjust_damping_to_material == 1) &&
-           (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier)));
+           (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier))) &&
+           (p.self_collisions == 0 || p.self_collisions == 1);
 }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
@@ -252,6 +253,12 @@ void enqueue_local_collision_iters(xpbd_ctx* c) {
 }
 
 // ---- the substep body (XPBDMeshObject_::update, XPBDMeshObject.cpp:426-505) ----
+// DeformableDeformableCollisionConstraint's alpha = 1e-8 (its Constraint
+// base, DeformableDeformableCollisionConstraint.cpp:12-18) over dt^2 (or dt)
+float self_alpha_tilde(const xpbd_ctx* c) {
+    return (float)(1e-8 / (c->prm.first_order ? c->prm.dt : c->prm.dt * c->prm.dt));
+}
+
 int enqueue_update(xpbd_ctx* c, bool write_vel) {
     const xpbd_params& p = c->prm;
     const int iters = p.num_iters;
@@ -304,6 +311,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
                 }
+                if (c->self_on) {
+                    Scope sc(c, K_CONTACT);
+                    launch_self_contacts(c->L(), c->selfs(), c->faces.p, c->x.p, c->dx.p, true, first_contact,
+                                         self_alpha_tilde(c), c->flags.p);
+                }
                 if (c->nbodies) {
                     Scope sc(c, K_CONTACT);
                     launch_rigid_contacts(c->L(), ca, c->rc_list.p, c->rc_count.p, c->sphere_tab.p, c->face_inst.p,
@@ -326,6 +338,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 if (have_faces) {
                     Scope sc(c, K_CONTACT);
                     launch_contacts_jacobi(c->L(), ca, c->x.p, c->dx.p, first_contact);
+                }
+                if (c->self_on) {
+                    Scope sc(c, K_CONTACT);
+                    launch_self_contacts(c->L(), c->selfs(), c->faces.p, c->x.p, c->dx.p, true, first_contact,
+                                         self_alpha_tilde(c), c->flags.p);
                 }
                 if (c->nbodies) {
                     Scope sc(c, K_CONTACT);
@@ -372,7 +389,12 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
                 }
             }
-            // rigid-body contacts after the static ones (projector type order)
+            // then the self contacts and the rigid-body contacts (projector type order)
+            if (c->self_on) {
+                Scope sc(c, K_CONTACT);
+                launch_self_contacts(c->L(), c->selfs(), c->faces.p, c->x.p, nullptr, false, first,
+                                     self_alpha_tilde(c), c->flags.p);
+            }
             if (c->nbodies) {
                 Scope sc(c, K_CONTACT);
                 launch_rigid_contacts(c->L(), ca, c->rc_list.p, c->rc_count.p, c->sphere_tab.p, c->face_inst.p,
@@ -555,6 +577,16 @@ int push_bodies(xpbd_ctx* c) {
 
 int detect(xpbd_ctx* c) {
     if (c->F == 0) return XPBD_OK;
+    if (c->n_spheres_total == 0) {
+        // no SDFs: the object pairs add nothing; self-collisions may
+        int st = xpbd_clear_collisions(c);
+        if (st) return st;
+        if (c->self_on) {
+            Scope sc(c, K_DETECT);
+            launch_self_detect(c->L(), c->selfs(), c->sgrid, c->x.p, c->faces.p);
+        }
+        return after_launches(c, "detect");
+    }
     if (c->sphere_dirty) {
         // pageable source: the copy is staged before the call returns, so the
         // host table may change right after; the upload is stream-ordered
@@ -574,6 +606,11 @@ int detect(xpbd_ctx* c) {
     if (c->nbodies) {
         Scope sc(c, K_DETECT);
         launch_rigid_compact(c->L(), c->contacts(), c->rc_list.p, c->rc_count.p);
+    }
+    // self-collision tests run after the object pairs (CollisionScene.cpp:44-50)
+    if (c->self_on) {
+        Scope sc(c, K_DETECT);
+        launch_self_detect(c->L(), c->selfs(), c->sgrid, c->x.p, c->faces.p);
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
     return after_launches(c, "detect");
@@ -608,6 +645,11 @@ void release(xpbd_ctx* c) {
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
     c->sphere_tab.release(); c->face_inst.release();
     c->rb.release(); c->rc_list.release(); c->rc_count.release();
+    c->s_tets.release(); c->s_contact.release(); c->s_Q.release(); c->s_X0.release(); c->s_X0f.release();
+    c->s_lam.release(); c->s_surf.release(); c->s_cell_count.release(); c->s_cell_off.release();
+    c->s_cell_fill.release(); c->s_cell_tets.release(); c->s_tet_cell.release(); c->s_overflow.release();
+    c->s_n_overflow.release(); c->s_hit_tet.release(); c->s_hit_list.release(); c->s_n_hits.release();
+    c->s_scan_part.release();
     c->patch_meta.release(); c->patch_verts.release();
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
@@ -694,6 +736,92 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
     XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NT + 1), cudaMemcpyHostToDevice));
     if (!dep.empty()) XPBD_CU(c, cudaMemcpy(c->flow_dep.p, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NT + 1)));
+    return XPBD_OK;
+}
+
+// Self-collision data: the surface vertices, tets in index order, Dm^-1 and
+// rest positions in double, and a uniform grid over the rest bounding box
+// padded by a quarter of its extent, cells 1.1x the widest tet box at rest
+// (a tet whose box outgrows a cell goes to the overflow list), at most
+// 2^22 cells.
+int build_self_collisions(xpbd_ctx* c, const std::vector<double>& X, const std::vector<double>& Q) {
+    const int V = c->V, T = c->T, F = c->F;
+    std::vector<char> on(V, 0);
+    for (size_t i = 0; i < c->faces_h.size(); i++) on[c->faces_h[i]] = 1;
+    std::vector<int> surf;
+    for (int v = 0; v < V; v++)
+        if (on[v]) surf.push_back(v);
+    double lo[3] = {1e300, 1e300, 1e300}, hi[3] = {-1e300, -1e300, -1e300}, wmax = 0;
+    for (int v = 0; v < V; v++)
+        for (int k = 0; k < 3; k++) {
+            lo[k] = std::min(lo[k], X[3 * (size_t)v + k]);
+            hi[k] = std::max(hi[k], X[3 * (size_t)v + k]);
+        }
+    std::vector<int4> tt(T);
+    for (int t = 0; t < T; t++) {
+        const int* e = &c->tets_h[4 * (size_t)t];
+        tt[t] = make_int4(e[0], e[1], e[2], e[3]);
+        for (int k = 0; k < 3; k++) {
+            double a = 1e300, b = -1e300;
+            for (int i = 0; i < 4; i++) {
+                a = std::min(a, X[3 * (size_t)e[i] + k]);
+                b = std::max(b, X[3 * (size_t)e[i] + k]);
+            }
+            wmax = std::max(wmax, b - a);
+        }
+    }
+    double ext = 0;
+    for (int k = 0; k < 3; k++) ext = std::max(ext, hi[k] - lo[k]);
+    double cell = std::max(1.1 * wmax, 1e-9 * std::max(ext, 1.0));
+    int n[3];
+    for (;;) {
+        long long cells = 1;
+        for (int k = 0; k < 3; k++) {
+            const double w = (hi[k] - lo[k]) + 0.5 * ext;
+            n[k] = std::max(1, (int)std::ceil(w / cell));
+            cells *= n[k];
+        }
+        if (cells <= (1LL << 22)) break;
+        cell *= 1.25;
+    }
+    xg::SelfGrid g;
+    g.ox = (float)(lo[0] - 0.25 * ext);
+    g.oy = (float)(lo[1] - 0.25 * ext);
+    g.oz = (float)(lo[2] - 0.25 * ext);
+    g.cell = (float)cell;
+    g.nx = n[0]; g.ny = n[1]; g.nz = n[2];
+    c->sgrid = g;
+    c->ncells = n[0] * n[1] * n[2];
+    c->n_surf = (int)surf.size();
+    std::vector<float4> X0f(V);
+    for (int v = 0; v < V; v++)
+        X0f[v] = make_float4((float)X[3 * (size_t)v], (float)X[3 * (size_t)v + 1], (float)X[3 * (size_t)v + 2], 0.f);
+    const int ns = std::max(c->n_surf, 1);
+    XPBD_CU(c, c->s_tets.alloc(T));
+    XPBD_CU(c, c->s_Q.alloc(9 * (size_t)T));
+    XPBD_CU(c, c->s_X0.alloc(3 * (size_t)V));
+    XPBD_CU(c, c->s_X0f.alloc(V));
+    XPBD_CU(c, c->s_surf.alloc(ns));
+    XPBD_CU(c, c->s_cell_count.alloc(c->ncells));
+    XPBD_CU(c, c->s_cell_fill.alloc(c->ncells));
+    XPBD_CU(c, c->s_cell_off.alloc(c->ncells + 1));
+    XPBD_CU(c, c->s_cell_tets.alloc(T));
+    XPBD_CU(c, c->s_tet_cell.alloc(T));
+    XPBD_CU(c, c->s_overflow.alloc(T));
+    XPBD_CU(c, c->s_n_overflow.alloc(1));
+    XPBD_CU(c, c->s_hit_tet.alloc(ns));
+    XPBD_CU(c, c->s_hit_list.alloc(ns));
+    XPBD_CU(c, c->s_n_hits.alloc(1));
+    XPBD_CU(c, c->s_contact.alloc(ns));
+    XPBD_CU(c, c->s_lam.alloc(ns));
+    XPBD_CU(c, c->s_scan_part.alloc(c->ncells / 4096 + 2));
+    XPBD_CU(c, cudaMemcpy(c->s_tets.p, tt.data(), sizeof(int4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->s_Q.p, Q.data(), sizeof(double) * 9 * (size_t)T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->s_X0.p, X.data(), sizeof(double) * 3 * (size_t)V, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->s_X0f.p, X0f.data(), sizeof(float4) * V, cudaMemcpyHostToDevice));
+    if (!surf.empty()) XPBD_CU(c, cudaMemcpy(c->s_surf.p, surf.data(), sizeof(int) * surf.size(), cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemset(c->s_n_hits.p, 0, sizeof(int)));
+    c->self_on = true;
     return XPBD_OK;
 }
 
@@ -964,6 +1092,10 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, c->rc_list.alloc(ns));
         XPBD_CU(c, c->rc_count.alloc(1));
         XPBD_CU(c, cudaMemset(c->rc_count.p, 0, sizeof(int)));
+        if (p.self_collisions) {
+            int st = build_self_collisions(c, Xcat, Q);
+            if (st) return st;
+        }
     }
     if (!lslots.empty()) {
         XPBD_CU(c, c->local_slots.alloc(T));
@@ -1423,6 +1555,7 @@ int xpbd_clear_collisions(xpbd_ctx* c) {
         XPBD_CU(c, cudaMemsetAsync(c->c_bary.p, 0, sizeof(float4) * (size_t)c->S * c->F, c->stream));
         XPBD_CU(c, cudaMemsetAsync(c->c_lam.p, 0, sizeof(float) * (size_t)c->S * c->F, c->stream));
         XPBD_CU(c, cudaMemsetAsync(c->rc_count.p, 0, sizeof(int), c->stream));
+        if (c->self_on) XPBD_CU(c, cudaMemsetAsync(c->s_n_hits.p, 0, sizeof(int), c->stream));
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), 0);
     return XPBD_OK;
@@ -1536,6 +1669,29 @@ int xpbd_get_collisions(xpbd_ctx* c, int32_t max_rows, double* rows, int32_t* n_
     return XPBD_OK;
 }
 
+int xpbd_get_self_contacts(xpbd_ctx* c, int32_t max_rows, int32_t* vf, double* lam, int32_t* n_out) {
+    if (!c || !n_out || max_rows < 0 || (max_rows > 0 && !vf)) return XPBD_ERR_INVALID;
+    *n_out = 0;
+    if (!c->self_on) return XPBD_OK;
+    int n = 0;
+    XPBD_CU(c, cudaMemcpyAsync(&n, c->s_n_hits.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    const int k = std::min(n, (int)max_rows);
+    if (k > 0) {
+        std::vector<int2> ct(k);
+        std::vector<float> l(k);
+        XPBD_CU(c, cudaMemcpy(ct.data(), c->s_contact.p, sizeof(int2) * k, cudaMemcpyDeviceToHost));
+        XPBD_CU(c, cudaMemcpy(l.data(), c->s_lam.p, sizeof(float) * k, cudaMemcpyDeviceToHost));
+        for (int i = 0; i < k; i++) {
+            vf[2 * i] = ct[i].x;
+            vf[2 * i + 1] = ct[i].y;
+            if (lam) lam[i] = l[i];
+        }
+    }
+    *n_out = n;
+    return XPBD_OK;
+}
+
 int xpbd_update(xpbd_ctx* c) {
     if (!c) return XPBD_ERR_INVALID;
     return run_update(c, false);
@@ -1559,7 +1715,7 @@ int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
     const double interval = c->prm.collision_rate > 0 ? 1.0 / c->prm.collision_rate : 1e300;
     for (int k = 0; k < nsteps; k++) {
         const bool cd = (c->time - c->last_cd > interval);
-        if (cd && c->n_spheres_total > 0) {
+        if (cd && (c->n_spheres_total > 0 || c->self_on)) {
             int st = detect(c);
             if (st) return st;
         } else if (cd) {

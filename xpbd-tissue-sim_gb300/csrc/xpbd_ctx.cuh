@@ -112,6 +112,17 @@ struct xpbd_ctx {
     std::vector<double> body_h;        // host copy, current after pull_bodies
     DevBuf<double> rb;                 // capacity n_inst * S records
     DevBuf<int> rc_list, rc_count;     // rigid contacts in slot order, their count
+    // self-collisions: grid, binning, hits and contacts (xg::SelfArrays)
+    bool self_on = false;
+    int n_surf = 0, ncells = 0;
+    xg::SelfGrid sgrid{};
+    DevBuf<int4> s_tets;
+    DevBuf<int2> s_contact;
+    DevBuf<double> s_Q, s_X0;
+    DevBuf<float4> s_X0f;
+    DevBuf<float> s_lam;
+    DevBuf<int> s_surf, s_cell_count, s_cell_off, s_cell_fill, s_cell_tets, s_tet_cell, s_overflow, s_n_overflow,
+        s_hit_tet, s_hit_list, s_n_hits, s_scan_part;
     DevBuf<int> face_inst;
     bool sphere_dirty = true;
     int n_spheres_total = 0;
@@ -170,6 +181,13 @@ struct xpbd_ctx {
 
     xg::TaskArrays tasks() {
         return xg::TaskArrays{flow_tasks.p, flow_dep_off.p, flow_dep.p, flow_epoch.p, flow_epoch.p + ntasks, ntasks};
+    }
+    xg::SelfArrays selfs() {
+        return xg::SelfArrays{s_tets.p,        s_Q.p,          s_X0.p,         s_X0f.p,      s_surf.p,
+                              n_surf,          s_cell_count.p, s_cell_off.p,   s_cell_fill.p, s_cell_tets.p,
+                              s_tet_cell.p,    s_overflow.p,   s_n_overflow.p, s_hit_tet.p,  s_hit_list.p,
+                              s_n_hits.p,      s_contact.p,    s_lam.p,        s_scan_part.p, T,
+                              F};
     }
     TetArrays tets() {
         return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};

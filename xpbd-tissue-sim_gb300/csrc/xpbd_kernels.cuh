@@ -111,6 +111,37 @@ struct TaskArrays {
     int ntasks;
 };
 
+// Self-collisions (DeformableDeformableCollisionConstraint): a uniform grid
+// over the positions, each tet in the cell of its centroid, queries over the
+// 27 cells around a point; tets larger than a cell in some axis go to an
+// overflow list that every query scans.
+struct SelfGrid {
+    float ox, oy, oz, cell;  // origin and cell size
+    int nx, ny, nz;
+};
+struct SelfArrays {
+    const int4* tets;       // [T] vertex indices in tet index order
+    const double* Q;        // [9T] Dm^-1, column-major, double
+    const double* X0;       // [3V] rest positions, double
+    const float4* X0f;      // [V] rest positions, float
+    const int* surf;        // [n_surf] surface vertices, ascending
+    int n_surf;
+    int* cell_count;        // [ncells] (zeroed before binning)
+    int* cell_off;          // [ncells + 1]
+    int* cell_fill;         // [ncells] (zeroed before binning)
+    int* cell_tets;         // [T]
+    int* tet_cell;          // [T] each tet's cell, -1 in the overflow list
+    int* overflow;          // [T]
+    int* n_overflow;        // [1] (zeroed before binning)
+    int* hit_tet;           // [n_surf] lowest tet holding the vertex, -1 none
+    int* hit_list;          // [n_surf] surface indices with a hit, ascending
+    int* n_hits;            // [1]
+    int2* contact;          // [n_surf] (vertex, face; face -1 = none), in hit order
+    float* lam;             // [n_surf]
+    int* scan_part;         // scan scratch, [ncells / 4096 + 2]
+    int T, F;
+};
+
 struct Flags {
     unsigned long long nonfinite;
     unsigned long long degenerate;
@@ -214,6 +245,10 @@ void launch_rigid_contacts(const Launch& s, const ContactArrays& c, const int* l
                            bool jacobi, bool first, Flags* flags);
 void launch_rigid_update(const Launch& s, double* rb, int nb, double dt, double g);
 void launch_rigid_velocity(const Launch& s, double* rb, int nb, double dt);
+// self-collision detection (after the SDF contacts) and projection
+void launch_self_detect(const Launch& s, const SelfArrays& a, const SelfGrid& g, const float4* x, const int4* faces);
+void launch_self_contacts(const Launch& s, const SelfArrays& a, const int4* faces, float4* x, float4* dx,
+                          bool jacobi, bool first, float alpha_tilde, Flags* flags);
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
                       int end, float4* x, bool first);
 void launch_attach_jacobi(const Launch& s, const int* vert, const float4* target, float* lam, int n, const float4* x,

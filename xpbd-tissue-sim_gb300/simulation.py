@@ -34,9 +34,12 @@ object in the solve, gravity and the angular Euler step after it
 integrated here on the host. The reference only builds graphics for
 `visualization`; there is no graphics here and the key is read and ignored.
 
+`self-collisions: true` turns on the solver's self-collision detection and
+constraints (XPBDMeshObject.cpp:719-762).
+
 Not provided (each raises NotImplementedError naming the key): a free rigid
-body colliding with more than one XPBD object, rigid meshes, self-collisions
-and the Virtuoso robot objects.
+body colliding with more than one XPBD object, rigid meshes and the Virtuoso
+robot objects.
 """
 from __future__ import annotations
 
@@ -336,8 +339,6 @@ class XPBDObject:
     """One XPBDMeshObject: its placed mesh and its GPU solver."""
 
     def __init__(self, cfg: XPBDMeshObjectConfig, sim: "Simulation"):
-        if cfg.self_collisions:
-            raise NotImplementedError("self-collisions are not provided by the GB300 solver")
         self.cfg = cfg
         path = cfg.filename if os.path.isabs(cfg.filename) else os.path.join(sim.base_dir, cfg.filename)
         X, tets, faces = msh.read_msh(path)
@@ -364,7 +365,8 @@ class XPBDObject:
                                    constraint_type=cfg.constraint_type, residual_policy=cfg.residual_policy,
                                    num_local_collision_iters=cfg.num_local_collision_iters,
                                    first_order=int(cfg.first_order), damping_multiplier=cfg.damping_multiplier,
-                                   adjust_damping_to_material=int(cfg.adjust_damping_to_material))
+                                   adjust_damping_to_material=int(cfg.adjust_damping_to_material),
+                                   self_collisions=int(cfg.self_collisions))
         if np.any(cfg.velocity != 0):
             self.solver.set_velocities(np.broadcast_to(cfg.velocity, self.X.shape))
 

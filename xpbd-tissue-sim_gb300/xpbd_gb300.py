@@ -64,6 +64,7 @@ class Params(C.Structure):
         ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32), ("gs_variant", C.c_int32),
         ("num_local_collision_iters", C.c_int32),
         ("first_order", C.c_int32), ("adjust_damping_to_material", C.c_int32), ("damping_multiplier", C.c_double),
+        ("self_collisions", C.c_int32),
     ]
 
 
@@ -140,6 +141,7 @@ def load(path: str | None = None):
         "xpbd_kernel_name": ([I32], C.c_char_p),
         "xpbd_launch_count": ([P, P], C.c_int),
         "xpbd_set_rigid_body": ([P, C.c_int32, C.c_int32, C.c_double, P, P, P], C.c_int),
+        "xpbd_get_self_contacts": ([P, C.c_int32, P, P, P], C.c_int),
         "xpbd_get_rigid_body": ([P, C.c_int32, C.c_int32, P], C.c_int),
         "xpbd_get_stream": ([P, P], C.c_int),
         "xpbd_create_batch": ([P, I32, P, P], C.c_int),
@@ -497,6 +499,16 @@ class XPBDSolver:
         out = np.zeros(13)
         self._ck(self.L.xpbd_get_rigid_body(self.h, int(instance), int(slot), _p(out)))
         return out[:3], out[3:7], out[7:10], out[10:13]
+
+    def self_contacts(self):
+        """(rows of (surface vertex, face), multipliers) of the last detection."""
+        n = C.c_int32()
+        self._ck(self.L.xpbd_get_self_contacts(self.h, 0, None, None, C.byref(n)))
+        vf = np.zeros((n.value, 2), np.int32)
+        lam = np.zeros(n.value)
+        if n.value:
+            self._ck(self.L.xpbd_get_self_contacts(self.h, n.value, _p(vf), _p(lam), C.byref(n)))
+        return vf, lam
 
     def launch_count(self) -> int:
         n = C.c_int64()
