@@ -233,9 +233,10 @@ void enqueue_local_collision_iters(xpbd_ctx* c) {
                     launch_project_local_gs(c->L(), c->tets(), c->local_slots.p, c->lcol_off[col], c->lcol_off[col + 1],
                                             c->tmask.p, c->x.p, separate ? pass : 2, c->flags.p);
                 }
-            for (int fc = 0; fc < c->n_face_colours; fc++) {
+            {
                 Scope sc(c, K_CONTACT);
-                launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, false);
+                launch_contacts_gs_lists(c->L(), ca, c->act_faces.p, c->act_off.p, c->n_face_colours, c->n_inst,
+                                         c->x.p, false);
             }
         } else {
             {
@@ -358,7 +359,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
-    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() && p.gs_variant >= 2 && c->ntasks > 0) {
+    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() && (p.gs_variant == 2 || p.gs_variant == 3) &&
+               c->ntasks > 0) {
         // every iteration and colour in one cooperative launch
         if (track && !warm) exact_residual_row(c, 0, false);
         cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
@@ -384,10 +386,9 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 }
             }
             if (have_faces) {
-                for (int fc = 0; fc < c->n_face_colours; fc++) {
-                    Scope sc(c, K_CONTACT);
-                    launch_contacts_gs(c->L(), ca, c->face_list.p, c->fcol_off[fc], c->fcol_off[fc + 1], c->x.p, first);
-                }
+                Scope sc(c, K_CONTACT);
+                launch_contacts_gs_lists(c->L(), ca, c->act_faces.p, c->act_off.p, c->n_face_colours, c->n_inst,
+                                         c->x.p, first);
             }
             // then the self contacts and the rigid-body contacts (projector type order)
             if (c->self_on) {
@@ -493,6 +494,13 @@ int sync_attachments(xpbd_ctx* c) {
 int prepare_update(xpbd_ctx* c) {
     int ast = sync_attachments(c);
     if (ast) return ast;
+    if (c->F && c->contact_lists_dirty) {
+        // the faces with active static contacts, after the contacts changed
+        Scope sc(c, K_DETECT);
+        launch_contact_lists(c->L(), c->contacts(), c->ifl.p, c->ifo_off.p, c->n_face_colours, c->n_inst,
+                             c->act_faces.p, c->act_off.p);
+        c->contact_lists_dirty = false;
+    }
     if (tracking(c) || c->warm_mode != XPBD_WARM_NONE) {
         // one extra row for on-demand residual queries, two for the warm start
         int st = ensure_residual_rows(c, c->prm.num_iters + 4);
@@ -613,6 +621,7 @@ int detect(xpbd_ctx* c) {
         launch_self_detect(c->L(), c->selfs(), c->sgrid, c->x.p, c->faces.p);
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), -1);  // unknown until read back
+    c->contact_lists_dirty = true;
     return after_launches(c, "detect");
 }
 
@@ -645,6 +654,7 @@ void release(xpbd_ctx* c) {
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
     c->sphere_tab.release(); c->face_inst.release();
     c->rb.release(); c->rc_list.release(); c->rc_count.release();
+    c->ifl.release(); c->ifo_off.release(); c->act_faces.release(); c->act_off.release();
     c->s_tets.release(); c->s_contact.release(); c->s_Q.release(); c->s_X0.release(); c->s_X0f.release();
     c->s_lam.release(); c->s_surf.release(); c->s_cell_count.release(); c->s_cell_off.release();
     c->s_cell_fill.release(); c->s_cell_tets.release(); c->s_tet_cell.release(); c->s_overflow.release();
@@ -1014,6 +1024,23 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         std::vector<int> fill(c->fcol_off.begin(), c->fcol_off.end() - 1);
         for (int f = 0; f < F; f++) flist[fill[fcol[f]]++] = f;
     }
+    // faces by (instance, colour, index) for the per-instance contact lists
+    const int nfc = c->n_face_colours;
+    std::vector<int> ifl(F), ifo((size_t)n_inst * (nfc + 1), 0);
+    {
+        std::vector<int> cnt((size_t)n_inst * nfc, 0);
+        for (int f = 0; f < F; f++) cnt[(size_t)finst[f] * nfc + fcol[f]]++;
+        int run = 0;
+        for (int k = 0; k < n_inst; k++) {
+            for (int col = 0; col < nfc; col++) {
+                ifo[(size_t)k * (nfc + 1) + col] = run;
+                run += cnt[(size_t)k * nfc + col];
+            }
+            ifo[(size_t)k * (nfc + 1) + nfc] = run;
+        }
+        std::vector<int> pos(ifo.begin(), ifo.end());
+        for (int f = 0; f < F; f++) ifl[pos[(size_t)finst[f] * (nfc + 1) + fcol[f]]++] = f;
+    }
     c->api_slots.assign(F, 0);
 
     // local collision iterations: a per-tet greedy colouring in tet index
@@ -1088,6 +1115,13 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, cudaMemset(c->c_lam.p, 0, sizeof(float) * ns));
         XPBD_CU(c, cudaMemcpy(c->faces.p, hf.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
         XPBD_CU(c, cudaMemcpy(c->face_list.p, flist.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+        XPBD_CU(c, c->ifl.alloc(F));
+        XPBD_CU(c, c->ifo_off.alloc(ifo.size()));
+        XPBD_CU(c, c->act_faces.alloc(F));
+        XPBD_CU(c, c->act_off.alloc(ifo.size()));
+        XPBD_CU(c, cudaMemcpy(c->ifl.p, ifl.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->ifo_off.p, ifo.data(), sizeof(int) * ifo.size(), cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemset(c->act_off.p, 0, sizeof(int) * ifo.size()));
         XPBD_CU(c, c->rb.alloc((size_t)kRigidRec * n_inst * c->S));
         XPBD_CU(c, c->rc_list.alloc(ns));
         XPBD_CU(c, c->rc_count.alloc(1));
@@ -1104,7 +1138,8 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     }
     // (faces allow contacts, which the dataflow sweep leaves to the launches)
-    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2 && F == 0) {
+    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && (p.gs_variant == 2 || p.gs_variant == 3) &&
+        F == 0) {
         int st = build_flow_tasks(c, pmeta, pverts);
         if (st) return st;
     }
@@ -1556,6 +1591,7 @@ int xpbd_clear_collisions(xpbd_ctx* c) {
         XPBD_CU(c, cudaMemsetAsync(c->c_lam.p, 0, sizeof(float) * (size_t)c->S * c->F, c->stream));
         XPBD_CU(c, cudaMemsetAsync(c->rc_count.p, 0, sizeof(int), c->stream));
         if (c->self_on) XPBD_CU(c, cudaMemsetAsync(c->s_n_hits.p, 0, sizeof(int), c->stream));
+        c->contact_lists_dirty = true;
     }
     std::fill(c->api_slots.begin(), c->api_slots.end(), 0);
     return XPBD_OK;
@@ -1595,6 +1631,7 @@ int xpbd_add_static_collision(xpbd_ctx* c, int32_t face, double u, double v, dou
     XPBD_CU(c, cudaMemcpy(c->c_lam.p + slot, &z, sizeof z, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->c_bary.p + slot, &b, sizeof b, cudaMemcpyHostToDevice));
     c->api_slots[face] = s + 1;
+    c->contact_lists_dirty = true;
     return XPBD_OK;
 }
 

@@ -112,6 +112,10 @@ struct xpbd_ctx {
     std::vector<double> body_h;        // host copy, current after pull_bodies
     DevBuf<double> rb;                 // capacity n_inst * S records
     DevBuf<int> rc_list, rc_count;     // rigid contacts in slot order, their count
+    // static contacts by instance and face colour: all faces (ifl, ifo_off) and,
+    // after each detection, those with an active contact (act_faces, act_off)
+    DevBuf<int> ifl, ifo_off, act_faces, act_off;
+    bool contact_lists_dirty = true;
     // self-collisions: grid, binning, hits and contacts (xg::SelfArrays)
     bool self_on = false;
     int n_surf = 0, ncells = 0;

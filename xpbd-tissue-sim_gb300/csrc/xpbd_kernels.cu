@@ -869,21 +869,15 @@ __global__ void k_contacts_jacobi(ContactArrays c, const float4* __restrict__ x,
     c.lam[slot] = lam;
 }
 
-// Gauss-Seidel contacts: one launch per surface-face colour; a thread owns a
-// face and walks its slots in order, updating positions in place.
-template <bool FIRST>
-__global__ void k_contacts_gs(ContactArrays c, const int* __restrict__ face_list, int begin, int end,
-                              float4* __restrict__ x) {
-    pdl_wait_then_release();
-    const int j = begin + blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= end) return;
-    const int f = face_list[j];
+// Gauss-Seidel contacts of one face: its slots in order, positions updated in
+// place (faces of one colour share no vertex)
+__device__ __forceinline__ void contact_face_gs(const ContactArrays& c, int f, float4* __restrict__ x, bool first) {
     const int4 fv = c.faces[f];
     for (int s = 0; s < c.S; s++) {
         const int slot = s * c.F + f;
         if (c.bary[slot].w != 1.f) continue;  // empty, or against a free rigid body
         float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
-        float lam = FIRST ? 0.f : c.lam[slot];
+        float lam = first ? 0.f : c.lam[slot];
         float d[3][3];
         if (contact_update(c, slot, xs, d, lam)) {
             x[fv.x] = make_float4(xs[0].x + d[0][0], xs[0].y + d[0][1], xs[0].z + d[0][2], xs[0].w);
@@ -891,6 +885,74 @@ __global__ void k_contacts_gs(ContactArrays c, const int* __restrict__ face_list
             x[fv.z] = make_float4(xs[2].x + d[2][0], xs[2].y + d[2][1], xs[2].z + d[2][2], xs[2].w);
         }
         c.lam[slot] = lam;
+    }
+}
+
+// After a detection: per instance and face colour, the faces holding an
+// active static contact, in face-list order. One block per instance; ifl
+// lists the faces by (instance, colour, index) with ranges
+// ifo_off[k * (ncol + 1) + colour]; act_faces reuses the same positions.
+__global__ void __launch_bounds__(kContactListThreads) k_contact_lists(ContactArrays c, const int* __restrict__ ifl,
+                                                                       const int* __restrict__ ifo_off, int ncol,
+                                                                       int* __restrict__ act_faces,
+                                                                       int* __restrict__ act_off) {
+    __shared__ int warp_tot[kContactListThreads / 32];
+    __shared__ int out;
+    pdl_wait_then_release();
+    const int k = blockIdx.x, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const int* off = ifo_off + (size_t)k * (ncol + 1);
+    int* aoff = act_off + (size_t)k * (ncol + 1);
+    if (tid == 0) out = off[0];
+    __syncthreads();
+    for (int col = 0; col < ncol; col++) {
+        if (tid == 0) aoff[col] = out;
+        for (int b0 = off[col]; b0 < off[col + 1]; b0 += kContactListThreads) {
+            const int j = b0 + tid;
+            bool hit = false;
+            int f = 0;
+            if (j < off[col + 1]) {
+                f = ifl[j];
+                for (int s = 0; s < c.S; s++) hit |= c.bary[s * c.F + f].w == 1.f;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (lane == 0) warp_tot[wid] = __popc(m);
+            __syncthreads();
+            int o = out;
+            for (int w = 0; w < wid; w++) o += warp_tot[w];
+            if (hit) act_faces[o + __popc(m & ((1u << lane) - 1u))] = f;
+            __syncthreads();
+            if (tid == 0) {
+                int t = 0;
+                for (int w = 0; w < kContactListThreads / 32; w++) t += warp_tot[w];
+                out += t;
+            }
+            __syncthreads();
+        }
+    }
+    if (tid == 0) aoff[ncol] = out;
+}
+
+constexpr int kMaxListColours = 63;  // colour offsets staged in shared memory up to this many
+
+// Gauss-Seidel contacts of every face colour in one launch: one block per
+// instance (instances share no vertex), the colours in order with a block
+// barrier between them (the faces of a colour share no vertex)
+__global__ void __launch_bounds__(kContactListThreads) k_contacts_gs_lists(ContactArrays c,
+                                                                           const int* __restrict__ act_faces,
+                                                                           const int* __restrict__ act_off, int ncol,
+                                                                           float4* __restrict__ x, bool first) {
+    __shared__ int soff[kMaxListColours + 1];
+    pdl_wait_then_release();
+    const int* aoff = act_off + (size_t)blockIdx.x * (ncol + 1);
+    const bool staged = ncol <= kMaxListColours;
+    if (staged)
+        for (int i = threadIdx.x; i <= ncol; i += blockDim.x) soff[i] = aoff[i];
+    __syncthreads();
+    for (int col = 0; col < ncol; col++) {
+        const int lo = staged ? soff[col] : aoff[col], hi = staged ? soff[col + 1] : aoff[col + 1];
+        if (lo == hi) continue;  // uniform: the bounds are the block's
+        for (int j = lo + threadIdx.x; j < hi; j += blockDim.x) contact_face_gs(c, act_faces[j], x, first);
+        __syncthreads();
     }
 }
 
@@ -2439,12 +2501,15 @@ void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float
     else go(k_contacts_jacobi<false>, nblk(n, 256), 256, s, c, x, dx);
 }
 
-void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
-                        bool first) {
-    const int n = end - begin;
-    if (n <= 0) return;
-    if (first) go(k_contacts_gs<true>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
-    else go(k_contacts_gs<false>, nblk(n, 128), 128, s, c, face_list, begin, end, x);
+void launch_contact_lists(const Launch& s, const ContactArrays& c, const int* ifl, const int* ifo_off, int ncol,
+                          int n_inst, int* act_faces, int* act_off) {
+    if (n_inst > 0 && c.F > 0) go(k_contact_lists, n_inst, kContactListThreads, s, c, ifl, ifo_off, ncol, act_faces, act_off);
+}
+
+void launch_contacts_gs_lists(const Launch& s, const ContactArrays& c, const int* act_faces, const int* act_off,
+                              int ncol, int n_inst, float4* x, bool first) {
+    if (n_inst > 0 && c.F > 0 && ncol > 0)
+        go(k_contacts_gs_lists, n_inst, kContactListThreads, s, c, act_faces, act_off, ncol, x, first);
 }
 
 void launch_prim_eval(cudaStream_t s, const float4* prim, const float4* pts, int n, float4* out) {

@@ -223,8 +223,14 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
 // min_blocks (variant 2): 0 = no register cap, 6 or 8 blocks per SM
 int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
-void launch_contacts_gs(const Launch& s, const ContactArrays& c, const int* face_list, int begin, int end, float4* x,
-                        bool first);
+// after a detection: per instance and face colour, the faces with an active
+// static contact (ifl: faces by instance, colour, index; ifo_off its ranges)
+constexpr int kContactListThreads = 512;
+void launch_contact_lists(const Launch& s, const ContactArrays& c, const int* ifl, const int* ifo_off, int ncol,
+                          int n_inst, int* act_faces, int* act_off);
+// every colour's Gauss-Seidel contacts in one launch, one block per instance
+void launch_contacts_gs_lists(const Launch& s, const ContactArrays& c, const int* act_faces, const int* act_off,
+                              int ncol, int n_inst, float4* x, bool first);
 // prim: one 3-float4 primitive entry; out[i] = (sdf, gradient) at pts[i]
 void launch_prim_eval(cudaStream_t s, const float4* prim, const float4* pts, int n, float4* out);
 // sphere_table: 3 float4 per (instance, slot) primitive entry
