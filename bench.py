@@ -424,9 +424,9 @@ def run_ours(args):
     for _ in range(e2e_steps):
         s.set_positions(x_host)           # H2D of the step's input state
         one_step()
-        x_host = s.positions()            # D2H of the step's result (synchronises)
+        s.positions(out=x_host)           # D2H of the step's result into the same host array (synchronises)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
-    h2d = d2h = 16 * w.V
+    h2d = d2h = int(x_host.nbytes)        # the caller's (V, 3) float64 arrays
 
     # ---- kernel roofline ----
     # Per-kernel launch counts and the small kernels' durations come from an

@@ -1082,6 +1082,17 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
 
     // device allocation + upload
     XPBD_CU(c, cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+    {
+        // coherent access to pageable host memory (Grace-Blackwell C2C): the
+        // position transfers run as kernels on the caller's arrays
+        int dev = 0, pma = 0;
+        XPBD_CU(c, cudaGetDevice(&dev));
+        if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+            cudaGetLastError();
+            pma = 0;
+        }
+        c->host_direct = pma == 1;
+    }
     XPBD_CU(c, c->x.alloc(V));
     XPBD_CU(c, c->prev.alloc(V));
     XPBD_CU(c, c->vel.alloc(V));
@@ -1287,17 +1298,43 @@ int xpbd_set_num_iters(xpbd_ctx* c, int32_t n) {
     return XPBD_OK;
 }
 
+}  // extern "C"
+
+namespace {
+// the device reads or writes the caller's array itself; returns after the
+// transfer, so the caller may reuse the array
+template <typename H>
+int host_direct_in(xpbd_ctx* c, float4* dst, const H* h, bool keep_w) {
+    launch_xyz_from_host(c->stream, dst, h, c->V, keep_w);
+    XPBD_CU(c, cudaGetLastError());
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+template <typename H>
+int host_direct_out(xpbd_ctx* c, H* h, const float4* src) {
+    launch_xyz_to_host(c->stream, h, src, c->V);
+    XPBD_CU(c, cudaGetLastError());
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    return XPBD_OK;
+}
+}  // namespace
+
+extern "C" {
+
 int xpbd_set_positions(xpbd_ctx* c, const double* x) {
     if (!c || !x) return XPBD_ERR_INVALID;
+    if (c->host_direct) return host_direct_in(c, c->x.p, x, true);
     return stage_positions_to_device(c, x, nullptr);
 }
 
 int xpbd_set_positions_f32(xpbd_ctx* c, const float* x) {
     if (!c || !x) return XPBD_ERR_INVALID;
+    if (c->host_direct) return host_direct_in(c, c->x.p, x, true);
     return stage_positions_to_device(c, nullptr, x);
 }
 
 static int get_xyz(xpbd_ctx* c, const float4* src, double* out) {
+    if (c->host_direct) return host_direct_out(c, out, src);
     int st = fetch(c, src);
     if (st) return st;
     for (int i = 0; i < c->V; i++) {
@@ -1315,6 +1352,7 @@ int xpbd_get_positions(xpbd_ctx* c, double* x) {
 
 int xpbd_get_positions_f32(xpbd_ctx* c, float* x) {
     if (!c || !x) return XPBD_ERR_INVALID;
+    if (c->host_direct) return host_direct_out(c, x, c->x.p);
     int st = fetch(c, c->x.p);
     if (st) return st;
     for (int i = 0; i < c->V; i++) {
@@ -1332,6 +1370,7 @@ int xpbd_get_prev_positions(xpbd_ctx* c, double* x) {
 
 int xpbd_set_velocities(xpbd_ctx* c, const double* v) {
     if (!c || !v) return XPBD_ERR_INVALID;
+    if (c->host_direct) return host_direct_in(c, c->vel.p, v, false);
     for (int i = 0; i < c->V; i++)
         c->h_stage[i] = make_float4((float)v[3 * i], (float)v[3 * i + 1], (float)v[3 * i + 2], 0.f);
     XPBD_CU(c, cudaMemcpyAsync(c->vel.p, c->h_stage, sizeof(float4) * c->V, cudaMemcpyHostToDevice, c->stream));

@@ -142,6 +142,9 @@ struct xpbd_ctx {
 
     // pinned staging
     float4* h_stage = nullptr;
+    // the device addresses pageable host memory coherently (Grace-Blackwell):
+    // positions cross the boundary by kernels on the caller's own arrays
+    bool host_direct = false;
     double* h_rows = nullptr;
     int h_rows_cap = 0;
     int last_rows = 0;

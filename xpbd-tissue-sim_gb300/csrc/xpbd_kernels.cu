@@ -1802,6 +1802,26 @@ __global__ void k_self_contacts_jacobi(SelfArrays a, const int4* __restrict__ fa
     for (int i = 0; i < 4; i++) add_vec4(dx + ids[i], d[i][0], d[i][1], d[i][2]);
 }
 
+// ---- host arrays the device addresses directly (coherent pageable memory
+// on a Grace-Blackwell system): 3 values per vertex, converted here ----
+template <typename H>
+__global__ void k_xyz_from_host(float4* __restrict__ x, const H* __restrict__ h, int V, bool keep_w) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float w = keep_w ? x[i].w : 0.f;  // inverse mass and fixed sign stay
+    x[i] = make_float4((float)h[3 * (size_t)i], (float)h[3 * (size_t)i + 1], (float)h[3 * (size_t)i + 2], w);
+}
+
+template <typename H>
+__global__ void k_xyz_to_host(H* __restrict__ h, const float4* __restrict__ x, int V) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float4 p = x[i];
+    h[3 * (size_t)i] = (H)p.x;
+    h[3 * (size_t)i + 1] = (H)p.y;
+    h[3 * (size_t)i + 2] = (H)p.z;
+}
+
 __global__ void k_finalize(float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel, int V,
                            float dt, bool write_vel) {
     pdl_wait_then_release();
@@ -2629,6 +2649,19 @@ void launch_self_contacts(const Launch& s, const SelfArrays& a, const int4* face
     if (jacobi) go(k_self_contacts_jacobi, nblk(a.n_surf, 128), 128, s, a, faces, (const float4*)x, dx, first,
                    alpha_tilde, flags);
     else go(k_self_contacts_gs, 1, 32, s, a, faces, x, first, alpha_tilde, flags);
+}
+
+void launch_xyz_from_host(cudaStream_t s, float4* x, const double* h, int V, bool keep_w) {
+    if (V > 0) k_xyz_from_host<double><<<nblk(V, 256), 256, 0, s>>>(x, h, V, keep_w);
+}
+void launch_xyz_from_host(cudaStream_t s, float4* x, const float* h, int V, bool keep_w) {
+    if (V > 0) k_xyz_from_host<float><<<nblk(V, 256), 256, 0, s>>>(x, h, V, keep_w);
+}
+void launch_xyz_to_host(cudaStream_t s, double* h, const float4* x, int V) {
+    if (V > 0) k_xyz_to_host<double><<<nblk(V, 256), 256, 0, s>>>(h, x, V);
+}
+void launch_xyz_to_host(cudaStream_t s, float* h, const float4* x, int V) {
+    if (V > 0) k_xyz_to_host<float><<<nblk(V, 256), 256, 0, s>>>(h, x, V);
 }
 
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,

@@ -255,6 +255,12 @@ void launch_rigid_velocity(const Launch& s, double* rb, int nb, double dt);
 void launch_self_detect(const Launch& s, const SelfArrays& a, const SelfGrid& g, const float4* x, const int4* faces);
 void launch_self_contacts(const Launch& s, const SelfArrays& a, const int4* faces, float4* x, float4* dx,
                           bool jacobi, bool first, float alpha_tilde, Flags* flags);
+// positions and velocities from / to host arrays the device can address
+// (keep_w: the float4's w is left as it is; else 0)
+void launch_xyz_from_host(cudaStream_t s, float4* x, const double* h, int V, bool keep_w);
+void launch_xyz_from_host(cudaStream_t s, float4* x, const float* h, int V, bool keep_w);
+void launch_xyz_to_host(cudaStream_t s, double* h, const float4* x, int V);
+void launch_xyz_to_host(cudaStream_t s, float* h, const float4* x, int V);
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
                       int end, float4* x, bool first);
 void launch_attach_jacobi(const Launch& s, const int* vert, const float4* target, float* lam, int n, const float4* x,

@@ -303,8 +303,12 @@ class XPBDSolver:
             raise XPBDError(st, self.L.xpbd_last_error(self.h).decode())
 
     # ---- state ----
-    def positions(self) -> np.ndarray:
-        out = np.zeros((self.V, 3))
+    def positions(self, out=None) -> np.ndarray:
+        """Current positions (V, 3) float64; into `out` (C-contiguous float64) when given."""
+        if out is None:
+            out = np.zeros((self.V, 3))
+        elif out.dtype != np.float64 or not out.flags.c_contiguous or out.shape != (self.V, 3):
+            raise ValueError("out must be a C-contiguous (V, 3) float64 array")
         self._ck(self.L.xpbd_get_positions(self.h, _p(out)))
         return out
 
