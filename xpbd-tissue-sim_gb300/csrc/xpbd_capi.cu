@@ -731,21 +731,72 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         }
         doff[j + 1] = (int)dep.size();
     }
-    const int per_sm = sweep_dataflow_blocks_per_sm(c->prm.gs_variant == 3, c->prm.gs_min_blocks);
+    const bool staged = c->prm.gs_variant == 3;
+    const int per_sm = sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
     XPBD_CU(c, cudaGetDevice(&dev));
     XPBD_CU(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
     if (per_sm <= 0 || sms <= 0) return fail(c, XPBD_ERR_CUDA, "dataflow sweep: no co-resident blocks");
-    c->ntasks = NT;
     c->flow_grid = per_sm * sms;
-    XPBD_CU(c, c->flow_tasks.alloc(NT));
-    XPBD_CU(c, c->flow_dep_off.alloc(NT + 1));
+    if (!staged) {
+        // no more warps than the largest colour has tasks
+        int maxc = 0;
+        for (int j0 = 0; j0 < NT;) {
+            int j1 = j0;
+            while (j1 < NT && tcol[j1] == tcol[j0]) j1++;
+            maxc = std::max(maxc, j1 - j0);
+            j0 = j1;
+        }
+        const int wpb = kPatchBlock / 32;
+        c->flow_grid = std::max(1, std::min(c->flow_grid, (maxc + wpb - 1) / wpb));
+        // Warp w runs tasks w, w + W, w + 2W, ... (W warps). Each colour's run
+        // of tasks is padded with empty tasks to a multiple of W, so warp w
+        // gets the k-th task of every colour with k = w mod W: the same part of
+        // the mesh colour after colour, whose dependencies are its own earlier
+        // tasks and its neighbours'.
+        const int W = c->flow_grid * (kPatchBlock / 32);
+        std::vector<int> newpos(NT);
+        int padded = 0;
+        for (int j0 = 0; j0 < NT;) {
+            int j1 = j0;
+            while (j1 < NT && tcol[j1] == tcol[j0]) j1++;
+            for (int j = j0; j < j1; j++) newpos[j] = padded + (j - j0);
+            padded += (j1 - j0 + W - 1) / W * W;
+            j0 = j1;
+        }
+        std::vector<int4> tp(padded, make_int4(0, 0, 0, 0));
+        std::vector<int> real(padded, -1);
+        for (int j = 0; j < NT; j++) {
+            tp[newpos[j]] = tasks[j];
+            real[newpos[j]] = j;
+        }
+        std::vector<int> dp_off(padded + 1, 0), dp;
+        for (int i = 0; i < padded; i++) {
+            if (real[i] >= 0)
+                for (int e = doff[real[i]]; e < doff[real[i] + 1]; e++) {
+                    const int d = newpos[dep[e] >> 1];
+                    // the same warp ran that task earlier (this iteration for a
+                    // lower colour, the previous one for a higher): program
+                    // order and the warp barrier before the loads cover it
+                    if (d % W == i % W) continue;
+                    dp.push_back((d << 1) | (dep[e] & 1));
+                }
+            dp_off[i + 1] = (int)dp.size();
+        }
+        tasks.swap(tp);
+        doff.swap(dp_off);
+        dep.swap(dp);
+    }
+    const int NTP = (int)tasks.size();
+    c->ntasks = NTP;
+    XPBD_CU(c, c->flow_tasks.alloc(NTP));
+    XPBD_CU(c, c->flow_dep_off.alloc(NTP + 1));
     XPBD_CU(c, c->flow_dep.alloc(std::max<size_t>(dep.size(), 1)));
-    XPBD_CU(c, c->flow_epoch.alloc(NT + 1));
-    XPBD_CU(c, cudaMemcpy(c->flow_tasks.p, tasks.data(), sizeof(int4) * NT, cudaMemcpyHostToDevice));
-    XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NT + 1), cudaMemcpyHostToDevice));
+    XPBD_CU(c, c->flow_epoch.alloc(NTP + 1));
+    XPBD_CU(c, cudaMemcpy(c->flow_tasks.p, tasks.data(), sizeof(int4) * NTP, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NTP + 1), cudaMemcpyHostToDevice));
     if (!dep.empty()) XPBD_CU(c, cudaMemcpy(c->flow_dep.p, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
-    XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NT + 1)));
+    XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NTP + 1)));
     return XPBD_OK;
 }
 
