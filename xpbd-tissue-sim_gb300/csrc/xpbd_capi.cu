@@ -747,14 +747,14 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
             maxc = std::max(maxc, j1 - j0);
             j0 = j1;
         }
-        const int wpb = kPatchBlock / 32;
+        const int wpb = kFlowBlock / 32;
         c->flow_grid = std::max(1, std::min(c->flow_grid, (maxc + wpb - 1) / wpb));
         // Warp w runs tasks w, w + W, w + 2W, ... (W warps). Each colour's run
         // of tasks is padded with empty tasks to a multiple of W, so warp w
         // gets the k-th task of every colour with k = w mod W: the same part of
         // the mesh colour after colour, whose dependencies are its own earlier
         // tasks and its neighbours'.
-        const int W = c->flow_grid * (kPatchBlock / 32);
+        const int W = c->flow_grid * (kFlowBlock / 32);
         std::vector<int> newpos(NT);
         int padded = 0;
         for (int j0 = 0; j0 < NT;) {

@@ -2566,14 +2566,14 @@ int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks) {
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow_staged<false>, kPatchBlock, 0);
     } else if (min_blocks == 8) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 8>, kPatchBlock, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 8>, kPatchBlock, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 8>, kFlowBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 8>, kFlowBlock, 0);
     } else if (min_blocks == 6) {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 6>, kPatchBlock, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 6>, kPatchBlock, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 6>, kFlowBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 6>, kFlowBlock, 0);
     } else {
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 1>, kPatchBlock, 0);
-        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 1>, kPatchBlock, 0);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_dataflow<true, 1>, kFlowBlock, 0);
+        if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_dataflow<false, 1>, kFlowBlock, 0);
     }
     if (e != cudaSuccess) return 0;
     return n < m ? n : m;
@@ -2585,7 +2585,7 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
     if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3(kPatchBlock);
+    cfg.blockDim = dim3(staged ? kPatchBlock : kFlowBlock);
     cfg.stream = s.s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;

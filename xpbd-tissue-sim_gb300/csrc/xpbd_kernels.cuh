@@ -100,6 +100,9 @@ enum RigidField {
 // reached the right iteration (lower colours: this one, higher colours: the
 // previous one), which is exactly the order of the colour-by-colour launches.
 constexpr int kTaskPatches = 32;
+// threads per block of the (register-prefetch) dataflow launch: one warp, so
+// the warps spread evenly over the SMs
+constexpr int kFlowBlock = 32;
 struct TaskArrays {
     const int4* task;     // [ntasks] first patch, patch count, first slot, slot count;
                           // tasks in colour order
