@@ -228,3 +228,37 @@ def test_free_bodies_from_config(lib, tmp_path):
         w = w / np.sqrt(1 + (1e-3 * w / 2) ** 2)
     assert abs(stone[3][2] - w) < 1e-12
     s.close()
+
+
+def test_free_body_in_a_batch_instance(lib):
+    """Two instances in one context, a fixed sphere on instance 0 and a free
+    sphere on instance 1: instance 1 and its body follow the same instance
+    stepped alone (to FP32 rounding drift of the shared colouring), and
+    instance 0 does not feel the free body."""
+    r = 0.03
+    m, inertia = _sphere(r)
+    X, tets, faces = G.grid_mesh(4, 4, 4, 0.1 / 4)
+    fixed = X[:, 2] == 0
+    c1 = np.array([0.05, 0.047, 0.1 + r + 0.0005])
+    kw = dict(num_iters=8, collision_rate=1000.0)
+    b = G.XPBDSolver(instances=[(X, tets, faces, 2e4, 0.45, 1000.0), (X, tets, faces, 2e4, 0.45, 1000.0)], **kw)
+    b.fix_vertices(np.concatenate([fixed, fixed]))
+    b.set_sdfs([G.SDF_SPHERE], [[0.05, 0.05, 0.16]], [[0, 0, 0, 1.0]], [[0.02, 0, 0]], instance=0)
+    b.set_sdfs([G.SDF_SPHERE], [c1], [[0, 0, 0, 1.0]], [[r, 0, 0]], instance=1)
+    b.set_rigid_body(0, m, inertia, [0, 0, -0.4], [0, 0, 0], instance=1)
+    one = G.XPBDSolver(X, tets, faces, 2e4, 0.45, 1000.0, **kw)
+    one.fix_vertices(fixed)
+    one.set_sdfs([G.SDF_SPHERE], [c1], [[0, 0, 0, 1.0]], [[r, 0, 0]])
+    one.set_rigid_body(0, m, inertia, [0, 0, -0.4], [0, 0, 0])
+    for _ in range(30):
+        b.step(1)
+        one.step(1)
+    V = len(X)
+    xb = b.positions()
+    assert np.abs(xb[V:] - one.positions()).max() <= 1e-4 * 0.1
+    for a, e in zip(b.rigid_body(0, instance=1), one.rigid_body(0)):
+        assert np.abs(a - e).max() <= 1e-4 * 0.1 / 1e-3
+    with pytest.raises(G.XPBDError):
+        b.rigid_body(0, instance=0)
+    assert np.all(np.isfinite(xb[:V])) and b.health()[0] == 0
+    b.close(); one.close()
