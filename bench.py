@@ -146,7 +146,7 @@ def measured_peaks():
 def profiled_traffic(kernel, workload_name, variant):
     """DRAM bytes per launch of `kernel` from the committed ncu figures
     (profiles/roofline_traffic.txt: `workload/kernel/v<variant> bytes summary`
-    lines; a launch is one colour for variants 0/1, one substep for 2/3)."""
+    lines; a launch is one colour for variants 0/1, one substep for 2-4)."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(p):
         return None
@@ -646,7 +646,7 @@ def main():
     ap.add_argument("--patch-tets", type=int, default=None, help="Gauss-Seidel patch size (1 = per-tet colouring)")
     ap.add_argument("--no-pdl", action="store_true", help="disable programmatic dependent launch")
     ap.add_argument("--min-blocks", type=int, default=0, choices=[0, 6, 8], help="patch kernel blocks/SM target")
-    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3], help="Gauss-Seidel sweep kernel variant")
+    ap.add_argument("--variant", type=int, default=None, choices=[0, 1, 2, 3, 4], help="Gauss-Seidel sweep kernel variant")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

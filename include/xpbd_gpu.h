@@ -103,7 +103,10 @@ typedef struct {
                                /* dependency counters (combined constraints, no    */
                                /* faces, no per-iteration residual; else as 0);    */
                                /* 3 dataflow with records staged by bulk copies    */
-                               /* (else as 1); default 2                           */
+                               /* (else as 1); 4 dataflow on version-stamped       */
+                               /* vertices: a patch polls the versions of its own  */
+                               /* vertices, no task counters or fences (else as 0);*/
+                               /* default 4                                        */
     int32_t num_local_collision_iters; /* num-local-collision-iters: passes    */
                                /* after the global solve over every contact    */
                                /* and the tets touching a vertex of a contact  */

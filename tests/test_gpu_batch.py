@@ -100,7 +100,7 @@ def test_batch_full_size_runs(lib):
     s.close()
 
 
-@pytest.mark.parametrize("solver,ncand", [(G.SOLVER_GAUSS_SEIDEL, 40), (G.SOLVER_JACOBI, 12)])
+@pytest.mark.parametrize("solver,ncand", [(G.SOLVER_GAUSS_SEIDEL, 48), (G.SOLVER_JACOBI, 12)])
 def test_autotuner_times_every_candidate_and_keeps_the_fastest(lib, solver, ncand):
     b = _small_batch(n=3)
     inst = [(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances]

@@ -71,12 +71,14 @@ def _oracle_pair(X, tets, faces, E, nu, rho, solver, iters, gpu=None, **kw):
 @pytest.mark.parametrize("solver,cap,var", [(G.SOLVER_JACOBI, 0, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 0),
                                             (G.SOLVER_GAUSS_SEIDEL, 1, 0), (G.SOLVER_GAUSS_SEIDEL, 5, 1),
                                             (G.SOLVER_GAUSS_SEIDEL, 5, 2), (G.SOLVER_GAUSS_SEIDEL, 2, 2),
-                                            (G.SOLVER_GAUSS_SEIDEL, 5, 3)])
+                                            (G.SOLVER_GAUSS_SEIDEL, 5, 3), (G.SOLVER_GAUSS_SEIDEL, 5, 4),
+                                            (G.SOLVER_GAUSS_SEIDEL, 2, 4)])
 def test_cube_trajectory_matches_fp64_oracle(lib, solver, cap, var):
     """Config-1 mesh (10^3 hexes, bottom fixed, seeded noise): 20 steps at the
     spec bound, then 100 steps within the FP32 band. Gauss-Seidel runs
     with hex patches (cap 5), per-tet colouring (cap 1), and every sweep
-    kernel variant (registers, shared-memory staging, dataflow)."""
+    kernel variant (registers, shared-memory staging, dataflow on task
+    counters, dataflow on vertex versions)."""
     w = W.cube()
     s = G.XPBDSolver(w.X, w.tets, None, w.E, w.nu, w.rho, num_iters=10, solver_type=solver, gs_patch_tets=cap,
                      gs_variant=var)
@@ -194,7 +196,8 @@ def test_gather_variant_is_deterministic_and_matches_atomic(lib):
 
 
 @pytest.mark.parametrize("solver,var", [(G.SOLVER_JACOBI, 0), (G.SOLVER_GAUSS_SEIDEL, 0),
-                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2)])
+                                        (G.SOLVER_GAUSS_SEIDEL, 1), (G.SOLVER_GAUSS_SEIDEL, 2),
+                                        (G.SOLVER_GAUSS_SEIDEL, 4)])
 def test_graph_and_direct_launch_agree(lib, solver, var):
     w = W.cube(n=5)
     out = []
@@ -458,20 +461,21 @@ def test_dataflow_single_sweep_matches_launch_order(lib):
     launches differ by FP32 rounding at most (an ordering error would show as
     a whole Gauss-Seidel update, ~1e-5 m here)."""
     a = _run_flow_case(0, 1, 1)[0]
-    for var in (1, 2, 3):
+    for var in (1, 2, 3, 4):
         b = _run_flow_case(var, 1, 1)[0]
         assert np.abs(a - b).max() <= 4e-8, (var, np.abs(a - b).max())
 
 
-@pytest.mark.parametrize("var", [2, 3])
+@pytest.mark.parametrize("var", [2, 3, 4])
 @pytest.mark.parametrize("policy", [G.RESIDUAL_NEVER, G.RESIDUAL_EVERY_SUBSTEP, G.RESIDUAL_EVERY_ITERATION])
 def test_dataflow_sweep_is_deterministic_and_close(lib, policy, var):
     """Sweep variants 2 and 3 (one cooperative launch, per-task dependency
     counters; 3 with bulk-copied records) project the same patches in the
-    same order as the colour-by-colour launches of variants 0 and 1: results
-    do not depend on timing (bit-identical reruns) and stay within FP32
-    rounding drift of the launches after 25 steps x 12 iterations; with the
-    per-iteration residual they run those launches themselves."""
+    same order as the colour-by-colour launches of variants 0 and 1, and
+    variant 4 (vertex versions) in the same order as variant 2: results do
+    not depend on timing (bit-identical reruns) and stay within FP32
+    rounding drift of the reference variant after 25 steps x 12 iterations;
+    with the per-iteration residual they run the colour launches themselves."""
     r0 = _run_flow_case(var, 12, 25, policy)
     r1 = _run_flow_case(var, 12, 25, policy)
     ref = _run_flow_case(var - 2, 12, 25, policy)
@@ -485,7 +489,7 @@ def test_dataflow_sweep_is_deterministic_and_close(lib, policy, var):
         np.testing.assert_allclose(r0[2], ref[2], rtol=1e-3, atol=1e-6 * ref[2][0])
 
 
-@pytest.mark.parametrize("var", [2, 3])
+@pytest.mark.parametrize("var", [2, 3, 4])
 def test_dataflow_sweep_full_block(lib, var):
     """The 1.31M-tet block, one kinematically driven step: variant 2 is
     reproducible bit for bit and within FP32 rounding of variant 0. (Over

@@ -36,12 +36,17 @@ bool valid_params(const xpbd_params& p) {
            (p.use_graphs == 0 || p.use_graphs == 1) && (p.use_pdl == 0 || p.use_pdl == 1) &&
            p.gs_patch_tets >= 0 && p.gs_patch_tets <= kMaxPatchTets &&
            (p.gs_min_blocks == 0 || p.gs_min_blocks == 6 || p.gs_min_blocks == 8) &&
-           p.gs_variant >= 0 && p.gs_variant <= 3 && p.num_local_collision_iters >= 0 &&
+           p.gs_variant >= 0 && p.gs_variant <= 4 && p.num_local_collision_iters >= 0 &&
            p.num_local_collision_iters <= 1000 && (p.first_order == 0 || p.first_order == 1) &&
            (p.adjust_damping_to_material == 0 || p.adjust_damping_to_material == 1) &&
            (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier))) &&
            (p.self_collisions == 0 || p.self_collisions == 1);
 }
+
+// The colour-launch kernel that stands in for a GS variant where the one-launch
+// sweeps do not apply (contacts, attachments, residual every iteration):
+// 0 = registers, 1 = staged records.
+int patch_kernel_variant(int gs_variant) { return gs_variant == 1 || gs_variant == 3 ? 1 : 0; }
 
 // Gauss-Seidel patch: a run of consecutive tets on at most kMaxPatchVerts
 // vertices, each tet sharing a vertex with the run.
@@ -359,14 +364,25 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
-    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() && (p.gs_variant == 2 || p.gs_variant == 3) &&
-               c->ntasks > 0) {
+    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() &&
+               (p.gs_variant == 2 || p.gs_variant == 3 || p.gs_variant == 4) && c->ntasks > 0) {
         // every iteration and colour in one cooperative launch
         if (track && !warm) exact_residual_row(c, 0, false);
-        cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
+        if (p.gs_variant == 4) {
+            // the abort flag (after the epochs, which variant 4 does not use)
+            cudaMemsetAsync(c->flow_epoch.p + c->ntasks, 0, sizeof(unsigned), s);
+        } else {
+            cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
+        }
         Scope sc(c, K_PROJECT_GS);
-        launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
-                              c->flow_grid, p.gs_variant == 3, p.gs_min_blocks);
+        if (p.gs_variant == 4) {
+            launch_sweep_versioned(c->L(), c->tets(), c->patches(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
+                                   c->xv.p, c->patch_w.p, c->V, c->npatches, c->flags.p, c->flow_grid,
+                                   p.gs_min_blocks);
+            c->launches += 2;  // the copies into and out of the versioned positions
+        } else
+            launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
+                                  c->flow_grid, p.gs_variant == 3, p.gs_min_blocks);
     } else {
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
         for (int it = 0; it < iters; it++) {
@@ -382,7 +398,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                     Scope sc(c, K_PROJECT_GS);
                     launch_project_patches(c->L(), c->tets(), c->patches(), c->pcol_off[col], c->pcol_off[col + 1],
                                            c->x.p, f, which, c->flags.p, c->prm.gs_min_blocks ? c->prm.gs_min_blocks : 6,
-                                           c->prm.gs_variant == 2 ? 0 : (c->prm.gs_variant == 3 ? 1 : c->prm.gs_variant));
+                                           patch_kernel_variant(c->prm.gs_variant));
                 }
             }
             if (have_faces) {
@@ -664,6 +680,7 @@ void release(xpbd_ctx* c) {
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
+    c->patch_ver.release(); c->xv.release(); c->patch_w.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
     c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
@@ -732,7 +749,8 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         doff[j + 1] = (int)dep.size();
     }
     const bool staged = c->prm.gs_variant == 3;
-    const int per_sm = sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
+    const int per_sm = c->prm.gs_variant == 4 ? sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks)
+                                              : sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
     XPBD_CU(c, cudaGetDevice(&dev));
     XPBD_CU(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -797,6 +815,41 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
     XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NTP + 1), cudaMemcpyHostToDevice));
     if (!dep.empty()) XPBD_CU(c, cudaMemcpy(c->flow_dep.p, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NTP + 1)));
+    if (c->prm.gs_variant == 4) {
+        // per patch and vertex slot: deg << 8 | pre, deg = patches containing
+        // the vertex, pre = those of a lower colour
+        std::vector<int> pcol(P);
+        for (int col = 0; col < c->n_tet_colours; col++)
+            for (int q = c->pcol_off[col]; q < c->pcol_off[col + 1]; q++) pcol[q] = col;
+        std::vector<int> vp_off(V + 1, 0);
+        for (int q = 0; q < P; q++)
+            for (int k = 0; k < (pmeta[q].y >> 8); k++) vp_off[pv(q, k) + 1]++;
+        for (int v = 0; v < V; v++) vp_off[v + 1] += vp_off[v];
+        std::vector<int> vcol(vp_off[V]), vfill(vp_off.begin(), vp_off.end() - 1);
+        for (int q = 0; q < P; q++)
+            for (int k = 0; k < (pmeta[q].y >> 8); k++) vcol[vfill[pv(q, k)]++] = pcol[q];
+        std::vector<int4> ver(P, make_int4(0, 0, 0, 0));
+        for (int q = 0; q < P; q++) {
+            int w[4] = {0, 0, 0, 0};
+            for (int k = 0; k < (pmeta[q].y >> 8); k++) {
+                const int v = pv(q, k), deg = vp_off[v + 1] - vp_off[v];
+                int pre = 0, same = 0;
+                for (int e = vp_off[v]; e < vp_off[v + 1]; e++) {
+                    pre += vcol[e] < pcol[q];
+                    same += vcol[e] == pcol[q];
+                }
+                if (same != 1) return fail(c, XPBD_ERR_STATE, "dataflow: vertex %d in two patches of colour %d", v, pcol[q]);
+                if (deg > 255) return fail(c, XPBD_ERR_STATE, "dataflow: vertex %d in %d patches (at most 255)", v, deg);
+                w[k >> 1] |= ((deg << 8) | pre) << (16 * (k & 1));
+            }
+            ver[q] = make_int4(w[0], w[1], w[2], w[3]);
+        }
+        XPBD_CU(c, c->patch_ver.alloc(P));
+        XPBD_CU(c, c->xv.alloc(V));
+        XPBD_CU(c, c->patch_w.alloc(2 * (size_t)P));
+        c->npatches = P;
+        XPBD_CU(c, cudaMemcpy(c->patch_ver.p, ver.data(), sizeof(int4) * P, cudaMemcpyHostToDevice));
+    }
     return XPBD_OK;
 }
 
@@ -1200,7 +1253,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     }
     // (faces allow contacts, which the dataflow sweep leaves to the launches)
-    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && (p.gs_variant == 2 || p.gs_variant == 3) &&
+    if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2 &&
         F == 0) {
         int st = build_flow_tasks(c, pmeta, pverts);
         if (st) return st;
@@ -1273,7 +1326,7 @@ int xpbd_default_params(xpbd_params* p) {
     p->use_pdl = 1;
     p->gs_patch_tets = 0;
     p->gs_min_blocks = 0;
-    p->gs_variant = 2;
+    p->gs_variant = 4;
     p->num_local_collision_iters = 0;
     p->first_order = 0;
     p->adjust_damping_to_material = 0;
@@ -2057,8 +2110,8 @@ int xpbd_autotune(const xpbd_mesh_desc* meshes, int32_t n_inst, xpbd_params* par
     if (base.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
         for (int patch : {1, 2, 3, 5})
             for (int pdl : {0, 1})
-                // variant x min blocks: (0,-) (1,6) (1,8) (2,uncapped) (3,-)
-                for (int var_minb : {6, 16, 18, 20, 30}) {
+                // variant x min blocks: (0,-) (1,6) (1,8) (2,uncapped) (3,-) (4,uncapped)
+                for (int var_minb : {6, 16, 18, 20, 30, 40}) {
                     xpbd_params q = base;
                     q.gs_patch_tets = patch;
                     q.use_pdl = pdl;

@@ -93,11 +93,15 @@ struct xpbd_ctx {
     DevBuf<int> d_att_v, d_att_order;
     DevBuf<float4> d_att_target;
     DevBuf<float> d_att_lam;
-    // dataflow Gauss-Seidel (sweep variant 2): tasks, dependencies, epochs
+    // dataflow Gauss-Seidel (sweep variants 2-4): tasks, dependencies, epochs
     int ntasks = 0, flow_grid = 0;
     DevBuf<int4> flow_tasks;
     DevBuf<int> flow_dep_off, flow_dep;
     DevBuf<unsigned> flow_epoch;  // ntasks epochs + the abort flag
+    DevBuf<int4> patch_ver;       // variant 4: per patch, 8 x 16-bit deg << 8 | pre
+    DevBuf<float4> xv;            // variant 4: version-stamped positions
+    DevBuf<float4> patch_w;       // variant 4: per patch, its 8 inverse masses
+    int npatches = 0;
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;

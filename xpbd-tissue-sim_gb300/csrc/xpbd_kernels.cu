@@ -188,79 +188,79 @@ __device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R g
             gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
 }
 
-// FP32 fast path of tet_eval: the same quantities with a shorter dependency
-// chain -- tree-shaped sums instead of left-to-right accumulation, 1/||F||
-// from rsqrt, 1/J from the hardware reciprocal. Results differ from tet_eval
-// only by FP32 rounding (a few ulp); near-degenerate elements never use it.
-__device__ __forceinline__ void tet_eval_fast(const TetState<float>& s, float& Cd, float& Ch, float gd[9], float gh[9],
-                                              float& J) {
-    float F[9];
-    tet_F(s, F);
-    const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
-                      (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
-    const float invC = rsqrtf(ss);
-    Cd = ss * invC;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            gd[3 * i + k] = invC * fmaf(F[k], s.q[i], fmaf(F[3 + k], s.q[3 + i], F[6 + k] * s.q[6 + i]));
-    float Fc[9];
-    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
-    // det F = f0 . (f1 x f2), the same cofactors as the gradient
-    J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
-    float fac;
-    if (J >= 1.f) {
-        Ch = -s.gam + logf(J);
-        fac = __frcp_rn(J);
-    } else {
-        const float d = J - 1.f;
-        Ch = -s.gam + d - d * d * 0.5f + d * d * d * (1.f / 3.f);
-        fac = fmaf(d, d, 1.f - d);
-    }
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            gh[3 * i + k] = fac * fmaf(Fc[k], s.q[i], fmaf(Fc[3 + k], s.q[3 + i], Fc[6 + k] * s.q[6 + i]));
-}
-
 __device__ __forceinline__ float dot3(const float* a, const float* b) {
     return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
 }
 
 // FP32 fast path of the combined 2x2 projection (same contract as
-// tet_project_combined below).
+// tet_project_combined below), with a shorter dependency chain:
+// - the gradients are formed unscaled, G_i = F q_i and H_i = cof(F) q_i (q_i
+//   the rows of Q, q_3 = -q_0 - q_1 - q_2), so they do not wait for 1/||F||
+//   (rsqrt) or the hydrostatic factor; both scales enter the 2x2 system and
+//   the update as scalars: grad C_dev,i = G_i / ||F||, grad C_hyd,i = fac H_i
+//   (DeviatoricConstraint.hpp:112-152, HydrostaticConstraint.hpp:123-221);
+// - tree-shaped sums, 1/||F|| from rsqrt, 1/J and 1/det from the hardware
+//   reciprocal; det F from the cofactors the gradient uses.
+// Results differ from tet_project_combined only by FP32 rounding (a few ulp);
+// near-degenerate elements never use it.
 __device__ __forceinline__ void tet_project_combined_fast(const TetState<float>& s, float lam0, float lam1, float& r0,
                                                           float& r1, float& dl0, float& dl1, float d[4][3], float& J) {
-    float Cd, Ch, gd[9], gh[9];
-    tet_eval_fast(s, Cd, Ch, gd, gh, J);
-    float gd3[3], gh3[3];
+    float F[9];
+    tet_F(s, F);
+    const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
+                      (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
+    const float invC = rsqrtf(ss);
+    const float Cd = ss * invC;
+    float Fc[9];
+    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
+    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
+    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
+    J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
+    float Ch, fac;
+    if (J >= 1.f) {
+        Ch = -s.gam + logf(J);
+        fac = __frcp_rn(J);
+    } else {
+        const float dd = J - 1.f;
+        Ch = -s.gam + dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f);
+        fac = fmaf(dd, dd, 1.f - dd);
+    }
+    float G[12], H[12];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+            G[3 * i + k] = fmaf(F[k], s.q[i], fmaf(F[3 + k], s.q[3 + i], F[6 + k] * s.q[6 + i]));
+            H[3 * i + k] = fmaf(Fc[k], s.q[i], fmaf(Fc[3 + k], s.q[3 + i], Fc[6 + k] * s.q[6 + i]));
+        }
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-        gd3[k] = -(gd[k] + gd[3 + k]) - gd[6 + k];
-        gh3[k] = -(gh[k] + gh[3 + k]) - gh[6 + k];
+        G[9 + k] = -(G[k] + G[3 + k]) - G[6 + k];
+        H[9 + k] = -(H[k] + H[3 + k]) - H[6 + k];
     }
-    const float aa[4] = {dot3(gd, gd), dot3(gd + 3, gd + 3), dot3(gd + 6, gd + 6), dot3(gd3, gd3)};
-    const float ab[4] = {dot3(gd, gh), dot3(gd + 3, gh + 3), dot3(gd + 6, gh + 6), dot3(gd3, gh3)};
-    const float bb[4] = {dot3(gh, gh), dot3(gh + 3, gh + 3), dot3(gh + 6, gh + 6), dot3(gh3, gh3)};
-    const float L00 = s.atd + (fmaf(s.w[0], aa[0], s.w[1] * aa[1]) + fmaf(s.w[2], aa[2], s.w[3] * aa[3]));
-    const float L01 = fmaf(s.w[0], ab[0], s.w[1] * ab[1]) + fmaf(s.w[2], ab[2], s.w[3] * ab[3]);
-    const float L11 = s.ath + (fmaf(s.w[0], bb[0], s.w[1] * bb[1]) + fmaf(s.w[2], bb[2], s.w[3] * bb[3]));
+    float gg[4], gh[4], hh[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        gg[i] = dot3(G + 3 * i, G + 3 * i);
+        gh[i] = dot3(G + 3 * i, H + 3 * i);
+        hh[i] = dot3(H + 3 * i, H + 3 * i);
+    }
+    const float sgg = fmaf(s.w[0], gg[0], s.w[1] * gg[1]) + fmaf(s.w[2], gg[2], s.w[3] * gg[3]);
+    const float sgh = fmaf(s.w[0], gh[0], s.w[1] * gh[1]) + fmaf(s.w[2], gh[2], s.w[3] * gh[3]);
+    const float shh = fmaf(s.w[0], hh[0], s.w[1] * hh[1]) + fmaf(s.w[2], hh[2], s.w[3] * hh[3]);
+    const float L00 = fmaf(invC * invC, sgg, s.atd);
+    const float L01 = (invC * fac) * sgh;
+    const float L11 = fmaf(fac * fac, shh, s.ath);
     r0 = fmaf(s.atd, lam0, Cd);
     r1 = fmaf(s.ath, lam1, Ch);
     const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
     dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
     dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
+    const float a = invC * dl0, b = fac * dl1;
 #pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const float* a = i < 3 ? gd + 3 * i : gd3;
-        const float* b = i < 3 ? gh + 3 * i : gh3;
+    for (int i = 0; i < 4; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * fmaf(a[k], dl0, b[k] * dl1);
-    }
+        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * fmaf(G[3 * i + k], a, H[3 * i + k] * b);
 }
 
 // Combined 2x2 projection. Returns the pre-update residuals r = C + at*lam and
@@ -2163,6 +2163,185 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
     }
 }
 
+// ---- dataflow Gauss-Seidel on version-stamped vertices ----
+// The sweep works on its own copy xv of the positions whose w word holds the
+// vertex's version: how many patch projections have written it in this
+// launch. In one iteration a vertex is written by each patch containing it,
+// in colour order, so the patch of colour c reads vertex v once its version
+// is it * deg(v) + pre(v, c) (deg: patches containing v, pre: those of a lower
+// colour) -- the state the colour-by-colour launches give it. A writer stores
+// position and version as one aligned 16-byte vector, so a reader that sees
+// the version also sees the position written with it: the poll is the load,
+// and no fence or task counter sits between two phases.
+
+__device__ __forceinline__ float4 ld_relaxed_f4(const float4* p) {
+    float4 v;
+    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p)
+                 : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed_f4(float4* p, float4 v) {
+    asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
+                 "f"(v.w)
+                 : "memory");
+}
+
+// Positions at version 0, and per patch the inverse masses of its 8 vertex
+// slots (two float4: the sweep reads them with its other per-patch records).
+__global__ void k_versions_in(float4* __restrict__ xv, float4* __restrict__ pw, const float4* __restrict__ x,
+                              PatchArrays pa, int V, int P) {
+    pdl_wait_then_release();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < V) {
+        const float4 p = x[i];
+        xv[i] = make_float4(p.x, p.y, p.z, __int_as_float(0));
+    }
+    if (i < P) {
+        const int nv = __ldg(&pa.meta[i].y) >> 8;
+        const int4 va = __ldg(pa.verts + 2 * (size_t)i), vb = __ldg(pa.verts + 2 * (size_t)i + 1);
+        const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+        float w[kMaxPatchVerts];
+#pragma unroll
+        for (int k = 0; k < kMaxPatchVerts; k++) w[k] = k < nv ? x[vid[k]].w : 0.f;
+        pw[2 * (size_t)i] = make_float4(w[0], w[1], w[2], w[3]);
+        pw[2 * (size_t)i + 1] = make_float4(w[4], w[5], w[6], w[7]);
+    }
+}
+
+__global__ void k_versions_out(float4* __restrict__ x, const float4* __restrict__ xv, int V) {
+    pdl_wait_then_release();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const float4 p = xv[i];
+    x[i] = make_float4(p.x, p.y, p.z, x[i].w);
+}
+
+// Warp w runs the w-th task of every colour (the task layout of
+// k_sweep_dataflow). A lane's patch reads its vertices when their versions
+// are due and writes them back one version later. The smallest unfinished
+// task always has its vertices due and its warp at it (all blocks are
+// co-resident), so the waits end; each is bounded anyway, and one that gives
+// up sets abort_flag so that every other waiter leaves. Inverse masses come
+// from the per-patch copy pw. Projections, order and arithmetic are those of
+// k_project_patch_reg.
+template <bool FIRST_ZERO, int MINB>
+__global__ void __launch_bounds__(kFlowBlock, MINB)
+    k_sweep_versioned(TetArrays t, PatchArrays pa, const int4* __restrict__ pver, TaskArrays ta, int iters,
+                      const float4* __restrict__ pw, float4* __restrict__ xv, Flags* flags) {
+    __shared__ float4 sv[kMaxPatchVerts][kFlowBlock];
+    const int tid = threadIdx.x, lane = tid & 31;
+    const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
+    const int nw = (gridDim.x * blockDim.x) >> 5;
+    pdl_wait_then_release();
+    for (int it = 0; it < iters; it++) {
+        for (int j = gw; j < ta.ntasks; j += nw) {
+            const int4 tk = __ldg(ta.task + j);
+            const int p = tk.x + lane;
+            bool ok = true;
+            if (lane < tk.y) {
+                const int4 meta = __ldg(pa.meta + p);
+                const int4 va = __ldg(pa.verts + 2 * (size_t)p), vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+                const int4 vr = __ldg(pver + p);
+                const float4 wa = __ldg(pw + 2 * (size_t)p), wb = __ldg(pw + 2 * (size_t)p + 1);
+                const float wv[kMaxPatchVerts] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
+                const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
+                float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
+                float2 lams[kMaxPatchTets];
+#pragma unroll
+                for (int i = 0; i < kMaxPatchTets; i++) {
+                    if (i < ntets) {
+                        r0[i] = __ldg(t.q0 + meta.x + i);
+                        r1[i] = __ldg(t.q1 + meta.x + i);
+                        r2[i] = __ldg(t.q2 + meta.x + i);
+                        // this lane alone writes these multipliers
+                        lams[i] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
+                    }
+                }
+                const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+                const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
+                int due[kMaxPatchVerts];
+                unsigned pending = 0;
+#pragma unroll
+                for (int k = 0; k < kMaxPatchVerts; k++) {
+                    const int h = (vw[k >> 1] >> (16 * (k & 1))) & 0xffff;  // deg << 8 | pre
+                    due[k] = it * (h >> 8) + (h & 0xff);
+                    if (k < nverts) {
+                        const float4 v = ld_relaxed_f4(xv + vid[k]);
+                        sv[k][tid] = make_float4(v.x, v.y, v.z, wv[k]);
+                        if (__float_as_int(v.w) < due[k]) pending |= 1u << k;
+                    }
+                }
+                unsigned n = 0;
+                while (pending) {
+                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(1024);  // polls cost L2 bandwidth the writers need
+#pragma unroll
+                    for (int k = 0; k < kMaxPatchVerts; k++) {
+                        if (pending & (1u << k)) {
+                            const float4 v = ld_relaxed_f4(xv + vid[k]);
+                            if (__float_as_int(v.w) >= due[k]) {
+                                sv[k][tid].x = v.x;
+                                sv[k][tid].y = v.y;
+                                sv[k][tid].z = v.z;
+                                pending &= ~(1u << k);
+                            }
+                        }
+                    }
+                }
+                if (ok) {
+                    const unsigned long long loc =
+                        (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+#pragma unroll
+                    for (int i = 0; i < kMaxPatchTets; i++) {
+                        if (i >= ntets) break;
+                        const int slot = meta.x + i;
+                        TetState<float> st;
+                        st.q[0] = r0[i].x; st.q[1] = r0[i].y; st.q[2] = r0[i].z; st.q[3] = r0[i].w;
+                        st.q[4] = r1[i].x; st.q[5] = r1[i].y; st.q[6] = r1[i].z; st.q[7] = r1[i].w;
+                        st.q[8] = r2[i].x; st.atd = r2[i].y; st.ath = r2[i].z; st.gam = r2[i].w;
+                        int l[4];
+                        float4 xp[4];
+#pragma unroll
+                        for (int q = 0; q < 4; q++) {
+                            l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+                            xp[q] = sv[l[q]][tid];
+                            st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+                            st.w[q] = fabsf(xp[q].w);
+                        }
+                        float2 lam = lams[i];
+                        float d[4][3], rsq;
+                        if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
+#pragma unroll
+                            for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
+                        }
+                        t.lam[slot] = lam;
+                    }
+                    // every vertex goes out one version later, moved or not
+#pragma unroll
+                    for (int k = 0; k < kMaxPatchVerts; k++) {
+                        if (k < nverts) {
+                            const float4 s = sv[k][tid];
+                            st_relaxed_f4(xv + vid[k], make_float4(s.x, s.y, s.z, __int_as_float(due[k] + 1)));
+                        }
+                    }
+                }
+            }
+            if (!__all_sync(0xffffffffu, ok)) {
+                if (lane == 0) {
+                    atomicExch(ta.abort_flag, 1u);
+                    atomicAdd(&flags->timeouts, 1ull);
+                }
+                return;
+            }
+        }
+    }
+}
+
 // ---- attachment constraints (AttachmentConstraint.hpp:15-100) ----
 // C = |x - target|, grad C = (x - target) / C (1e-12 per component when C <
 // 1e-12), alpha = 0, an equality constraint projected by the scalar rule of
@@ -2636,6 +2815,47 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
     if (first_zero) XG_FLOW(true, 1);
     XG_FLOW(false, 1);
 #undef XG_FLOW
+}
+
+int sweep_versioned_blocks_per_sm(int min_blocks) {
+    int n = 0, m = 0;
+    cudaError_t e;
+#define XG_VOCC(M)                                                                                 \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_versioned<true, M>, kFlowBlock, 0); \
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_versioned<false, M>, kFlowBlock, 0)
+    if (min_blocks == 8) { XG_VOCC(8); }
+    else if (min_blocks == 6) { XG_VOCC(6); }
+    else { XG_VOCC(1); }
+#undef XG_VOCC
+    if (e != cudaSuccess) return 0;
+    return n < m ? n : m;
+}
+
+cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
+                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, float4* xv,
+                                   float4* pw, int V, int P, Flags* flags, int grid, int min_blocks) {
+    if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
+    go(k_versions_in, nblk(V > P ? V : P, 256), 256, s, xv, pw, (const float4*)x, pa, V, P);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kFlowBlock);
+    cfg.stream = s.s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const float4* pwc = pw;
+    cudaError_t e;
+#define XG_VER(F, M) e = cudaLaunchKernelEx(&cfg, k_sweep_versioned<F, M>, t, pa, pver, ta, iters, pwc, xv, flags)
+    if (min_blocks == 8) { if (first_zero) XG_VER(true, 8); else XG_VER(false, 8); }
+    else if (min_blocks == 6) { if (first_zero) XG_VER(true, 6); else XG_VER(false, 6); }
+    else if (first_zero) XG_VER(true, 1);
+    else XG_VER(false, 1);
+#undef XG_VER
+    if (e != cudaSuccess) return e;
+    go(k_versions_out, nblk(V, 256), 256, s, x, (const float4*)xv, V);
+    return cudaSuccess;
 }
 
 void launch_rigid_sync_table(const Launch& s, const double* rb, int nb, float4* table) {

@@ -225,6 +225,15 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
                                   int min_blocks);
 // min_blocks (variant 2): 0 = no register cap, 6 or 8 blocks per SM
 int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
+// Variant 4: the dataflow sweep on version-stamped vertices. Copies x into
+// xv (version 0) and the patches' inverse masses into pw (2P), runs every
+// iteration and colour in one cooperative launch and copies the positions
+// back; pver holds per patch and vertex slot the 16-bit deg << 8 | pre of
+// that vertex (patches containing it, those of a lower colour).
+cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
+                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, float4* xv,
+                                   float4* pw, int V, int P, Flags* flags, int grid, int min_blocks);
+int sweep_versioned_blocks_per_sm(int min_blocks);
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 // after a detection: per instance and face colour, the faces with an active
 // static contact (ifl: faces by instance, colour, index; ifo_off its ranges)
