@@ -511,6 +511,51 @@ def test_dataflow_sweep_full_block(lib, var):
     assert np.abs(out[0] - out[1]).max() <= 1e-6
 
 
+def _fan(n=300, seed=7):
+    """n tets that share vertex 0 and nothing else, so every tet is its own
+    colour and vertex 0 lies in n single-tet patches."""
+    rng = np.random.default_rng(seed)
+    X, tets = [np.zeros(3)], []
+    for _ in range(n):
+        d = rng.normal(size=3)
+        c = 0.05 * d / np.linalg.norm(d)
+        base = len(X)
+        X.extend(c + 0.02 * rng.normal(size=(3, 3)))
+        tets.append([0, base, base + 1, base + 2])
+    return np.array(X), np.array(tets, dtype=np.int32)
+
+
+def _launches_and_positions(X, tets, var, steps=2, **kw):
+    s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=4, gs_variant=var, **kw)
+    s.step(1)
+    s.synchronize()
+    l0 = s.launch_count()
+    s.step(steps)
+    s.synchronize()
+    n, x = s.launch_count() - l0, s.positions()
+    s.close()
+    return n, x
+
+
+def test_versioned_sweep_falls_back_past_255_patches_per_vertex(lib):
+    """Variant 4 keeps deg and pre of a vertex in 8 bits each. A vertex in more
+    than 255 patches makes the context run the task-counter sweep (variant 2)
+    instead of failing: the same launches and bit-identical positions as
+    variant 2, the colour launches' order. On a regular mesh variant 4 runs its
+    own sweep: two more launches per step (the version copies in and out)."""
+    X, tets = _fan()
+    n4, x4 = _launches_and_positions(X, tets, 4, gs_patch_tets=1)
+    n2, x2 = _launches_and_positions(X, tets, 2, gs_patch_tets=1)
+    _, x0 = _launches_and_positions(X, tets, 0, gs_patch_tets=1)
+    assert n4 == n2
+    np.testing.assert_array_equal(x4, x2)
+    assert np.abs(x2 - x0).max() <= 1e-6
+    w = W.cube(n=4)
+    m4, _ = _launches_and_positions(w.X, w.tets, 4)
+    m2, _ = _launches_and_positions(w.X, w.tets, 2)
+    assert m4 == m2 + 2 * 2
+
+
 @pytest.mark.parametrize("solver,adjust", [(G.SOLVER_GAUSS_SEIDEL, 0), (G.SOLVER_JACOBI, 0),
                                            (G.SOLVER_GAUSS_SEIDEL, 1)])
 def test_first_order_trajectory_matches_fp64_oracle(lib, solver, adjust):

@@ -368,14 +368,15 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
                (p.gs_variant == 2 || p.gs_variant == 3 || p.gs_variant == 4) && c->ntasks > 0) {
         // every iteration and colour in one cooperative launch
         if (track && !warm) exact_residual_row(c, 0, false);
-        if (p.gs_variant == 4) {
+        const bool versioned = p.gs_variant == 4 && c->flow_versioned;
+        if (versioned) {
             // the abort flag (after the epochs, which variant 4 does not use)
             cudaMemsetAsync(c->flow_epoch.p + c->ntasks, 0, sizeof(unsigned), s);
         } else {
             cudaMemsetAsync(c->flow_epoch.p, 0, sizeof(unsigned) * (size_t)(c->ntasks + 1), s);
         }
         Scope sc(c, K_PROJECT_GS);
-        if (p.gs_variant == 4) {
+        if (versioned) {
             launch_sweep_versioned(c->L(), c->tets(), c->patches(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
                                    c->xv.p, c->patch_w.p, c->V, c->npatches, c->flags.p, c->flow_grid,
                                    p.gs_min_blocks);
@@ -749,7 +750,9 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         doff[j + 1] = (int)dep.size();
     }
     const bool staged = c->prm.gs_variant == 3;
-    const int per_sm = c->prm.gs_variant == 4 ? sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks)
+    // variant 4 may fall back to variant 2 (below), so its grid fits both
+    const int per_sm = c->prm.gs_variant == 4 ? std::min(sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks),
+                                                         sweep_dataflow_blocks_per_sm(false, c->prm.gs_min_blocks))
                                               : sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
     XPBD_CU(c, cudaGetDevice(&dev));
@@ -815,6 +818,7 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
     XPBD_CU(c, cudaMemcpy(c->flow_dep_off.p, doff.data(), sizeof(int) * (NTP + 1), cudaMemcpyHostToDevice));
     if (!dep.empty()) XPBD_CU(c, cudaMemcpy(c->flow_dep.p, dep.data(), sizeof(int) * dep.size(), cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemset(c->flow_epoch.p, 0, sizeof(unsigned) * (NTP + 1)));
+    c->flow_versioned = false;
     if (c->prm.gs_variant == 4) {
         // per patch and vertex slot: deg << 8 | pre, deg = patches containing
         // the vertex, pre = those of a lower colour
@@ -839,11 +843,15 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
                     same += vcol[e] == pcol[q];
                 }
                 if (same != 1) return fail(c, XPBD_ERR_STATE, "dataflow: vertex %d in two patches of colour %d", v, pcol[q]);
-                if (deg > 255) return fail(c, XPBD_ERR_STATE, "dataflow: vertex %d in %d patches (at most 255)", v, deg);
+                // a vertex in more than 255 patches does not fit the 8-bit
+                // fields: this context runs the task-counter sweep (variant 2),
+                // whose task layout and co-residency this grid also satisfies
+                if (deg > 255) return XPBD_OK;
                 w[k >> 1] |= ((deg << 8) | pre) << (16 * (k & 1));
             }
             ver[q] = make_int4(w[0], w[1], w[2], w[3]);
         }
+        c->flow_versioned = true;
         XPBD_CU(c, c->patch_ver.alloc(P));
         XPBD_CU(c, c->xv.alloc(V));
         XPBD_CU(c, c->patch_w.alloc(2 * (size_t)P));

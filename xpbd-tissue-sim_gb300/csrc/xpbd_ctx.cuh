@@ -102,6 +102,7 @@ struct xpbd_ctx {
     DevBuf<float4> xv;            // variant 4: version-stamped positions
     DevBuf<float4> patch_w;       // variant 4: per patch, its 8 inverse masses
     int npatches = 0;
+    bool flow_versioned = false;  // variant 4 tables built (else variant 2 runs)
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
