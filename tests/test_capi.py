@@ -79,6 +79,16 @@ def test_create_rejects_bad_parameters_before_touching_a_device(lib):
         assert st == G.XPBD_ERR_INVALID and not h.value
 
 
+def test_create_rejects_empty_meshes(lib):
+    """A mesh without tets or without vertices is an invalid input, refused
+    before a device is touched."""
+    X, tets, _ = G.grid_mesh(1, 1, 1, 1.0)
+    p = G.default_params()
+    for Xe, te in [(X, tets[:0]), (X[:0], tets)]:
+        st, h = _create(lib, np.ascontiguousarray(Xe), np.ascontiguousarray(te), p)
+        assert st == G.XPBD_ERR_INVALID and not h.value
+
+
 def test_create_without_gpu_reports_no_device(lib):
     import torch
     if torch.cuda.is_available():
