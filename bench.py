@@ -205,6 +205,23 @@ def cpu_sample(w, target_s=15.0, threads_note="1 thread"):
     return 1.0 / t_full, sample, t_full
 
 
+def max_over_ranks(value, dist=None, device="cpu"):
+    """The job's time is its slowest rank's: a MAX all-reduce of each rank's
+    timed milliseconds (the identity on one rank)."""
+    if dist is None:
+        return float(value)
+    import torch
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, ms_step):
+    """Whole-job substeps/s: every rank advances its own replica one substep per
+    step, and the step takes the slowest rank's time."""
+    return world * 1e3 / ms_step
+
+
 def run_reference(args):
     """The reference's CPU algorithm (FP64 oracle port, reference order, 1
     thread): W warm-up and K timed steps on the full mesh. Each step runs k of
@@ -399,12 +416,9 @@ def run_ours(args):
     launches = s.launch_count() - launches0
     ms = sum(a.elapsed_time(b) for a, b in evs)
     s.synchronize()
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, dist, "cuda")
     ms_step = ms / args.steps
-    substeps = world * 1e3 / ms_step
+    substeps = job_rate(world, ms_step)
     if args.quick:
         # timed region only (used for profiler runs)
         if rank == 0:
@@ -420,12 +434,14 @@ def run_ours(args):
     x_host = s.positions()
     s.synchronize()
     e2e_steps = max(3, min(args.steps, 20))
+    if dist:
+        dist.barrier()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         s.set_positions(x_host)           # H2D of the step's input state
         one_step()
         s.positions(out=x_host)           # D2H of the step's result into the same host array (synchronises)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_s = max_over_ranks((time.perf_counter() - t0) / e2e_steps, dist, "cuda")
     h2d = d2h = int(x_host.nbytes)        # the caller's (V, 3) float64 arrays
 
     # ---- kernel roofline ----
