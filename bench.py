@@ -653,7 +653,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="block", choices=["block", "beam", "cube", "batched", "learned"])
-    ap.add_argument("--train-steps", type=int, default=200, help="learned: solver steps of online training")
+    ap.add_argument("--train-steps", type=int, default=2000, help="learned: solver steps of online training")
     ap.add_argument("--episode", type=int, default=50, help="learned: steps per loading path")
     ap.add_argument("--autotune", action="store_true", help="batched: pick launch parameters with the autotuner")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
