@@ -111,3 +111,23 @@ def test_ragged_batch_reproduces_each_instance_alone(lib, solver, var, with_face
             assert np.abs(part - xs).max() <= 1e-6
         s1.close()
     b.close()
+
+
+def test_meshes_the_reference_cannot_solve_are_refused(lib):
+    """Inputs for which the reference's setup divides by zero or takes the
+    log of a negative number (ElementConstraint.hpp:23-51, ElasticMaterial.hpp:31-32)
+    are refused with XPBD_ERR_INVALID at creation: a tet whose rest vertices
+    are coplanar, a non-finite vertex, E <= 0, nu outside (-1, 0.5), density <= 0."""
+    X, tets, _ = _one_tet()
+    flat = X.copy()
+    flat[3] = [0.05, 0.05, 0.0]                 # in the plane of the other three
+    nan = X.copy()
+    nan[2, 1] = np.nan
+    cases = [(flat, 3e3, 0.45, 1000.0), (nan, 3e3, 0.45, 1000.0), (X, 0.0, 0.45, 1000.0),
+             (X, 3e3, 0.5, 1000.0), (X, 3e3, 0.45, -1.0)]
+    for Xc, E, nu, rho in cases:
+        with pytest.raises(G.XPBDError) as e:
+            G.XPBDSolver(Xc, tets, None, E, nu, rho)
+        assert e.value.status == G.XPBD_ERR_INVALID
+    s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0)     # the valid tet is accepted
+    s.close()
