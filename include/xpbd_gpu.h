@@ -303,6 +303,15 @@ int xpbd_total_strain_energy(xpbd_ctx* ctx, double* e);
  * and projections that took the FP64 near-degenerate path (|det F| < 1e-3). */
 int xpbd_health(xpbd_ctx* ctx, int64_t* nonfinite, int64_t* degenerate);
 
+/* Test hook for the bounded waits of the versioned dataflow sweep (gs_variant
+ * 4; no counterpart in the reference). vertex >= 0: every patch containing
+ * that vertex waits for a version the sweep never writes (unreachable while
+ * num_iters x (patches per vertex) < 255), and each wait gives up after
+ * poll_limit polls; the next update then skips that work, xpbd_synchronize
+ * returns XPBD_ERR_TIMEOUT and xpbd_health clears the count. vertex < 0 puts the
+ * tables and the default limit back. XPBD_ERR_STATE without the versioned
+ * sweep. Stalls no GPU: every wait is bounded and the kernel returns. */
+int xpbd_debug_stall_vertex(xpbd_ctx* ctx, int32_t vertex, int32_t poll_limit);
 /* Colouring in use (coloured Gauss-Seidel). Tets are grouped into patches
  * (runs of up to gs_patch_tets consecutive tets on at most 8 vertices) and the
  * patches are coloured so that patches of one colour share no vertex; each

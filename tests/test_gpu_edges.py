@@ -131,3 +131,37 @@ def test_meshes_the_reference_cannot_solve_are_refused(lib):
         assert e.value.status == G.XPBD_ERR_INVALID
     s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0)     # the valid tet is accepted
     s.close()
+
+
+def test_a_wait_that_runs_out_reports_timeout_and_the_context_recovers(lib):
+    """The versioned sweep's waits are bounded. A vertex whose due version is
+    never written (the test hook) makes its patches' waits give up after 4,096
+    polls; the abort flag sends every other waiter home, the kernel returns,
+    xpbd_synchronize reports XPBD_ERR_TIMEOUT and xpbd_health clears it. With
+    the tables restored the same context steps on and matches a fresh one."""
+    w = W.cube(n=5)
+    s = G.XPBDSolver(w.X, w.tets, None, 3e3, 0.45, 1000.0, num_iters=6)
+    s.fix_vertices(w.fixed)
+    s.set_positions(w.x0)
+    s.step(1)
+    s.synchronize()
+    s.debug_stall_vertex(int(np.nonzero(~w.fixed)[0][7]), 4096)
+    s.step(1)
+    with pytest.raises(G.XPBDError) as e:
+        s.synchronize()
+    assert e.value.status == G.XPBD_ERR_TIMEOUT
+    s.health()                     # clears the counters
+    s.debug_stall_vertex(-1)
+    # from one state, the recovered context and a fresh one take the same 3 steps
+    f = G.XPBDSolver(w.X, w.tets, None, 3e3, 0.45, 1000.0, num_iters=6)
+    f.fix_vertices(w.fixed)
+    out = []
+    for c in (s, f):
+        c.set_positions(w.x0)
+        c.set_velocities(np.zeros_like(w.X))
+        c.step(3)
+        c.synchronize()
+        assert c.health()[0] == 0
+        out.append(c.positions())
+        c.close()
+    np.testing.assert_array_equal(out[0], out[1])

@@ -852,6 +852,7 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
             ver[q] = make_int4(w[0], w[1], w[2], w[3]);
         }
         c->flow_versioned = true;
+        c->patch_ver_h = ver;
         XPBD_CU(c, c->patch_ver.alloc(P));
         XPBD_CU(c, c->xv.alloc(V));
         XPBD_CU(c, c->patch_w.alloc(2 * (size_t)P));
@@ -1924,7 +1925,7 @@ int xpbd_synchronize(xpbd_ctx* c) {
     Flags f{};
     XPBD_CU(c, cudaMemcpy(&f, c->flags.p, sizeof f, cudaMemcpyDeviceToHost));
     if (f.timeouts)
-        return fail(c, XPBD_ERR_TIMEOUT, "%llu blocks gave up waiting for their staged data (work skipped)", f.timeouts);
+        return fail(c, XPBD_ERR_TIMEOUT, "%llu bounded device waits gave up (their work was skipped)", f.timeouts);
     if (f.nonfinite) return fail(c, XPBD_ERR_NUMERIC, "%llu projections produced non-finite updates", f.nonfinite);
     return XPBD_OK;
 }
@@ -2018,6 +2019,34 @@ int xpbd_total_strain_energy(xpbd_ctx* c, double* e) {
     XPBD_CU(c, cudaStreamSynchronize(c->stream));
     *e = v;
     return after_launches(c, "strain energy");
+}
+
+int xpbd_debug_stall_vertex(xpbd_ctx* c, int32_t vertex, int32_t poll_limit) {
+    if (!c) return XPBD_ERR_INVALID;
+    if (!c->flow_versioned || c->patch_ver_h.empty())
+        return fail(c, XPBD_ERR_STATE, "no versioned dataflow sweep in this context");
+    if (vertex >= c->V || (vertex >= 0 && poll_limit <= 0)) return XPBD_ERR_INVALID;
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));  // no sweep in flight reads the tables
+    std::vector<int4> ver = c->patch_ver_h;
+    if (vertex >= 0) {
+        const int P = c->npatches;
+        std::vector<int4> meta(P), verts(2 * (size_t)P);
+        XPBD_CU(c, cudaMemcpy(meta.data(), c->patch_meta.p, sizeof(int4) * P, cudaMemcpyDeviceToHost));
+        XPBD_CU(c, cudaMemcpy(verts.data(), c->patch_verts.p, sizeof(int4) * 2 * (size_t)P, cudaMemcpyDeviceToHost));
+        for (int q = 0; q < P; q++) {
+            const int4 a = verts[2 * (size_t)q], b = verts[2 * (size_t)q + 1];
+            const int vid[kMaxPatchVerts] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            int* w = &ver[q].x;
+            for (int k = 0; k < (meta[q].y >> 8); k++)
+                if (vid[k] == vertex) w[k >> 1] |= 0xff << (16 * (k & 1));  // pre = 255
+        }
+        c->flow_poll_limit = (unsigned)poll_limit;
+    } else {
+        c->flow_poll_limit = kFlowLimit;
+    }
+    XPBD_CU(c, cudaMemcpy(c->patch_ver.p, ver.data(), sizeof(int4) * ver.size(), cudaMemcpyHostToDevice));
+    c->graph_dirty = true;  // the poll limit is a launch argument
+    return XPBD_OK;
 }
 
 int xpbd_health(xpbd_ctx* c, int64_t* nonfinite, int64_t* degenerate) {

@@ -103,6 +103,8 @@ struct xpbd_ctx {
     DevBuf<float4> patch_w;       // variant 4: per patch, its 8 inverse masses
     int npatches = 0;
     bool flow_versioned = false;  // variant 4 tables built (else variant 2 runs)
+    std::vector<int4> patch_ver_h;  // host copy of patch_ver
+    unsigned flow_poll_limit = xg::kFlowLimit;
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -192,7 +194,8 @@ struct xpbd_ctx {
     }
 
     xg::TaskArrays tasks() {
-        return xg::TaskArrays{flow_tasks.p, flow_dep_off.p, flow_dep.p, flow_epoch.p, flow_epoch.p + ntasks, ntasks};
+        return xg::TaskArrays{flow_tasks.p, flow_dep_off.p, flow_dep.p, flow_epoch.p, flow_epoch.p + ntasks, ntasks,
+                              flow_poll_limit};
     }
     xg::SelfArrays selfs() {
         return xg::SelfArrays{s_tets.p,        s_Q.p,          s_X0.p,         s_X0f.p,      s_surf.p,

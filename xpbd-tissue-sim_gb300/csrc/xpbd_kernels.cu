@@ -1909,7 +1909,7 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
 }
 
 // ---- dataflow Gauss-Seidel: all iterations and colours in one cooperative launch ----
-constexpr unsigned kFlowLimit = 1u << 21;  // polls of one dependency before giving up
+
 
 __device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
     unsigned v;
@@ -1972,7 +1972,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
                 const unsigned* f = ta.epoch + (e >> 1);
                 unsigned n = 0;
                 while (ld_acquire_u32(f) < need) {
-                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                    if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
                         ok = false;
                         break;
                     }
@@ -2089,7 +2089,7 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
                 const unsigned* f = ta.epoch + (e >> 1);
                 unsigned n = 0;
                 while (ld_acquire_u32(f) < need) {
-                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                    if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
                         ok = false;
                         break;
                     }
@@ -2275,7 +2275,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 }
                 unsigned n = 0;
                 while (pending) {
-                    if (++n > kFlowLimit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                    if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
                         ok = false;
                         break;
                     }

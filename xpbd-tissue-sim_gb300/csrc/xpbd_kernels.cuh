@@ -100,6 +100,7 @@ enum RigidField {
 // reached the right iteration (lower colours: this one, higher colours: the
 // previous one), which is exactly the order of the colour-by-colour launches.
 constexpr int kTaskPatches = 32;
+constexpr unsigned kFlowLimit = 1u << 21;  // default polls of one dependency before giving up
 // threads per block of the (register-prefetch) dataflow launch: one warp, so
 // the warps spread evenly over the SMs
 constexpr int kFlowBlock = 32;
@@ -112,6 +113,7 @@ struct TaskArrays {
                           // variant 3: iterations); zeroed before each launch
     unsigned* abort_flag; // set when a wait gives up; every waiter then leaves
     int ntasks;
+    unsigned poll_limit;  // polls of one wait before it gives up
 };
 
 // Self-collisions (DeformableDeformableCollisionConstraint): a uniform grid

@@ -134,6 +134,7 @@ def load(path: str | None = None):
         "xpbd_get_lambda": ([P, P], C.c_int),
         "xpbd_total_strain_energy": ([P, P], C.c_int),
         "xpbd_health": ([P, P, P], C.c_int),
+        "xpbd_debug_stall_vertex": ([P, I32, I32], C.c_int),
         "xpbd_num_colours": ([P, P, P], C.c_int),
         "xpbd_get_tet_colours": ([P, P], C.c_int),
         "xpbd_get_sweep_order": ([P, P], C.c_int),
@@ -464,6 +465,11 @@ class XPBDSolver:
         a, b = C.c_int64(), C.c_int64()
         self._ck(self.L.xpbd_health(self.h, C.byref(a), C.byref(b)))
         return a.value, b.value
+
+    def debug_stall_vertex(self, vertex: int, poll_limit: int = 0):
+        """Test hook: the versioned sweep's waits on `vertex` never complete and
+        give up after `poll_limit` polls (vertex < 0 restores the tables)."""
+        self._ck(self.L.xpbd_debug_stall_vertex(self.h, int(vertex), int(poll_limit)))
 
     def colours(self):
         nt, nf = C.c_int32(), C.c_int32()
