@@ -13,455 +13,11 @@
 //   fixed/vel    src/simobject/XPBDMeshObject.cpp:497-535
 //   collisions   src/collision/CollisionScene.cpp:171-214,253-283
 //                src/solver/constraint/StaticDeformableCollisionConstraint.cpp:20-49
-// Every kernel is memory-bound; see the HBM layout in xpbd_kernels.cuh.
-#include <cuda_runtime.h>
-
-#include <utility>
-
-#include "xpbd_kernels.cuh"
+#include "xpbd_device.cuh"
 
 namespace xg {
 
 namespace {
-
-constexpr float kDegenerateJ = 1e-3f;  // |det F| below this takes the FP64 path
-
-// Programmatic dependent launch: a kernel may start while its predecessor on
-// the stream still runs; it must wait before touching anything the
-// predecessor writes. Dependents are released only after this kernel's own
-// wait, so a pre-wait prologue overlaps at most the direct predecessor.
-__device__ __forceinline__ void pdl_wait_then_release() {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-    asm volatile("griddepcontrol.wait;" ::: "memory");
-    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-#endif
-}
-
-// ---- TMA (bulk async copy) + mbarrier helpers ----
-__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-
-__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
-}
-
-// 1-D bulk copy global -> shared; both addresses 16-byte aligned, bytes a
-// multiple of 16; completion is counted on the mbarrier.
-__device__ __forceinline__ void tma_load_1d(void* dst, const void* src, unsigned bytes, unsigned long long* bar) {
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(src), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, unsigned parity) {
-    unsigned ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for phase `parity` of the barrier: false after `limit` tries.
-__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsigned parity, unsigned limit) {
-    for (unsigned i = 0; i < limit; i++)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-constexpr unsigned kWaitLimit = 1u << 20;
-
-__device__ __forceinline__ float warp_sum(float v) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Fixed-order block sum: FP32 inside a warp, FP64 across warps.
-__device__ __forceinline__ void block_sum_store(float v, double* slot) {
-    __shared__ double sw[32];
-    v = warp_sum(v);
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sw[wid] = (double)v;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        double s = 0.0;
-        const int nw = (blockDim.x + 31) >> 5;
-        for (int i = 0; i < nw; i++) s += sw[i];
-        *slot = s;
-    }
-}
-
-__device__ __forceinline__ void add_vec4(float4* addr, float a, float b, float c) {
-#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 900
-    atomicAdd(addr, make_float4(a, b, c, 0.f));  // one 16-byte vector reduction at L2
-#else
-    atomicAdd(&addr->x, a);
-    atomicAdd(&addr->y, b);
-    atomicAdd(&addr->z, c);
-#endif
-}
-
-// ---------------------------------------------------------------------------
-// Per-tet math, templated on the arithmetic type (float fast path, double for
-// near-degenerate elements).
-// ---------------------------------------------------------------------------
-template <typename R>
-struct TetState {
-    R p[4][3];
-    R w[4];
-    R q[9];  // Q column-major: q[3c + r] = Q(r, c)
-    R atd, ath, gam;
-};
-
-template <typename R>
-__device__ __forceinline__ R dev_log(R v) { return log(v); }
-template <>
-__device__ __forceinline__ float dev_log<float>(float v) { return logf(v); }
-template <typename R>
-__device__ __forceinline__ R dev_sqrt(R v) { return sqrt(v); }
-template <>
-__device__ __forceinline__ float dev_sqrt<float>(float v) { return sqrtf(v); }
-
-// F = Ds Q (ElementConstraint.hpp:78-119), its Frobenius norm (C_dev) and det.
-template <typename R>
-__device__ __forceinline__ void tet_F(const TetState<R>& s, R F[9]) {
-    R X[9];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) X[3 * i + k] = s.p[i][k] - s.p[3][k];
-#pragma unroll
-    for (int c = 0; c < 3; c++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            F[3 * c + k] = X[k] * s.q[3 * c + 0] + X[3 + k] * s.q[3 * c + 1] + X[6 + k] * s.q[3 * c + 2];
-}
-
-template <typename R>
-__device__ __forceinline__ R tet_detF(const R F[9]) {
-    return F[0] * F[4] * F[8] - F[0] * F[7] * F[5] - F[3] * F[1] * F[8] + F[3] * F[7] * F[2] + F[6] * F[1] * F[5] -
-           F[6] * F[4] * F[2];
-}
-
-// Values and gradients of both constraints (HydrostaticConstraint.hpp:123-221,
-// DeviatoricConstraint.hpp:112-152). gd/gh hold vertices 0..2; vertex 3 is
-// minus their sum.
-template <typename R>
-__device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R gd[9], R gh[9], R& J) {
-    R F[9];
-    tet_F(s, F);
-    R ss = 0;
-#pragma unroll
-    for (int i = 0; i < 9; i++) ss += F[i] * F[i];
-    Cd = dev_sqrt(ss);
-    const R invC = R(1) / Cd;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            gd[3 * i + k] = invC * (F[k] * s.q[i] + F[3 + k] * s.q[3 + i] + F[6 + k] * s.q[6 + i]);
-    J = tet_detF(F);
-    R fac;
-    if (J >= R(1)) {
-        Ch = -s.gam + dev_log(J);
-        fac = R(1) / J;
-    } else {
-        const R d = J - R(1);
-        Ch = -s.gam + d - d * d / R(2) + d * d * d / R(3);
-        fac = R(1) - d + d * d;
-    }
-    R Fc[9];
-    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
-}
-
-__device__ __forceinline__ float dot3(const float* a, const float* b) {
-    return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
-}
-
-// FP32 fast path of the combined 2x2 projection (same contract as
-// tet_project_combined below), with a shorter dependency chain:
-// - the gradients are formed unscaled, G_i = F q_i and H_i = cof(F) q_i (q_i
-//   the rows of Q, q_3 = -q_0 - q_1 - q_2), so they do not wait for 1/||F||
-//   (rsqrt) or the hydrostatic factor; both scales enter the 2x2 system and
-//   the update as scalars: grad C_dev,i = G_i / ||F||, grad C_hyd,i = fac H_i
-//   (DeviatoricConstraint.hpp:112-152, HydrostaticConstraint.hpp:123-221);
-// - tree-shaped sums, 1/||F|| from rsqrt, 1/J and 1/det from the hardware
-//   reciprocal; det F from the cofactors the gradient uses.
-// Results differ from tet_project_combined only by FP32 rounding (a few ulp);
-// near-degenerate elements never use it.
-__device__ __forceinline__ void tet_project_combined_fast(const TetState<float>& s, float lam0, float lam1, float& r0,
-                                                          float& r1, float& dl0, float& dl1, float d[4][3], float& J) {
-    float F[9];
-    tet_F(s, F);
-    const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
-                      (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
-    const float invC = rsqrtf(ss);
-    const float Cd = ss * invC;
-    float Fc[9];
-    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
-    J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
-    float Ch, fac;
-    if (J >= 1.f) {
-        Ch = -s.gam + logf(J);
-        fac = __frcp_rn(J);
-    } else {
-        const float dd = J - 1.f;
-        Ch = -s.gam + dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f);
-        fac = fmaf(dd, dd, 1.f - dd);
-    }
-    float G[12], H[12];
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) {
-            G[3 * i + k] = fmaf(F[k], s.q[i], fmaf(F[3 + k], s.q[3 + i], F[6 + k] * s.q[6 + i]));
-            H[3 * i + k] = fmaf(Fc[k], s.q[i], fmaf(Fc[3 + k], s.q[3 + i], Fc[6 + k] * s.q[6 + i]));
-        }
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        G[9 + k] = -(G[k] + G[3 + k]) - G[6 + k];
-        H[9 + k] = -(H[k] + H[3 + k]) - H[6 + k];
-    }
-    float gg[4], gh[4], hh[4];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        gg[i] = dot3(G + 3 * i, G + 3 * i);
-        gh[i] = dot3(G + 3 * i, H + 3 * i);
-        hh[i] = dot3(H + 3 * i, H + 3 * i);
-    }
-    const float sgg = fmaf(s.w[0], gg[0], s.w[1] * gg[1]) + fmaf(s.w[2], gg[2], s.w[3] * gg[3]);
-    const float sgh = fmaf(s.w[0], gh[0], s.w[1] * gh[1]) + fmaf(s.w[2], gh[2], s.w[3] * gh[3]);
-    const float shh = fmaf(s.w[0], hh[0], s.w[1] * hh[1]) + fmaf(s.w[2], hh[2], s.w[3] * hh[3]);
-    const float L00 = fmaf(invC * invC, sgg, s.atd);
-    const float L01 = (invC * fac) * sgh;
-    const float L11 = fmaf(fac * fac, shh, s.ath);
-    r0 = fmaf(s.atd, lam0, Cd);
-    r1 = fmaf(s.ath, lam1, Ch);
-    const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
-    dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
-    dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
-    const float a = invC * dl0, b = fac * dl1;
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * fmaf(G[3 * i + k], a, H[3 * i + k] * b);
-}
-
-// Combined 2x2 projection. Returns the pre-update residuals r = C + at*lam and
-// the lambda increments; writes the 4 vertex updates to d[4][3].
-template <typename R>
-__device__ __forceinline__ void tet_project_combined(const TetState<R>& s, R lam0, R lam1, R& r0, R& r1, R& dl0,
-                                                     R& dl1, R d[4][3], R& J) {
-    R Cd, Ch, gd[9], gh[9];
-    tet_eval(s, Cd, Ch, gd, gh, J);
-    R gd3[3], gh3[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) {
-        gd3[k] = -gd[k] - gd[3 + k] - gd[6 + k];
-        gh3[k] = -gh[k] - gh[3 + k] - gh[6 + k];
-    }
-    R L00 = s.atd, L01 = 0, L11 = s.ath;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const R* a = i < 3 ? gd + 3 * i : gd3;
-        const R* b = i < 3 ? gh + 3 * i : gh3;
-        L00 += s.w[i] * (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-        L01 += s.w[i] * (a[0] * b[0] + a[1] * b[1] + a[2] * b[2]);
-        L11 += s.w[i] * (b[0] * b[0] + b[1] * b[1] + b[2] * b[2]);
-    }
-    r0 = Cd + s.atd * lam0;
-    r1 = Ch + s.ath * lam1;
-    const R det = L00 * L11 - L01 * L01;
-    dl0 = (-r0 * L11 + r1 * L01) / det;
-    dl1 = (-r1 * L00 + r0 * L01) / det;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const R* a = i < 3 ? gd + 3 * i : gd3;
-        const R* b = i < 3 ? gh + 3 * i : gh3;
-#pragma unroll
-        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * (a[k] * dl0 + b[k] * dl1);
-    }
-}
-
-// Scalar projection of one element constraint (which = 0 dev, 1 hyd).
-template <typename R>
-__device__ __forceinline__ void tet_project_single(const TetState<R>& s, int which, R lam, R& r, R& dl, R d[4][3],
-                                                   R& J) {
-    R Cd, Ch, gd[9], gh[9];
-    tet_eval(s, Cd, Ch, gd, gh, J);
-    const R* g = which == 0 ? gd : gh;
-    const R at = which == 0 ? s.atd : s.ath;
-    const R C = which == 0 ? Cd : Ch;
-    R g3[3];
-#pragma unroll
-    for (int k = 0; k < 3; k++) g3[k] = -g[k] - g[3 + k] - g[6 + k];
-    R L = at;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const R* a = i < 3 ? g + 3 * i : g3;
-        L += s.w[i] * (a[0] * a[0] + a[1] * a[1] + a[2] * a[2]);
-    }
-    r = C + at * lam;
-    dl = -r / L;
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        const R* a = i < 3 ? g + 3 * i : g3;
-#pragma unroll
-        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * a[k] * dl;
-    }
-}
-
-// Static per-tet data (indices, Dm^-1, compliances): never written while the
-// solver runs, so it may be loaded before the dependency wait.
-__device__ __forceinline__ void load_tet_static(const TetArrays& t, int slot, int4& e, TetState<float>& s) {
-    e = __ldg(t.idx + slot);
-    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
-    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
-    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
-    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
-}
-
-// A vertex moved by a projection's update. The adds are not contracted with
-// the update's last multiply, so every Gauss-Seidel kernel variant rounds the
-// same way and their results agree bit for bit.
-__device__ __forceinline__ float4 moved(const float4& p, const float* d) {
-    return make_float4(__fadd_rn(p.x, d[0]), __fadd_rn(p.y, d[1]), __fadd_rn(p.z, d[2]), p.w);
-}
-
-__device__ __forceinline__ void gather_tet(const float4* __restrict__ x, const int4& e, TetState<float>& s,
-                                           float4 xp[4]) {
-    xp[0] = x[e.x]; xp[1] = x[e.y]; xp[2] = x[e.z]; xp[3] = x[e.w];
-#pragma unroll
-    for (int i = 0; i < 4; i++) {
-        s.p[i][0] = xp[i].x; s.p[i][1] = xp[i].y; s.p[i][2] = xp[i].z;
-        s.w[i] = fabsf(xp[i].w);
-    }
-}
-
-// FP64 guard path for near-degenerate / inverted elements. Kept out of line
-// so the FP32 path keeps its register budget; everything crosses the call by
-// value (static tet data is re-read by slot) so no caller array needs an
-// address.
-struct Fp64Out {
-    float r0, r1, dl0, dl1;
-    float d[12];
-};
-
-__device__ __forceinline__ TetState<double> fp64_state(const TetArrays& t, int slot, float4 p0, float4 p1, float4 p2,
-                                                       float4 p3) {
-    TetState<double> s;
-    const float4 ps[4] = {p0, p1, p2, p3};
-    for (int i = 0; i < 4; i++) {
-        s.p[i][0] = ps[i].x; s.p[i][1] = ps[i].y; s.p[i][2] = ps[i].z;
-        s.w[i] = fabsf(ps[i].w);
-    }
-    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
-    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
-    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
-    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
-    return s;
-}
-
-__device__ __noinline__ Fp64Out project_combined_fp64(TetArrays t, int slot, float4 p0, float4 p1, float4 p2,
-                                                      float4 p3, float lam0, float lam1) {
-    const TetState<double> s = fp64_state(t, slot, p0, p1, p2, p3);
-    double r0, r1, dl0, dl1, dd[4][3], J;
-    tet_project_combined(s, (double)lam0, (double)lam1, r0, r1, dl0, dl1, dd, J);
-    Fp64Out o;
-    o.r0 = (float)r0; o.r1 = (float)r1; o.dl0 = (float)dl0; o.dl1 = (float)dl1;
-    for (int i = 0; i < 4; i++)
-        for (int k = 0; k < 3; k++) o.d[3 * i + k] = (float)dd[i][k];
-    return o;
-}
-
-__device__ __noinline__ Fp64Out project_single_fp64(TetArrays t, int slot, float4 p0, float4 p1, float4 p2, float4 p3,
-                                                    int which, float lam) {
-    const TetState<double> s = fp64_state(t, slot, p0, p1, p2, p3);
-    double rr, dl, dd[4][3], J;
-    tet_project_single(s, which, (double)lam, rr, dl, dd, J);
-    Fp64Out o;
-    o.r0 = (float)rr; o.r1 = 0.f; o.dl0 = (float)dl; o.dl1 = 0.f;
-    for (int i = 0; i < 4; i++)
-        for (int k = 0; k < 3; k++) o.d[3 * i + k] = (float)dd[i][k];
-    return o;
-}
-
-// One tet projection in the chosen constraint form. On return d holds the
-// vertex updates, lam the updated multipliers and rsq the squared residual of
-// the state the projection saw. Returns false when the update is non-finite
-// (then nothing may be applied).
-template <bool SEPARATE>
-__device__ __forceinline__ bool project_one(const TetState<float>& s, const TetArrays& t, int slot, const float4 xp[4],
-                                            float2& lam, float d[4][3], float& rsq, Flags* flags) {
-    float J;
-    if (!SEPARATE) {
-        float r0, r1, dl0, dl1;
-        tet_project_combined_fast(s, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
-        if (fabsf(J) < kDegenerateJ) {
-            const Fp64Out o = project_combined_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], lam.x, lam.y);
-            r0 = o.r0; r1 = o.r1; dl0 = o.dl0; dl1 = o.dl1;
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int k = 0; k < 3; k++) d[i][k] = o.d[3 * i + k];
-            atomicAdd(&flags->degenerate, 1ull);
-        }
-        rsq = r0 * r0 + r1 * r1;
-        if (!(isfinite(dl0) && isfinite(dl1))) {
-            atomicAdd(&flags->nonfinite, 1ull);
-            return false;
-        }
-        lam.x += dl0;
-        lam.y += dl1;
-    } else {
-        // Jacobi form of the separate configuration: Dev and Hyd both see the
-        // same positions, their updates are summed.
-        float r0, r1, dl0, dl1, d1[4][3];
-        tet_project_single(s, 0, lam.x, r0, dl0, d, J);
-        tet_project_single(s, 1, lam.y, r1, dl1, d1, J);
-        if (fabsf(J) < kDegenerateJ) {
-            const Fp64Out a = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], 0, lam.x);
-            const Fp64Out b = project_single_fp64(t, slot, xp[0], xp[1], xp[2], xp[3], 1, lam.y);
-            r0 = a.r0; dl0 = a.dl0; r1 = b.r0; dl1 = b.dl0;
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int k = 0; k < 3; k++) {
-                    d[i][k] = a.d[3 * i + k];
-                    d1[i][k] = b.d[3 * i + k];
-                }
-            atomicAdd(&flags->degenerate, 1ull);
-        }
-        rsq = r0 * r0 + r1 * r1;
-        if (!(isfinite(dl0) && isfinite(dl1))) {
-            atomicAdd(&flags->nonfinite, 1ull);
-            return false;
-        }
-        lam.x += dl0;
-        lam.y += dl1;
-#pragma unroll
-        for (int i = 0; i < 4; i++)
-#pragma unroll
-            for (int k = 0; k < 3; k++) d[i][k] += d1[i][k];
-    }
-    return true;
-}
 
 // ---------------------------------------------------------------------------
 // Kernels
@@ -1128,733 +684,6 @@ __global__ void k_detect(ContactArrays c, const float4* __restrict__ x, const fl
     c.bary[slot] = bary;
 }
 
-// ---- free rigid bodies: two-way coupling (FP64, one thread) ----
-// GeometryUtils quatMult / rotateVectorByQuat / inverseQuat
-// (src/utils/GeometryUtils.cpp:81-102), quaternions (x, y, z, w)
-__device__ __forceinline__ void dquat_mult(const double* a, const double* b, double* r) {
-    r[0] = a[3] * b[0] + a[0] * b[3] + a[1] * b[2] - a[2] * b[1];
-    r[1] = a[3] * b[1] + a[1] * b[3] + a[2] * b[0] - a[0] * b[2];
-    r[2] = a[3] * b[2] + a[2] * b[3] + a[0] * b[1] - a[1] * b[0];
-    r[3] = a[3] * b[3] - a[0] * b[0] - a[1] * b[1] - a[2] * b[2];
-}
-__device__ __forceinline__ void dquat_rotate(const double* v, const double* q, double* o) {
-    const double ud = q[0] * v[0] + q[1] * v[1] + q[2] * v[2];
-    const double s = 2 * q[3] * q[3] - 1;
-    const double cx = q[1] * v[2] - q[2] * v[1], cy = q[2] * v[0] - q[0] * v[2], cz = q[0] * v[1] - q[1] * v[0];
-    o[0] = 2 * ud * q[0] + s * v[0] + 2 * q[3] * cx;
-    o[1] = 2 * ud * q[1] + s * v[1] + 2 * q[3] * cy;
-    o[2] = 2 * ud * q[2] + s * v[2] + 2 * q[3] * cz;
-}
-__device__ __forceinline__ void dquat_inverse(const double* q, double* r) {
-    const double n2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3];
-    r[0] = -q[0] / n2; r[1] = -q[1] / n2; r[2] = -q[2] / n2; r[3] = q[3] / n2;
-}
-__device__ __forceinline__ void dcross(const double* a, const double* b, double* r) {
-    r[0] = a[1] * b[2] - a[2] * b[1];
-    r[1] = a[2] * b[0] - a[0] * b[2];
-    r[2] = a[0] * b[1] - a[1] * b[0];
-}
-
-// The body's SDF at its current pose (SphereSDF / BoxSDF / CylinderSDF::evaluate;
-// RigidObject::globalToBody): the orientation may be off unit length inside a
-// solve, and the rotation formula is applied to it as it stands
-__device__ double sdf_body(const double* rb, const double* x) {
-    const double* p = rb + RB_P;
-    const int kind = (int)rb[RB_KIND];
-    const double* d = rb + RB_D;
-    if (kind == 0) {
-        const double a = x[0] - p[0], b = x[1] - p[1], c = x[2] - p[2];
-        return sqrt(a * a + b * b + c * c) - d[0];
-    }
-    double qi[4], b[3];
-    dquat_inverse(rb + RB_Q, qi);
-    const double rel[3] = {x[0] - p[0], x[1] - p[1], x[2] - p[2]};
-    dquat_rotate(rel, qi, b);
-    if (kind == 1) {
-        double o = 0, mq = -1e300;
-        for (int k = 0; k < 3; k++) {
-            const double q = fabs(b[k]) - 0.5 * d[k];
-            const double m = fmax(q, 0.0);
-            o += m * m;
-            mq = fmax(mq, q);
-        }
-        return sqrt(o) + fmin(mq, 0.0);
-    }
-    const double xy = sqrt(b[0] * b[0] + b[1] * b[1]) - d[0];
-    const double z = fabs(b[2]) - 0.5 * d[1];
-    const double ox = fmax(xy, 0.0), oz = fmax(z, 0.0);
-    return sqrt(ox * ox + oz * oz) + fmin(fmax(xy, z), 0.0);
-}
-
-// PositionalRigidBodyXPBDHelper::update (RigidBodyConstraint.hpp): the body's
-// increments for a contact at pt pushing along -n, from its current pose
-__device__ void rigid_contact_delta(const double* rb, double dlam, const double* pt, const double* n, double* dp,
-                                    double* dq) {
-    const double dir[3] = {-n[0], -n[1], -n[2]};
-    double qi[4], rbody[3], nb[3], t[3], cr[3], wb[3], ws[3];
-    dquat_inverse(rb + RB_Q, qi);
-    const double rel[3] = {pt[0] - rb[RB_P], pt[1] - rb[RB_P + 1], pt[2] - rb[RB_P + 2]};
-    dquat_rotate(rel, qi, rbody);
-    dquat_rotate(dir, qi, nb);
-    for (int k = 0; k < 3; k++) dp[k] = dlam * dir[k] / rb[RB_M];
-    for (int k = 0; k < 3; k++) t[k] = dlam * nb[k];
-    dcross(rbody, t, cr);
-    for (int k = 0; k < 3; k++) wb[k] = 0.5 * rb[RB_II + k] * cr[k];
-    dquat_rotate(wb, rb + RB_Q, ws);
-    const double w4[4] = {ws[0], ws[1], ws[2], 0.0};
-    dquat_mult(w4, rb + RB_Q, dq);
-}
-
-// table entries of the free bodies from their poses (the detection's view)
-__global__ void k_rigid_sync_table(const double* __restrict__ rb, int nb, float4* __restrict__ table) {
-    pdl_wait_then_release();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
-    const double* r = rb + (size_t)i * kRigidRec;
-    const size_t e = (size_t)r[RB_ENTRY];
-    table[3 * e] = make_float4((float)r[RB_P], (float)r[RB_P + 1], (float)r[RB_P + 2], table[3 * e].w);
-    table[3 * e + 1] = make_float4((float)r[RB_Q], (float)r[RB_Q + 1], (float)r[RB_Q + 2], (float)r[RB_Q + 3]);
-}
-
-// slots of the rigid contacts (active = 2) in slot order, one block
-constexpr int kCompactThreads = 1024;
-__global__ void __launch_bounds__(kCompactThreads) k_rigid_compact(ContactArrays c, int* __restrict__ list,
-                                                                   int* __restrict__ count) {
-    __shared__ int warp_tot[kCompactThreads / 32];
-    __shared__ int base;
-    pdl_wait_then_release();
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int ns = c.S * c.F;
-    if (tid == 0) base = 0;
-    __syncthreads();
-    for (int b0 = 0; b0 < ns; b0 += kCompactThreads) {
-        const int slot = b0 + tid;
-        const bool hit = slot < ns && c.bary[slot].w == 2.f;
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (lane == 0) warp_tot[wid] = __popc(m);
-        __syncthreads();
-        int off = base;
-        for (int w = 0; w < wid; w++) off += warp_tot[w];
-        if (hit) list[off + __popc(m & ((1u << lane) - 1u))] = slot;
-        __syncthreads();
-        if (tid == 0) {
-            int t = 0;
-            for (int w = 0; w < kCompactThreads / 32; w++) t += warp_tot[w];
-            base += t;
-        }
-        __syncthreads();
-    }
-    if (tid == 0) *count = base;
-}
-
-// RigidDeformableCollisionConstraint projected by RigidBodyConstraintProjector
-// (RigidDeformableCollisionConstraint.cpp:35-55, RigidBodyConstraintProjector.hpp:97-158):
-// C = the body's SDF at the barycentric point, gradient (u n, v n, w n),
-// skipped when C > 0, alpha = 0, the multiplier from the deformable weights
-// alone; the vertices and the body move by the increments. Every contact
-// moves the body that the next one reads, so one thread walks the list.
-// Gauss-Seidel applies each update at once; Jacobi reads one state, adds the
-// vertex updates to dx and sums the body increments, applied at the end
-// (XPBDGaussSeidelSolver.hpp:61-95, XPBDJacobiSolver.hpp:79-114).
-__global__ void k_rigid_contacts(ContactArrays c, const int* __restrict__ list, const int* __restrict__ count,
-                                 const float4* __restrict__ table, const int* __restrict__ face_inst,
-                                 double* __restrict__ rb, int nb, float4* __restrict__ x, float4* __restrict__ dx,
-                                 bool jacobi, bool first, Flags* flags) {
-    pdl_wait_then_release();
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    if (jacobi)
-        for (int i = 0; i < nb; i++)
-            for (int k = 0; k < 7; k++) rb[(size_t)i * kRigidRec + RB_ACC + k] = 0.0;
-    const int n = *count;
-    for (int j = 0; j < n; j++) {
-        const int slot = list[j];
-        const int f = slot % c.F, sl = slot / c.F;
-        const size_t e = (size_t)face_inst[f] * c.S + sl;
-        const int body = (int)table[3 * e + 2].w - 1;
-        if (body < 0 || body >= nb) continue;  // the host resets the list when bodies change
-        double* r = rb + (size_t)body * kRigidRec;
-        const int4 fv = c.faces[f];
-        const int vi[3] = {fv.x, fv.y, fv.z};
-        const float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
-        const float4 bb = c.bary[slot];
-        const double b[3] = {(double)bb.x, (double)bb.y, (double)bb.z};
-        float lam = first ? 0.f : c.lam[slot];
-        double a[3];
-        a[0] = b[0] * (double)xs[0].x + b[1] * (double)xs[1].x + b[2] * (double)xs[2].x;
-        a[1] = b[0] * (double)xs[0].y + b[1] * (double)xs[1].y + b[2] * (double)xs[2].y;
-        a[2] = b[0] * (double)xs[0].z + b[1] * (double)xs[1].z + b[2] * (double)xs[2].z;
-        const double C = sdf_body(r, a);
-        if (!(C > 0)) {
-            const float4 nf = c.n[slot];
-            const double nn[3] = {(double)nf.x, (double)nf.y, (double)nf.z};
-            double L = 0;
-            for (int i = 0; i < 3; i++) {
-                const double gx = b[i] * nn[0], gy = b[i] * nn[1], gz = b[i] * nn[2];
-                L += (double)fabsf(xs[i].w) * (gx * gx + gy * gy + gz * gz);
-            }
-            const double dl = -C / L;
-            if (!isfinite(dl)) {
-                atomicAdd(&flags->nonfinite, 1ull);
-            } else {
-                lam = (float)((double)lam + dl);
-                for (int i = 0; i < 3; i++) {
-                    const double w = (double)fabsf(xs[i].w);
-                    const double d0 = w * (b[i] * nn[0]) * dl, d1 = w * (b[i] * nn[1]) * dl,
-                                 d2 = w * (b[i] * nn[2]) * dl;
-                    if (jacobi) {
-                        float4 a4 = dx[vi[i]];
-                        a4.x += (float)d0; a4.y += (float)d1; a4.z += (float)d2;
-                        dx[vi[i]] = a4;
-                    } else {
-                        x[vi[i]] = make_float4((float)((double)xs[i].x + d0), (float)((double)xs[i].y + d1),
-                                               (float)((double)xs[i].z + d2), xs[i].w);
-                    }
-                }
-                const float4 pf = c.p[slot];
-                const double pt[3] = {(double)pf.x, (double)pf.y, (double)pf.z};
-                double dp[3], dq[4];
-                rigid_contact_delta(r, dl, pt, nn, dp, dq);
-                if (jacobi) {
-                    for (int k = 0; k < 3; k++) r[RB_ACC + k] += dp[k];
-                    for (int k = 0; k < 4; k++) r[RB_ACC + 3 + k] += dq[k];
-                } else {
-                    for (int k = 0; k < 3; k++) r[RB_P + k] = r[RB_P + k] + dp[k];
-                    for (int k = 0; k < 4; k++) r[RB_Q + k] = r[RB_Q + k] + dq[k];
-                }
-            }
-        }
-        c.lam[slot] = lam;
-    }
-    if (jacobi)
-        for (int i = 0; i < nb; i++) {
-            double* r = rb + (size_t)i * kRigidRec;
-            for (int k = 0; k < 3; k++) r[RB_P + k] += r[RB_ACC + k];
-            for (int k = 0; k < 4; k++) r[RB_Q + k] += r[RB_ACC + 3 + k];
-        }
-}
-
-// RigidObject::update (src/simobject/RigidObject.cpp:41-60)
-__global__ void k_rigid_update(double* __restrict__ rb, int nb, double dt, double g) {
-    pdl_wait_then_release();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
-    double* r = rb + (size_t)i * kRigidRec;
-    const double m = r[RB_M];
-    const double f[3] = {0.0, 0.0, -m * g};
-    for (int k = 0; k < 3; k++) r[RB_V + k] = r[RB_V + k] + dt * f[k] / m;
-    for (int k = 0; k < 3; k++) r[RB_P + k] = r[RB_P + k] + dt * r[RB_V + k];
-    double qi[4], wb[3], Iw[3], cr[3], w[3];
-    dquat_inverse(r + RB_Q, qi);
-    dquat_rotate(r + RB_W, qi, wb);
-    for (int k = 0; k < 3; k++) Iw[k] = r[RB_I + k] * wb[k];
-    dcross(wb, Iw, cr);
-    for (int k = 0; k < 3; k++) wb[k] = wb[k] + dt * r[RB_II + k] * (0.0 - cr[k]);
-    dquat_rotate(wb, r + RB_Q, w);
-    for (int k = 0; k < 3; k++) r[RB_W + k] = w[k];
-    const double w4[4] = {w[0], w[1], w[2], 0.0};
-    double dq[4];
-    dquat_mult(w4, r + RB_Q, dq);
-    double q[4];
-    for (int k = 0; k < 4; k++) q[k] = r[RB_Q + k] + 0.5 * dt * dq[k];
-    const double nq = sqrt(q[0] * q[0] + q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-    for (int k = 0; k < 4; k++) r[RB_Q + k] = q[k] / nq;
-}
-
-// RigidObject::velocityUpdate (src/simobject/RigidObject.cpp:62-77)
-__global__ void k_rigid_velocity(double* __restrict__ rb, int nb, double dt) {
-    pdl_wait_then_release();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= nb) return;
-    double* r = rb + (size_t)i * kRigidRec;
-    for (int k = 0; k < 3; k++) r[RB_V + k] = (r[RB_P + k] - r[RB_PP + k]) / dt;
-    double qi[4], dq[4];
-    dquat_inverse(r + RB_QP, qi);
-    dquat_mult(r + RB_Q, qi, dq);
-    const double sg = dq[3] < 0 ? -1.0 : 1.0;
-    for (int k = 0; k < 3; k++) r[RB_W + k] = sg * (2 / dt * dq[k]);
-    for (int k = 0; k < 3; k++) r[RB_PP + k] = r[RB_P + k];
-    for (int k = 0; k < 4; k++) r[RB_QP + k] = r[RB_Q + k];
-}
-
-// ---- self-collisions: detection (selfCollisionCheck, XPBDMeshObject.cpp:719-762)
-// and DeformableDeformableCollisionConstraint ----
-
-// exclusive scan of n ints in three launches (block sums, their scan, the
-// blocks' scans with offsets); out[n] = total
-constexpr int kScanThreads = 1024, kScanItems = 4, kScanChunk = kScanThreads * kScanItems;
-
-__device__ __forceinline__ int block_excl_scan(int v, int* total) {
-    __shared__ int wsum[kScanThreads / 32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = v;
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += y;
-    }
-    if (lane == 31) wsum[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-        int w = lane < kScanThreads / 32 ? wsum[lane] : 0;
-        int wi = w;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, wi, o);
-            if (lane >= o) wi += y;
-        }
-        if (lane < kScanThreads / 32) wsum[lane] = wi - w;  // exclusive warp offsets
-    }
-    __syncthreads();
-    const int res = wsum[wid] + incl - v;
-    if (total) {
-        __shared__ int tot;
-        if (threadIdx.x == kScanThreads - 1) tot = res + v;
-        __syncthreads();
-        *total = tot;
-    }
-    __syncthreads();
-    return res;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_partials(const int* __restrict__ in, int n, int* __restrict__ part) {
-    pdl_wait_then_release();
-    const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-    int s = 0;
-#pragma unroll
-    for (int i = 0; i < kScanItems; i++)
-        if (base + i < n) s += in[base + i];
-    int total = 0;
-    block_excl_scan(s, &total);
-    if (threadIdx.x == 0) part[blockIdx.x] = total;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_part_single(int* __restrict__ part, int nb) {
-    pdl_wait_then_release();
-    __shared__ int carry;
-    if (threadIdx.x == 0) carry = 0;
-    __syncthreads();
-    for (int b0 = 0; b0 < nb; b0 += kScanThreads) {
-        const int i = b0 + threadIdx.x;
-        const int v = i < nb ? part[i] : 0;
-        int total = 0;
-        const int ex = block_excl_scan(v, &total);
-        if (i < nb) part[i] = carry + ex;
-        __syncthreads();
-        if (threadIdx.x == 0) carry += total;
-        __syncthreads();
-    }
-    if (threadIdx.x == 0) part[nb] = carry;
-}
-
-__global__ void __launch_bounds__(kScanThreads) k_scan_apply(const int* __restrict__ in, int n,
-                                                             const int* __restrict__ part, int* __restrict__ out,
-                                                             int nb) {
-    pdl_wait_then_release();
-    const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
-    int v[kScanItems], s = 0;
-#pragma unroll
-    for (int i = 0; i < kScanItems; i++) {
-        v[i] = base + i < n ? in[base + i] : 0;
-        s += v[i];
-    }
-    int run = part[blockIdx.x] + block_excl_scan(s, nullptr);
-#pragma unroll
-    for (int i = 0; i < kScanItems; i++) {
-        if (base + i < n) out[base + i] = run;
-        run += v[i];
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = part[nb];
-}
-
-__device__ __forceinline__ int grid_cell1(float v, float o, float cell, int n) {
-    float f = (v - o) / cell;
-    f = fminf(fmaxf(f, 0.f), (float)(n - 1));  // NaN gives 0
-    return (int)f;
-}
-
-// each tet in the cell of its centroid, or in the overflow list when its box
-// is wider than a cell in some axis
-__global__ void k_self_bin_count(SelfArrays a, SelfGrid g, const float4* __restrict__ x) {
-    pdl_wait_then_release();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.T) return;
-    const int4 e = a.tets[t];
-    const float4 p0 = x[e.x], p1 = x[e.y], p2 = x[e.z], p3 = x[e.w];
-    const float ex = fmaxf(fmaxf(p0.x, p1.x), fmaxf(p2.x, p3.x)) - fminf(fminf(p0.x, p1.x), fminf(p2.x, p3.x));
-    const float ey = fmaxf(fmaxf(p0.y, p1.y), fmaxf(p2.y, p3.y)) - fminf(fminf(p0.y, p1.y), fminf(p2.y, p3.y));
-    const float ez = fmaxf(fmaxf(p0.z, p1.z), fmaxf(p2.z, p3.z)) - fminf(fminf(p0.z, p1.z), fminf(p2.z, p3.z));
-    int c = -1;
-    if (ex <= g.cell && ey <= g.cell && ez <= g.cell) {
-        const int cx = grid_cell1(0.25f * (p0.x + p1.x + p2.x + p3.x), g.ox, g.cell, g.nx);
-        const int cy = grid_cell1(0.25f * (p0.y + p1.y + p2.y + p3.y), g.oy, g.cell, g.ny);
-        const int cz = grid_cell1(0.25f * (p0.z + p1.z + p2.z + p3.z), g.oz, g.cell, g.nz);
-        c = (cz * g.ny + cy) * g.nx + cx;
-        atomicAdd(a.cell_count + c, 1);
-    } else {
-        a.overflow[atomicAdd(a.n_overflow, 1)] = t;
-    }
-    a.tet_cell[t] = c;
-}
-
-__global__ void k_self_bin_fill(SelfArrays a) {
-    pdl_wait_then_release();
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= a.T) return;
-    const int c = a.tet_cell[t];
-    if (c < 0) return;
-    a.cell_tets[a.cell_off[c] + atomicAdd(a.cell_fill + c, 1)] = t;
-}
-
-// EmbreeTetMeshGeometry::isPointInTetrahedron (EmbreeTetMeshGeometry.cpp:20-47),
-// float, with every product and sum rounded on its own (no contraction), as
-// the host computes it
-__device__ __forceinline__ bool same_side_f(const float* p, const float* a, const float* b, const float* c,
-                                            const float* d) {
-    const float ab0 = __fsub_rn(b[0], a[0]), ab1 = __fsub_rn(b[1], a[1]), ab2 = __fsub_rn(b[2], a[2]);
-    const float ac0 = __fsub_rn(c[0], a[0]), ac1 = __fsub_rn(c[1], a[1]), ac2 = __fsub_rn(c[2], a[2]);
-    const float n0 = __fsub_rn(__fmul_rn(ab1, ac2), __fmul_rn(ab2, ac1));
-    const float n1 = __fsub_rn(__fmul_rn(ab2, ac0), __fmul_rn(ab0, ac2));
-    const float n2 = __fsub_rn(__fmul_rn(ab0, ac1), __fmul_rn(ab1, ac0));
-    const float sp = __fadd_rn(__fadd_rn(__fmul_rn(n0, __fsub_rn(p[0], a[0])), __fmul_rn(n1, __fsub_rn(p[1], a[1]))),
-                               __fmul_rn(n2, __fsub_rn(p[2], a[2])));
-    const float sd = __fadd_rn(__fadd_rn(__fmul_rn(n0, __fsub_rn(d[0], a[0])), __fmul_rn(n1, __fsub_rn(d[1], a[1]))),
-                               __fmul_rn(n2, __fsub_rn(d[2], a[2])));
-    return __fmul_rn(sp, sd) >= 0.f;
-}
-
-// EmbreeScene::tetMeshSelfCollisionQuery: the lowest-index tet holding the
-// surface vertex among those that do not have it as a vertex
-__global__ void k_self_query(SelfArrays a, SelfGrid g, const float4* __restrict__ x) {
-    pdl_wait_then_release();
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= a.n_surf) return;
-    const int v = a.surf[k];
-    const float4 pv = x[v];
-    const float p[3] = {pv.x, pv.y, pv.z};
-    int best = INT_MAX;
-    auto test = [&](int t) {
-        if (t >= best) return;
-        const int4 e = a.tets[t];
-        if (e.x == v || e.y == v || e.z == v || e.w == v) return;
-        const float4 q0 = x[e.x], q1 = x[e.y], q2 = x[e.z], q3 = x[e.w];
-        const float v0[3] = {q0.x, q0.y, q0.z}, v1[3] = {q1.x, q1.y, q1.z}, v2[3] = {q2.x, q2.y, q2.z},
-                    v3[3] = {q3.x, q3.y, q3.z};
-        if (same_side_f(p, v0, v1, v2, v3) && same_side_f(p, v0, v1, v3, v2) && same_side_f(p, v0, v2, v3, v1) &&
-            same_side_f(p, v1, v2, v3, v0))
-            best = t;
-    };
-    const int cx = grid_cell1(p[0], g.ox, g.cell, g.nx), cy = grid_cell1(p[1], g.oy, g.cell, g.ny),
-              cz = grid_cell1(p[2], g.oz, g.cell, g.nz);
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.nz - 1); z++)
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, g.ny - 1); y++)
-            for (int xx = max(cx - 1, 0); xx <= min(cx + 1, g.nx - 1); xx++) {
-                const int c = (z * g.ny + y) * g.nx + xx;
-                for (int i = a.cell_off[c]; i < a.cell_off[c + 1]; i++) test(a.cell_tets[i]);
-            }
-    const int no = *a.n_overflow;
-    for (int i = 0; i < no; i++) test(a.overflow[i]);
-    a.hit_tet[k] = best == INT_MAX ? -1 : best;
-}
-
-// the surface indices with a hit, ascending (one block)
-__global__ void __launch_bounds__(kCompactThreads) k_self_compact(SelfArrays a) {
-    __shared__ int warp_tot[kCompactThreads / 32];
-    __shared__ int base;
-    pdl_wait_then_release();
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    if (tid == 0) base = 0;
-    __syncthreads();
-    for (int b0 = 0; b0 < a.n_surf; b0 += kCompactThreads) {
-        const int k = b0 + tid;
-        const bool hit = k < a.n_surf && a.hit_tet[k] >= 0;
-        const unsigned m = __ballot_sync(0xffffffffu, hit);
-        if (lane == 0) warp_tot[wid] = __popc(m);
-        __syncthreads();
-        int off = base;
-        for (int w = 0; w < wid; w++) off += warp_tot[w];
-        if (hit) a.hit_list[off + __popc(m & ((1u << lane) - 1u))] = k;
-        __syncthreads();
-        if (tid == 0) {
-            int t = 0;
-            for (int w = 0; w < kCompactThreads / 32; w++) t += warp_tot[w];
-            base += t;
-        }
-        __syncthreads();
-    }
-    if (tid == 0) *a.n_hits = base;
-}
-
-// Distance from p to triangle (a, b, c) in float: Ericson, Real-Time Collision
-// Detection 5.1.5 (the method EmbreeMeshGeometry::_closestPointTriangle uses)
-__device__ float point_triangle_distance_f(const float* p, const float* a, const float* b, const float* c) {
-    auto dot = [](const float* u, const float* v) {
-        return __fadd_rn(__fadd_rn(__fmul_rn(u[0], v[0]), __fmul_rn(u[1], v[1])), __fmul_rn(u[2], v[2]));
-    };
-    const float ab[3] = {__fsub_rn(b[0], a[0]), __fsub_rn(b[1], a[1]), __fsub_rn(b[2], a[2])};
-    const float ac[3] = {__fsub_rn(c[0], a[0]), __fsub_rn(c[1], a[1]), __fsub_rn(c[2], a[2])};
-    const float ap[3] = {__fsub_rn(p[0], a[0]), __fsub_rn(p[1], a[1]), __fsub_rn(p[2], a[2])};
-    const float bp[3] = {__fsub_rn(p[0], b[0]), __fsub_rn(p[1], b[1]), __fsub_rn(p[2], b[2])};
-    const float cp[3] = {__fsub_rn(p[0], c[0]), __fsub_rn(p[1], c[1]), __fsub_rn(p[2], c[2])};
-    const float d1 = dot(ab, ap), d2 = dot(ac, ap), d3 = dot(ab, bp), d4 = dot(ac, bp), d5 = dot(ab, cp),
-                d6 = dot(ac, cp);
-    float o[3];
-    if (d1 <= 0.f && d2 <= 0.f) {
-        o[0] = a[0]; o[1] = a[1]; o[2] = a[2];
-    } else if (d3 >= 0.f && d4 <= d3) {
-        o[0] = b[0]; o[1] = b[1]; o[2] = b[2];
-    } else if (d6 >= 0.f && d5 <= d6) {
-        o[0] = c[0]; o[1] = c[1]; o[2] = c[2];
-    } else {
-        const float vc = __fsub_rn(__fmul_rn(d1, d4), __fmul_rn(d3, d2));
-        const float vb = __fsub_rn(__fmul_rn(d5, d2), __fmul_rn(d1, d6));
-        const float va = __fsub_rn(__fmul_rn(d3, d6), __fmul_rn(d5, d4));
-        if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
-            const float v = __fdiv_rn(d1, __fsub_rn(d1, d3));
-            for (int k = 0; k < 3; k++) o[k] = __fadd_rn(a[k], __fmul_rn(v, ab[k]));
-        } else if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
-            const float v = __fdiv_rn(d2, __fsub_rn(d2, d6));
-            for (int k = 0; k < 3; k++) o[k] = __fadd_rn(a[k], __fmul_rn(v, ac[k]));
-        } else if (va <= 0.f && __fsub_rn(d4, d3) >= 0.f && __fsub_rn(d5, d6) >= 0.f) {
-            const float v = __fdiv_rn(__fsub_rn(d4, d3), __fadd_rn(__fsub_rn(d4, d3), __fsub_rn(d5, d6)));
-            for (int k = 0; k < 3; k++) o[k] = __fadd_rn(b[k], __fmul_rn(v, __fsub_rn(c[k], b[k])));
-        } else {
-            const float den = __fdiv_rn(1.f, __fadd_rn(__fadd_rn(va, vb), vc));
-            const float v = __fmul_rn(vb, den), w = __fmul_rn(vc, den);
-            for (int k = 0; k < 3; k++) o[k] = __fadd_rn(__fadd_rn(a[k], __fmul_rn(v, ab[k])), __fmul_rn(w, ac[k]));
-        }
-    }
-    const float e0 = __fsub_rn(p[0], o[0]), e1 = __fsub_rn(p[1], o[1]), e2 = __fsub_rn(p[2], o[2]);
-    return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(e0, e0), __fmul_rn(e1, e1)), __fmul_rn(e2, e2)));
-}
-
-// DeformableMeshSDF::closestSurfaceFaceToPointInTet (DeformableMeshSDF.cpp:68-82),
-// one warp per hit: the vertex mapped to rest space through the tet it is in
-// (F = Ds Dm^-1 in double, none when |det F| < 1e-8), then the closest face of
-// the rest surface (float; of equally close faces the lowest index)
-__global__ void k_self_face(SelfArrays a, const float4* __restrict__ x, const int4* __restrict__ faces) {
-    pdl_wait_then_release();
-    const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-    if (w >= *a.n_hits) return;
-    const int k = a.hit_list[w];
-    const int v = a.surf[k], t = a.hit_tet[k];
-    const int4 e = a.tets[t];
-    const int ids[5] = {e.x, e.y, e.z, e.w, v};
-    double xd[5][3];
-    for (int i = 0; i < 5; i++) {
-        const float4 q = x[ids[i]];
-        xd[i][0] = q.x; xd[i][1] = q.y; xd[i][2] = q.z;
-    }
-    // F = Ds Q (column-major), as the host's compute_F
-    const double* Q = a.Q + 9 * (size_t)t;
-    double D[9], F[9];
-    for (int i = 0; i < 3; i++)
-        for (int r = 0; r < 3; r++) D[3 * i + r] = xd[i][r] - xd[3][r];
-    for (int c = 0; c < 3; c++)
-        for (int r = 0; r < 3; r++) F[3 * c + r] = D[r] * Q[3 * c] + D[3 + r] * Q[3 * c + 1] + D[6 + r] * Q[3 * c + 2];
-    auto M = [&F](int r, int c) { return F[c * 3 + r]; };
-    const double c00 = M(1, 1) * M(2, 2) - M(1, 2) * M(2, 1);
-    const double c10 = M(1, 2) * M(2, 0) - M(1, 0) * M(2, 2);
-    const double c20 = M(1, 0) * M(2, 1) - M(1, 1) * M(2, 0);
-    const double det = M(0, 0) * c00 + M(0, 1) * c10 + M(0, 2) * c20;
-    int face = -1;
-    if (!(fabs(det) < 1e-8)) {
-        const double inv = 1.0 / det;
-        double Fi[9];
-        Fi[0] = c00 * inv; Fi[1] = c10 * inv; Fi[2] = c20 * inv;
-        Fi[3] = (M(0, 2) * M(2, 1) - M(0, 1) * M(2, 2)) * inv;
-        Fi[4] = (M(0, 0) * M(2, 2) - M(0, 2) * M(2, 0)) * inv;
-        Fi[5] = (M(0, 1) * M(2, 0) - M(0, 0) * M(2, 1)) * inv;
-        Fi[6] = (M(0, 1) * M(1, 2) - M(0, 2) * M(1, 1)) * inv;
-        Fi[7] = (M(0, 2) * M(1, 0) - M(0, 0) * M(1, 2)) * inv;
-        Fi[8] = (M(0, 0) * M(1, 1) - M(0, 1) * M(1, 0)) * inv;
-        const double rel[3] = {xd[4][0] - xd[3][0], xd[4][1] - xd[3][1], xd[4][2] - xd[3][2]};
-        float pm[3];
-        for (int r = 0; r < 3; r++)
-            pm[r] = (float)(Fi[r] * rel[0] + Fi[3 + r] * rel[1] + Fi[6 + r] * rel[2] + a.X0[3 * (size_t)e.w + r]);
-        float bd = INFINITY;
-        int bf = INT_MAX;
-        for (int f = lane; f < a.F; f += 32) {
-            const int4 fv = faces[f];
-            const float4 A = a.X0f[fv.x], B = a.X0f[fv.y], Cc = a.X0f[fv.z];
-            const float pa[3] = {A.x, A.y, A.z}, pb[3] = {B.x, B.y, B.z}, pc[3] = {Cc.x, Cc.y, Cc.z};
-            const float d = point_triangle_distance_f(pm, pa, pb, pc);
-            if (d < bd) {
-                bd = d;
-                bf = f;
-            }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float od = __shfl_xor_sync(0xffffffffu, bd, o);
-            const int of = __shfl_xor_sync(0xffffffffu, bf, o);
-            if (od < bd || (od == bd && of < bf)) {
-                bd = od;
-                bf = of;
-            }
-        }
-        face = bf == INT_MAX ? -1 : bf;
-    }
-    if (lane == 0) a.contact[w] = make_int2(v, face);
-}
-
-// DeformableDeformableCollisionConstraint::evaluate / gradient
-// (DeformableDeformableCollisionConstraint.cpp): C = (q - p1).a/|a| + 1e-5,
-// a = (p2 - p1) x (p3 - p1); the gradient as the reference writes it (the
-// third face vertex's term uses q - p2). g: q, p1, p2, p3 x 3
-__device__ float self_contact_eval(const float* q, const float* p1, const float* p2, const float* p3, float* g) {
-    const float e1[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
-    const float e2[3] = {p3[0] - p1[0], p3[1] - p1[1], p3[2] - p1[2]};
-    const float av[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-    const float an = sqrtf(av[0] * av[0] + av[1] * av[1] + av[2] * av[2]);
-    const float u1[3] = {q[0] - p1[0], q[1] - p1[1], q[2] - p1[2]};
-    const float u2[3] = {q[0] - p2[0], q[1] - p2[1], q[2] - p2[2]};
-    const float C = (u1[0] * av[0] + u1[1] * av[1] + u1[2] * av[2]) / an + 1e-5f;
-    const float an3 = an * an * an;
-    float r1[3], r2[3];
-    const float ad1 = av[0] * u1[0] + av[1] * u1[1] + av[2] * u1[2];
-    const float ad2 = av[0] * u2[0] + av[1] * u2[1] + av[2] * u2[2];
-    for (int k = 0; k < 3; k++) {
-        r1[k] = u1[k] / an - av[k] * ad1 / an3;
-        r2[k] = u2[k] / an - av[k] * ad2 / an3;
-    }
-    auto cross = [](const float* x, const float* y, float* r) {
-        r[0] = x[1] * y[2] - x[2] * y[1];
-        r[1] = x[2] * y[0] - x[0] * y[2];
-        r[2] = x[0] * y[1] - x[1] * y[0];
-    };
-    float t[3];
-    for (int k = 0; k < 3; k++) g[k] = av[k] / an;
-    const float d32[3] = {p3[0] - p2[0], p3[1] - p2[1], p3[2] - p2[2]};
-    cross(r1, d32, t);
-    for (int k = 0; k < 3; k++) g[3 + k] = -av[k] / an + t[k];
-    const float d13[3] = {p1[0] - p3[0], p1[1] - p3[1], p1[2] - p3[2]};
-    cross(r1, d13, t);
-    for (int k = 0; k < 3; k++) g[6 + k] = t[k];
-    const float d21[3] = {p2[0] - p1[0], p2[1] - p1[1], p2[2] - p1[2]};
-    cross(r2, d21, t);
-    for (int k = 0; k < 3; k++) g[9 + k] = t[k];
-    return C;
-}
-
-// ConstraintProjector::project (ConstraintProjector.hpp:111-172) of self
-// contact j: skipped when C > 0; alpha~ = 1e-8/dt^2 (or /dt)
-__device__ bool self_update(const SelfArrays& a, int j, const int4* __restrict__ faces, const float4* x, bool first,
-                            float at, int ids[4], float4 xs[4], float d[4][3], Flags* flags) {
-    const int2 ct = a.contact[j];
-    if (ct.y < 0) return false;
-    const int4 fv = faces[ct.y];
-    ids[0] = ct.x; ids[1] = fv.x; ids[2] = fv.y; ids[3] = fv.z;
-    float p[4][3];
-    for (int i = 0; i < 4; i++) {
-        xs[i] = x[ids[i]];
-        p[i][0] = xs[i].x; p[i][1] = xs[i].y; p[i][2] = xs[i].z;
-    }
-    float g[12];
-    const float C = self_contact_eval(p[0], p[1], p[2], p[3], g);
-    float lam = first ? 0.f : a.lam[j];
-    bool ok = false;
-    if (!(C > 0.f)) {
-        float L = at;
-        for (int i = 0; i < 4; i++)
-            L += fabsf(xs[i].w) * (g[3 * i] * g[3 * i] + g[3 * i + 1] * g[3 * i + 1] + g[3 * i + 2] * g[3 * i + 2]);
-        const float dl = (-C - at * lam) / L;
-        if (!isfinite(dl)) {
-            atomicAdd(&flags->nonfinite, 1ull);
-        } else {
-            lam += dl;
-            for (int i = 0; i < 4; i++)
-                for (int k = 0; k < 3; k++) d[i][k] = fabsf(xs[i].w) * g[3 * i + k] * dl;
-            ok = true;
-        }
-    }
-    a.lam[j] = lam;
-    return ok;
-}
-
-// Gauss-Seidel: the contacts in detection (vertex) order, one thread
-__global__ void k_self_contacts_gs(SelfArrays a, const int4* __restrict__ faces, float4* __restrict__ x, bool first,
-                                   float at, Flags* flags) {
-    pdl_wait_then_release();
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    const int n = *a.n_hits;
-    for (int j = 0; j < n; j++) {
-        int ids[4];
-        float4 xs[4];
-        float d[4][3];
-        if (!self_update(a, j, faces, x, first, at, ids, xs, d, flags)) continue;
-        for (int i = 0; i < 4; i++) {
-            const float4 c = x[ids[i]];  // a vertex may repeat: add to the current value
-            x[ids[i]] = make_float4(c.x + d[i][0], c.y + d[i][1], c.z + d[i][2], c.w);
-        }
-    }
-}
-
-// Jacobi: every contact from the same positions, updates summed into dx
-__global__ void k_self_contacts_jacobi(SelfArrays a, const int4* __restrict__ faces, const float4* __restrict__ x,
-                                       float4* __restrict__ dx, bool first, float at, Flags* flags) {
-    pdl_wait_then_release();
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *a.n_hits) return;
-    int ids[4];
-    float4 xs[4];
-    float d[4][3];
-    if (!self_update(a, j, faces, x, first, at, ids, xs, d, flags)) return;
-    for (int i = 0; i < 4; i++) add_vec4(dx + ids[i], d[i][0], d[i][1], d[i][2]);
-}
-
-// ---- host arrays the device addresses directly (coherent pageable memory
-// on a Grace-Blackwell system): 3 values per vertex, converted here ----
-// A block moves its 256 vertices' 3 x 256 values through shared memory, so the
-// host side is read and written in whole 16-byte pieces covering full cache
-// lines (when the block's run of the array is 16-byte aligned).
-constexpr int kHostIoThreads = 256;
-
-template <typename H>
-__global__ void __launch_bounds__(kHostIoThreads) k_xyz_from_host(float4* __restrict__ x, const H* __restrict__ h,
-                                                                  int V, bool keep_w) {
-    __shared__ __align__(16) H buf[3 * kHostIoThreads];
-    const int tid = threadIdx.x, v0 = blockIdx.x * kHostIoThreads;
-    const int n = min(kHostIoThreads, V - v0), nv = 3 * n;
-    const H* src = h + 3 * (size_t)v0;
-    constexpr int kPer16 = 16 / (int)sizeof(H);
-    if (((uintptr_t)src & 15) == 0) {
-        for (int i = tid; i < nv / kPer16; i += kHostIoThreads)
-            reinterpret_cast<uint4*>(buf)[i] = __ldcv(reinterpret_cast<const uint4*>(src) + i);
-        for (int i = nv / kPer16 * kPer16 + tid; i < nv; i += kHostIoThreads) buf[i] = src[i];
-    } else {
-        for (int i = tid; i < nv; i += kHostIoThreads) buf[i] = src[i];
-    }
-    __syncthreads();
-    if (tid < n) {
-        const int i = v0 + tid;
-        const float w = keep_w ? x[i].w : 0.f;  // inverse mass and fixed sign stay
-        x[i] = make_float4((float)buf[3 * tid], (float)buf[3 * tid + 1], (float)buf[3 * tid + 2], w);
-    }
-}
-
-template <typename H>
-__global__ void __launch_bounds__(kHostIoThreads) k_xyz_to_host(H* __restrict__ h, const float4* __restrict__ x,
-                                                                int V) {
-    __shared__ __align__(16) H buf[3 * kHostIoThreads];
-    const int tid = threadIdx.x, v0 = blockIdx.x * kHostIoThreads;
-    const int n = min(kHostIoThreads, V - v0), nv = 3 * n;
-    if (tid < n) {
-        const float4 p = x[v0 + tid];
-        buf[3 * tid] = (H)p.x;
-        buf[3 * tid + 1] = (H)p.y;
-        buf[3 * tid + 2] = (H)p.z;
-    }
-    __syncthreads();
-    H* dst = h + 3 * (size_t)v0;
-    constexpr int kPer16 = 16 / (int)sizeof(H);
-    if (((uintptr_t)dst & 15) == 0) {
-        for (int i = tid; i < nv / kPer16; i += kHostIoThreads)
-            reinterpret_cast<uint4*>(dst)[i] = reinterpret_cast<const uint4*>(buf)[i];
-        for (int i = nv / kPer16 * kPer16 + tid; i < nv; i += kHostIoThreads) dst[i] = buf[i];
-    } else {
-        for (int i = tid; i < nv; i += kHostIoThreads) dst[i] = buf[i];
-    }
-}
 
 __global__ void k_finalize(float4* __restrict__ x, const float4* __restrict__ prev, float4* __restrict__ vel, int V,
                            float dt, bool write_vel) {
@@ -2620,25 +1449,9 @@ __global__ void k_reduce_rows(const double* __restrict__ partial, int stride, do
     if (threadIdx.x == 0) out[row] = sh[0];
 }
 
-inline int nblk(long long n, int b) { return (int)((n + b - 1) / b); }
-
-// cudaLaunchKernelEx with programmatic stream serialization when L.pdl.
-template <typename... KArgs, typename... Args>
-void go(void (*kernel)(KArgs...), int grid, int block, const Launch& L, Args&&... args) {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)grid);
-    cfg.blockDim = dim3((unsigned)block);
-    cfg.dynamicSmemBytes = 0;
-    cfg.stream = L.s;
-    cudaLaunchAttribute attr[1];
-    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    attr[0].val.programmaticStreamSerializationAllowed = L.pdl ? 1 : 0;
-    cfg.attrs = attr;
-    cfg.numAttrs = 1;
-    cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-
 }  // namespace
+
+
 
 int residual_blocks(int T, int block) { return nblk(T, block); }
 
@@ -2856,66 +1669,6 @@ cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const Pa
     if (e != cudaSuccess) return e;
     go(k_versions_out, nblk(V, 256), 256, s, x, (const float4*)xv, V);
     return cudaSuccess;
-}
-
-void launch_rigid_sync_table(const Launch& s, const double* rb, int nb, float4* table) {
-    if (nb > 0) go(k_rigid_sync_table, nblk(nb, 32), 32, s, rb, nb, table);
-}
-
-void launch_rigid_compact(const Launch& s, const ContactArrays& c, int* list, int* count) {
-    go(k_rigid_compact, 1, kCompactThreads, s, c, list, count);
-}
-
-void launch_rigid_contacts(const Launch& s, const ContactArrays& c, const int* list, const int* count,
-                           const float4* table, const int* face_inst, double* rb, int nb, float4* x, float4* dx,
-                           bool jacobi, bool first, Flags* flags) {
-    if (nb > 0) go(k_rigid_contacts, 1, 32, s, c, list, count, table, face_inst, rb, nb, x, dx, jacobi, first, flags);
-}
-
-void launch_rigid_update(const Launch& s, double* rb, int nb, double dt, double g) {
-    if (nb > 0) go(k_rigid_update, nblk(nb, 32), 32, s, rb, nb, dt, g);
-}
-
-void launch_rigid_velocity(const Launch& s, double* rb, int nb, double dt) {
-    if (nb > 0) go(k_rigid_velocity, nblk(nb, 32), 32, s, rb, nb, dt);
-}
-
-void launch_self_detect(const Launch& s, const SelfArrays& a, const SelfGrid& g, const float4* x, const int4* faces) {
-    if (a.n_surf <= 0 || a.T <= 0) return;
-    const int ncells = g.nx * g.ny * g.nz;
-    cudaMemsetAsync(a.cell_count, 0, sizeof(int) * (size_t)ncells, s.s);
-    cudaMemsetAsync(a.cell_fill, 0, sizeof(int) * (size_t)ncells, s.s);
-    cudaMemsetAsync(a.n_overflow, 0, sizeof(int), s.s);
-    go(k_self_bin_count, nblk(a.T, 256), 256, s, a, g, x);
-    const int nb = (ncells + kScanChunk - 1) / kScanChunk;
-    go(k_scan_partials, nb, kScanThreads, s, (const int*)a.cell_count, ncells, a.scan_part);
-    go(k_scan_part_single, 1, kScanThreads, s, a.scan_part, nb);
-    go(k_scan_apply, nb, kScanThreads, s, (const int*)a.cell_count, ncells, (const int*)a.scan_part, a.cell_off, nb);
-    go(k_self_bin_fill, nblk(a.T, 256), 256, s, a);
-    go(k_self_query, nblk(a.n_surf, 128), 128, s, a, g, x);
-    go(k_self_compact, 1, kCompactThreads, s, a);
-    go(k_self_face, nblk(32 * a.n_surf, 256), 256, s, a, x, faces);
-}
-
-void launch_self_contacts(const Launch& s, const SelfArrays& a, const int4* faces, float4* x, float4* dx,
-                          bool jacobi, bool first, float alpha_tilde, Flags* flags) {
-    if (a.n_surf <= 0) return;
-    if (jacobi) go(k_self_contacts_jacobi, nblk(a.n_surf, 128), 128, s, a, faces, (const float4*)x, dx, first,
-                   alpha_tilde, flags);
-    else go(k_self_contacts_gs, 1, 32, s, a, faces, x, first, alpha_tilde, flags);
-}
-
-void launch_xyz_from_host(cudaStream_t s, float4* x, const double* h, int V, bool keep_w) {
-    if (V > 0) k_xyz_from_host<double><<<nblk(V, kHostIoThreads), kHostIoThreads, 0, s>>>(x, h, V, keep_w);
-}
-void launch_xyz_from_host(cudaStream_t s, float4* x, const float* h, int V, bool keep_w) {
-    if (V > 0) k_xyz_from_host<float><<<nblk(V, kHostIoThreads), kHostIoThreads, 0, s>>>(x, h, V, keep_w);
-}
-void launch_xyz_to_host(cudaStream_t s, double* h, const float4* x, int V) {
-    if (V > 0) k_xyz_to_host<double><<<nblk(V, kHostIoThreads), kHostIoThreads, 0, s>>>(h, x, V);
-}
-void launch_xyz_to_host(cudaStream_t s, float* h, const float4* x, int V) {
-    if (V > 0) k_xyz_to_host<float><<<nblk(V, kHostIoThreads), kHostIoThreads, 0, s>>>(h, x, V);
 }
 
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,
