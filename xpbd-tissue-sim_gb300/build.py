@@ -12,8 +12,8 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libxpbd_gpu.so")
-SOURCES = ["xpbd_kernels.cu", "xpbd_rigid.cu", "xpbd_self.cu", "xpbd_hostio.cu", "xpbd_capi.cu", "xpbd_mesh.cu",
-           "xpbd_mlp.cu", "xpbd_warm.cu", "xpbd_noalloc.cu"]
+SOURCES = ["xpbd_kernels.cu", "xpbd_rigid.cu", "xpbd_self.cu", "xpbd_hostio.cu", "xpbd_build.cu", "xpbd_capi.cu",
+           "xpbd_mesh.cu", "xpbd_mlp.cu", "xpbd_warm.cu", "xpbd_noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "-I", os.path.join(ROOT, "include")]
 
