@@ -511,6 +511,28 @@ def test_dataflow_sweep_full_block(lib, var):
     assert np.abs(out[0] - out[1]).max() <= 1e-6
 
 
+def test_versioned_sweep_equals_fenced_sweep_over_100_block_steps(lib):
+    """Variant 4 reads a vertex's position and version as one 16-byte vector
+    and relies on seeing the position written with that version; variant 2
+    orders the same sweep with release/acquire alone. On the 1.31M-tet block
+    driven for 100 substeps (3,000 sweeps, 1,024 warps racing on shared
+    vertices), two variant-4 runs and a variant-2 run end bit-identical: one
+    torn read would have changed the trajectory."""
+    w = W.block()
+    out = []
+    for var in (4, 4, 2):
+        s = W.make_solver(w, gs_variant=var)
+        for k in range(100):
+            W.drive_gpu(s, w, k + 1)
+            s.step(1)
+        s.synchronize()
+        assert s.health()[0] == 0
+        out.append(s.positions())
+        s.close()
+    np.testing.assert_array_equal(out[0], out[1])
+    np.testing.assert_array_equal(out[0], out[2])
+
+
 def _fan(n=300, seed=7):
     """n tets that share vertex 0 and nothing else, so every tet is its own
     colour and vertex 0 lies in n single-tet patches."""
