@@ -427,20 +427,35 @@ __global__ void k_contacts_jacobi(ContactArrays c, const float4* __restrict__ x,
 
 // Gauss-Seidel contacts of one face: its slots in order, positions updated in
 // place (faces of one colour share no vertex)
+// The face's static contacts in slot order. The slots' active flags are read
+// together and the face's vertices once: each contact moves them in registers
+// for the next, and they are stored once (no other thread touches them while
+// this colour runs: the faces of a colour share no vertex).
 __device__ __forceinline__ void contact_face_gs(const ContactArrays& c, int f, float4* __restrict__ x, bool first) {
     const int4 fv = c.faces[f];
+    unsigned act = 0;
+    for (int s = 0; s < c.S; s++)
+        if (c.bary[s * c.F + f].w == 1.f) act |= 1u << s;  // not empty, not against a free rigid body
+    if (!act) return;
+    float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
+    bool moved_any = false;
     for (int s = 0; s < c.S; s++) {
+        if (!(act & (1u << s))) continue;
         const int slot = s * c.F + f;
-        if (c.bary[slot].w != 1.f) continue;  // empty, or against a free rigid body
-        float4 xs[3] = {x[fv.x], x[fv.y], x[fv.z]};
         float lam = first ? 0.f : c.lam[slot];
         float d[3][3];
         if (contact_update(c, slot, xs, d, lam)) {
-            x[fv.x] = make_float4(xs[0].x + d[0][0], xs[0].y + d[0][1], xs[0].z + d[0][2], xs[0].w);
-            x[fv.y] = make_float4(xs[1].x + d[1][0], xs[1].y + d[1][1], xs[1].z + d[1][2], xs[1].w);
-            x[fv.z] = make_float4(xs[2].x + d[2][0], xs[2].y + d[2][1], xs[2].z + d[2][2], xs[2].w);
+#pragma unroll
+            for (int i = 0; i < 3; i++)
+                xs[i] = make_float4(xs[i].x + d[i][0], xs[i].y + d[i][1], xs[i].z + d[i][2], xs[i].w);
+            moved_any = true;
         }
         c.lam[slot] = lam;
+    }
+    if (moved_any) {
+        x[fv.x] = xs[0];
+        x[fv.y] = xs[1];
+        x[fv.z] = xs[2];
     }
 }
 
