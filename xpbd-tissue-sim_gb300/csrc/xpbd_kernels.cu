@@ -1014,9 +1014,12 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
 // in colour order, so the patch of colour c reads vertex v once its version
 // is it * deg(v) + pre(v, c) (deg: patches containing v, pre: those of a lower
 // colour) -- the state the colour-by-colour launches give it. A writer stores
-// position and version as one aligned 16-byte vector, so a reader that sees
-// the version also sees the position written with it: the poll is the load,
-// and no fence or task counter sits between two phases.
+// position and version as one aligned 16-byte vector and a reader loads them
+// the same way; the hardware serves an aligned 16-byte access as one request
+// to one L2 sector, so a reader that sees the version sees the position
+// written with it (the PTX memory model itself promises single-copy atomicity
+// only up to 64 bits). The poll is the load, and no fence or task counter
+// sits between two phases.
 
 __device__ __forceinline__ float4 ld_relaxed_f4(const float4* p) {
     float4 v;
@@ -1068,8 +1071,8 @@ __global__ void k_versions_out(float4* __restrict__ x, const float4* __restrict_
 // task always has its vertices due and its warp at it (all blocks are
 // co-resident), so the waits end; each is bounded anyway, and one that gives
 // up sets abort_flag so that every other waiter leaves. Inverse masses come
-// from the per-patch copy pw. Projections, order and arithmetic are those of
-// k_project_patch_reg.
+// from the per-patch copy pw. The projections and their order are those of
+// the colour launches; the results equal k_sweep_dataflow's bit for bit.
 template <bool FIRST_ZERO, int MINB>
 __global__ void __launch_bounds__(kFlowBlock, MINB)
     k_sweep_versioned(TetArrays t, PatchArrays pa, const int4* __restrict__ pver, TaskArrays ta, int iters,
