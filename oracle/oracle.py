@@ -52,6 +52,9 @@ def lib():
         L.xo_grid_mesh.argtypes = [I, I, I, D, D, D, P, P, P, I]
         L.xo_greedy_colour.argtypes = [LL, I, P, LL, P]
         L.xo_greedy_colour.restype = I
+        L.xo_set_rel_tol.argtypes = [P, D]
+        L.xo_iters_done.argtypes = [P]
+        L.xo_iters_done.restype = I
         _lib = L
     return _lib
 
@@ -245,6 +248,15 @@ class Oracle:
         True when the warm start was kept (not rejected by the residual test)."""
         lam0 = np.ascontiguousarray(lam0, np.float64)
         return bool(self.L.xo_update_warm(C.c_void_p(self.h), _p(lam0), int(record), int(fallback)))
+
+    def set_rel_tol(self, tol):
+        """Convergence measurement: update() stops its sweeps once ||r|| <=
+        tol * ||r(x_pred, 0)|| (at most num_iter sweeps); 0 turns it off."""
+        self.L.xo_set_rel_tol(C.c_void_p(self.h), float(tol))
+
+    def iters_done(self):
+        """Sweeps the last update() ran."""
+        return self.L.xo_iters_done(C.c_void_p(self.h))
 
     def velocity_update(self):
         self.L.xo_velocity_update(self.h)

@@ -980,6 +980,9 @@ struct Object {
     double time = 0, last_cd = 0, cd_interval = 1e300;
     // per-iteration residual trajectory of the last update(): ||r||_2
     std::vector<double> res_history;
+    // relative-residual stop of update() (0 = off) and the sweeps it ran
+    double rel_tol = 0.0;
+    int iters_done = 0;
 
     // Setup: rest shape, materials, masses (XPBDMeshObject.cpp:277-331,
     // 352-417; HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
@@ -1344,9 +1347,16 @@ struct Object {
         for (auto& at : attachments) at.lambda = 0;
         for (auto& sc : self_contacts) sc.lambda = 0;
         res_history.clear();
+        // convergence measurement (not a reference feature): with rel_tol > 0
+        // the sweeps stop once ||r|| <= rel_tol * ||r(x_pred, 0)||, at most
+        // num_iter of them; iters_done counts the sweeps run
+        const double r_first = rel_tol > 0 ? residual_norm() : 0.0;
+        iters_done = 0;
         for (int it = 0; it < num_iter; it++) {
             if (record_residual) res_history.push_back(residual_norm());
             iterate();
+            iters_done = it + 1;
+            if (rel_tol > 0 && residual_norm() <= rel_tol * r_first) break;
         }
         if (record_residual) res_history.push_back(residual_norm());
         local_iterations();

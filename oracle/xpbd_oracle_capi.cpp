@@ -306,6 +306,12 @@ int xo_update_warm(void* p, const double* lam0, int record, int fallback) {
     });
 }
 
+void xo_set_rel_tol(void* p, double tol) {
+    with((Handle*)p, [&](auto& o) { o.rel_tol = tol; return 0; });
+}
+int xo_iters_done(void* p) {
+    return with((Handle*)p, [&](auto& o) { return o.iters_done; });
+}
 void xo_update(void* p, int record) {
     with((Handle*)p, [&](auto& o) { o.update(record != 0); return 0; });
 }
@@ -436,6 +442,22 @@ void xo_elem_eval(const double* x4, const double* Q, double gamma, double* F, do
 void xo_project_combined(const double* x4, const double* w, const double* Q, const double* at, double gamma,
                          double* lam, double* dx) {
     xo::project_combined(x4, x4 + 3, x4 + 6, x4 + 9, w, Q, at, gamma, lam, dx);
+}
+void xo_project_single(int which, const double* x4, const double* w, const double* Q, double at, double gamma,
+                       double* lam, double* dx) {
+    xo::project_single_elem(which, x4, x4 + 3, x4 + 6, x4 + 9, w, Q, at, gamma, lam, dx);
+}
+// one static contact projection on face x3 (3 x 3); returns 0 when skipped
+// (C > 0), else 1 with the 9 updates in dx
+int xo_project_contact(const double* x3, const double* w, double u, double v, double wb, const double* p,
+                       const double* n, double* lam, double* dx) {
+    xo::Contact<double> ct{};
+    ct.u = u; ct.v_ = v; ct.w = wb;
+    for (int k = 0; k < 3; k++) { ct.p[k] = p[k]; ct.n[k] = n[k]; }
+    ct.lambda = *lam;
+    const bool on = xo::project_contact(x3, x3 + 3, x3 + 6, w, ct, dx);
+    *lam = ct.lambda;
+    return on ? 1 : 0;
 }
 
 }  // extern "C"

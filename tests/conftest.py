@@ -1,4 +1,5 @@
 import os
+import subprocess
 import sys
 
 import pytest
@@ -29,3 +30,15 @@ def oracle_mod():
 
     oracle.build()
     return oracle
+
+
+def reference_dir():
+    """The reference checkout, when this machine has one: XPBD_REFERENCE_DIR,
+    else the checkout the oracle's reference recipe (oracle/ref/Makefile)
+    builds from. None when absent (the GPU machine has none)."""
+    d = os.environ.get("XPBD_REFERENCE_DIR")
+    if not d:
+        r = subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "print-ref"],
+                           capture_output=True, text=True)
+        d = r.stdout.strip()
+    return d if d and os.path.isdir(d) else None

@@ -4,7 +4,8 @@
                         resource/cube/cube2.msh, cube4.msh (written by its
                         MeshUtils::createBeamMsh) and resource/general/single.msh.
                         Read from a checkout of the reference given by
-                        --reference (default /root/reference); only this
+                        --reference (default: XPBD_REFERENCE_DIR, else the
+                        checkout oracle/ref/Makefile builds from); only this
                         script reads it, the tests use the .npz.
   oracle_trajectories.npz  FP64 oracle runs on a seeded 3x3x3 cube (sequential
                         Gauss-Seidel, Jacobi, coloured Gauss-Seidel; 10 steps,
@@ -51,8 +52,13 @@ def oracle_runs():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--reference", default="/root/reference")
+    ap.add_argument("--reference", default=None)
     a = ap.parse_args()
+    if a.reference is None:
+        import subprocess
+        a.reference = os.environ.get("XPBD_REFERENCE_DIR") or subprocess.run(
+            ["make", "-s", "-C", os.path.join(ROOT, "oracle", "ref"), "print-ref"], capture_output=True,
+            text=True).stdout.strip()
     meshes = {}
     for key, rel in [("cube2", "resource/cube/cube2.msh"), ("cube4", "resource/cube/cube4.msh"),
                      ("single", "resource/general/single.msh")]:

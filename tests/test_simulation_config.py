@@ -10,8 +10,10 @@ import msh
 import simulation as S
 import xpbd_gb300 as G
 import yaml_lite as Y
+from conftest import reference_dir
 
-REF_CONFIGS = "/root/reference/config"
+REF = reference_dir()
+REF_CONFIGS = os.path.join(REF, "config") if REF else None
 
 CONFIG = """
 ## a test scene
@@ -74,7 +76,7 @@ def test_yaml_subset():
         Y.loads("a: &anchor 1")
 
 
-@pytest.mark.skipif(not os.path.isdir(REF_CONFIGS), reason="reference configs not present")
+@pytest.mark.skipif(not (REF_CONFIGS and os.path.isdir(REF_CONFIGS)), reason="reference configs not present")
 def test_every_reference_config_parses():
     import glob
     files = sorted(glob.glob(os.path.join(REF_CONFIGS, "**", "*.yaml"), recursive=True))
@@ -132,7 +134,7 @@ def test_msh_round_trip(tmp_path):
 def test_msh_reader_matches_reference_meshes():
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_meshes.npz"))
     for name in ("cube2", "cube4"):
-        p = f"/root/reference/resource/cube/{name}.msh"
+        p = os.path.join(REF, "resource", "cube", f"{name}.msh") if REF else ""
         if not os.path.exists(p):
             pytest.skip("reference meshes not present")
         X, tets, faces = msh.read_msh(p)
