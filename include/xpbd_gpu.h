@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 5
+#define XPBD_ABI_VERSION 6
 
 /* status codes */
 #define XPBD_OK 0
@@ -123,6 +123,13 @@ typedef struct {
                                /* XPBDMeshObject.cpp:719-762) and adds a          */
                                /* DeformableDeformableCollisionConstraint with    */
                                /* the closest rest-surface face; needs faces     */
+    int32_t gs_poll_ns;        /* versioned sweep (gs_variant 4): back-off in ns  */
+                               /* between two polls of a vertex that is not yet   */
+                               /* due; 0 = 1024                                   */
+    int32_t gs_topology_reload;/* versioned sweep: 1 reloads each task's patch    */
+                               /* records from global memory every phase; 0 keeps */
+                               /* a warp's task topology in shared memory when it */
+                               /* fits (default)                                  */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,
@@ -201,7 +208,7 @@ int xpbd_set_spheres(xpbd_ctx* ctx, int32_t n, const double* centers3n, const do
 int xpbd_set_instance_spheres(xpbd_ctx* ctx, int32_t instance, int32_t n, const double* centers3n,
                               const double* radii);
 /* Fixed rigid primitives as SDFs: spheres, boxes and cylinders
- * (SphereSDF / BoxSDF / CylinderSDF, src/geometry/*SDF.cpp) at a position with
+ * (SphereSDF / BoxSDF / CylinderSDF, src/geometry/{Sphere,Box,Cylinder}SDF.cpp) at a position with
  * an orientation quaternion (x, y, z, w), as RigidSphere / RigidBox /
  * RigidCylinder hold them (RigidObject::globalToBody, RigidObject.cpp:94-97).
  * dims: sphere (radius, -, -), box (full size x, y, z), cylinder (radius,
@@ -272,6 +279,22 @@ int xpbd_num_attachments(xpbd_ctx* ctx, int32_t* n);
 /* XPBDMeshObject_::update (XPBDMeshObject.cpp:426-505): prev <- x, inertial
  * move, solve (lambda <- 0, num_iters sweeps), fixed reset. Asynchronous. */
 int xpbd_update(xpbd_ctx* ctx);
+/* XPBDSolver::solve() (XPBDSolver.hpp:66-97) alone: every projector's lambda
+ * <- 0, then num_iters sweeps over all constraints on the device positions as
+ * they stand (set them with xpbd_set_positions after a host-side inertial
+ * move). No inertial move, no local collision passes, no fixed-vertex reset:
+ * XPBDMeshObject_::_projectConstraints (XPBDMeshObject.cpp:472-505) does those
+ * around its solve() call. The residual is recorded as the policy asks.
+ * Asynchronous. */
+int xpbd_solve(xpbd_ctx* ctx);
+/* XPBDSolver::solve(projector_references, num_iter, false) (XPBDSolver.hpp:106-125)
+ * over the set XPBDMeshObject_::_gatherProjectorsForLocalCollisionIterations
+ * builds (XPBDMeshObject.cpp:764-825): num_iter passes over the static contacts
+ * and the elastic projectors of every tet touching a vertex of a contact with
+ * lambda != 0, with no re-initialisation of the multipliers. Needs surface
+ * faces and num_local_collision_iters > 0 at creation (XPBD_ERR_STATE
+ * otherwise). Asynchronous. */
+int xpbd_solve_local(xpbd_ctx* ctx, int32_t num_iter);
 /* XPBDMeshObject_::velocityUpdate (XPBDMeshObject.cpp:507-535). */
 int xpbd_velocity_update(xpbd_ctx* ctx);
 /* Simulation::_timeStep for this object, n times (Simulation.cpp:197-276):

@@ -8,6 +8,8 @@
 //   GPUXPBDSolver(obj, num_iter, residual_policy)   XPBDSolver.hpp:47-51
 //   setup()                                         XPBDSolver.hpp:56-61
 //   solve()                                         XPBDSolver.hpp:66-97
+//   solveLocal(num_iter) = solve(refs, num_iter,    XPBDSolver.hpp:106-125
+//     false) over the local collision set
 //   constraintResidual()                            XPBDSolver.hpp:135
 //   numIterations()                                 XPBDSolver.hpp:139
 //   addStaticCollisionConstraint(...)               XPBDMeshObject.cpp:180-206
@@ -20,11 +22,20 @@
 //   obj->vertexFixed(i), and per-element material accessors supplied by the
 //   caller through MaterialFn (E, nu, density of element i).
 //
-// Unlike the reference's solve(), which works on the mesh in place, this
-// solver owns a device copy: solve() runs prediction, projection and the fixed
-// reset on the device (the whole of XPBDMeshObject_::update) and writes the
-// result back into the mesh. Callers that keep the state on the device use
-// update()/step() and read back only when needed.
+// solve() means what the reference's does: every projector's lambda <- 0,
+// then num_iter sweeps over the mesh's current positions -- no inertial move
+// and no fixed-vertex reset, which XPBDMeshObject_::update and
+// _projectConstraints do around it (XPBDMeshObject.cpp:426-505). The
+// reference's solver works on the mesh in place; this one owns a device copy,
+// so solve() uploads the mesh's positions, solves on the device and writes
+// the result back into the mesh. A binding dropped in at
+// XPBDMeshObject.cpp:476 therefore keeps the host's inertial move before it
+// and the host's fixed-vertex loop after it. solveLocal(n) is the
+// solve(refs, n, false) call that follows (XPBDMeshObject.cpp:483).
+//
+// updateOnDevice() runs the whole of XPBDMeshObject_::update (prediction,
+// projection, local passes, fixed reset) on the device; callers that keep the
+// state there use it or step() and read back only when needed.
 #pragma once
 
 #include <cstdint>
@@ -99,15 +110,23 @@ class GPUXPBDSolver {
         T_ = T;
     }
 
-    // XPBDMeshObject_::update on the device, then the mesh is refreshed.
+    // XPBDSolver::solve() (XPBDSolver.hpp:66-97) on the mesh's positions.
     void solve() {
         upload_positions();
-        check(xpbd_update(ctx_));
+        check(xpbd_solve(ctx_));
+        download_positions();
+    }
+    // XPBDSolver::solve(refs, num_iter, false) over the local collision set
+    // (XPBDMeshObject.cpp:483, 764-825); the context needs
+    // params().num_local_collision_iters > 0 before setup().
+    void solveLocal(int num_iter) {
+        upload_positions();
+        check(xpbd_solve_local(ctx_, num_iter));
         download_positions();
     }
 
-    // device-resident variants
-    void update() { check(xpbd_update(ctx_)); }
+    // device-resident variants: XPBDMeshObject_::update on the device
+    void updateOnDevice() { check(xpbd_update(ctx_)); }
     void velocityUpdate() { check(xpbd_velocity_update(ctx_)); }
     void step(int n) { check(xpbd_step(ctx_, n)); }
     void upload_positions() {

@@ -512,12 +512,12 @@ def test_dataflow_sweep_full_block(lib, var):
 
 
 def test_versioned_sweep_equals_fenced_sweep_over_100_block_steps(lib):
-    """Variant 4 reads a vertex's position and version as one 16-byte vector
-    and relies on seeing the position written with that version; variant 2
-    orders the same sweep with release/acquire alone. On the 1.31M-tet block
-    driven for 100 substeps (3,000 sweeps, 1,024 warps racing on shared
-    vertices), two variant-4 runs and a variant-2 run end bit-identical: one
-    torn read would have changed the trajectory."""
+    """Variant 4 reads a vertex as four 64-bit words, each coordinate beside
+    the version it was written with, and polls again unless all three carry
+    the due version; variant 2 orders the same sweep with release/acquire
+    alone. On the 1.31M-tet block driven for 100 substeps (3,000 sweeps,
+    1,024 warps racing on shared vertices), two variant-4 runs and a
+    variant-2 run end bit-identical."""
     w = W.block()
     out = []
     for var in (4, 4, 2):

@@ -123,7 +123,7 @@ void release(xpbd_ctx* c) {
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
-    c->patch_ver.release(); c->xv.release(); c->patch_w.release();
+    c->patch_ver.release(); c->xv.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
     c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
@@ -193,7 +193,7 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
     }
     const bool staged = c->prm.gs_variant == 3;
     // variant 4 may fall back to variant 2 (below), so its grid fits both
-    const int per_sm = c->prm.gs_variant == 4 ? std::min(sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks),
+    const int per_sm = c->prm.gs_variant == 4 ? std::min(sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, 0),
                                                          sweep_dataflow_blocks_per_sm(false, c->prm.gs_min_blocks))
                                               : sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
@@ -297,8 +297,16 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         c->patch_ver_h = ver;
         XPBD_CU(c, c->patch_ver.alloc(P));
         XPBD_CU(c, c->xv.alloc(V));
-        XPBD_CU(c, c->patch_w.alloc(2 * (size_t)P));
         c->npatches = P;
+        // the task topology stays in shared memory when every warp owns few
+        // enough tasks and the grid stays co-resident with that memory
+        const int W = c->flow_grid * (kFlowBlock / 32);
+        const int per_warp = (NTP + W - 1) / W;
+        c->flow_resident = false;
+        if (per_warp <= kResidentTasks && !c->prm.gs_topology_reload) {
+            const int res_sm = sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, per_warp);
+            c->flow_resident = (long long)res_sm * sms >= c->flow_grid;
+        }
         XPBD_CU(c, cudaMemcpy(c->patch_ver.p, ver.data(), sizeof(int4) * P, cudaMemcpyHostToDevice));
     }
     return XPBD_OK;
@@ -759,7 +767,7 @@ void drop_graphs(xpbd_ctx* c) {
             cudaGraphExecDestroy(g);
             g = nullptr;
         }
-    c->graph_kernels[0] = c->graph_kernels[1] = 0;
+    c->graph_kernels[0] = c->graph_kernels[1] = c->graph_kernels[2] = 0;
     c->graph_dirty = false;
 }
 

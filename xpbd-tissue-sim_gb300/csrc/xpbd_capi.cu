@@ -42,7 +42,8 @@ bool valid_params(const xpbd_params& p) {
            p.num_local_collision_iters <= 1000 && (p.first_order == 0 || p.first_order == 1) &&
            (p.adjust_damping_to_material == 0 || p.adjust_damping_to_material == 1) &&
            (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier))) &&
-           (p.self_collisions == 0 || p.self_collisions == 1);
+           (p.self_collisions == 0 || p.self_collisions == 1) && p.gs_poll_ns >= 0 && p.gs_poll_ns <= 1000000 &&
+           (p.gs_topology_reload == 0 || p.gs_topology_reload == 1);
 }
 
 // The colour-launch kernel that stands in for a GS variant where the one-launch
@@ -151,7 +152,7 @@ void enqueue_warm_start(xpbd_ctx* c) {
 // the reference lists once per incident contact vertex is projected once per
 // pass here, in per-tet colour order (Gauss-Seidel) or from the same x
 // (Jacobi).
-void enqueue_local_collision_iters(xpbd_ctx* c) {
+void enqueue_local_collision_iters(xpbd_ctx* c, int passes) {
     const xpbd_params& p = c->prm;
     const bool separate = p.constraint_type == XPBD_CONSTRAINT_SEPARATE;
     const ContactArrays ca = c->contacts();
@@ -161,7 +162,7 @@ void enqueue_local_collision_iters(xpbd_ctx* c) {
         launch_mark_local(c->L(), ca, c->tets(), c->T, c->vmask.p, c->tmask.p);
     }
     const int ncol = (int)c->lcol_off.size() - 1;
-    for (int it = 0; it < p.num_local_collision_iters; it++) {
+    for (int it = 0; it < passes; it++) {
         if (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
             for (int pass = 0; pass < (separate ? 2 : 1); pass++)
                 for (int col = 0; col < ncol; col++) {
@@ -196,7 +197,10 @@ float self_alpha_tilde(const xpbd_ctx* c) {
     return (float)(1e-8 / (c->prm.first_order ? c->prm.dt : c->prm.dt * c->prm.dt));
 }
 
-int enqueue_update(xpbd_ctx* c, bool write_vel) {
+// solve_only: XPBDSolver::solve() alone (XPBDSolver.hpp:66-97) -- lambda <- 0
+// and num_iters sweeps on the current positions, with no inertial move, no
+// local collision passes, no fixed reset and no rigid-body update.
+int enqueue_update(xpbd_ctx* c, bool write_vel, bool solve_only) {
     const xpbd_params& p = c->prm;
     const int iters = p.num_iters;
     const bool track = tracking(c);
@@ -207,7 +211,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
     cudaStream_t s = c->stream;
     const ContactArrays ca = c->contacts();
     const bool have_faces = c->F > 0;
-    {
+    if (!solve_only) {
         Scope sc(c, K_PREDICT);
         if (p.first_order) launch_predict_first_order(c->L(), c->x.p, c->prev.p, c->gdz.p, c->V);
         else launch_predict(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, dz);
@@ -227,8 +231,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         if (track) cudaMemsetAsync(c->lam.p, 0, sizeof(float2) * (size_t)c->T, s);
     }
     const bool jacobi = p.solver_type == XPBD_SOLVER_JACOBI;
-    const bool local = have_faces && p.num_local_collision_iters > 0 && c->local_slots.p;
-    const bool fuse_final = !track && !local;
+    const bool local = !solve_only && have_faces && p.num_local_collision_iters > 0 && c->local_slots.p;
+    const bool fuse_final = !track && !local && !solve_only;
     if (jacobi) {
         const bool gather = p.jacobi_variant == XPBD_JACOBI_GATHER;
         if (track && !every_iter && !warm) exact_residual_row(c, 0, false);
@@ -309,8 +313,7 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         Scope sc(c, K_PROJECT_GS);
         if (versioned) {
             launch_sweep_versioned(c->L(), c->tets(), c->patches(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
-                                   c->xv.p, c->patch_w.p, c->V, c->npatches, c->flags.p, c->flow_grid,
-                                   p.gs_min_blocks);
+                                   c->xv.p, c->V, c->flags.p, c->flow_grid, p.gs_min_blocks, c->flow_resident);
             c->launches += 2;  // the copies into and out of the versioned positions
         } else
             launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
@@ -369,7 +372,8 @@ int enqueue_update(xpbd_ctx* c, bool write_vel) {
         }
         cudaMemcpyAsync(c->h_rows, c->res_rows.p, sizeof(double) * (iters + 1), cudaMemcpyDeviceToHost, s);
     }
-    if (local) enqueue_local_collision_iters(c);
+    if (solve_only) return XPBD_OK;
+    if (local) enqueue_local_collision_iters(c, p.num_local_collision_iters);
     if (!jacobi || !fuse_final || iters == 0) {
         Scope sc(c, K_FINALIZE);
         launch_finalize(c->L(), c->x.p, c->prev.p, c->vel.p, c->V, dt, write_vel);
@@ -457,18 +461,19 @@ int prepare_update(xpbd_ctx* c) {
     return XPBD_OK;
 }
 
-int run_update(xpbd_ctx* c, bool write_vel) {
+int run_update(xpbd_ctx* c, bool write_vel, bool solve_only) {
     int st = prepare_update(c);
     if (st) return st;
     if (c->graph_dirty) drop_graphs(c);
+    const int gi = solve_only ? 2 : (write_vel ? 1 : 0);
     if (c->prm.use_graphs && !c->prof.on) {
-        cudaGraphExec_t& ge = c->gexec[write_vel ? 1 : 0];
+        cudaGraphExec_t& ge = c->gexec[gi];
         if (!ge) {
             cudaGraph_t g = nullptr;
             XPBD_CU(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             const long long before = c->launches;
-            enqueue_update(c, write_vel);
-            c->graph_kernels[write_vel ? 1 : 0] = c->launches - before;
+            enqueue_update(c, write_vel, solve_only);
+            c->graph_kernels[gi] = c->launches - before;
             c->launches = before;
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             if (e != cudaSuccess) return cuda_check(c, e, "cudaStreamEndCapture");
@@ -480,9 +485,9 @@ int run_update(xpbd_ctx* c, bool write_vel) {
             }
         }
         XPBD_CU(c, cudaGraphLaunch(ge, c->stream));
-        c->launches += c->graph_kernels[write_vel ? 1 : 0];
+        c->launches += c->graph_kernels[gi];
     } else {
-        enqueue_update(c, write_vel);
+        enqueue_update(c, write_vel, solve_only);
     }
     c->rows_pending = tracking(c);
     c->last_rows = c->prm.num_iters + 1;
@@ -649,6 +654,7 @@ int xpbd_create_batch(const xpbd_mesh_desc* ms, int32_t n_inst, const xpbd_param
     xpbd_ctx* c = new (std::nothrow) xpbd_ctx();
     if (!c) return XPBD_ERR_CAPACITY;
     c->prm = *p;
+    c->flow_poll_ns = p->gs_poll_ns > 0 ? (unsigned)p->gs_poll_ns : kPollNs;
     c->V = (int)V;
     c->T = (int)T;
     c->F = (int)F;
@@ -1154,7 +1160,24 @@ int xpbd_get_self_contacts(xpbd_ctx* c, int32_t max_rows, int32_t* vf, double* l
 
 int xpbd_update(xpbd_ctx* c) {
     if (!c) return XPBD_ERR_INVALID;
-    return run_update(c, false);
+    return run_update(c, false, false);
+}
+
+int xpbd_solve(xpbd_ctx* c) {
+    if (!c) return XPBD_ERR_INVALID;
+    return run_update(c, false, true);
+}
+
+int xpbd_solve_local(xpbd_ctx* c, int32_t num_iter) {
+    if (!c || num_iter < 0) return XPBD_ERR_INVALID;
+    if (!c->F || !c->local_slots.p)
+        return fail(c, XPBD_ERR_STATE,
+                    "xpbd_solve_local: the context has no local collision passes (surface faces and "
+                    "num_local_collision_iters > 0 at creation)");
+    int st = prepare_update(c);
+    if (st) return st;
+    if (num_iter > 0 && c->F > 0) enqueue_local_collision_iters(c, num_iter);
+    return after_launches(c, "local collision passes");
 }
 
 int xpbd_velocity_update(xpbd_ctx* c) {
@@ -1182,7 +1205,7 @@ int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
             int st = xpbd_clear_collisions(c);
             if (st) return st;
         }
-        int st = run_update(c, true);
+        int st = run_update(c, true, false);
         if (st) return st;
         if (c->time - c->last_cd > interval) c->last_cd = c->time;
         c->time += c->prm.dt;

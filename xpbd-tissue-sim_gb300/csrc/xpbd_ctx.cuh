@@ -99,12 +99,13 @@ struct xpbd_ctx {
     DevBuf<int> flow_dep_off, flow_dep;
     DevBuf<unsigned> flow_epoch;  // ntasks epochs + the abort flag
     DevBuf<int4> patch_ver;       // variant 4: per patch, 8 x 16-bit deg << 8 | pre
-    DevBuf<float4> xv;            // variant 4: version-stamped positions
-    DevBuf<float4> patch_w;       // variant 4: per patch, its 8 inverse masses
+    DevBuf<xg::VerRec> xv;        // variant 4: version-stamped vertex records
+    bool flow_resident = false;   // variant 4: task topology kept in shared memory
     int npatches = 0;
     bool flow_versioned = false;  // variant 4 tables built (else variant 2 runs)
     std::vector<int4> patch_ver_h;  // host copy of patch_ver
     unsigned flow_poll_limit = xg::kFlowLimit;
+    unsigned flow_poll_ns = xg::kPollNs;
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -161,8 +162,9 @@ struct xpbd_ctx {
     double time = 0, last_cd = 0;
 
     // graphs: [write_vel]
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    long long graph_kernels[2] = {0, 0};  // kernels captured in each graph
+    // captured substep bodies: update, step (update + velocities), solve only
+    cudaGraphExec_t gexec[3] = {nullptr, nullptr, nullptr};
+    long long graph_kernels[3] = {0, 0, 0};  // kernels captured in each graph
     bool graph_dirty = true;
 
     Prof prof;
@@ -194,8 +196,8 @@ struct xpbd_ctx {
     }
 
     xg::TaskArrays tasks() {
-        return xg::TaskArrays{flow_tasks.p, flow_dep_off.p, flow_dep.p, flow_epoch.p, flow_epoch.p + ntasks, ntasks,
-                              flow_poll_limit};
+        return xg::TaskArrays{flow_tasks.p,       flow_dep_off.p, flow_dep.p,      flow_epoch.p,
+                              flow_epoch.p + ntasks, ntasks,        flow_poll_limit, flow_poll_ns};
     }
     xg::SelfArrays selfs() {
         return xg::SelfArrays{s_tets.p,        s_Q.p,          s_X0.p,         s_X0f.p,      s_surf.p,

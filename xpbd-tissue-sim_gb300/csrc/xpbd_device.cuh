@@ -71,18 +71,20 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 
 constexpr unsigned kWaitLimit = 1u << 20;
 
-__device__ __forceinline__ float warp_sum(float v) {
+// FP64 butterfly over the warp (each step is two 32-bit shuffles).
+__device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-// Fixed-order block sum: FP32 inside a warp, FP64 across warps.
-__device__ __forceinline__ void block_sum_store(float v, double* slot) {
+// Fixed-order block sum in FP64 from the lane up: the caller widens each
+// lane's term before squaring, the warp and the block add in double.
+__device__ __forceinline__ void block_sum_store(double v, double* slot) {
     __shared__ double sw[32];
     v = warp_sum(v);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) sw[wid] = (double)v;
+    if (lane == 0) sw[wid] = v;
     __syncthreads();
     if (threadIdx.x == 0) {
         double s = 0.0;
@@ -180,6 +182,25 @@ __device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R g
 #pragma unroll
         for (int k = 0; k < 3; k++)
             gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
+}
+
+// Constraint values only (no gradients): C_dev = ||F||_F and C_hyd
+// (DeviatoricConstraint.hpp:112-116, HydrostaticConstraint.hpp:123-153).
+template <typename R>
+__device__ __forceinline__ void tet_C(const TetState<R>& s, R& Cd, R& Ch) {
+    R F[9];
+    tet_F(s, F);
+    R ss = 0;
+#pragma unroll
+    for (int i = 0; i < 9; i++) ss += F[i] * F[i];
+    Cd = dev_sqrt(ss);
+    const R J = tet_detF(F);
+    if (J >= R(1)) {
+        Ch = -s.gam + dev_log(J);
+    } else {
+        const R d = J - R(1);
+        Ch = -s.gam + d - d * d / R(2) + d * d * d / R(3);
+    }
 }
 
 __device__ __forceinline__ float dot3(const float* a, const float* b) {
@@ -398,11 +419,11 @@ __device__ __noinline__ Fp64Out project_single_fp64(TetArrays t, int slot, float
 
 // One tet projection in the chosen constraint form. On return d holds the
 // vertex updates, lam the updated multipliers and rsq the squared residual of
-// the state the projection saw. Returns false when the update is non-finite
+// the state the projection saw (squared and added in FP64). Returns false when the update is non-finite
 // (then nothing may be applied).
 template <bool SEPARATE>
 __device__ __forceinline__ bool project_one(const TetState<float>& s, const TetArrays& t, int slot, const float4 xp[4],
-                                            float2& lam, float d[4][3], float& rsq, Flags* flags) {
+                                            float2& lam, float d[4][3], double& rsq, Flags* flags) {
     float J;
     if (!SEPARATE) {
         float r0, r1, dl0, dl1;
@@ -416,7 +437,7 @@ __device__ __forceinline__ bool project_one(const TetState<float>& s, const TetA
                 for (int k = 0; k < 3; k++) d[i][k] = o.d[3 * i + k];
             atomicAdd(&flags->degenerate, 1ull);
         }
-        rsq = r0 * r0 + r1 * r1;
+        rsq = fma((double)r0, (double)r0, (double)r1 * (double)r1);
         if (!(isfinite(dl0) && isfinite(dl1))) {
             atomicAdd(&flags->nonfinite, 1ull);
             return false;
@@ -442,7 +463,7 @@ __device__ __forceinline__ bool project_one(const TetState<float>& s, const TetA
                 }
             atomicAdd(&flags->degenerate, 1ull);
         }
-        rsq = r0 * r0 + r1 * r1;
+        rsq = fma((double)r0, (double)r0, (double)r1 * (double)r1);
         if (!(isfinite(dl0) && isfinite(dl1))) {
             atomicAdd(&flags->nonfinite, 1ull);
             return false;

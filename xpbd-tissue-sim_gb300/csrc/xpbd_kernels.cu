@@ -63,7 +63,7 @@ template <bool FIRST, bool SEPARATE, bool RES>
 __global__ void __launch_bounds__(256) k_project_jacobi(TetArrays t, int T, const float4* __restrict__ x,
                                                         float4* __restrict__ dx, ResidualSink res, Flags* flags) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    float rsq = 0.f;
+    double rsq = 0.0;
     int4 e;
     TetState<float> s;
     if (slot < T) load_tet_static(t, slot, e, s);
@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) k_project_jacobi_write(TetArrays t, int T
                                                               float4* __restrict__ dxt, ResidualSink res,
                                                               Flags* flags) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    float rsq = 0.f;
+    double rsq = 0.0;
     int4 e;
     TetState<float> s;
     if (slot < T) load_tet_static(t, slot, e, s);
@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t
         float d[4][3];
         bool ok;
         if (WHICH == 2) {
-            float rsq;
+            double rsq;
             ok = project_one<false>(st, t, slot, xp, lam, d, rsq, flags);
         } else {
             float J, r, dl;
@@ -341,7 +341,7 @@ __global__ void __launch_bounds__(kPatchBlock) k_project_patch_reg(TetArrays t, 
         float d[4][3];
         bool ok;
         if (WHICH == 2) {
-            float rsq;
+            double rsq;
             ok = project_one<false>(st[i], t, slot, xp, lam, d, rsq, flags);
         } else {
             float J, r, dl;
@@ -718,14 +718,17 @@ __global__ void k_velocity(const float4* __restrict__ x, const float4* __restric
     vel[i] = make_float4((xx.x - p.x) / dt, (xx.y - p.y) / dt, (xx.z - p.z) / dt, 0.f);
 }
 
-// Exact residual / energy at the current state. rvec (optional) receives the
-// per-constraint residuals in the reference's order via the slot->tet map.
+// Exact residual / energy of the current (FP32) state, evaluated in FP64:
+// C from the positions widened to double, r = C + alpha~ lambda and r^2 in
+// double, so the norm that decides convergence carries no FP32 evaluation
+// noise. rvec (optional) receives the per-constraint residuals (rounded to
+// float) in the reference's order via the slot->tet map.
 __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const float4* __restrict__ x, bool separate,
                                                   const int* __restrict__ perm, float* __restrict__ rvec,
                                                   ResidualSink res, double* __restrict__ energy_partial, float dt2,
                                                   bool zero_lam) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
-    float rsq = 0.f, en = 0.f;
+    double rsq = 0.0, en = 0.0;
     int4 e;
     TetState<float> s;
     if (slot < T) load_tet_static(t, slot, e, s);
@@ -734,15 +737,25 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
         float4 xp[4];
         gather_tet(x, e, s, xp);
         const float2 lam = zero_lam ? make_float2(0.f, 0.f) : t.lam[slot];
-        float Cd, Ch, gd[9], gh[9], J;
-        tet_eval(s, Cd, Ch, gd, gh, J);
-        const float r0 = Cd + s.atd * lam.x, r1 = Ch + s.ath * lam.y;
-        rsq = r0 * r0 + r1 * r1;
-        en = Cd * Cd / (s.atd * dt2) + Ch * Ch / (s.ath * dt2);
+        TetState<double> sd;
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+#pragma unroll
+            for (int k = 0; k < 3; k++) sd.p[i][k] = s.p[i][k];
+            sd.w[i] = s.w[i];
+        }
+#pragma unroll
+        for (int i = 0; i < 9; i++) sd.q[i] = s.q[i];
+        sd.atd = s.atd; sd.ath = s.ath; sd.gam = s.gam;
+        double Cd, Ch;
+        tet_C(sd, Cd, Ch);
+        const double r0 = fma(sd.atd, (double)lam.x, Cd), r1 = fma(sd.ath, (double)lam.y, Ch);
+        rsq = fma(r0, r0, r1 * r1);
+        en = Cd * Cd / (sd.atd * dt2) + Ch * Ch / (sd.ath * dt2);
         if (rvec) {
             const int tt = perm ? perm[slot] : slot;
-            if (!separate) { rvec[2 * (size_t)tt] = r0; rvec[2 * (size_t)tt + 1] = r1; }
-            else { rvec[tt] = r0; rvec[(size_t)T + tt] = r1; }
+            if (!separate) { rvec[2 * (size_t)tt] = (float)r0; rvec[2 * (size_t)tt + 1] = (float)r1; }
+            else { rvec[tt] = (float)r0; rvec[(size_t)T + tt] = (float)r1; }
         }
     }
     if (res.partial) block_sum_store(rsq, res.partial + (size_t)res.row * res.stride + res.offset + blockIdx.x);
@@ -862,7 +875,8 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
                         st.w[q] = fabsf(xp[q].w);
                     }
                     float2 lam = lams[i];
-                    float d[4][3], rsq;
+                    float d[4][3];
+                    double rsq;
                     if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
                         for (int q = 0; q < 4; q++)
@@ -989,7 +1003,8 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
                         st.w[q] = fabsf(xp[q].w);
                     }
                     float2 lam = lams[i];
-                    float d[4][3], rsq;
+                    float d[4][3];
+                    double rsq;
                     if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
                         for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
@@ -1008,61 +1023,58 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
 }
 
 // ---- dataflow Gauss-Seidel on version-stamped vertices ----
-// The sweep works on its own copy xv of the positions whose w word holds the
-// vertex's version: how many patch projections have written it in this
-// launch. In one iteration a vertex is written by each patch containing it,
-// in colour order, so the patch of colour c reads vertex v once its version
-// is it * deg(v) + pre(v, c) (deg: patches containing v, pre: those of a lower
-// colour) -- the state the colour-by-colour launches give it. A writer stores
-// position and version as one aligned 16-byte vector and a reader loads them
-// the same way; the hardware serves an aligned 16-byte access as one request
-// to one L2 sector, so a reader that sees the version sees the position
-// written with it (the PTX memory model itself promises single-copy atomicity
-// only up to 64 bits). The poll is the load, and no fence or task counter
-// sits between two phases.
+// The sweep works on its own copy xv of the positions, one 32-byte record per
+// vertex (VerRec): the words (x, ver), (y, ver), (z, ver), (w, 0), where ver
+// is the vertex's version -- how many patch projections have written it in
+// this launch. In one iteration a vertex is written by each patch containing
+// it, in colour order, so the patch of colour c reads vertex v once its
+// version is it * deg(v) + pre(v, c) (deg: patches containing v, pre: those
+// of a lower colour) -- the state the colour-by-colour launches give it.
+// Each coordinate travels in one aligned 64-bit word with the version it was
+// written with, and the PTX memory model makes an aligned 64-bit access
+// single-copy atomic (a vector access counts as one access per element): a
+// reader that sees the due version in all three words holds the three
+// coordinates written with it, and a read that met a write half-way shows an
+// older version in some word and is polled again. A record is one 32-byte
+// L2 sector, read and written by one 256-bit vector access (.v4.b64). The
+// poll is the load; no fence or task counter sits between two phases.
 
-__device__ __forceinline__ float4 ld_relaxed_f4(const float4* p) {
-    float4 v;
-    asm volatile("ld.relaxed.gpu.global.v4.f32 {%0, %1, %2, %3}, [%4];"
-                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+__device__ __forceinline__ void ld_ver(const VerRec* p, unsigned long long& a, unsigned long long& b,
+                                       unsigned long long& c, unsigned long long& d) {
+    asm volatile("ld.relaxed.gpu.global.v4.b64 {%0, %1, %2, %3}, [%4];"
+                 : "=l"(a), "=l"(b), "=l"(c), "=l"(d)
                  : "l"(p)
                  : "memory");
-    return v;
 }
-__device__ __forceinline__ void st_relaxed_f4(float4* p, float4 v) {
-    asm volatile("st.relaxed.gpu.global.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(p), "f"(v.x), "f"(v.y), "f"(v.z),
-                 "f"(v.w)
+// the fourth word (the inverse mass) is written back unchanged
+__device__ __forceinline__ void st_ver(VerRec* p, float x, float y, float z, float w, unsigned ver) {
+    const unsigned long long hi = (unsigned long long)ver << 32;
+    const unsigned long long a = hi | __float_as_uint(x), b = hi | __float_as_uint(y), c = hi | __float_as_uint(z);
+    const unsigned long long d = __float_as_uint(w);
+    asm volatile("st.relaxed.gpu.global.v4.b64 [%0], {%1, %2, %3, %4};" ::"l"(p), "l"(a), "l"(b), "l"(c), "l"(d)
                  : "memory");
 }
-
-// Positions at version 0, and per patch the inverse masses of its 8 vertex
-// slots (two float4: the sweep reads them with its other per-patch records).
-__global__ void k_versions_in(float4* __restrict__ xv, float4* __restrict__ pw, const float4* __restrict__ x,
-                              PatchArrays pa, int V, int P) {
-    pdl_wait_then_release();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < V) {
-        const float4 p = x[i];
-        xv[i] = make_float4(p.x, p.y, p.z, __int_as_float(0));
-    }
-    if (i < P) {
-        const int nv = __ldg(&pa.meta[i].y) >> 8;
-        const int4 va = __ldg(pa.verts + 2 * (size_t)i), vb = __ldg(pa.verts + 2 * (size_t)i + 1);
-        const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
-        float w[kMaxPatchVerts];
-#pragma unroll
-        for (int k = 0; k < kMaxPatchVerts; k++) w[k] = k < nv ? x[vid[k]].w : 0.f;
-        pw[2 * (size_t)i] = make_float4(w[0], w[1], w[2], w[3]);
-        pw[2 * (size_t)i + 1] = make_float4(w[4], w[5], w[6], w[7]);
-    }
+__device__ __forceinline__ float ver_val(unsigned long long w) { return __uint_as_float((unsigned)w); }
+__device__ __forceinline__ int ver_of(unsigned long long w) { return (int)(w >> 32); }
+__device__ __forceinline__ int ver_min(unsigned long long a, unsigned long long b, unsigned long long c) {
+    return min(ver_of(a), min(ver_of(b), ver_of(c)));
 }
 
-__global__ void k_versions_out(float4* __restrict__ x, const float4* __restrict__ xv, int V) {
+// Positions at version 0, the inverse mass in the fourth word.
+__global__ void k_versions_in(VerRec* __restrict__ xv, const float4* __restrict__ x, int V) {
     pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
-    const float4 p = xv[i];
-    x[i] = make_float4(p.x, p.y, p.z, x[i].w);
+    const float4 p = x[i];
+    xv[i] = VerRec{__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z), __float_as_uint(p.w)};
+}
+
+__global__ void k_versions_out(float4* __restrict__ x, const VerRec* __restrict__ xv, int V) {
+    pdl_wait_then_release();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    const VerRec r = xv[i];
+    x[i] = make_float4(ver_val(r.x), ver_val(r.y), ver_val(r.z), x[i].w);
 }
 
 // Warp w runs the w-th task of every colour (the task layout of
@@ -1070,30 +1082,66 @@ __global__ void k_versions_out(float4* __restrict__ x, const float4* __restrict_
 // are due and writes them back one version later. The smallest unfinished
 // task always has its vertices due and its warp at it (all blocks are
 // co-resident), so the waits end; each is bounded anyway, and one that gives
-// up sets abort_flag so that every other waiter leaves. Inverse masses come
-// from the per-patch copy pw. The projections and their order are those of
-// the colour launches; the results equal k_sweep_dataflow's bit for bit.
-template <bool FIRST_ZERO, int MINB>
+// up sets abort_flag so that every other waiter leaves. The projections and
+// their order are those of the colour launches; the results equal
+// k_sweep_dataflow's bit for bit.
+// RESIDENT: the warp's tasks' topology (patch record, vertex ids, version
+// words: four int4 per lane and task) is read once into shared memory, before
+// the wait on the previous kernel, so a phase's first poll does not wait for
+// the task, patch and vertex-id loads.
+template <bool FIRST_ZERO, bool RESIDENT, int MINB>
 __global__ void __launch_bounds__(kFlowBlock, MINB)
     k_sweep_versioned(TetArrays t, PatchArrays pa, const int4* __restrict__ pver, TaskArrays ta, int iters,
-                      const float4* __restrict__ pw, float4* __restrict__ xv, Flags* flags) {
+                      VerRec* __restrict__ xv, Flags* flags) {
+    static_assert(kFlowBlock == 32, "one warp per block: the topology is indexed by lane");
+    extern __shared__ int4 topo[];  // RESIDENT: [task k][meta, verts a, verts b, versions][lane]
     __shared__ float4 sv[kMaxPatchVerts][kFlowBlock];
     const int tid = threadIdx.x, lane = tid & 31;
     const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (RESIDENT) {
+        int k = 0;
+        for (int j = gw; j < ta.ntasks; j += nw, k++) {
+            const int4 tk = __ldg(ta.task + j);
+            int4 meta = make_int4(0, 0, 0, 0), va = meta, vb = meta, vr = meta;
+            if (lane < tk.y) {
+                const int p = tk.x + lane;
+                meta = __ldg(pa.meta + p);
+                va = __ldg(pa.verts + 2 * (size_t)p);
+                vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+                vr = __ldg(pver + p);
+            }
+            topo[(4 * k + 0) * 32 + lane] = meta;
+            topo[(4 * k + 1) * 32 + lane] = va;
+            topo[(4 * k + 2) * 32 + lane] = vb;
+            topo[(4 * k + 3) * 32 + lane] = vr;
+        }
+        __syncwarp();
+    }
     pdl_wait_then_release();
     for (int it = 0; it < iters; it++) {
-        for (int j = gw; j < ta.ntasks; j += nw) {
-            const int4 tk = __ldg(ta.task + j);
-            const int p = tk.x + lane;
+        int k = 0;
+        for (int j = gw; j < ta.ntasks; j += nw, k++) {
+            int4 meta, va, vb, vr;
+            if (RESIDENT) {
+                meta = topo[(4 * k + 0) * 32 + lane];
+                va = topo[(4 * k + 1) * 32 + lane];
+                vb = topo[(4 * k + 2) * 32 + lane];
+                vr = topo[(4 * k + 3) * 32 + lane];
+            } else {
+                const int4 tk = __ldg(ta.task + j);
+                meta = va = vb = vr = make_int4(0, 0, 0, 0);
+                if (lane < tk.y) {
+                    const int p = tk.x + lane;
+                    meta = __ldg(pa.meta + p);
+                    va = __ldg(pa.verts + 2 * (size_t)p);
+                    vb = __ldg(pa.verts + 2 * (size_t)p + 1);
+                    vr = __ldg(pver + p);
+                }
+            }
+            const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
             bool ok = true;
-            if (lane < tk.y) {
-                const int4 meta = __ldg(pa.meta + p);
-                const int4 va = __ldg(pa.verts + 2 * (size_t)p), vb = __ldg(pa.verts + 2 * (size_t)p + 1);
-                const int4 vr = __ldg(pver + p);
-                const float4 wa = __ldg(pw + 2 * (size_t)p), wb = __ldg(pw + 2 * (size_t)p + 1);
-                const float wv[kMaxPatchVerts] = {wa.x, wa.y, wa.z, wa.w, wb.x, wb.y, wb.z, wb.w};
-                const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
+            if (nverts > 0) {
                 float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
                 float2 lams[kMaxPatchTets];
 #pragma unroll
@@ -1111,13 +1159,14 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 int due[kMaxPatchVerts];
                 unsigned pending = 0;
 #pragma unroll
-                for (int k = 0; k < kMaxPatchVerts; k++) {
-                    const int h = (vw[k >> 1] >> (16 * (k & 1))) & 0xffff;  // deg << 8 | pre
-                    due[k] = it * (h >> 8) + (h & 0xff);
-                    if (k < nverts) {
-                        const float4 v = ld_relaxed_f4(xv + vid[k]);
-                        sv[k][tid] = make_float4(v.x, v.y, v.z, wv[k]);
-                        if (__float_as_int(v.w) < due[k]) pending |= 1u << k;
+                for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+                    const int h = (vw[k2 >> 1] >> (16 * (k2 & 1))) & 0xffff;  // deg << 8 | pre
+                    due[k2] = it * (h >> 8) + (h & 0xff);
+                    if (k2 < nverts) {
+                        unsigned long long a, b, c, d;
+                        ld_ver(xv + vid[k2], a, b, c, d);
+                        sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
+                        if (ver_min(a, b, c) < due[k2]) pending |= 1u << k2;
                     }
                 }
                 unsigned n = 0;
@@ -1126,16 +1175,17 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                         ok = false;
                         break;
                     }
-                    __nanosleep(1024);  // polls cost L2 bandwidth the writers need
+                    __nanosleep(ta.poll_ns);  // polls cost L2 bandwidth the writers need
 #pragma unroll
-                    for (int k = 0; k < kMaxPatchVerts; k++) {
-                        if (pending & (1u << k)) {
-                            const float4 v = ld_relaxed_f4(xv + vid[k]);
-                            if (__float_as_int(v.w) >= due[k]) {
-                                sv[k][tid].x = v.x;
-                                sv[k][tid].y = v.y;
-                                sv[k][tid].z = v.z;
-                                pending &= ~(1u << k);
+                    for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+                        if (pending & (1u << k2)) {
+                            unsigned long long a, b, c, d;
+                            ld_ver(xv + vid[k2], a, b, c, d);
+                            if (ver_min(a, b, c) >= due[k2]) {
+                                sv[k2][tid].x = ver_val(a);
+                                sv[k2][tid].y = ver_val(b);
+                                sv[k2][tid].z = ver_val(c);
+                                pending &= ~(1u << k2);
                             }
                         }
                     }
@@ -1161,7 +1211,8 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                             st.w[q] = fabsf(xp[q].w);
                         }
                         float2 lam = lams[i];
-                        float d[4][3], rsq;
+                        float d[4][3];
+                        double rsq;
                         if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
                             for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
@@ -1170,10 +1221,10 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     }
                     // every vertex goes out one version later, moved or not
 #pragma unroll
-                    for (int k = 0; k < kMaxPatchVerts; k++) {
-                        if (k < nverts) {
-                            const float4 s = sv[k][tid];
-                            st_relaxed_f4(xv + vid[k], make_float4(s.x, s.y, s.z, __int_as_float(due[k] + 1)));
+                    for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+                        if (k2 < nverts) {
+                            const float4 sp = sv[k2][tid];
+                            st_ver(xv + vid[k2], sp.x, sp.y, sp.z, sp.w, (unsigned)(due[k2] + 1));
                         }
                     }
                 }
@@ -1295,7 +1346,7 @@ __global__ void k_project_local_gs(TetArrays t, const int* __restrict__ order, i
     float d[4][3];
     bool ok;
     if (which == 2) {
-        float rsq;
+        double rsq;
         ok = project_one<false>(s, t, slot, xp, lam, d, rsq, flags);
     } else {
         float J, r, dl;
@@ -1337,7 +1388,8 @@ __global__ void k_project_local_jacobi(TetArrays t, int T, const unsigned char* 
     float4 xp[4];
     gather_tet(x, e, s, xp);
     float2 lam = t.lam[slot];
-    float d[4][3], rsq;
+    float d[4][3];
+    double rsq;
     if (project_one<SEPARATE>(s, t, slot, xp, lam, d, rsq, flags)) {
         add_vec4(dx + e.x, d[0][0], d[0][1], d[0][2]);
         add_vec4(dx + e.y, d[1][0], d[1][1], d[1][2]);
@@ -1648,44 +1700,61 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
 #undef XG_FLOW
 }
 
-int sweep_versioned_blocks_per_sm(int min_blocks) {
+int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp) {
     int n = 0, m = 0;
     cudaError_t e;
-#define XG_VOCC(M)                                                                                 \
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_versioned<true, M>, kFlowBlock, 0); \
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_versioned<false, M>, kFlowBlock, 0)
-    if (min_blocks == 8) { XG_VOCC(8); }
-    else if (min_blocks == 6) { XG_VOCC(6); }
-    else { XG_VOCC(1); }
+    const size_t smem = sweep_versioned_smem(tasks_per_warp);
+    const bool res = tasks_per_warp > 0;
+#define XG_VOCC(R, M)                                                                                              \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_versioned<true, R, M>, kFlowBlock, smem);       \
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_versioned<false, R, M>,   \
+                                                                             kFlowBlock, smem)
+    if (res) {
+        if (min_blocks == 8) { XG_VOCC(true, 8); }
+        else if (min_blocks == 6) { XG_VOCC(true, 6); }
+        else { XG_VOCC(true, 1); }
+    } else {
+        if (min_blocks == 8) { XG_VOCC(false, 8); }
+        else if (min_blocks == 6) { XG_VOCC(false, 6); }
+        else { XG_VOCC(false, 1); }
+    }
 #undef XG_VOCC
     if (e != cudaSuccess) return 0;
     return n < m ? n : m;
 }
 
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
-                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, float4* xv,
-                                   float4* pw, int V, int P, Flags* flags, int grid, int min_blocks) {
+                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
+                                   Flags* flags, int grid, int min_blocks, bool resident) {
     if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
-    go(k_versions_in, nblk(V > P ? V : P, 256), 256, s, xv, pw, (const float4*)x, pa, V, P);
+    go(k_versions_in, nblk(V, 256), 256, s, xv, (const float4*)x, V);
+    const int warps = grid * (kFlowBlock / 32);
+    const int per_warp = (ta.ntasks + warps - 1) / warps;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kFlowBlock);
+    cfg.dynamicSmemBytes = resident ? sweep_versioned_smem(per_warp) : 0;
     cfg.stream = s.s;
     cudaLaunchAttribute attr[1];
     attr[0].id = cudaLaunchAttributeCooperative;
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const float4* pwc = pw;
     cudaError_t e;
-#define XG_VER(F, M) e = cudaLaunchKernelEx(&cfg, k_sweep_versioned<F, M>, t, pa, pver, ta, iters, pwc, xv, flags)
-    if (min_blocks == 8) { if (first_zero) XG_VER(true, 8); else XG_VER(false, 8); }
-    else if (min_blocks == 6) { if (first_zero) XG_VER(true, 6); else XG_VER(false, 6); }
-    else if (first_zero) XG_VER(true, 1);
-    else XG_VER(false, 1);
+#define XG_VER(F, R, M) e = cudaLaunchKernelEx(&cfg, k_sweep_versioned<F, R, M>, t, pa, pver, ta, iters, xv, flags)
+#define XG_VER_M(F, R)                       \
+    if (min_blocks == 8) { XG_VER(F, R, 8); } \
+    else if (min_blocks == 6) { XG_VER(F, R, 6); } \
+    else { XG_VER(F, R, 1); }
+    if (resident) {
+        if (first_zero) { XG_VER_M(true, true) } else { XG_VER_M(false, true) }
+    } else {
+        if (first_zero) { XG_VER_M(true, false) } else { XG_VER_M(false, false) }
+    }
+#undef XG_VER_M
 #undef XG_VER
     if (e != cudaSuccess) return e;
-    go(k_versions_out, nblk(V, 256), 256, s, x, (const float4*)xv, V);
+    go(k_versions_out, nblk(V, 256), 256, s, x, (const VerRec*)xv, V);
     return cudaSuccess;
 }
 

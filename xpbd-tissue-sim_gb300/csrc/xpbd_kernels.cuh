@@ -114,7 +114,22 @@ struct TaskArrays {
     unsigned* abort_flag; // set when a wait gives up; every waiter then leaves
     int ntasks;
     unsigned poll_limit;  // polls of one wait before it gives up
+    unsigned poll_ns;     // variant 4: back-off between two polls of a vertex not yet due
 };
+
+// Variant 4's vertex record: four aligned 64-bit words (x, ver), (y, ver),
+// (z, ver), (w, 0); low 32 bits the float's bits, high 32 bits the version
+// (projections that wrote the vertex in this launch). w is the inverse mass,
+// which the sweep reads and writes back unchanged. 32-byte aligned: one
+// 256-bit access moves a record.
+struct alignas(32) VerRec {
+    unsigned long long x, y, z, w;
+};
+constexpr unsigned kPollNs = 1024;  // default back-off of variant 4's polls
+// variant 4 keeps the topology of a warp's tasks (patch records, vertex ids,
+// version words: 64 B per lane and task) in shared memory across iterations
+// when the warp owns at most this many tasks per iteration
+constexpr int kResidentTasks = 10;
 
 // Self-collisions (DeformableDeformableCollisionConstraint): a uniform grid
 // over the positions, each tet in the cell of its centroid, queries over the
@@ -228,14 +243,19 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
 // min_blocks (variant 2): 0 = no register cap, 6 or 8 blocks per SM
 int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 // Variant 4: the dataflow sweep on version-stamped vertices. Copies x into
-// xv (version 0) and the patches' inverse masses into pw (2P), runs every
-// iteration and colour in one cooperative launch and copies the positions
-// back; pver holds per patch and vertex slot the 16-bit deg << 8 | pre of
-// that vertex (patches containing it, those of a lower colour).
+// the records xv (version 0), runs every iteration and colour in one
+// cooperative launch and copies the positions back; pver holds per patch and
+// vertex slot the 16-bit deg << 8 | pre of that vertex (patches containing
+// it, those of a lower colour). resident: each warp's task topology stays in
+// shared memory (ntasks / warps <= kResidentTasks; sweep_versioned_smem bytes
+// per block).
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
-                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, float4* xv,
-                                   float4* pw, int V, int P, Flags* flags, int grid, int min_blocks);
-int sweep_versioned_blocks_per_sm(int min_blocks);
+                                   const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
+                                   Flags* flags, int grid, int min_blocks, bool resident);
+// blocks per SM of the versioned sweep with the dynamic shared memory it
+// needs when each warp owns `tasks_per_warp` tasks (0: not resident)
+int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp);
+inline size_t sweep_versioned_smem(int tasks_per_warp) { return (size_t)tasks_per_warp * 4 * 32 * sizeof(int4); }
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 // after a detection: per instance and face colour, the faces with an active
 // static contact (ifl: faces by instance, colour, index; ifo_off its ranges)

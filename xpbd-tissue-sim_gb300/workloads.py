@@ -19,6 +19,11 @@ Boundary conditions follow the reference's patterns: clamp by min-y
 (src/simulation/BeamSimulation.cpp:31-34), fix the bottom by min-z
 (src/simulation/GraspingSimulation.cpp:41), kinematic vertices as fixVertex plus
 a prescribed position (GraspingSimulation.cpp:155,241).
+
+The builders take the grid generator as `mesher` (the library's
+xpbd_gb300.grid_mesh by default); the CPU reference arm passes the oracle's
+own generator, so building a workload there loads nothing of the GPU library.
+This module imports xpbd_gb300 only inside the functions that make solvers.
 """
 from __future__ import annotations
 
@@ -26,7 +31,16 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-import xpbd_gb300 as G
+# solver-type codes of the C ABI (XPBD_SOLVER_GAUSS_SEIDEL, XPBD_SOLVER_JACOBI)
+GAUSS_SEIDEL = 0
+JACOBI = 1
+
+
+def _mesher(mesher):
+    if mesher is not None:
+        return mesher
+    import xpbd_gb300 as G
+    return G.grid_mesh
 
 
 @dataclass
@@ -43,7 +57,7 @@ class Workload:
     dt: float = 1e-3
     g: float = 9.81
     iters: int = 10
-    solver: int = G.SOLVER_GAUSS_SEIDEL
+    solver: int = GAUSS_SEIDEL
     steps: int = 100
     sphere_r: float = 0.0
     sphere_c0: np.ndarray | None = None  # centre at t = 0
@@ -69,26 +83,26 @@ class Workload:
         return self.kin_dir * min(step / self.kin_ramp_steps, 1.0)
 
 
-def cube(n: int = 10, seed: int = 0, noise: float = 1e-3) -> Workload:
-    X, tets, faces = G.grid_mesh(n, n, n, 1.0 / n)
+def cube(n: int = 10, seed: int = 0, noise: float = 1e-3, mesher=None) -> Workload:
+    X, tets, faces = _mesher(mesher)(n, n, n, 1.0 / n)
     rng = np.random.default_rng(seed)
     x0 = X + rng.uniform(-noise, noise, X.shape)
     T = tets.shape[0]
     return Workload("cube", X, tets, faces, np.full(T, 3e3), np.full(T, 0.45), np.full(T, 1000.0),
-                    fixed=X[:, 2] == X[:, 2].min(), x0=x0, iters=10, solver=G.SOLVER_GAUSS_SEIDEL, steps=200)
+                    fixed=X[:, 2] == X[:, 2].min(), x0=x0, iters=10, solver=GAUSS_SEIDEL, steps=200)
 
 
 def beam(nl: int = 100, nw: int = 10, nh: int = 10, length: float = 0.5, with_sphere: bool = True,
-         jacobi: bool = False) -> Workload:
+         jacobi: bool = False, mesher=None) -> Workload:
     h = length / nl
-    X, tets, faces = G.grid_mesh(nw, nl, nh, h)
+    X, tets, faces = _mesher(mesher)(nw, nl, nh, h)
     T = tets.shape[0]
     top = X[:, 2].max()
     r = 0.03
     c0 = np.array([X[:, 0].max() / 2, X[:, 1].max() / 2, top + r - 0.002])
     w = Workload("beam", X, tets, faces, np.full(T, 1e4), np.full(T, 0.49), np.full(T, 1000.0),
                  fixed=X[:, 1] == X[:, 1].min(), x0=X.copy(), iters=20,
-                 solver=G.SOLVER_JACOBI if jacobi else G.SOLVER_GAUSS_SEIDEL, steps=500)
+                 solver=JACOBI if jacobi else GAUSS_SEIDEL, steps=500)
     if with_sphere:
         w.sphere_r = r
         w.sphere_c0 = c0
@@ -96,15 +110,16 @@ def beam(nl: int = 100, nw: int = 10, nh: int = 10, length: float = 0.5, with_sp
     return w
 
 
-def block(n: int = 64, size: float = 0.1, seed: int = 0, E_range=(1e3, 1e5), iters: int = 30) -> Workload:
-    X, tets, faces = G.grid_mesh(n, n, n, size / n)
+def block(n: int = 64, size: float = 0.1, seed: int = 0, E_range=(1e3, 1e5), iters: int = 30,
+          mesher=None) -> Workload:
+    X, tets, faces = _mesher(mesher)(n, n, n, size / n)
     T = tets.shape[0]
     rng = np.random.default_rng(seed)
     E = np.exp(rng.uniform(np.log(E_range[0]), np.log(E_range[1]), T))
     zmin, zmax = X[:, 2].min(), X[:, 2].max()
     top = np.nonzero(X[:, 2] == zmax)[0].astype(np.int32)
     return Workload("block", X, tets, faces, E, np.full(T, 0.45), np.full(T, 1000.0),
-                    fixed=X[:, 2] == zmin, x0=X.copy(), iters=iters, solver=G.SOLVER_GAUSS_SEIDEL, steps=100,
+                    fixed=X[:, 2] == zmin, x0=X.copy(), iters=iters, solver=GAUSS_SEIDEL, steps=100,
                     kin_idx=top, kin_dir=np.array([0.0, 0.0, 0.01]), kin_ramp_steps=100)
 
 
@@ -132,7 +147,7 @@ class Batch:
 
 
 def batched(n: int = 256, seed: int = 0, t_range=(2_000, 100_000), iters: int = 20,
-            solver: int = G.SOLVER_GAUSS_SEIDEL) -> Batch:
+            solver: int = GAUSS_SEIDEL, mesher=None) -> Batch:
     """n cube/beam instances with tet counts log-uniform in t_range (seeded grid
     dims, T = 5 nx ny nz), E log-uniform in [1e3, 1e5] Pa, nu in [0.40, 0.49],
     rho 1000, bottom fixed, 1-4 seeded spheres descending at 0.05 m/s onto the
@@ -148,7 +163,7 @@ def batched(n: int = 256, seed: int = 0, t_range=(2_000, 100_000), iters: int = 
             m = max(2, int(round((target / 4) ** (1 / 3))))
             nx, ny, nz = m, 4 * m, m
         h = 0.05 / nx
-        X, tets, faces = G.grid_mesh(nx, ny, nz, h)
+        X, tets, faces = _mesher(mesher)(nx, ny, nz, h)
         T = tets.shape[0]
         E = np.full(T, float(np.exp(rng.uniform(np.log(1e3), np.log(1e5)))))
         nu = np.full(T, float(rng.uniform(0.40, 0.49)))
@@ -167,8 +182,9 @@ def batched(n: int = 256, seed: int = 0, t_range=(2_000, 100_000), iters: int = 
     return Batch(out)
 
 
-def make_batch_solver(b: Batch, **params) -> G.XPBDSolver:
+def make_batch_solver(b: Batch, **params):
     """One context holding every instance of the batch."""
+    import xpbd_gb300 as G
     w0 = b.instances[0]
     kw = dict(dt=w0.dt, g_accel=w0.g, num_iters=w0.iters, solver_type=w0.solver, collision_rate=w0.collision_rate)
     kw.update(params)
@@ -178,7 +194,7 @@ def make_batch_solver(b: Batch, **params) -> G.XPBDSolver:
     return s
 
 
-def drive_batch(s: G.XPBDSolver, b: Batch):
+def drive_batch(s, b: Batch):
     """Sphere centres of every instance at the solver's current time."""
     t = s.time
     for k, w in enumerate(b.instances):
@@ -186,9 +202,10 @@ def drive_batch(s: G.XPBDSolver, b: Batch):
         s.set_spheres(c + w.sphere_v * t, r, instance=k)
 
 
-def make_solver(w: Workload, **params) -> G.XPBDSolver:
+def make_solver(w: Workload, **params):
     """GPU solver set up for a workload: fixed vertices, kinematic group,
     initial positions, spheres."""
+    import xpbd_gb300 as G
     kw = dict(dt=w.dt, g_accel=w.g, num_iters=w.iters, solver_type=w.solver, collision_rate=w.collision_rate)
     kw.update(params)
     faces = w.faces if w.sphere_r > 0 else None
@@ -200,7 +217,7 @@ def make_solver(w: Workload, **params) -> G.XPBDSolver:
     return s
 
 
-def drive_gpu(s: G.XPBDSolver, w: Workload, step: int):
+def drive_gpu(s, w: Workload, step: int):
     """Per-step kinematic inputs (sphere centre, kinematic offset) for step `step`
     at the solver's current time."""
     if w.sphere_r > 0:

@@ -64,7 +64,8 @@ class Params(C.Structure):
         ("gs_patch_tets", C.c_int32), ("gs_min_blocks", C.c_int32), ("gs_variant", C.c_int32),
         ("num_local_collision_iters", C.c_int32),
         ("first_order", C.c_int32), ("adjust_damping_to_material", C.c_int32), ("damping_multiplier", C.c_double),
-        ("self_collisions", C.c_int32),
+        ("self_collisions", C.c_int32), ("gs_poll_ns", C.c_int32),
+        ("gs_topology_reload", C.c_int32),
     ]
 
 
@@ -124,6 +125,8 @@ def load(path: str | None = None):
         "xpbd_add_static_collision": ([P, I32, D, D, D, P, P], C.c_int),
         "xpbd_get_collisions": ([P, I32, P, P], C.c_int),
         "xpbd_update": ([P], C.c_int),
+        "xpbd_solve": ([P], C.c_int),
+        "xpbd_solve_local": ([P, I32], C.c_int),
         "xpbd_velocity_update": ([P], C.c_int),
         "xpbd_step": ([P, I32], C.c_int),
         "xpbd_synchronize": ([P], C.c_int),
@@ -418,6 +421,15 @@ class XPBDSolver:
     # ---- stepping ----
     def update(self):
         self._ck(self.L.xpbd_update(self.h))
+
+    def solve(self):
+        """XPBDSolver::solve(): lambda <- 0 and num_iters sweeps on the current
+        positions (no inertial move, no fixed reset)."""
+        self._ck(self.L.xpbd_solve(self.h))
+
+    def solve_local(self, num_iter):
+        """XPBDSolver::solve(refs, num_iter, false) over the local collision set."""
+        self._ck(self.L.xpbd_solve_local(self.h, int(num_iter)))
 
     def velocity_update(self):
         self._ck(self.L.xpbd_velocity_update(self.h))
