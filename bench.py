@@ -144,19 +144,26 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic(kernel, workload_name, variant):
+def profiled_traffic(kernel, workload_name, variant, sweeps=None):
     """DRAM bytes per launch of `kernel` from the committed ncu figures
-    (profiles/roofline_traffic.txt: `workload/kernel/v<variant> bytes summary`
-    lines; a launch is one colour for variants 0/1, one substep for 2-4)."""
+    (profiles/roofline_traffic.txt: `workload/kernel/v<variant>[@sweeps] bytes
+    summary` lines; a launch is one colour for variants 0/1, one substep for
+    2-4). The entry captured at the launch's own sweep count is preferred.
+    Returns (bytes, key) or (None, None)."""
     p = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
     if not os.path.exists(p):
-        return None
+        return None, None
+    found = {}
     with open(p) as f:
         for line in f:
             parts = line.split()
-            if len(parts) >= 2 and not line.startswith("#") and parts[0] == f"{workload_name}/{kernel}/v{variant}":
-                return float(parts[1])
-    return None
+            if len(parts) >= 2 and not line.startswith("#"):
+                found[parts[0]] = float(parts[1])
+    base = f"{workload_name}/{kernel}/v{variant}"
+    for key in ([f"{base}@{sweeps}"] if sweeps else []) + [base]:
+        if key in found:
+            return found[key], key
+    return None, None
 
 
 def algorithmic_bytes(w, kernel):
@@ -528,13 +535,12 @@ def run_ours(args):
     if sweep_bytes is not None:
         per_launch = sweep_bytes / (nl_step / w.iters) if dom == "project_gs" else sweep_bytes
         achieved = per_launch / (ms_launch * 1e-3) / 1e9
-        traffic = profiled_traffic(dom, w.name, s.params.gs_variant)
-        if traffic is not None and dom == "project_gs" and nl_step == 1:
-            traffic *= w.iters / 30.0  # the committed figure is for a 30-sweep launch
+        traffic, tkey = profiled_traffic(dom, w.name, s.params.gs_variant, w.iters if nl_step == 1 else None)
         roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                     "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs",
                     "algorithmic_bytes_per_launch": per_launch, "avg_launch_ms": ms_launch,
                     "launches_per_step": nl_step, "traffic": traffic,
+                    "traffic_source": f"profiles/roofline_traffic.txt {tkey}" if tkey else None,
                     "timing": "graph-timed step minus the other kernels' event-timed share, per launch"}
     kernel_share = {k: v[0] * v[1] / 3 for k, v in prof.items()}
 
