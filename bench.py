@@ -322,6 +322,8 @@ def run_batched(args):
     extra = {}
     if args.patch_tets is not None:
         extra["gs_patch_tets"] = args.patch_tets
+    if args.variant is not None:
+        extra["gs_variant"] = args.variant
     tune = None
     if args.autotune:
         best, cand = G.autotune([(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances], trial_steps=3,

@@ -124,6 +124,8 @@ void release(xpbd_ctx* c) {
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
     c->patch_ver.release(); c->xv.release();
+    c->vdeg_p.release(); c->vdeg_c.release(); c->factive.release(); c->vface_off.release(); c->vface.release();
+    c->fcol_d.release(); c->cm_off.release(); c->n_ctasks.release(); c->ctask.release(); c->cface.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
     c->mlp_p.release(); c->mlp_m.release(); c->mlp_v.release(); c->mlp_g.release(); c->mlp_w4f.release();
     c->mlp_tiles.release(); c->mat.release(); c->feat.release(); c->pred.release(); c->target.release();
@@ -193,9 +195,13 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
     }
     const bool staged = c->prm.gs_variant == 3;
     // variant 4 may fall back to variant 2 (below), so its grid fits both
-    const int per_sm = c->prm.gs_variant == 4 ? std::min(sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, 0),
-                                                         sweep_dataflow_blocks_per_sm(false, c->prm.gs_min_blocks))
-                                              : sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
+    const bool with_faces = c->F > 0;  // variant 4 may then run the contacts inside the sweep
+    const int per_sm =
+        c->prm.gs_variant == 4
+            ? std::min(std::min(sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, 0, false),
+                                with_faces ? sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, 0, true) : 1 << 20),
+                       sweep_dataflow_blocks_per_sm(false, c->prm.gs_min_blocks))
+            : sweep_dataflow_blocks_per_sm(staged, c->prm.gs_min_blocks);
     int dev = 0, sms = 0;
     XPBD_CU(c, cudaGetDevice(&dev));
     XPBD_CU(c, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
@@ -304,11 +310,62 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
         const int per_warp = (NTP + W - 1) / W;
         c->flow_resident = false;
         if (per_warp <= kResidentTasks && !c->prm.gs_topology_reload) {
-            const int res_sm = sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, per_warp);
+            int res_sm = sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, per_warp, false);
+            if (with_faces) res_sm = std::min(res_sm, sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, per_warp, true));
             c->flow_resident = (long long)res_sm * sms >= c->flow_grid;
         }
         XPBD_CU(c, cudaMemcpy(c->patch_ver.p, ver.data(), sizeof(int4) * P, cudaMemcpyHostToDevice));
     }
+    return XPBD_OK;
+}
+
+// Static tables of the versioned sweep's contact phases: per vertex its
+// patch count and its surface faces (CSR), per face its colour, and room for
+// the per-detection tables. Needs every vertex's writes per iteration --
+// patches plus the faces containing it -- to fit the 8-bit fields, and at
+// most 64 face colours; otherwise the contacts keep their own launches.
+int build_flow_contacts(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vector<int4>& pverts,
+                        const std::vector<int>& fcol) {
+    c->flow_contacts = false;
+    const int V = c->V, F = c->F, P = (int)pmeta.size();
+    if (!c->flow_versioned || F == 0 || c->n_face_colours > 64) return XPBD_OK;
+    std::vector<int> degp(V, 0);
+    for (int q = 0; q < P; q++)
+        for (int k = 0; k < (pmeta[q].y >> 8); k++) {
+            const int4& a = pverts[2 * (size_t)q + (k >> 2)];
+            const int kk = k & 3;
+            degp[kk == 0 ? a.x : (kk == 1 ? a.y : (kk == 2 ? a.z : a.w))]++;
+        }
+    std::vector<int> off(V + 1, 0);
+    for (int f = 0; f < F; f++)
+        for (int q = 0; q < 3; q++) off[c->faces_h[3 * f + q] + 1]++;
+    for (int v = 0; v < V; v++) off[v + 1] += off[v];
+    std::vector<int> ent(std::max(off[V], 1)), fill(off.begin(), off.end() - 1);
+    for (int f = 0; f < F; f++)
+        for (int q = 0; q < 3; q++) ent[fill[c->faces_h[3 * f + q]]++] = f;
+    std::vector<unsigned char> dp(V);
+    for (int v = 0; v < V; v++) {
+        if (degp[v] + (off[v + 1] - off[v]) > 255) return XPBD_OK;
+        dp[v] = (unsigned char)degp[v];
+    }
+    const size_t ncm = (size_t)c->n_face_colours * c->n_inst + 1;
+    XPBD_CU(c, c->vdeg_p.alloc(V));
+    XPBD_CU(c, c->vdeg_c.alloc(V));
+    XPBD_CU(c, c->factive.alloc(F));
+    XPBD_CU(c, c->vface_off.alloc(V + 1));
+    XPBD_CU(c, c->vface.alloc(ent.size()));
+    XPBD_CU(c, c->fcol_d.alloc(F));
+    XPBD_CU(c, c->cm_off.alloc(ncm));
+    XPBD_CU(c, c->n_ctasks.alloc(1));
+    XPBD_CU(c, c->ctask.alloc((size_t)F / 32 + c->n_face_colours + 1));
+    XPBD_CU(c, c->cface.alloc(F));
+    XPBD_CU(c, cudaMemcpy(c->vdeg_p.p, dp.data(), V, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemset(c->vdeg_c.p, 0, V));
+    XPBD_CU(c, cudaMemset(c->n_ctasks.p, 0, sizeof(int)));
+    XPBD_CU(c, cudaMemcpy(c->vface_off.p, off.data(), sizeof(int) * (V + 1), cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->vface.p, ent.data(), sizeof(int) * ent.size(), cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->fcol_d.p, fcol.data(), sizeof(int) * F, cudaMemcpyHostToDevice));
+    c->flow_contacts = true;
     return XPBD_OK;
 }
 
@@ -711,11 +768,16 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         XPBD_CU(c, c->tmask.alloc(T));
         XPBD_CU(c, cudaMemcpy(c->local_slots.p, lslots.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     }
-    // (faces allow contacts, which the dataflow sweep leaves to the launches)
+    // with faces only the versioned sweep (variant 4) takes the contacts into
+    // its phases; variants 2 and 3 leave them to the launches
     if (!pmeta.empty() && p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL && p.gs_variant >= 2 &&
-        F == 0) {
+        (F == 0 || (p.gs_variant == 4 && p.constraint_type == XPBD_CONSTRAINT_COMBINED && !p.self_collisions))) {
         int st = build_flow_tasks(c, pmeta, pverts);
         if (st) return st;
+        if (F > 0) {
+            st = build_flow_contacts(c, pmeta, pverts, fcol);
+            if (st) return st;
+        }
     }
     if (!pmeta.empty()) {
         XPBD_CU(c, c->patch_meta.alloc(pmeta.size()));

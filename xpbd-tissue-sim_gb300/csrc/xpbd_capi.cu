@@ -299,9 +299,12 @@ int enqueue_update(xpbd_ctx* c, bool write_vel, bool solve_only) {
                 launch_apply(c->L(), c->x.p, c->dx.p, c->V, c->prev.p, c->vel.p, last && fuse_final, dt, write_vel);
             }
         }
-    } else if (!separate && !every_iter && !have_faces && c->att_v.empty() &&
+    } else if (!separate && !every_iter && c->att_v.empty() &&
+               (!have_faces || (p.gs_variant == 4 && c->flow_versioned && c->flow_contacts && !c->self_on &&
+                                !c->nbodies)) &&
                (p.gs_variant == 2 || p.gs_variant == 3 || p.gs_variant == 4) && c->ntasks > 0) {
-        // every iteration and colour in one cooperative launch
+        // every iteration and colour in one cooperative launch (with faces:
+        // the versioned sweep, static contacts after each iteration's patches)
         if (track && !warm) exact_residual_row(c, 0, false);
         const bool versioned = p.gs_variant == 4 && c->flow_versioned;
         if (versioned) {
@@ -312,8 +315,10 @@ int enqueue_update(xpbd_ctx* c, bool write_vel, bool solve_only) {
         }
         Scope sc(c, K_PROJECT_GS);
         if (versioned) {
+            const xg::FlowContacts fc = have_faces ? c->flowc() : xg::FlowContacts{nullptr, nullptr, nullptr, nullptr};
             launch_sweep_versioned(c->L(), c->tets(), c->patches(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
-                                   c->xv.p, c->V, c->flags.p, c->flow_grid, p.gs_min_blocks, c->flow_resident);
+                                   c->xv.p, c->V, c->flags.p, c->flow_grid, p.gs_min_blocks, c->flow_resident, ca,
+                                   fc);
             c->launches += 2;  // the copies into and out of the versioned positions
         } else
             launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
@@ -451,6 +456,11 @@ int prepare_update(xpbd_ctx* c) {
         Scope sc(c, K_DETECT);
         launch_contact_lists(c->L(), c->contacts(), c->ifl.p, c->ifo_off.p, c->n_face_colours, c->n_inst,
                              c->act_faces.p, c->act_off.p);
+        if (c->flow_contacts)
+            launch_flow_contact_tables(c->L(), c->contacts(), c->act_faces.p, c->act_off.p, c->n_face_colours,
+                                       c->n_inst, c->vface_off.p, c->vface.p, c->fcol_d.p, c->vdeg_p.p,
+                                       c->factive.p, c->cm_off.p, c->ctask.p, c->n_ctasks.p, c->cface.p,
+                                       c->vdeg_c.p, c->V);
         c->contact_lists_dirty = false;
     }
     if (tracking(c) || c->warm_mode != XPBD_WARM_NONE) {

@@ -101,6 +101,12 @@ struct xpbd_ctx {
     DevBuf<int4> patch_ver;       // variant 4: per patch, 8 x 16-bit deg << 8 | pre
     DevBuf<xg::VerRec> xv;        // variant 4: version-stamped vertex records
     bool flow_resident = false;   // variant 4: task topology kept in shared memory
+    // variant 4 with static contacts inside the sweep (FlowContacts)
+    bool flow_contacts = false;
+    DevBuf<unsigned char> vdeg_p, vdeg_c, factive;  // patches / active faces per vertex, face flags
+    DevBuf<int> vface_off, vface, fcol_d, cm_off, n_ctasks;
+    DevBuf<int2> ctask;
+    DevBuf<int4> cface;
     int npatches = 0;
     bool flow_versioned = false;  // variant 4 tables built (else variant 2 runs)
     std::vector<int4> patch_ver_h;  // host copy of patch_ver
@@ -198,6 +204,9 @@ struct xpbd_ctx {
     xg::TaskArrays tasks() {
         return xg::TaskArrays{flow_tasks.p,       flow_dep_off.p, flow_dep.p,      flow_epoch.p,
                               flow_epoch.p + ntasks, ntasks,        flow_poll_limit, flow_poll_ns};
+    }
+    xg::FlowContacts flowc() {
+        return xg::FlowContacts{ctask.p, cface.p, n_ctasks.p, vdeg_c.p};
     }
     xg::SelfArrays selfs() {
         return xg::SelfArrays{s_tets.p,        s_Q.p,          s_X0.p,         s_X0f.p,      s_surf.p,

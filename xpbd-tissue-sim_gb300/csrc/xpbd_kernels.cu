@@ -446,8 +446,7 @@ __device__ __forceinline__ void contact_face_gs(const ContactArrays& c, int f, f
         float d[3][3];
         if (contact_update(c, slot, xs, d, lam)) {
 #pragma unroll
-            for (int i = 0; i < 3; i++)
-                xs[i] = make_float4(xs[i].x + d[i][0], xs[i].y + d[i][1], xs[i].z + d[i][2], xs[i].w);
+            for (int i = 0; i < 3; i++) xs[i] = moved(xs[i], d[i]);
             moved_any = true;
         }
         c.lam[slot] = lam;
@@ -1089,10 +1088,15 @@ __global__ void k_versions_out(float4* __restrict__ x, const VerRec* __restrict_
 // words: four int4 per lane and task) is read once into shared memory, before
 // the wait on the previous kernel, so a phase's first poll does not wait for
 // the task, patch and vertex-id loads.
-template <bool FIRST_ZERO, bool RESIDENT, int MINB>
+// CONTACTS: after every iteration's patch tasks come the contact tasks
+// (FlowContacts): a lane takes one face with an active static contact,
+// polls its three vertices, projects the face's contacts in slot order
+// (contact_face_gs) and writes the vertices back one version later; a
+// vertex's writes per iteration then include its active faces (vdegc).
+template <bool FIRST_ZERO, bool RESIDENT, bool CONTACTS, int MINB>
 __global__ void __launch_bounds__(kFlowBlock, MINB)
     k_sweep_versioned(TetArrays t, PatchArrays pa, const int4* __restrict__ pver, TaskArrays ta, int iters,
-                      VerRec* __restrict__ xv, Flags* flags) {
+                      VerRec* __restrict__ xv, Flags* flags, ContactArrays ca, FlowContacts fc) {
     static_assert(kFlowBlock == 32, "one warp per block: the topology is indexed by lane");
     extern __shared__ int4 topo[];  // RESIDENT: [task k][meta, verts a, verts b, versions][lane]
     __shared__ float4 sv[kMaxPatchVerts][kFlowBlock];
@@ -1119,9 +1123,28 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
         __syncwarp();
     }
     pdl_wait_then_release();
-    for (int it = 0; it < iters; it++) {
+    if (RESIDENT && CONTACTS) {
+        // this detection's active faces add to each vertex's writes per iteration
         int k = 0;
         for (int j = gw; j < ta.ntasks; j += nw, k++) {
+            const int nv = topo[(4 * k + 0) * 32 + lane].y >> 8;
+            const int4 va = topo[(4 * k + 1) * 32 + lane], vb = topo[(4 * k + 2) * 32 + lane];
+            const int4 vr = topo[(4 * k + 3) * 32 + lane];
+            const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+            int vw[4] = {vr.x, vr.y, vr.z, vr.w};
+#pragma unroll
+            for (int k2 = 0; k2 < kMaxPatchVerts; k2++)
+                if (k2 < nv) vw[k2 >> 1] += (int)__ldg(fc.vdegc + vid[k2]) << (8 + 16 * (k2 & 1));
+            topo[(4 * k + 3) * 32 + lane] = make_int4(vw[0], vw[1], vw[2], vw[3]);
+        }
+        __syncwarp();
+    }
+    const int ntot = ta.ntasks + (CONTACTS ? *fc.ntasks : 0);
+    for (int it = 0; it < iters; it++) {
+        int k = 0;
+        for (int j = gw; j < ntot; j += nw) {
+          bool ok = true;
+          if (j < ta.ntasks) {
             int4 meta, va, vb, vr;
             if (RESIDENT) {
                 meta = topo[(4 * k + 0) * 32 + lane];
@@ -1139,8 +1162,8 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     vr = __ldg(pver + p);
                 }
             }
+            k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
-            bool ok = true;
             if (nverts > 0) {
                 float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
                 float2 lams[kMaxPatchTets];
@@ -1161,7 +1184,9 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
 #pragma unroll
                 for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
                     const int h = (vw[k2 >> 1] >> (16 * (k2 & 1))) & 0xffff;  // deg << 8 | pre
-                    due[k2] = it * (h >> 8) + (h & 0xff);
+                    int deg = h >> 8;
+                    if (CONTACTS && !RESIDENT && k2 < nverts) deg += __ldg(fc.vdegc + vid[k2]);
+                    due[k2] = it * deg + (h & 0xff);
                     if (k2 < nverts) {
                         unsigned long long a, b, c, d;
                         ld_ver(xv + vid[k2], a, b, c, d);
@@ -1229,6 +1254,64 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     }
                 }
             }
+          } else if (CONTACTS) {
+            const int2 ct = fc.task[j - ta.ntasks];
+            if (lane < ct.y) {
+                const int4 e = fc.face[ct.x + lane];
+                const int4 fv = __ldg(ca.faces + e.x);
+                const int vid3[3] = {fv.x, fv.y, fv.z};
+                const int dw[3] = {e.y & 0xffff, (e.y >> 16) & 0xffff, e.z & 0xffff};
+                int due3[3];
+                float4 xs[3];
+                unsigned pending = 0;
+#pragma unroll
+                for (int q = 0; q < 3; q++) {
+                    due3[q] = it * (dw[q] & 0xff) + (dw[q] >> 8);
+                    unsigned long long a, b, c, d;
+                    ld_ver(xv + vid3[q], a, b, c, d);
+                    xs[q] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
+                    if (ver_min(a, b, c) < due3[q]) pending |= 1u << q;
+                }
+                unsigned n = 0;
+                while (pending) {
+                    if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                        ok = false;
+                        break;
+                    }
+                    __nanosleep(ta.poll_ns);
+#pragma unroll
+                    for (int q = 0; q < 3; q++) {
+                        if (pending & (1u << q)) {
+                            unsigned long long a, b, c, d;
+                            ld_ver(xv + vid3[q], a, b, c, d);
+                            if (ver_min(a, b, c) >= due3[q]) {
+                                xs[q].x = ver_val(a);
+                                xs[q].y = ver_val(b);
+                                xs[q].z = ver_val(c);
+                                pending &= ~(1u << q);
+                            }
+                        }
+                    }
+                }
+                if (ok) {
+                    // the face's contacts in slot order (contact_face_gs)
+                    for (int sl = 0; sl < ca.S; sl++) {
+                        const int slot = sl * ca.F + e.x;
+                        if (ca.bary[slot].w != 1.f) continue;
+                        float lam = it == 0 ? 0.f : ca.lam[slot];
+                        float d[3][3];
+                        if (contact_update(ca, slot, xs, d, lam)) {
+#pragma unroll
+                            for (int q = 0; q < 3; q++) xs[q] = moved(xs[q], d[q]);
+                        }
+                        ca.lam[slot] = lam;
+                    }
+#pragma unroll
+                    for (int q = 0; q < 3; q++)
+                        st_ver(xv + vid3[q], xs[q].x, xs[q].y, xs[q].z, xs[q].w, (unsigned)(due3[q] + 1));
+                }
+            }
+          }
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) {
                     atomicExch(ta.abort_flag, 1u);
@@ -1700,24 +1783,25 @@ cudaError_t launch_sweep_dataflow(const Launch& s, const TetArrays& t, const Pat
 #undef XG_FLOW
 }
 
-int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp) {
+int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp, bool contacts) {
     int n = 0, m = 0;
-    cudaError_t e;
+    cudaError_t e = cudaSuccess;
     const size_t smem = sweep_versioned_smem(tasks_per_warp);
     const bool res = tasks_per_warp > 0;
-#define XG_VOCC(R, M)                                                                                              \
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_versioned<true, R, M>, kFlowBlock, smem);       \
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_versioned<false, R, M>,   \
-                                                                             kFlowBlock, smem)
+#define XG_VOCC(R, C, M)                                                                                             \
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_sweep_versioned<true, R, C, M>, kFlowBlock, smem);       \
+    if (e == cudaSuccess)                                                                                            \
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&m, k_sweep_versioned<false, R, C, M>, kFlowBlock, smem)
+#define XG_VOCC_M(R, C)                         \
+    if (min_blocks == 8) { XG_VOCC(R, C, 8); }   \
+    else if (min_blocks == 6) { XG_VOCC(R, C, 6); } \
+    else { XG_VOCC(R, C, 1); }
     if (res) {
-        if (min_blocks == 8) { XG_VOCC(true, 8); }
-        else if (min_blocks == 6) { XG_VOCC(true, 6); }
-        else { XG_VOCC(true, 1); }
+        if (contacts) { XG_VOCC_M(true, true) } else { XG_VOCC_M(true, false) }
     } else {
-        if (min_blocks == 8) { XG_VOCC(false, 8); }
-        else if (min_blocks == 6) { XG_VOCC(false, 6); }
-        else { XG_VOCC(false, 1); }
+        if (contacts) { XG_VOCC_M(false, true) } else { XG_VOCC_M(false, false) }
     }
+#undef XG_VOCC_M
 #undef XG_VOCC
     if (e != cudaSuccess) return 0;
     return n < m ? n : m;
@@ -1725,11 +1809,13 @@ int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp) {
 
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
                                    const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
-                                   Flags* flags, int grid, int min_blocks, bool resident) {
+                                   Flags* flags, int grid, int min_blocks, bool resident, const ContactArrays& ca,
+                                   const FlowContacts& fc) {
     if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
     go(k_versions_in, nblk(V, 256), 256, s, xv, (const float4*)x, V);
     const int warps = grid * (kFlowBlock / 32);
     const int per_warp = (ta.ntasks + warps - 1) / warps;
+    const bool contacts = fc.task != nullptr;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)grid);
     cfg.blockDim = dim3(kFlowBlock);
@@ -1740,22 +1826,156 @@ cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const Pa
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e;
-#define XG_VER(F, R, M) e = cudaLaunchKernelEx(&cfg, k_sweep_versioned<F, R, M>, t, pa, pver, ta, iters, xv, flags)
-#define XG_VER_M(F, R)                       \
-    if (min_blocks == 8) { XG_VER(F, R, 8); } \
-    else if (min_blocks == 6) { XG_VER(F, R, 6); } \
-    else { XG_VER(F, R, 1); }
+    cudaError_t e = cudaSuccess;
+#define XG_VER(F, R, C, M) \
+    e = cudaLaunchKernelEx(&cfg, k_sweep_versioned<F, R, C, M>, t, pa, pver, ta, iters, xv, flags, ca, fc)
+#define XG_VER_M(F, R, C)                       \
+    if (min_blocks == 8) { XG_VER(F, R, C, 8); } \
+    else if (min_blocks == 6) { XG_VER(F, R, C, 6); } \
+    else { XG_VER(F, R, C, 1); }
+#define XG_VER_C(F, R)                              \
+    if (contacts) { XG_VER_M(F, R, true) } else { XG_VER_M(F, R, false) }
     if (resident) {
-        if (first_zero) { XG_VER_M(true, true) } else { XG_VER_M(false, true) }
+        if (first_zero) { XG_VER_C(true, true) } else { XG_VER_C(false, true) }
     } else {
-        if (first_zero) { XG_VER_M(true, false) } else { XG_VER_M(false, false) }
+        if (first_zero) { XG_VER_C(true, false) } else { XG_VER_C(false, false) }
     }
+#undef XG_VER_C
 #undef XG_VER_M
 #undef XG_VER
     if (e != cudaSuccess) return e;
     go(k_versions_out, nblk(V, 256), 256, s, x, (const VerRec*)xv, V);
     return cudaSuccess;
+}
+
+// ---- the versioned sweep's contact tables (after each detection) ----
+// faces holding at least one active static contact
+__global__ void k_face_active(ContactArrays c, unsigned char* __restrict__ factive) {
+    pdl_wait_then_release();
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= c.F) return;
+    unsigned char a = 0;
+    for (int s = 0; s < c.S; s++) a |= c.bary[(size_t)s * c.F + f].w == 1.f;
+    factive[f] = a;
+}
+
+// active faces containing each vertex
+__global__ void k_vertex_contact_degree(const int* __restrict__ vface_off, const int* __restrict__ vface,
+                                        const unsigned char* __restrict__ factive, unsigned char* __restrict__ vdegc,
+                                        int V) {
+    pdl_wait_then_release();
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    int n = 0;
+    for (int e = vface_off[v]; e < vface_off[v + 1]; e++) n += factive[vface[e]];
+    vdegc[v] = (unsigned char)n;
+}
+
+constexpr int kScanThreads = 1024;
+constexpr int kMaxFlowFaceColours = 64;
+
+// Colour-major offsets of the active faces (colour, instance) from the
+// per-instance lists, and the contact tasks: per colour, runs of up to 32.
+// One block.
+__global__ void __launch_bounds__(kScanThreads) k_contact_task_table(const int* __restrict__ act_off, int ncol,
+                                                                    int n_inst, int* __restrict__ cm_off,
+                                                                    int2* __restrict__ ctask,
+                                                                    int* __restrict__ n_ctasks) {
+    __shared__ int part[kScanThreads];
+    __shared__ int col_tasks_off[kMaxFlowFaceColours + 1];
+    pdl_wait_then_release();
+    const int tid = threadIdx.x;
+    const int n = ncol * n_inst;
+    const int per = (n + kScanThreads - 1) / kScanThreads;
+    const int lo = min(n, tid * per), hi = min(n, lo + per);
+    auto count = [&](int i) {
+        const int col = i / n_inst, k = i % n_inst;
+        const int* a = act_off + (size_t)k * (ncol + 1);
+        return a[col + 1] - a[col];
+    };
+    int sum = 0;
+    for (int i = lo; i < hi; i++) sum += count(i);
+    part[tid] = sum;
+    __syncthreads();
+    if (tid == 0) {
+        int run = 0;
+        for (int i = 0; i < kScanThreads; i++) {
+            const int v = part[i];
+            part[i] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    int run = part[tid];
+    for (int i = lo; i < hi; i++) {
+        cm_off[i] = run;
+        run += count(i);
+    }
+    if (tid == kScanThreads - 1) cm_off[n] = run;
+    __syncthreads();
+    if (tid == 0) {
+        int t = 0;
+        for (int col = 0; col < ncol; col++) {
+            col_tasks_off[col] = t;
+            const int tot = cm_off[(col + 1) * n_inst] - cm_off[col * n_inst];
+            t += (tot + 31) / 32;
+        }
+        col_tasks_off[ncol] = t;
+        *n_ctasks = t;
+    }
+    __syncthreads();
+    for (int col = 0; col < ncol; col++) {
+        const int base = cm_off[col * n_inst], tot = cm_off[(col + 1) * n_inst] - base;
+        const int t0 = col_tasks_off[col], nt = col_tasks_off[col + 1] - t0;
+        for (int i = tid; i < nt; i += kScanThreads) ctask[t0 + i] = make_int2(base + 32 * i, min(32, tot - 32 * i));
+    }
+}
+
+// The colour-major face entries with, per face vertex, its writes per
+// iteration (patches + active faces) and those before this face (patches +
+// active faces of a lower colour). One block per instance.
+__global__ void k_contact_faces_fill(ContactArrays c, const int* __restrict__ act_faces,
+                                     const int* __restrict__ act_off, int ncol, int n_inst,
+                                     const int* __restrict__ cm_off, const int* __restrict__ vface_off,
+                                     const int* __restrict__ vface, const int* __restrict__ fcol,
+                                     const unsigned char* __restrict__ vdegp,
+                                     const unsigned char* __restrict__ factive, int4* __restrict__ cface) {
+    pdl_wait_then_release();
+    const int k = blockIdx.x;
+    const int* a = act_off + (size_t)k * (ncol + 1);
+    for (int col = 0; col < ncol; col++) {
+        const int dst0 = cm_off[col * n_inst + k];
+        for (int i = a[col] + threadIdx.x; i < a[col + 1]; i += blockDim.x) {
+            const int f = act_faces[i];
+            const int4 fv = c.faces[f];
+            const int vs[3] = {fv.x, fv.y, fv.z};
+            int w[3];
+            for (int q = 0; q < 3; q++) {
+                const int v = vs[q];
+                int deg = 0, pre = 0;
+                for (int e = vface_off[v]; e < vface_off[v + 1]; e++) {
+                    const int g = vface[e];
+                    if (factive[g]) {
+                        deg++;
+                        pre += fcol[g] < col;
+                    }
+                }
+                w[q] = (vdegp[v] + deg) | ((vdegp[v] + pre) << 8);
+            }
+            cface[dst0 + (i - a[col])] = make_int4(f, w[0] | (w[1] << 16), w[2], 0);
+        }
+    }
+}
+
+void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
+                                int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,
+                                const unsigned char* vdegp, unsigned char* factive, int* cm_off, int2* ctask,
+                                int* n_ctasks, int4* cface, unsigned char* vdegc, int V) {
+    go(k_face_active, nblk(ca.F, 256), 256, s, ca, factive);
+    go(k_vertex_contact_degree, nblk(V, 256), 256, s, vface_off, vface, (const unsigned char*)factive, vdegc, V);
+    go(k_contact_task_table, 1, kScanThreads, s, act_off, ncol, n_inst, cm_off, ctask, n_ctasks);
+    go(k_contact_faces_fill, n_inst, 256, s, ca, act_faces, act_off, ncol, n_inst, (const int*)cm_off, vface_off,
+       vface, fcol, vdegp, (const unsigned char*)factive, cface);
 }
 
 void launch_attach_gs(const Launch& s, const int* vert, const float4* target, float* lam, const int* order, int begin,

@@ -126,6 +126,21 @@ struct alignas(32) VerRec {
     unsigned long long x, y, z, w;
 };
 constexpr unsigned kPollNs = 1024;  // default back-off of variant 4's polls
+
+// Static contacts inside variant 4's sweep: after each detection, the faces
+// with an active static contact in colour-major order (colour, instance,
+// index), cut into tasks of up to 32 faces of one colour that follow the
+// patch tasks of every iteration. A vertex is then written per iteration by
+// each patch containing it and then by each active face containing it, in
+// face-colour order; vdegc[v] counts those faces, and face[i] carries, per
+// face vertex, its writes per iteration and the writes before this face's.
+struct FlowContacts {
+    const int2* task;         // [*ntasks] (first entry of face[], faces in the task)
+    const int4* face;         // (face, due words of vertices 0-1, vertex 2, 0): per vertex
+                              // (writes per iteration) | (writes before this face) << 8
+    const int* ntasks;        // contact tasks per iteration (written after each detection)
+    const unsigned char* vdegc;  // [V] active contact faces containing the vertex
+};
 // variant 4 keeps the topology of a warp's tasks (patch records, vertex ids,
 // version words: 64 B per lane and task) in shared memory across iterations
 // when the warp owns at most this many tasks per iteration
@@ -249,12 +264,22 @@ int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 // it, those of a lower colour). resident: each warp's task topology stays in
 // shared memory (ntasks / warps <= kResidentTasks; sweep_versioned_smem bytes
 // per block).
+// fc.task != nullptr: the static contacts of ca run inside the sweep (FlowContacts).
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
                                    const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
-                                   Flags* flags, int grid, int min_blocks, bool resident);
+                                   Flags* flags, int grid, int min_blocks, bool resident, const ContactArrays& ca,
+                                   const FlowContacts& fc);
 // blocks per SM of the versioned sweep with the dynamic shared memory it
-// needs when each warp owns `tasks_per_warp` tasks (0: not resident)
-int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp);
+// needs when each warp owns `tasks_per_warp` tasks (0: not resident), with or
+// without the contact phases
+int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp, bool contacts);
+// After a detection (the per-instance active lists built): the sweep's
+// contact tables. vface_off/vface/fcol/vdegp are static: per vertex its
+// surface faces (CSR) and patch count, per face its colour.
+void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
+                                int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,
+                                const unsigned char* vdegp, unsigned char* factive, int* cm_off, int2* ctask,
+                                int* n_ctasks, int4* cface, unsigned char* vdegc, int V);
 inline size_t sweep_versioned_smem(int tasks_per_warp) { return (size_t)tasks_per_warp * 4 * 32 * sizeof(int4); }
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 // after a detection: per instance and face colour, the faces with an active
