@@ -306,6 +306,54 @@ def run_reference(args):
     return 0
 
 
+def batched_leg(steps=10, warmup=3, variants=(4, 1)):
+    """The batched configuration (256 instances, 20 Gauss-Seidel sweeps, 1-4
+    spheres each) for the default run's line: each sweep variant timed with
+    CUDA events (L2 flushed between steps) -- variant 4 is the one
+    cooperative launch per substep with the contacts inside, variant 1 the
+    colour launches with bulk-staged records -- and the faster reported.
+    Every instance's substep completes with the batched step, so an
+    instance's step latency is the step time; p50/p99 are over the timed
+    steps."""
+    import numpy as np
+    import torch
+
+    import workloads as W
+    b = W.batched()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    legs = {}
+    for var in variants:
+        s = W.make_batch_solver(b, gs_variant=var)
+        for _ in range(warmup):
+            W.drive_batch(s, b)
+            s.step(1)
+        s.synchronize()
+        st = torch.cuda.ExternalStream(s.stream_handle())
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        l0 = s.launch_count()
+        for k in range(steps):
+            with torch.cuda.stream(st):
+                flush.zero_()
+            W.drive_batch(s, b)
+            evs[k][0].record(st)
+            s.step(1)
+            evs[k][1].record(st)
+        torch.cuda.synchronize()
+        per = [a.elapsed_time(c) for a, c in evs]
+        legs[var] = {"ms_per_step": float(np.mean(per)), "steps_per_s": 1e3 / float(np.mean(per)),
+                     "launches_per_step": (s.launch_count() - l0) / steps,
+                     "instance_latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))}}
+        s.close()
+    best = min(legs, key=lambda v: legs[v]["ms_per_step"])
+    return {"workload": f"{len(b.instances)} cube/beam instances, {b.T:,} tets, {b.V:,} vertices, tet counts "
+                        "log-uniform [2k,100k], 1-4 descending spheres each, coloured Gauss-Seidel",
+            "iterations": b.iters, "value": legs[best]["steps_per_s"], "unit": "batch substeps/s",
+            "best_variant": best, "tet_projections_per_s": b.T * b.iters * legs[best]["steps_per_s"],
+            "variants": {("persistent sweep, contacts inside (4)" if v == 4 else f"colour launches ({v})"): legs[v]
+                         for v in legs},
+            "latency_note": "every instance completes with the batched step; percentiles over the timed steps"}
+
+
 def run_batched(args):
     """256 independent instances (2k-100k tets each, 1-4 spheres) advanced by
     the same launches in one context. value = batch substeps/s (every instance
@@ -592,15 +640,22 @@ def run_ours(args):
         sub, sample, _ = cpu_sample(w)
         line["cpu_baseline"] = {"value": sub, "unit": UNIT, "cores": 1, "kind": "port",
                                 "sample": sample + f"; {w.iters} sweeps = this line's iteration count"}
+    s.close()
+    if rank == 0 and args.workload == "block" and not args.no_legs:
+        # the two system forms beside the plain solver, as extra keys
+        line["batched"] = batched_leg()
+        lr = learned_leg(args)
+        line["learned"] = {k: lr.get(k) for k in ["value", "unit", "plain_substeps_per_s_at_1e-3",
+                                                  "ms_per_substep_at_1e-3", "speedup_at_1e-3", "evaluation",
+                                                  "warm_start_overhead_ms", "training", "roofline_mlp", "config"]}
     if rank == 0:
         print(json.dumps(line), flush=True)
-    s.close()
     if dist:
         dist.destroy_process_group()
     return 0
 
 
-def run_learned(args):
+def learned_leg(args):
     """The block mesh with the learned warm start (per-tet MLP on the tensor
     cores). Online training on seeded loading paths: episodes of `episode`
     steps from rest in which the top face is moved 1 cm along a seeded
@@ -726,7 +781,11 @@ def run_learned(args):
                          "frac": (achieved / peak) if achieved and peak else None,
                          "flop_per_launch": flop, "avg_launch_ms": mlp_ms},
     }
-    print(json.dumps(line), flush=True)
+    return line
+
+
+def run_learned(args):
+    print(json.dumps(learned_leg(args)), flush=True)
     return 0
 
 
@@ -741,6 +800,7 @@ def main():
     ap.add_argument("--episode", type=int, default=50, help="learned: steps per loading path")
     ap.add_argument("--autotune", action="store_true", help="batched: pick launch parameters with the autotuner")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-legs", action="store_true", help="skip the batched and learned legs of the default run")
     ap.add_argument("--quick", action="store_true", help="timed steps only (no e2e/roofline/CPU legs)")
     ap.add_argument("--solver", default=None, choices=["Gauss-Seidel", "Jacobi"], help="override the workload's solver")
     ap.add_argument("--patch-tets", type=int, default=None, help="Gauss-Seidel patch size (1 = per-tet colouring)")

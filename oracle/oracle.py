@@ -53,6 +53,9 @@ def lib():
         L.xo_greedy_colour.argtypes = [LL, I, P, LL, P]
         L.xo_greedy_colour.restype = I
         L.xo_set_rel_tol.argtypes = [P, D]
+        L.xo_update_start.argtypes = [P, P, P, I]
+        L.xo_last_r_plain.argtypes = [P]
+        L.xo_last_r_plain.restype = D
         L.xo_iters_done.argtypes = [P]
         L.xo_iters_done.restype = I
         _lib = L
@@ -248,6 +251,17 @@ class Oracle:
         True when the warm start was kept (not rejected by the residual test)."""
         lam0 = np.ascontiguousarray(lam0, np.float64)
         return bool(self.L.xo_update_warm(C.c_void_p(self.h), _p(lam0), int(record), int(fallback)))
+
+    def update_start(self, dx0=None, lam0=None, record=False):
+        """Update from a given start (warm-start experiments): positions moved
+        by dx0 (V x 3) after the inertial move, multipliers starting at lam0
+        (T x 2); last_r_plain() is ||r(x_pred, 0)||."""
+        d = None if dx0 is None else np.ascontiguousarray(dx0, np.float64)
+        l = None if lam0 is None else np.ascontiguousarray(lam0, np.float64)
+        self.L.xo_update_start(C.c_void_p(self.h), _p(d), _p(l), int(record))
+
+    def last_r_plain(self):
+        return self.L.xo_last_r_plain(C.c_void_p(self.h))
 
     def set_rel_tol(self, tol):
         """Convergence measurement: update() stops its sweeps once ||r|| <=

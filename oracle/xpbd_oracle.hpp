@@ -1287,6 +1287,39 @@ struct Object {
         }
     }
 
+    // Update from a given start (warm-start experiments, not a reference
+    // feature): after the inertial move, ||r(x_pred, 0)|| is kept in
+    // last_r_plain (the plain solver's normaliser), then the positions move
+    // by dx0 (3V, may be empty) and the multipliers start at lam0 (2 per tet;
+    // empty: 0) before the sweeps.
+    double last_r_plain = 0.0;
+    void update_start(const std::vector<R>& dx0, const std::vector<R>& lam0, bool record_residual) {
+        prev = x;
+        move_inertially();
+        std::fill(lam.begin(), lam.end(), R(0));
+        for (auto& ct : contacts) ct.lambda = 0;
+        for (auto& at : attachments) at.lambda = 0;
+        for (auto& sc : self_contacts) sc.lambda = 0;
+        last_r_plain = residual_norm();
+        if (!dx0.empty())
+            for (long long i = 0; i < 3 * V; i++) x[i] += dx0[i];
+        if (!lam0.empty()) lam = lam0;
+        res_history.clear();
+        iters_done = 0;
+        for (int it = 0; it < num_iter; it++) {
+            if (record_residual) res_history.push_back(residual_norm());
+            iterate();
+            iters_done = it + 1;
+            // rel_tol > 0: stop at ||r|| <= rel_tol * ||r(x_pred, 0)||
+            if (rel_tol > 0 && residual_norm() <= rel_tol * last_r_plain) break;
+        }
+        if (record_residual) res_history.push_back(residual_norm());
+        local_iterations();
+        for (long long i = 0; i < V; i++)
+            if (fixed[i])
+                for (int k = 0; k < 3; k++) x[3 * i + k] = prev[3 * i + k];
+    }
+
     // Warm-started update: the multipliers start at lam0 (2 per tet, dev/hyd)
     // and the positions take the matching correction x += M^-1 grad C(x)^T lam0
     // (summed over tets at the predicted positions) before the sweeps; the

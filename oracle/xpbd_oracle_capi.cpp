@@ -306,6 +306,19 @@ int xo_update_warm(void* p, const double* lam0, int record, int fallback) {
     });
 }
 
+void xo_update_start(void* p, const double* dx0, const double* lam0, int record) {
+    with((Handle*)p, [&](auto& o) {
+        using R = typename std::decay_t<decltype(o.x)>::value_type;
+        std::vector<R> d, l;
+        if (dx0) d.assign(dx0, dx0 + 3 * o.V);
+        if (lam0) l.assign(lam0, lam0 + 2 * o.T);
+        o.update_start(d, l, record != 0);
+        return 0;
+    });
+}
+double xo_last_r_plain(void* p) {
+    return with((Handle*)p, [&](auto& o) { return o.last_r_plain; });
+}
 void xo_set_rel_tol(void* p, double tol) {
     with((Handle*)p, [&](auto& o) { o.rel_tol = tol; return 0; });
 }
