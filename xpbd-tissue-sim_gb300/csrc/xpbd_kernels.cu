@@ -717,10 +717,11 @@ __global__ void k_velocity(const float4* __restrict__ x, const float4* __restric
     vel[i] = make_float4((xx.x - p.x) / dt, (xx.y - p.y) / dt, (xx.z - p.z) / dt, 0.f);
 }
 
-// Exact residual / energy of the current (FP32) state, evaluated in FP64:
-// C from the positions widened to double, r = C + alpha~ lambda and r^2 in
-// double, so the norm that decides convergence carries no FP32 evaluation
-// noise. rvec (optional) receives the per-constraint residuals (rounded to
+// Exact residual / energy at the current state: C in FP32 (tet_C), then
+// r = C + alpha~ lambda, r^2 and the sums in FP64 (the product of the two
+// floats is exact in double), so the reduction that decides convergence adds
+// no FP32 rounding of its own; GB300's FP64 rate is low, so C itself stays
+// FP32. rvec (optional) receives the per-constraint residuals (rounded to
 // float) in the reference's order via the slot->tet map.
 __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const float4* __restrict__ x, bool separate,
                                                   const int* __restrict__ perm, float* __restrict__ rvec,
@@ -736,21 +737,12 @@ __global__ void __launch_bounds__(256) k_residual(TetArrays t, int T, const floa
         float4 xp[4];
         gather_tet(x, e, s, xp);
         const float2 lam = zero_lam ? make_float2(0.f, 0.f) : t.lam[slot];
-        TetState<double> sd;
-#pragma unroll
-        for (int i = 0; i < 4; i++) {
-#pragma unroll
-            for (int k = 0; k < 3; k++) sd.p[i][k] = s.p[i][k];
-            sd.w[i] = s.w[i];
-        }
-#pragma unroll
-        for (int i = 0; i < 9; i++) sd.q[i] = s.q[i];
-        sd.atd = s.atd; sd.ath = s.ath; sd.gam = s.gam;
-        double Cd, Ch;
-        tet_C(sd, Cd, Ch);
-        const double r0 = fma(sd.atd, (double)lam.x, Cd), r1 = fma(sd.ath, (double)lam.y, Ch);
+        float Cf, Chf;
+        tet_C(s, Cf, Chf);
+        const double Cd = Cf, Ch = Chf;
+        const double r0 = fma((double)s.atd, (double)lam.x, Cd), r1 = fma((double)s.ath, (double)lam.y, Ch);
         rsq = fma(r0, r0, r1 * r1);
-        en = Cd * Cd / (sd.atd * dt2) + Ch * Ch / (sd.ath * dt2);
+        en = Cd * Cd / ((double)s.atd * dt2) + Ch * Ch / ((double)s.ath * dt2);
         if (rvec) {
             const int tt = perm ? perm[slot] : slot;
             if (!separate) { rvec[2 * (size_t)tt] = (float)r0; rvec[2 * (size_t)tt + 1] = (float)r1; }
