@@ -1132,6 +1132,32 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
         __syncwarp();
     }
     const int ntot = ta.ntasks + (CONTACTS ? *fc.ntasks : 0);
+    // !RESIDENT: software pipeline over this warp's patch tasks. While a task
+    // runs, the next one's patch records are in flight and the descriptor of
+    // the one after that, so a task starts polling without a dependent load.
+    // (Each warp cycles through the same tasks every iteration: after its
+    // last patch task of an iteration comes its first one, gw.)
+    auto next_patch_task = [&](int j) { return j + nw < ta.ntasks ? j + nw : gw; };
+    int2 tk_next = make_int2(0, 0);  // descriptor (first patch, patches) of the task after the next
+    int4 nmeta = make_int4(0, 0, 0, 0), nva = nmeta, nvb = nmeta, nvr = nmeta;
+    auto load_records = [&](int2 tk, int4& m, int4& a, int4& b, int4& r) {
+        m = a = b = r = make_int4(0, 0, 0, 0);
+        if (lane < tk.y) {
+            const int p = tk.x + lane;
+            m = __ldg(pa.meta + p);
+            a = __ldg(pa.verts + 2 * (size_t)p);
+            b = __ldg(pa.verts + 2 * (size_t)p + 1);
+            r = __ldg(pver + p);
+        }
+    };
+    auto load_desc = [&](int j) {
+        const int4 d = __ldg(ta.task + j);
+        return make_int2(d.x, d.y);
+    };
+    if (!RESIDENT && gw < ta.ntasks) {
+        load_records(load_desc(gw), nmeta, nva, nvb, nvr);
+        tk_next = load_desc(next_patch_task(gw));
+    }
     for (int it = 0; it < iters; it++) {
         int k = 0;
         for (int j = gw; j < ntot; j += nw) {
@@ -1144,15 +1170,10 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 vb = topo[(4 * k + 2) * 32 + lane];
                 vr = topo[(4 * k + 3) * 32 + lane];
             } else {
-                const int4 tk = __ldg(ta.task + j);
-                meta = va = vb = vr = make_int4(0, 0, 0, 0);
-                if (lane < tk.y) {
-                    const int p = tk.x + lane;
-                    meta = __ldg(pa.meta + p);
-                    va = __ldg(pa.verts + 2 * (size_t)p);
-                    vb = __ldg(pa.verts + 2 * (size_t)p + 1);
-                    vr = __ldg(pver + p);
-                }
+                meta = nmeta; va = nva; vb = nvb; vr = nvr;
+                const int jn = next_patch_task(j);
+                load_records(tk_next, nmeta, nva, nvb, nvr);
+                tk_next = load_desc(next_patch_task(jn));
             }
             k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
