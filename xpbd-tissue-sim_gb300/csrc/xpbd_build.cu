@@ -107,7 +107,7 @@ void release(xpbd_ctx* c) {
     drop_graphs(c);
     for (auto e : c->prof.pool) cudaEventDestroy(e);
     c->x.release(); c->prev.release(); c->vel.release(); c->dx.release(); c->dxt.release();
-    c->tet_idx.release(); c->q0.release(); c->q1.release(); c->q2.release(); c->lam.release();
+    c->tet_idx.release(); c->q0.release(); c->q1.release(); c->q2.release(); c->m0.release(); c->m1.release(); c->m2.release(); c->lam.release();
     c->perm.release(); c->csr_off.release(); c->csr_ent.release(); c->faces.release(); c->face_list.release();
     c->c_bary.release(); c->c_p.release(); c->c_n.release(); c->c_lam.release();
     c->kin_idx.release(); c->kin_rest.release(); c->flags.release();
@@ -614,7 +614,7 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     // CombinedNeohookeanConstraintProjector.cpp:35, ConstraintProjector.hpp:133-140)
     const double dt2 = p.first_order ? p.dt : p.dt * p.dt;
     std::vector<int4> hidx(T);
-    std::vector<float4> h0(T), h1(T), h2(T);
+    std::vector<float4> h0(T), h1(T), h2(T), hm0(T), hm1(T), hm2(T);
     std::vector<float2> hmat(T);
     c->alpha_t_d.resize(T);
     c->alpha_t_h.resize(T);
@@ -626,7 +626,18 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
         const float atd = (float)(ad[t] / dt2), ath = (float)(ah[t] / dt2);
         h0[sidx] = make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]);
         h1[sidx] = make_float4((float)q[4], (float)q[5], (float)q[6], (float)q[7]);
-        h2[sidx] = make_float4((float)q[8], atd, ath, (float)gm[t]);
+        h2[sidx] = make_float4((float)q[8], 0.f, 0.f, 0.f);
+        {
+            // M = Q Q^T (q[3c + r] = Q(r, c)) and det Q, in FP64
+            double M[3][3];
+            for (int i = 0; i < 3; i++)
+                for (int j = 0; j < 3; j++) M[i][j] = q[i] * q[j] + q[3 + i] * q[3 + j] + q[6 + i] * q[6 + j];
+            const double dq = q[0] * (q[4] * q[8] - q[7] * q[5]) - q[3] * (q[1] * q[8] - q[7] * q[2]) +
+                              q[6] * (q[1] * q[5] - q[4] * q[2]);
+            hm0[sidx] = make_float4((float)M[0][0], (float)M[1][1], (float)M[2][2], (float)M[0][1]);
+            hm1[sidx] = make_float4((float)M[0][2], (float)M[1][2], (float)dq, atd);
+            hm2[sidx] = make_float4(ath, (float)gm[t], 0.f, 0.f);
+        }
         c->alpha_t_d[sidx] = atd;
         c->alpha_t_h[sidx] = ath;
         hmat[sidx] = make_float2((float)(std::log10(Ecat[t]) / 5.0), (float)nucat[t]);
@@ -721,6 +732,9 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     XPBD_CU(c, c->q0.alloc(T));
     XPBD_CU(c, c->q1.alloc(T));
     XPBD_CU(c, c->q2.alloc(T));
+    XPBD_CU(c, c->m0.alloc(T));
+    XPBD_CU(c, c->m1.alloc(T));
+    XPBD_CU(c, c->m2.alloc(T));
     XPBD_CU(c, c->lam.alloc(T));
     XPBD_CU(c, c->perm.alloc(T));
     XPBD_CU(c, c->flags.alloc(1));
@@ -796,6 +810,9 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     XPBD_CU(c, cudaMemcpy(c->q0.p, h0.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->q1.p, h1.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->q2.p, h2.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->m0.p, hm0.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->m1.p, hm1.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
+    XPBD_CU(c, cudaMemcpy(c->m2.p, hm2.data(), sizeof(float4) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->perm.p, c->tet_of_slot.data(), sizeof(int) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemcpy(c->mat.p, hmat.data(), sizeof(float2) * T, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemset(c->warm_stats.p, 0, 2 * sizeof(unsigned long long)));

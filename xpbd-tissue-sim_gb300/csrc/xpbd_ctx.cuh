@@ -71,7 +71,8 @@ struct xpbd_ctx {
     // device state
     DevBuf<float4> x, prev, vel, dx, dxt;
     DevBuf<int4> tet_idx;
-    DevBuf<float4> q0, q1, q2;
+    DevBuf<float4> m0, m1, m2;  // projection records (M = Q Q^T, det Q, compliances)
+    DevBuf<float4> q0, q1, q2;  // Q, for the network features
     DevBuf<float2> lam;
     DevBuf<int> perm, csr_off, csr_ent;
     DevBuf<int4> faces;
@@ -216,7 +217,7 @@ struct xpbd_ctx {
                               F};
     }
     TetArrays tets() {
-        return TetArrays{tet_idx.p, q0.p, q1.p, q2.p, lam.p};
+        return TetArrays{tet_idx.p, m0.p, m1.p, m2.p, lam.p, q0.p, q1.p, q2.p};
     }
     Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
     PatchArrays patches() const { return PatchArrays{patch_meta.p, patch_verts.p}; }

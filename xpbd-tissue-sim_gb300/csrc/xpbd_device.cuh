@@ -107,12 +107,26 @@ __device__ __forceinline__ void add_vec4(float4* addr, float a, float b, float c
 // ---------------------------------------------------------------------------
 // Per-tet math, templated on the arithmetic type (float fast path, double for
 // near-degenerate elements).
+//
+// The static record of a tet holds M = Q Q^T and det Q (Q = Dm^-1) instead of
+// Q. With the edges X_i = p_i - p_3 (i < 3), F = [X_0 X_1 X_2] Q
+// (ElementConstraint.hpp:78-119) and q_i the rows of Q (q_3 = -q_0 - q_1 -
+// q_2), everything the two constraints need follows exactly:
+//   G_i = F q_i         = sum_j M_ij X_j
+//   ||F||^2             = sum_i X_i . G_i
+//   cof(F) q_i          = det Q N_i,  N_0 = X_1 x X_2, N_1 = X_2 x X_0, N_2 = X_0 x X_1
+//   det F               = det Q (X_0 . N_0)
+//   G_i . cof(F) q_i    = det F |q_i|^2 = det F M_ii   (F^T cof F = det F I)
+// so grad C_dev,i = G_i / ||F|| (DeviatoricConstraint.hpp:112-152) and
+// grad C_hyd,i = fac det Q N_i (HydrostaticConstraint.hpp:123-221). F itself
+// is never formed; the results agree with the F-based evaluation to rounding.
 // ---------------------------------------------------------------------------
 template <typename R>
 struct TetState {
     R p[4][3];
     R w[4];
-    R q[9];  // Q column-major: q[3c + r] = Q(r, c)
+    R m[6];  // M00 M11 M22 M01 M02 M12
+    R dq;    // det Q
     R atd, ath, gam;
 };
 
@@ -125,157 +139,182 @@ __device__ __forceinline__ R dev_sqrt(R v) { return sqrt(v); }
 template <>
 __device__ __forceinline__ float dev_sqrt<float>(float v) { return sqrtf(v); }
 
-// F = Ds Q (ElementConstraint.hpp:78-119), its Frobenius norm (C_dev) and det.
+// Edges X_i, G_i = F q_i and the face normals N_i (cof(F) q_i / det Q).
 template <typename R>
-__device__ __forceinline__ void tet_F(const TetState<R>& s, R F[9]) {
-    R X[9];
+__device__ __forceinline__ void tet_geom(const TetState<R>& s, R X[3][3], R G[3][3], R N[3][3]) {
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) X[3 * i + k] = s.p[i][k] - s.p[3][k];
+        for (int k = 0; k < 3; k++) X[i][k] = s.p[i][k] - s.p[3][k];
+    const R M[3][3] = {{s.m[0], s.m[3], s.m[4]}, {s.m[3], s.m[1], s.m[5]}, {s.m[4], s.m[5], s.m[2]}};
 #pragma unroll
-    for (int c = 0; c < 3; c++)
+    for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++)
-            F[3 * c + k] = X[k] * s.q[3 * c + 0] + X[3 + k] * s.q[3 * c + 1] + X[6 + k] * s.q[3 * c + 2];
+        for (int k = 0; k < 3; k++) G[i][k] = M[i][0] * X[0][k] + M[i][1] * X[1][k] + M[i][2] * X[2][k];
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const R* a = X[(i + 1) % 3];
+        const R* b = X[(i + 2) % 3];
+        N[i][0] = a[1] * b[2] - a[2] * b[1];
+        N[i][1] = a[2] * b[0] - a[0] * b[2];
+        N[i][2] = a[0] * b[1] - a[1] * b[0];
+    }
 }
 
+// C_hyd and the scale fac of its gradient, both branches of
+// HydrostaticConstraint.hpp:123-221 (log J for J >= 1, its cubic Taylor
+// polynomial below).
 template <typename R>
-__device__ __forceinline__ R tet_detF(const R F[9]) {
-    return F[0] * F[4] * F[8] - F[0] * F[7] * F[5] - F[3] * F[1] * F[8] + F[3] * F[7] * F[2] + F[6] * F[1] * F[5] -
-           F[6] * F[4] * F[2];
+__device__ __forceinline__ R tet_hyd(R J, R gam, R& fac) {
+    if (J >= R(1)) {
+        fac = R(1) / J;
+        return -gam + dev_log(J);
+    }
+    const R d = J - R(1);
+    fac = R(1) - d + d * d;
+    return -gam + d - d * d / R(2) + d * d * d / R(3);
 }
 
-// Values and gradients of both constraints (HydrostaticConstraint.hpp:123-221,
-// DeviatoricConstraint.hpp:112-152). gd/gh hold vertices 0..2; vertex 3 is
-// minus their sum.
+// Values and gradients of both constraints. gd/gh hold vertices 0..2; vertex
+// 3 is minus their sum.
 template <typename R>
 __device__ __forceinline__ void tet_eval(const TetState<R>& s, R& Cd, R& Ch, R gd[9], R gh[9], R& J) {
-    R F[9];
-    tet_F(s, F);
+    R X[3][3], G[3][3], N[3][3];
+    tet_geom(s, X, G, N);
     R ss = 0;
 #pragma unroll
-    for (int i = 0; i < 9; i++) ss += F[i] * F[i];
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) ss += X[i][k] * G[i][k];
     Cd = dev_sqrt(ss);
     const R invC = R(1) / Cd;
-#pragma unroll
-    for (int i = 0; i < 3; i++)
-#pragma unroll
-        for (int k = 0; k < 3; k++)
-            gd[3 * i + k] = invC * (F[k] * s.q[i] + F[3 + k] * s.q[3 + i] + F[6 + k] * s.q[6 + i]);
-    J = tet_detF(F);
+    J = s.dq * (X[0][0] * N[0][0] + X[0][1] * N[0][1] + X[0][2] * N[0][2]);
     R fac;
-    if (J >= R(1)) {
-        Ch = -s.gam + dev_log(J);
-        fac = R(1) / J;
-    } else {
-        const R d = J - R(1);
-        Ch = -s.gam + d - d * d / R(2) + d * d * d / R(3);
-        fac = R(1) - d + d * d;
-    }
-    R Fc[9];
-    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
+    Ch = tet_hyd(J, s.gam, fac);
+    const R fh = fac * s.dq;
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++)
-            gh[3 * i + k] = fac * (Fc[k] * s.q[i] + Fc[3 + k] * s.q[3 + i] + Fc[6 + k] * s.q[6 + i]);
+        for (int k = 0; k < 3; k++) {
+            gd[3 * i + k] = invC * G[i][k];
+            gh[3 * i + k] = fh * N[i][k];
+        }
 }
 
 // Constraint values only (no gradients): C_dev = ||F||_F and C_hyd
 // (DeviatoricConstraint.hpp:112-116, HydrostaticConstraint.hpp:123-153).
 template <typename R>
 __device__ __forceinline__ void tet_C(const TetState<R>& s, R& Cd, R& Ch) {
-    R F[9];
-    tet_F(s, F);
+    R X[3][3], G[3][3], N[3][3];
+    tet_geom(s, X, G, N);
     R ss = 0;
-#pragma unroll
-    for (int i = 0; i < 9; i++) ss += F[i] * F[i];
-    Cd = dev_sqrt(ss);
-    const R J = tet_detF(F);
-    if (J >= R(1)) {
-        Ch = -s.gam + dev_log(J);
-    } else {
-        const R d = J - R(1);
-        Ch = -s.gam + d - d * d / R(2) + d * d * d / R(3);
-    }
-}
-
-__device__ __forceinline__ float dot3(const float* a, const float* b) {
-    return fmaf(a[0], b[0], fmaf(a[1], b[1], a[2] * b[2]));
-}
-
-// FP32 fast path of the combined 2x2 projection (same contract as
-// tet_project_combined below), with a shorter dependency chain:
-// - the gradients are formed unscaled, G_i = F q_i and H_i = cof(F) q_i (q_i
-//   the rows of Q, q_3 = -q_0 - q_1 - q_2), so they do not wait for 1/||F||
-//   (rsqrt) or the hydrostatic factor; both scales enter the 2x2 system and
-//   the update as scalars: grad C_dev,i = G_i / ||F||, grad C_hyd,i = fac H_i
-//   (DeviatoricConstraint.hpp:112-152, HydrostaticConstraint.hpp:123-221);
-// - tree-shaped sums, 1/||F|| from rsqrt, 1/J and 1/det from the hardware
-//   reciprocal; det F from the cofactors the gradient uses.
-// Results differ from tet_project_combined only by FP32 rounding (a few ulp);
-// near-degenerate elements never use it.
-__device__ __forceinline__ void tet_project_combined_fast(const TetState<float>& s, float lam0, float lam1, float& r0,
-                                                          float& r1, float& dl0, float& dl1, float d[4][3], float& J) {
-    float F[9];
-    tet_F(s, F);
-    const float ss = ((fmaf(F[0], F[0], F[1] * F[1]) + fmaf(F[2], F[2], F[3] * F[3])) +
-                      (fmaf(F[4], F[4], F[5] * F[5]) + fmaf(F[6], F[6], F[7] * F[7]))) + F[8] * F[8];
-    const float invC = rsqrtf(ss);
-    const float Cd = ss * invC;
-    float Fc[9];
-    Fc[0] = F[4] * F[8] - F[5] * F[7]; Fc[1] = F[5] * F[6] - F[3] * F[8]; Fc[2] = F[3] * F[7] - F[4] * F[6];
-    Fc[3] = F[7] * F[2] - F[8] * F[1]; Fc[4] = F[8] * F[0] - F[6] * F[2]; Fc[5] = F[6] * F[1] - F[7] * F[0];
-    Fc[6] = F[1] * F[5] - F[2] * F[4]; Fc[7] = F[2] * F[3] - F[0] * F[5]; Fc[8] = F[0] * F[4] - F[1] * F[3];
-    J = fmaf(F[0], Fc[0], fmaf(F[1], Fc[1], F[2] * Fc[2]));
-    float Ch, fac;
-    if (J >= 1.f) {
-        Ch = -s.gam + logf(J);
-        fac = __frcp_rn(J);
-    } else {
-        const float dd = J - 1.f;
-        Ch = -s.gam + dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f);
-        fac = fmaf(dd, dd, 1.f - dd);
-    }
-    float G[12], H[12];
 #pragma unroll
     for (int i = 0; i < 3; i++)
 #pragma unroll
-        for (int k = 0; k < 3; k++) {
-            G[3 * i + k] = fmaf(F[k], s.q[i], fmaf(F[3 + k], s.q[3 + i], F[6 + k] * s.q[6 + i]));
-            H[3 * i + k] = fmaf(Fc[k], s.q[i], fmaf(Fc[3 + k], s.q[3 + i], Fc[6 + k] * s.q[6 + i]));
-        }
+        for (int k = 0; k < 3; k++) ss += X[i][k] * G[i][k];
+    Cd = dev_sqrt(ss);
+    const R J = s.dq * (X[0][0] * N[0][0] + X[0][1] * N[0][1] + X[0][2] * N[0][2]);
+    R fac;
+    Ch = tet_hyd(J, s.gam, fac);
+}
+
+// One-instruction hardware approximations (PTX rsqrt.approx, rcp.approx,
+// lg2.approx) for the FP32 fast path. Their error is about an ulp of the
+// result; for log J near 1 it is an absolute error below an ulp of C_hyd,
+// which is dominated by -gamma.
+__device__ __forceinline__ float rsqrt_approx(float x) {
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float log_approx(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y * 0.693147180559945f;  // ln 2
+}
+__device__ __forceinline__ float2 splat2(float v) { return make_float2(v, v); }
+
+// FP32 fast path of the combined 2x2 projection (same contract as
+// tet_project_combined below), written for issue slots, the limit of the
+// Gauss-Seidel chain:
+// - the edge / face-normal form above: no F, no cofactor matrix, and the
+//   cross term sum_i w_i grad C_dev,i . grad C_hyd,i = J sum_i w_i M_ii / ||F||
+//   * fac without a dot product;
+// - (G_ik, N_ik) held as float2 pairs, so their squares, sums and the vertex
+//   updates run as packed FP32x2 instructions (FFMA2 / FADD2 / FMUL2);
+// - the hydrostatic term without a branch (both forms are a few
+//   instructions), 1/||F||, 1/J and 1/det from single MUFU approximations.
+// Near-degenerate elements never use it.
+__device__ __forceinline__ void tet_project_combined_fast(const TetState<float>& s, float lam0, float lam1, float& r0,
+                                                          float& r1, float& dl0, float& dl1, float d[4][3], float& J) {
+    float X[3][3];
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-        G[9 + k] = -(G[k] + G[3 + k]) - G[6 + k];
-        H[9 + k] = -(H[k] + H[3 + k]) - H[6 + k];
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) X[i][k] = s.p[i][k] - s.p[3][k];
+    const float M[3][3] = {{s.m[0], s.m[3], s.m[4]}, {s.m[3], s.m[1], s.m[5]}, {s.m[4], s.m[5], s.m[2]}};
+    float2 GN[3][3];  // (G_ik, N_ik)
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) GN[i][k].x = fmaf(M[i][0], X[0][k], fmaf(M[i][1], X[1][k], M[i][2] * X[2][k]));
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+        const float* a = X[(i + 1) % 3];
+        const float* b = X[(i + 2) % 3];
+        GN[i][0].y = a[1] * b[2] - a[2] * b[1];
+        GN[i][1].y = a[2] * b[0] - a[0] * b[2];
+        GN[i][2].y = a[0] * b[1] - a[1] * b[0];
     }
-    float gg[4], gh[4], hh[4];
+    const float ss = (fmaf(X[0][0], GN[0][0].x, fmaf(X[0][1], GN[0][1].x, X[0][2] * GN[0][2].x)) +
+                      fmaf(X[1][0], GN[1][0].x, fmaf(X[1][1], GN[1][1].x, X[1][2] * GN[1][2].x))) +
+                     fmaf(X[2][0], GN[2][0].x, fmaf(X[2][1], GN[2][1].x, X[2][2] * GN[2][2].x));
+    const float invC = rsqrt_approx(ss);
+    const float Cd = ss * invC;
+    J = s.dq * fmaf(X[0][0], GN[0][0].y, fmaf(X[0][1], GN[0][1].y, X[0][2] * GN[0][2].y));
+    const float dd = J - 1.f;
+    const bool ge = J >= 1.f;
+    const float Ch = -s.gam + (ge ? log_approx(J) : dd - dd * dd * 0.5f + dd * dd * dd * (1.f / 3.f));
+    const float fac = ge ? rcp_approx(J) : fmaf(dd, dd, 1.f - dd);
+    const float fh = fac * s.dq;  // grad C_hyd,i = fh N_i
+    float2 S[3];                  // -(G_3, N_3)
+#pragma unroll
+    for (int k = 0; k < 3; k++) S[k] = __fadd2_rn(__fadd2_rn(GN[0][k], GN[1][k]), GN[2][k]);
+    float2 sq[4];  // (|G_i|^2, |N_i|^2)
 #pragma unroll
     for (int i = 0; i < 4; i++) {
-        gg[i] = dot3(G + 3 * i, G + 3 * i);
-        gh[i] = dot3(G + 3 * i, H + 3 * i);
-        hh[i] = dot3(H + 3 * i, H + 3 * i);
+        const float2* v = i < 3 ? GN[i] : S;
+        sq[i] = __ffma2_rn(v[0], v[0], __ffma2_rn(v[1], v[1], __fmul2_rn(v[2], v[2])));
     }
-    const float sgg = fmaf(s.w[0], gg[0], s.w[1] * gg[1]) + fmaf(s.w[2], gg[2], s.w[3] * gg[3]);
-    const float sgh = fmaf(s.w[0], gh[0], s.w[1] * gh[1]) + fmaf(s.w[2], gh[2], s.w[3] * gh[3]);
-    const float shh = fmaf(s.w[0], hh[0], s.w[1] * hh[1]) + fmaf(s.w[2], hh[2], s.w[3] * hh[3]);
-    const float L00 = fmaf(invC * invC, sgg, s.atd);
-    const float L01 = (invC * fac) * sgh;
-    const float L11 = fmaf(fac * fac, shh, s.ath);
+    const float2 s01 = __ffma2_rn(splat2(s.w[0]), sq[0], __fmul2_rn(splat2(s.w[1]), sq[1]));
+    const float2 s23 = __ffma2_rn(splat2(s.w[2]), sq[2], __fmul2_rn(splat2(s.w[3]), sq[3]));
+    const float2 sgn = __fadd2_rn(s01, s23);  // (sum w |G|^2, sum w |N|^2)
+    const float msum = (s.m[0] + s.m[1]) + (s.m[2] + 2.f * ((s.m[3] + s.m[4]) + s.m[5]));  // |q_3|^2
+    const float sw = fmaf(s.w[0], s.m[0], s.w[1] * s.m[1]) + fmaf(s.w[2], s.m[2], s.w[3] * msum);
+    const float L00 = fmaf(invC * invC, sgn.x, s.atd);
+    const float L01 = (invC * fac) * (J * sw);
+    const float L11 = fmaf(fh * fh, sgn.y, s.ath);
     r0 = fmaf(s.atd, lam0, Cd);
     r1 = fmaf(s.ath, lam1, Ch);
-    const float inv_det = __frcp_rn(fmaf(L00, L11, -L01 * L01));
+    const float inv_det = rcp_approx(fmaf(L00, L11, -L01 * L01));
     dl0 = fmaf(-r0, L11, r1 * L01) * inv_det;
     dl1 = fmaf(-r1, L00, r0 * L01) * inv_det;
-    const float a = invC * dl0, b = fac * dl1;
+    const float2 ab = make_float2(invC * dl0, fh * dl1);
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int i = 0; i < 4; i++) {
+        const float2* v = i < 3 ? GN[i] : S;
+        const float2 abi = __fmul2_rn(splat2(i < 3 ? s.w[i] : -s.w[3]), ab);
 #pragma unroll
-        for (int k = 0; k < 3; k++) d[i][k] = s.w[i] * fmaf(G[3 * i + k], a, H[3 * i + k] * b);
+        for (int k = 0; k < 3; k++) {
+            const float2 t = __fmul2_rn(v[k], abi);
+            d[i][k] = t.x + t.y;
+        }
+    }
 }
 
 // Combined 2x2 projection. Returns the pre-update residuals r = C + at*lam and
@@ -342,21 +381,27 @@ __device__ __forceinline__ void tet_project_single(const TetState<R>& s, int whi
     }
 }
 
-// Static per-tet data (indices, Dm^-1, compliances): never written while the
-// solver runs, so it may be loaded before the dependency wait.
+// The static record (m0, m1, m2) into a tet state.
+template <typename R>
+__device__ __forceinline__ void unpack_static(const float4& a, const float4& b, const float4& c, TetState<R>& s) {
+    s.m[0] = a.x; s.m[1] = a.y; s.m[2] = a.z; s.m[3] = a.w;
+    s.m[4] = b.x; s.m[5] = b.y; s.dq = b.z; s.atd = b.w;
+    s.ath = c.x; s.gam = c.y;
+}
+
+// Static per-tet data (indices, M and det Q, compliances): never written
+// while the solver runs, so it may be loaded before the dependency wait.
 __device__ __forceinline__ void load_tet_static(const TetArrays& t, int slot, int4& e, TetState<float>& s) {
     e = __ldg(t.idx + slot);
-    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
-    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
-    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
-    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
+    unpack_static(__ldg(t.m0 + slot), __ldg(t.m1 + slot), __ldg(t.m2 + slot), s);
 }
 
 // A vertex moved by a projection's update. The adds are not contracted with
 // the update's last multiply, so every Gauss-Seidel kernel variant rounds the
 // same way and their results agree bit for bit.
 __device__ __forceinline__ float4 moved(const float4& p, const float* d) {
-    return make_float4(__fadd_rn(p.x, d[0]), __fadd_rn(p.y, d[1]), __fadd_rn(p.z, d[2]), p.w);
+    const float2 xy = __fadd2_rn(make_float2(p.x, p.y), make_float2(d[0], d[1]));
+    return make_float4(xy.x, xy.y, __fadd_rn(p.z, d[2]), p.w);
 }
 
 __device__ __forceinline__ void gather_tet(const float4* __restrict__ x, const int4& e, TetState<float>& s,
@@ -386,10 +431,7 @@ __device__ __forceinline__ TetState<double> fp64_state(const TetArrays& t, int s
         s.p[i][0] = ps[i].x; s.p[i][1] = ps[i].y; s.p[i][2] = ps[i].z;
         s.w[i] = fabsf(ps[i].w);
     }
-    const float4 a = __ldg(t.q0 + slot), b = __ldg(t.q1 + slot), c = __ldg(t.q2 + slot);
-    s.q[0] = a.x; s.q[1] = a.y; s.q[2] = a.z; s.q[3] = a.w;
-    s.q[4] = b.x; s.q[5] = b.y; s.q[6] = b.z; s.q[7] = b.w;
-    s.q[8] = c.x; s.atd = c.y; s.ath = c.z; s.gam = c.w;
+    unpack_static(__ldg(t.m0 + slot), __ldg(t.m1 + slot), __ldg(t.m2 + slot), s);
     return s;
 }
 

@@ -173,7 +173,7 @@ template <bool FIRST, int WHICH, int MINB>
 __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t, PatchArrays pa, int pbegin, int pend,
                                                                float4* __restrict__ x, Flags* flags) {
     // the block's patches own the contiguous slot range [s0, s1): their static
-    // tet records arrive by three bulk copies (q0, q1, q2) before the
+    // tet records arrive by three bulk copies (m0, m1, m2) before the
     // dependency wait, costing no registers
     __shared__ __align__(128) float4 sq[3][kPatchBlock * kMaxPatchTets];
     __shared__ float4 sv[kMaxPatchVerts][kPatchBlock];
@@ -192,9 +192,9 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t
         const unsigned bytes = (unsigned)(s1 - s0) * 16u;
         s_first = s0;
         mbar_arrive_expect_tx(&bar, 3u * bytes);
-        tma_load_1d(sq[0], t.q0 + s0, bytes, &bar);
-        tma_load_1d(sq[1], t.q1 + s0, bytes, &bar);
-        tma_load_1d(sq[2], t.q2 + s0, bytes, &bar);
+        tma_load_1d(sq[0], t.m0 + s0, bytes, &bar);
+        tma_load_1d(sq[1], t.m1 + s0, bytes, &bar);
+        tma_load_1d(sq[2], t.m2 + s0, bytes, &bar);
     }
     int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
     int ntets = 0, nverts = 0;
@@ -234,12 +234,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_project_patch(TetArrays t
         if (i >= ntets) break;
         const int slot = meta.x + i;
         TetState<float> st;
-        {
-            const float4 a = sq[0][base + i], b = sq[1][base + i], c = sq[2][base + i];
-            st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
-            st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
-            st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
-        }
+        unpack_static(sq[0][base + i], sq[1][base + i], sq[2][base + i], st);
         int l[4];
         float4 xp[4];
 #pragma unroll
@@ -794,7 +789,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
             const bool active = lane < tk.y;
             // static data first: it does not depend on other tasks
             int4 meta = make_int4(0, 0, 0, 0), va = make_int4(0, 0, 0, 0), vb = make_int4(0, 0, 0, 0);
-            float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
+            float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // m0, m1, m2 records
             int ntets = 0, nverts = 0;
             if (active) {
                 meta = __ldg(pa.meta + p);
@@ -805,9 +800,9 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
 #pragma unroll
                 for (int i = 0; i < kMaxPatchTets; i++) {
                     if (i < ntets) {
-                        r0[i] = __ldg(t.q0 + meta.x + i);
-                        r1[i] = __ldg(t.q1 + meta.x + i);
-                        r2[i] = __ldg(t.q2 + meta.x + i);
+                        r0[i] = __ldg(t.m0 + meta.x + i);
+                        r1[i] = __ldg(t.m1 + meta.x + i);
+                        r2[i] = __ldg(t.m2 + meta.x + i);
                     }
                 }
             }
@@ -853,9 +848,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
                     if (i >= ntets) break;
                     const int slot = meta.x + i;
                     TetState<float> st;
-                    st.q[0] = r0[i].x; st.q[1] = r0[i].y; st.q[2] = r0[i].z; st.q[3] = r0[i].w;
-                    st.q[4] = r1[i].x; st.q[5] = r1[i].y; st.q[6] = r1[i].z; st.q[7] = r1[i].w;
-                    st.q[8] = r2[i].x; st.atd = r2[i].y; st.ath = r2[i].z; st.gam = r2[i].w;
+                    unpack_static(r0[i], r1[i], r2[i], st);
                     int l[4];
                     float4 xp[4];
 #pragma unroll
@@ -887,7 +880,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
 }
 
 // Dataflow sweep with the task's static tet records staged in shared memory:
-// lane 0 issues three bulk copies (q0, q1, q2 over the task's contiguous slot
+// lane 0 issues three bulk copies (m0, m1, m2 over the task's contiguous slot
 // range) before the dependency wait; each warp owns its staging buffer and
 // mbarrier. Same projections, order and arithmetic as k_sweep_dataflow.
 constexpr int kFlowWarps = kPatchBlock / 32;
@@ -915,9 +908,9 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const unsigned bytes = (unsigned)tk.w * 16u;
                 mbar_arrive_expect_tx(&bar[wib], 3u * bytes);
-                tma_load_1d(sq[wib][0], t.q0 + tk.z, bytes, &bar[wib]);
-                tma_load_1d(sq[wib][1], t.q1 + tk.z, bytes, &bar[wib]);
-                tma_load_1d(sq[wib][2], t.q2 + tk.z, bytes, &bar[wib]);
+                tma_load_1d(sq[wib][0], t.m0 + tk.z, bytes, &bar[wib]);
+                tma_load_1d(sq[wib][1], t.m1 + tk.z, bytes, &bar[wib]);
+                tma_load_1d(sq[wib][2], t.m2 + tk.z, bytes, &bar[wib]);
             }
             const int p = tk.x + lane;
             const bool active = lane < tk.y;
@@ -978,12 +971,7 @@ __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArr
                     if (i >= ntets) break;
                     const int slot = meta.x + i;
                     TetState<float> st;
-                    {
-                        const float4 a = sq[wib][0][base + i], b = sq[wib][1][base + i], c = sq[wib][2][base + i];
-                        st.q[0] = a.x; st.q[1] = a.y; st.q[2] = a.z; st.q[3] = a.w;
-                        st.q[4] = b.x; st.q[5] = b.y; st.q[6] = b.z; st.q[7] = b.w;
-                        st.q[8] = c.x; st.atd = c.y; st.ath = c.z; st.gam = c.w;
-                    }
+                    unpack_static(sq[wib][0][base + i], sq[wib][1][base + i], sq[wib][2][base + i], st);
                     int l[4];
                     float4 xp[4];
 #pragma unroll
@@ -1178,14 +1166,14 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
             if (nverts > 0) {
-                float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // q0, q1, q2 records
+                float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // m0, m1, m2 records
                 float2 lams[kMaxPatchTets];
 #pragma unroll
                 for (int i = 0; i < kMaxPatchTets; i++) {
                     if (i < ntets) {
-                        r0[i] = __ldg(t.q0 + meta.x + i);
-                        r1[i] = __ldg(t.q1 + meta.x + i);
-                        r2[i] = __ldg(t.q2 + meta.x + i);
+                        r0[i] = __ldg(t.m0 + meta.x + i);
+                        r1[i] = __ldg(t.m1 + meta.x + i);
+                        r2[i] = __ldg(t.m2 + meta.x + i);
                         // this lane alone writes these multipliers
                         lams[i] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
                     }
@@ -1236,9 +1224,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                         if (i >= ntets) break;
                         const int slot = meta.x + i;
                         TetState<float> st;
-                        st.q[0] = r0[i].x; st.q[1] = r0[i].y; st.q[2] = r0[i].z; st.q[3] = r0[i].w;
-                        st.q[4] = r1[i].x; st.q[5] = r1[i].y; st.q[6] = r1[i].z; st.q[7] = r1[i].w;
-                        st.q[8] = r2[i].x; st.atd = r2[i].y; st.ath = r2[i].z; st.gam = r2[i].w;
+                        unpack_static(r0[i], r1[i], r2[i], st);
                         int l[4];
                         float4 xp[4];
 #pragma unroll
@@ -1510,13 +1496,21 @@ __global__ void k_mlp_features(TetArrays t, const float4* __restrict__ x, const 
     load_tet_static(t, slot, e, st);
     float4 xp[4];
     gather_tet(x, e, st, xp);
-    float F[9];
-    tet_F(st, F);
+    // F = [X_0 X_1 X_2] Q (ElementConstraint.hpp:78-119), Q column-major
+    const float4 qa = __ldg(t.q0 + slot), qb = __ldg(t.q1 + slot), qc = __ldg(t.q2 + slot);
+    const float q[9] = {qa.x, qa.y, qa.z, qa.w, qb.x, qb.y, qb.z, qb.w, qc.x};
+    float Ds[9];
+#pragma unroll
+    for (int i = 0; i < 3; i++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) Ds[3 * i + k] = st.p[i][k] - st.p[3][k];
     const float2 lam = t.lam[slot];
     const float2 m = mat[slot];
     float f[16];
 #pragma unroll
-    for (int k = 0; k < 9; k++) f[k] = F[k];
+    for (int c = 0; c < 3; c++)
+#pragma unroll
+        for (int k = 0; k < 3; k++) f[3 * c + k] = Ds[k] * q[3 * c] + Ds[3 + k] * q[3 * c + 1] + Ds[6 + k] * q[3 * c + 2];
     f[9] = st.atd * lam.x;
     f[10] = st.ath * lam.y;
     f[11] = m.x;
@@ -1538,10 +1532,10 @@ __global__ void k_mlp_targets(TetArrays t, int s0, int n, float* __restrict__ Y)
     pdl_wait_then_release();
     if (i >= n) return;
     const int slot = s0 + i;
-    const float4 c = __ldg(t.q2 + slot);
+    const float atd = __ldg(t.m1 + slot).w, ath = __ldg(t.m2 + slot).x;
     const float2 lam = t.lam[slot];
-    Y[2 * (size_t)i] = c.y * lam.x;
-    Y[2 * (size_t)i + 1] = c.z * lam.y;
+    Y[2 * (size_t)i] = atd * lam.x;
+    Y[2 * (size_t)i + 1] = ath * lam.y;
 }
 
 // Warm start: lambda <- lambda0 and x += M^-1 grad C(x)^T lambda0 summed over

@@ -6,10 +6,13 @@
 //   vel    float4[V]  velocity xyz
 //   dx     float4[V]  Jacobi accumulator (zero between sweeps)
 //   tet_idx int4[T]   vertex indices, in solver slot order
-//   tet_q0  float4[T] Q(0,0) Q(1,0) Q(2,0) Q(0,1)      (Q = Dm^-1, column-major)
-//   tet_q1  float4[T] Q(1,1) Q(2,1) Q(0,2) Q(1,2)
-//   tet_q2  float4[T] Q(2,2) alpha_tilde_dev alpha_tilde_hyd gamma
+//   tet_m0  float4[T] M00 M11 M22 M01                  (M = Q Q^T, Q = Dm^-1)
+//   tet_m1  float4[T] M02 M12 det(Q) alpha_tilde_dev
+//   tet_m2  float4[T] alpha_tilde_hyd gamma 0 0
 //   lam     float2[T] (lambda_dev, lambda_hyd)
+//   tet_q0  float4[T] Q(0,0) Q(1,0) Q(2,0) Q(0,1)      (Q column-major; read only
+//   tet_q1  float4[T] Q(1,1) Q(2,1) Q(0,2) Q(1,2)       for the warm-start network's
+//   tet_q2  float4[T] Q(2,2) 0 0 0                      deformation-gradient features)
 // One tet costs 16 + 48 + 8 (+8 write) = 80 bytes of streamed data per sweep.
 #pragma once
 
@@ -41,10 +44,13 @@ enum KernelId {
 
 struct TetArrays {
     const int4* idx;
+    const float4* m0;
+    const float4* m1;
+    const float4* m2;
+    float2* lam;
     const float4* q0;
     const float4* q1;
     const float4* q2;
-    float2* lam;
 };
 
 struct ContactArrays {
