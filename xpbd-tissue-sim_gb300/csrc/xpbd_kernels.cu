@@ -1080,9 +1080,14 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     static_assert(kFlowBlock == 32, "one warp per block: the topology is indexed by lane");
     extern __shared__ int4 topo[];  // RESIDENT: [task k][meta, verts a, verts b, versions][lane]
     __shared__ float4 sv[kMaxPatchVerts][kFlowBlock];
+    __shared__ __align__(128) float4 srec[3][kTaskSlots];  // the task's m0, m1, m2 records
+    __shared__ __align__(8) unsigned long long bar;
     const int tid = threadIdx.x, lane = tid & 31;
     const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
+    if (lane == 0) mbar_init(&bar, 1);
+    __syncwarp();
+    unsigned phase = 0;
     if (RESIDENT) {
         int k = 0;
         for (int j = gw; j < ta.ntasks; j += nw, k++) {
@@ -1165,22 +1170,35 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             }
             k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
+            // The task's static records (a contiguous slot range of at most
+            // kTaskSlots) arrive in shared memory by three bulk copies that
+            // do not pass through the load/store pipe the polls use.
+            // Padding tasks (colour runs are padded to the warp count) have no
+            // patch and copy nothing; a range longer than the buffer (never
+            // built) is refused without a copy.
+            const int s0 = __reduce_min_sync(0xffffffffu, nverts > 0 ? meta.x : INT_MAX);
+            const int s1 = __reduce_max_sync(0xffffffffu, nverts > 0 ? meta.x + ntets : 0);
+            const bool copy = s1 > s0 && s1 - s0 <= kTaskSlots;
+            if (s1 > s0 && !copy) ok = false;
+            __syncwarp();  // the previous task's reads of srec are done
+            if (copy && lane == 0) {
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const unsigned bytes = (unsigned)(s1 - s0) * 16u;
+                mbar_arrive_expect_tx(&bar, 3u * bytes);
+                tma_load_1d(srec[0], t.m0 + s0, bytes, &bar);
+                tma_load_1d(srec[1], t.m1 + s0, bytes, &bar);
+                tma_load_1d(srec[2], t.m2 + s0, bytes, &bar);
+            }
+            const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+            int due[kMaxPatchVerts];
+            float2 lams[kMaxPatchTets];
             if (nverts > 0) {
-                float4 r0[kMaxPatchTets], r1[kMaxPatchTets], r2[kMaxPatchTets];  // m0, m1, m2 records
-                float2 lams[kMaxPatchTets];
 #pragma unroll
                 for (int i = 0; i < kMaxPatchTets; i++) {
-                    if (i < ntets) {
-                        r0[i] = __ldg(t.m0 + meta.x + i);
-                        r1[i] = __ldg(t.m1 + meta.x + i);
-                        r2[i] = __ldg(t.m2 + meta.x + i);
-                        // this lane alone writes these multipliers
-                        lams[i] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
-                    }
+                    // this lane alone writes these multipliers
+                    if (i < ntets) lams[i] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
                 }
-                const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
                 const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
-                int due[kMaxPatchVerts];
                 unsigned pending = 0;
 #pragma unroll
                 for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
@@ -1208,14 +1226,23 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                             unsigned long long a, b, c, d;
                             ld_ver(xv + vid[k2], a, b, c, d);
                             if (ver_min(a, b, c) >= due[k2]) {
-                                sv[k2][tid].x = ver_val(a);
-                                sv[k2][tid].y = ver_val(b);
-                                sv[k2][tid].z = ver_val(c);
+                                sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
                                 pending &= ~(1u << k2);
                             }
                         }
                     }
                 }
+            }
+            if (copy) {
+                // the copies land (or not) whatever happened above
+                const bool staged = __all_sync(0xffffffffu, mbar_wait_bounded(&bar, phase, kWaitLimit)) != 0;
+                phase ^= 1u;
+                if (!staged) {
+                    ok = false;
+                    if (lane == 0) mbar_wait_bounded(&bar, phase ^ 1u, kWaitLimit);
+                }
+            }
+            if (nverts > 0) {
                 if (ok) {
                     const unsigned long long loc =
                         (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
@@ -1223,8 +1250,9 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     for (int i = 0; i < kMaxPatchTets; i++) {
                         if (i >= ntets) break;
                         const int slot = meta.x + i;
+                        const int r = slot - s0;
                         TetState<float> st;
-                        unpack_static(r0[i], r1[i], r2[i], st);
+                        unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
                         int l[4];
                         float4 xp[4];
 #pragma unroll
