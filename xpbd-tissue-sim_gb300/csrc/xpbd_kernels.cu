@@ -885,6 +885,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
 // mbarrier. Same projections, order and arithmetic as k_sweep_dataflow.
 constexpr int kFlowWarps = kPatchBlock / 32;
 constexpr int kTaskSlots = kTaskPatches * kMaxPatchTets;
+static_assert(kTaskSlots % 32 == 0, "whole multiplier records per lane");
 
 template <bool FIRST_ZERO>
 __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArrays t, PatchArrays pa, TaskArrays ta,
@@ -1081,6 +1082,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     extern __shared__ int4 topo[];  // RESIDENT: [task k][meta, verts a, verts b, versions][lane]
     __shared__ float4 sv[kMaxPatchVerts][kFlowBlock];
     __shared__ __align__(128) float4 srec[3][kTaskSlots];  // the task's m0, m1, m2 records
+    __shared__ float2 slam[kTaskSlots];                   // and its multipliers
     __shared__ __align__(8) unsigned long long bar;
     const int tid = threadIdx.x, lane = tid & 31;
     const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
@@ -1189,15 +1191,21 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 tma_load_1d(srec[1], t.m1 + s0, bytes, &bar);
                 tma_load_1d(srec[2], t.m2 + s0, bytes, &bar);
             }
+            // The task's multipliers, read and (after the task) written back by
+            // coalesced accesses; only this warp touches them meanwhile. The
+            // loads are in flight during the polls and land in slam after them.
+            constexpr int kLamPerLane = kTaskSlots / 32;
+            const int ns = copy ? s1 - s0 : 0;
+            float2 lt[kLamPerLane];
+#pragma unroll
+            for (int u = 0; u < kLamPerLane; u++) {
+                const int r = lane + 32 * u;
+                lt[u] = make_float2(0.f, 0.f);
+                if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = t.lam[s0 + r];
+            }
             const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
             int due[kMaxPatchVerts];
-            float2 lams[kMaxPatchTets];
             if (nverts > 0) {
-#pragma unroll
-                for (int i = 0; i < kMaxPatchTets; i++) {
-                    // this lane alone writes these multipliers
-                    if (i < ntets) lams[i] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
-                }
                 const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
                 unsigned pending = 0;
 #pragma unroll
@@ -1233,6 +1241,10 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     }
                 }
             }
+#pragma unroll
+            for (int u = 0; u < kLamPerLane; u++)
+                if (lane + 32 * u < ns) slam[lane + 32 * u] = lt[u];
+            __syncwarp();  // slam filled
             if (copy) {
                 // the copies land (or not) whatever happened above
                 const bool staged = __all_sync(0xffffffffu, mbar_wait_bounded(&bar, phase, kWaitLimit)) != 0;
@@ -1262,14 +1274,14 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                             st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
                             st.w[q] = fabsf(xp[q].w);
                         }
-                        float2 lam = lams[i];
+                        float2 lam = slam[r];
                         float d[4][3];
                         double rsq;
                         if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
 #pragma unroll
                             for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
                         }
-                        t.lam[slot] = lam;
+                        slam[r] = lam;
                     }
                     // every vertex goes out one version later, moved or not
 #pragma unroll
@@ -1281,6 +1293,13 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     }
                 }
             }
+            __syncwarp();  // every lane's multipliers are in slam
+#pragma unroll
+            for (int u = 0; u < kLamPerLane; u++)
+                if (lane + 32 * u < ns) lt[u] = slam[lane + 32 * u];
+#pragma unroll
+            for (int u = 0; u < kLamPerLane; u++)
+                if (lane + 32 * u < ns) t.lam[s0 + lane + 32 * u] = lt[u];
           } else if (CONTACTS) {
             const int2 ct = fc.task[j - ta.ntasks];
             if (lane < ct.y) {

@@ -131,7 +131,7 @@ struct TaskArrays {
 struct alignas(32) VerRec {
     unsigned long long x, y, z, w;
 };
-constexpr unsigned kPollNs = 1024;  // default back-off of variant 4's polls
+constexpr unsigned kPollNs = 768;  // default back-off of variant 4's polls
 
 // Static contacts inside variant 4's sweep: after each detection, the faces
 // with an active static contact in colour-major order (colour, instance,
