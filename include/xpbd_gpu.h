@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 6
+#define XPBD_ABI_VERSION 7
 
 /* status codes */
 #define XPBD_OK 0
@@ -172,6 +172,18 @@ int xpbd_num_instances(xpbd_ctx* ctx, int32_t* n);
 /* offsets of each instance into the concatenated arrays, n + 1 entries each
  * (any pointer may be NULL) */
 int xpbd_instance_offsets(xpbd_ctx* ctx, int64_t* vertex_offsets, int64_t* tet_offsets, int64_t* face_offsets);
+/* Per-instance completion times of a batched substep (GPU-side measurement,
+ * no reference counterpart). With stamps on, each xpbd_step / xpbd_update
+ * substep records the device clock when it starts, when each task of the
+ * persistent sweep (gs_variant 4) finishes its last iteration, and when the
+ * substep's last kernel ends. xpbd_instance_latencies then gives, for the
+ * last substep, ms[k] = start -> the end of instance k's last sweep task (its
+ * final projections written; n_instances entries) and *batch_ms = start ->
+ * end of the substep (after the batch-wide copy-out and velocity update).
+ * XPBD_ERR_STATE without a persistent versioned sweep or before a stamped
+ * substep; stamps cost one clock read and store per task and substep. */
+int xpbd_set_latency_stamps(xpbd_ctx* ctx, int32_t on);
+int xpbd_instance_latencies(xpbd_ctx* ctx, double* ms, double* batch_ms);
 int xpbd_destroy(xpbd_ctx* ctx);
 const char* xpbd_last_error(const xpbd_ctx* ctx);
 

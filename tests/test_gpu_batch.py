@@ -118,3 +118,38 @@ def test_autotuner_times_every_candidate_and_keeps_the_fastest(lib, solver, ncan
     s.step(2)
     s.synchronize()
     s.close()
+
+
+def test_instance_latency_stamps(lib):
+    """Per-instance completion times of the persistent sweep: one per
+    instance, inside the substep, spread over it, and the stamps change no
+    result (a run without them ends bit-identical)."""
+    b = _small_batch(n=6, seed=4)
+    s = W.make_batch_solver(b, gs_variant=4)
+    plain = W.make_batch_solver(b, gs_variant=4)
+    with pytest.raises(G.XPBDError):
+        s.instance_latencies()  # nothing stamped yet
+    s.set_latency_stamps(True)
+    for _ in range(6):
+        for x in (s, plain):
+            W.drive_batch(x, b)
+            x.step(1)
+        ms, batch_ms = s.instance_latencies()
+        assert ms.shape == (len(b.instances),)
+        assert np.all(ms > 0) and np.all(ms <= batch_ms + 1e-6), (ms, batch_ms)
+    np.testing.assert_array_equal(s.positions(), plain.positions())
+    s.set_latency_stamps(False)
+    W.drive_batch(s, b)
+    s.step(1)
+    with pytest.raises(G.XPBDError):
+        s.instance_latencies()
+    s.close()
+    plain.close()
+
+
+def test_latency_stamps_need_the_versioned_sweep(lib):
+    b = _small_batch(n=2, seed=4)
+    s = W.make_batch_solver(b, gs_variant=1)
+    with pytest.raises(G.XPBDError):
+        s.set_latency_stamps(True)
+    s.close()

@@ -328,7 +328,7 @@ int build_flow_contacts(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::
                         const std::vector<int>& fcol) {
     c->flow_contacts = false;
     const int V = c->V, F = c->F, P = (int)pmeta.size();
-    if (!c->flow_versioned || F == 0 || c->n_face_colours > 64) return XPBD_OK;
+    if (!c->flow_versioned || F == 0 || c->n_face_colours > kMaxFlowFaceColours) return XPBD_OK;
     std::vector<int> degp(V, 0);
     for (int q = 0; q < P; q++)
         for (int k = 0; k < (pmeta[q].y >> 8); k++) {

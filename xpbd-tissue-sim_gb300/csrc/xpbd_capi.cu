@@ -1023,6 +1023,71 @@ int xpbd_instance_offsets(xpbd_ctx* c, int64_t* voff, int64_t* toff, int64_t* fo
     return XPBD_OK;
 }
 
+int xpbd_set_latency_stamps(xpbd_ctx* c, int32_t on) {
+    if (!c || (on != 0 && on != 1)) return XPBD_ERR_INVALID;
+    if (on && !(c->flow_versioned && c->ntasks > 0))
+        return fail(c, XPBD_ERR_STATE, "latency stamps need the persistent versioned sweep (gs_variant 4)");
+    if (on && !c->lat.p) {
+        // every patch task, and at most one contact task per face plus one per face colour
+        XPBD_CU(c, c->lat.alloc(2 + (size_t)c->ntasks + (size_t)c->F + kMaxFlowFaceColours));
+        XPBD_CU(c, cudaMemset(c->lat.p, 0, sizeof(unsigned long long) * c->lat.n));
+    }
+    if (on && c->task_inst_h.empty()) {
+        // the instances each patch task's slot range touches
+        std::vector<int4> tk(c->ntasks);
+        XPBD_CU(c, cudaMemcpy(tk.data(), c->flow_tasks.p, sizeof(int4) * tk.size(), cudaMemcpyDeviceToHost));
+        c->task_inst_h.assign(c->ntasks, make_int2(-1, -1));
+        for (int j = 0; j < c->ntasks; j++) {
+            if (tk[j].y <= 0) continue;  // padding task
+            int lo = c->n_inst, hi = -1;
+            for (int sl = tk[j].z; sl < tk[j].z + tk[j].w; sl++) {
+                const int64_t t = c->tet_of_slot[sl];
+                const int k = (int)(std::upper_bound(c->toff.begin(), c->toff.end(), t) - c->toff.begin()) - 1;
+                lo = std::min(lo, k);
+                hi = std::max(hi, k);
+            }
+            c->task_inst_h[j] = make_int2(lo, hi);
+        }
+    }
+    if ((bool)on != c->lat_on) c->graph_dirty = true;  // the stamp pointer is a launch argument
+    c->lat_on = on != 0;
+    c->lat_have = false;
+    return XPBD_OK;
+}
+
+int xpbd_instance_latencies(xpbd_ctx* c, double* ms, double* batch_ms) {
+    if (!c || !ms) return XPBD_ERR_INVALID;
+    if (!c->lat_on || !c->lat_have) return fail(c, XPBD_ERR_STATE, "no stamped substep since the stamps were turned on");
+    XPBD_CU(c, cudaStreamSynchronize(c->stream));
+    int nct = 0;
+    if (c->F && c->flow_contacts) XPBD_CU(c, cudaMemcpy(&nct, c->n_ctasks.p, sizeof(int), cudaMemcpyDeviceToHost));
+    const size_t ntot = (size_t)c->ntasks + nct;
+    std::vector<unsigned long long> st(2 + ntot);
+    XPBD_CU(c, cudaMemcpy(st.data(), c->lat.p, sizeof(unsigned long long) * st.size(), cudaMemcpyDeviceToHost));
+    std::vector<unsigned long long> done(c->n_inst, 0);
+    for (int j = 0; j < c->ntasks; j++) {
+        const int2 r = c->task_inst_h[j];
+        for (int k = r.x; k >= 0 && k <= r.y; k++) done[k] = std::max(done[k], st[2 + j]);
+    }
+    if (nct > 0) {
+        // contact task -> its faces -> their instances
+        std::vector<int2> ct(nct);
+        XPBD_CU(c, cudaMemcpy(ct.data(), c->ctask.p, sizeof(int2) * nct, cudaMemcpyDeviceToHost));
+        const int ne = ct.back().x + ct.back().y;
+        std::vector<int4> fe(std::max(ne, 0));
+        if (ne > 0) XPBD_CU(c, cudaMemcpy(fe.data(), c->cface.p, sizeof(int4) * ne, cudaMemcpyDeviceToHost));
+        for (int j = 0; j < nct; j++)
+            for (int e = ct[j].x; e < ct[j].x + ct[j].y; e++) {
+                const int f = fe[e].x;
+                const int k = (int)(std::upper_bound(c->foff.begin(), c->foff.end(), (int64_t)f) - c->foff.begin()) - 1;
+                done[k] = std::max(done[k], st[2 + c->ntasks + j]);
+            }
+    }
+    for (int k = 0; k < c->n_inst; k++) ms[k] = done[k] > st[0] ? (double)(done[k] - st[0]) * 1e-6 : 0.0;
+    if (batch_ms) *batch_ms = st[1] > st[0] ? (double)(st[1] - st[0]) * 1e-6 : 0.0;
+    return XPBD_OK;
+}
+
 int xpbd_clear_collisions(xpbd_ctx* c) {
     if (!c) return XPBD_ERR_INVALID;
     if (c->F) {
@@ -1170,7 +1235,14 @@ int xpbd_get_self_contacts(xpbd_ctx* c, int32_t max_rows, int32_t* vf, double* l
 
 int xpbd_update(xpbd_ctx* c) {
     if (!c) return XPBD_ERR_INVALID;
-    return run_update(c, false, false);
+    if (c->lat_on) launch_stamp(c->L(), c->lat.p);
+    int st = run_update(c, false, false);
+    if (st) return st;
+    if (c->lat_on) {
+        launch_stamp(c->L(), c->lat.p + 1);
+        c->lat_have = true;
+    }
+    return XPBD_OK;
 }
 
 int xpbd_solve(xpbd_ctx* c) {
@@ -1208,6 +1280,7 @@ int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
     const double interval = c->prm.collision_rate > 0 ? 1.0 / c->prm.collision_rate : 1e300;
     for (int k = 0; k < nsteps; k++) {
         const bool cd = (c->time - c->last_cd > interval);
+        if (c->lat_on) launch_stamp(c->L(), c->lat.p);
         if (cd && (c->n_spheres_total > 0 || c->self_on)) {
             int st = detect(c);
             if (st) return st;
@@ -1217,6 +1290,10 @@ int xpbd_step(xpbd_ctx* c, int32_t nsteps) {
         }
         int st = run_update(c, true, false);
         if (st) return st;
+        if (c->lat_on) {
+            launch_stamp(c->L(), c->lat.p + 1);
+            c->lat_have = true;
+        }
         if (c->time - c->last_cd > interval) c->last_cd = c->time;
         c->time += c->prm.dt;
     }

@@ -113,6 +113,11 @@ struct xpbd_ctx {
     std::vector<int4> patch_ver_h;  // host copy of patch_ver
     unsigned flow_poll_limit = xg::kFlowLimit;
     unsigned flow_poll_ns = xg::kPollNs;
+    // per-instance latency stamps (xpbd_set_latency_stamps): [0] substep start,
+    // [1] substep end, [2 + j] task j's end of its last iteration
+    DevBuf<unsigned long long> lat;
+    bool lat_on = false, lat_have = false;
+    std::vector<int2> task_inst_h;  // patch task -> first and last instance it touches
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -204,7 +209,8 @@ struct xpbd_ctx {
 
     xg::TaskArrays tasks() {
         return xg::TaskArrays{flow_tasks.p,       flow_dep_off.p, flow_dep.p,      flow_epoch.p,
-                              flow_epoch.p + ntasks, ntasks,        flow_poll_limit, flow_poll_ns};
+                              flow_epoch.p + ntasks, ntasks,        flow_poll_limit, flow_poll_ns,
+                              lat_on ? lat.p : nullptr};
     }
     xg::FlowContacts flowc() {
         return xg::FlowContacts{ctask.p, cface.p, n_ctasks.p, vdeg_c.p};

@@ -1040,6 +1040,18 @@ __device__ __forceinline__ int ver_min(unsigned long long a, unsigned long long 
     return min(ver_of(a), min(ver_of(b), ver_of(c)));
 }
 
+// The device clock in ns (%globaltimer).
+__device__ __forceinline__ unsigned long long clock_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t)::"memory");
+    return t;
+}
+
+__global__ void k_stamp(unsigned long long* p) {
+    pdl_wait_then_release();
+    *p = clock_ns();
+}
+
 // Positions at version 0, the inverse mass in the fourth word.
 __global__ void k_versions_in(VerRec* __restrict__ xv, const float4* __restrict__ x, int V) {
     pdl_wait_then_release();
@@ -1358,6 +1370,10 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 }
             }
           }
+            if (ta.stamp && it == iters - 1) {
+                __syncwarp();  // the task's stores are issued
+                if (lane == 0) ta.stamp[2 + j] = clock_ns();
+            }
             if (!__all_sync(0xffffffffu, ok)) {
                 if (lane == 0) {
                     atomicExch(ta.abort_flag, 1u);
@@ -1926,7 +1942,6 @@ __global__ void k_vertex_contact_degree(const int* __restrict__ vface_off, const
 }
 
 constexpr int kScanThreads = 1024;
-constexpr int kMaxFlowFaceColours = 64;
 
 // Colour-major offsets of the active faces (colour, instance) from the
 // per-instance lists, and the contact tasks: per colour, runs of up to 32.
@@ -2020,6 +2035,8 @@ __global__ void k_contact_faces_fill(ContactArrays c, const int* __restrict__ ac
         }
     }
 }
+
+void launch_stamp(const Launch& s, unsigned long long* p) { go(k_stamp, 1, 1, s, p); }
 
 void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
                                 int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,

@@ -121,6 +121,8 @@ struct TaskArrays {
     int ntasks;
     unsigned poll_limit;  // polls of one wait before it gives up
     unsigned poll_ns;     // variant 4: back-off between two polls of a vertex not yet due
+    unsigned long long* stamp;  // variant 4, optional: stamp[2 + j] = device clock (ns) when
+                                // task j ends its last iteration
 };
 
 // Variant 4's vertex record: four aligned 64-bit words (x, ver), (y, ver),
@@ -131,6 +133,8 @@ struct TaskArrays {
 struct alignas(32) VerRec {
     unsigned long long x, y, z, w;
 };
+// face colours the versioned sweep's contact phases handle (more keep their own launches)
+constexpr int kMaxFlowFaceColours = 64;
 constexpr unsigned kPollNs = 768;  // default back-off of variant 4's polls
 
 // Static contacts inside variant 4's sweep: after each detection, the faces
@@ -282,6 +286,8 @@ int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp, bool conta
 // After a detection (the per-instance active lists built): the sweep's
 // contact tables. vface_off/vface/fcol/vdegp are static: per vertex its
 // surface faces (CSR) and patch count, per face its colour.
+// one thread writes the device clock (ns) to *p once the stream's earlier work is done
+void launch_stamp(const Launch& s, unsigned long long* p);
 void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
                                 int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,
                                 const unsigned char* vdegp, unsigned char* factive, int* cm_off, int2* ctask,

@@ -151,6 +151,8 @@ def load(path: str | None = None):
         "xpbd_create_batch": ([P, I32, P, P], C.c_int),
         "xpbd_num_instances": ([P, P], C.c_int),
         "xpbd_instance_offsets": ([P, P, P, P], C.c_int),
+        "xpbd_set_latency_stamps": ([P, I32], C.c_int),
+        "xpbd_instance_latencies": ([P, P, P], C.c_int),
         "xpbd_set_instance_spheres": ([P, I32, I32, P, P], C.c_int),
         "xpbd_autotune": ([P, I32, P, I32, P, I32], C.c_int),
         "xpbd_mlp_init": ([P, C.c_uint64], C.c_int),
@@ -398,6 +400,20 @@ class XPBDSolver:
         v, t, f = np.zeros(n, np.int64), np.zeros(n, np.int64), np.zeros(n, np.int64)
         self._ck(self.L.xpbd_instance_offsets(self.h, _p(v), _p(t), _p(f)))
         return v, t, f
+
+    def set_latency_stamps(self, on: bool = True):
+        """Stamp each substep's start and end and each persistent-sweep task's
+        last iteration with the device clock (gs_variant 4 only)."""
+        self._ck(self.L.xpbd_set_latency_stamps(self.h, int(bool(on))))
+
+    def instance_latencies(self):
+        """For the last stamped substep: (ms per instance from the substep's
+        start to the end of that instance's last sweep task, ms of the whole
+        substep)."""
+        ms = np.zeros(self.n_instances, np.float64)
+        b = C.c_double(0.0)
+        self._ck(self.L.xpbd_instance_latencies(self.h, _p(ms), C.byref(b)))
+        return ms, b.value
 
     def clear_collisions(self):
         self._ck(self.L.xpbd_clear_collisions(self.h))
