@@ -1184,6 +1184,13 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             }
             k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
+            const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
+            // The first polls go out before anything else the task issues:
+            // their round trip is the phase's critical path.
+            unsigned long long pw[kMaxPatchVerts][4];
+#pragma unroll
+            for (int k2 = 0; k2 < kMaxPatchVerts; k2++)
+                if (k2 < nverts) ld_ver(xv + vid[k2], pw[k2][0], pw[k2][1], pw[k2][2], pw[k2][3]);
             // The task's static records (a contiguous slot range of at most
             // kTaskSlots) arrive in shared memory by three bulk copies that
             // do not pass through the load/store pipe the polls use.
@@ -1215,7 +1222,6 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 lt[u] = make_float2(0.f, 0.f);
                 if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = t.lam[s0 + r];
             }
-            const int vid[kMaxPatchVerts] = {va.x, va.y, va.z, va.w, vb.x, vb.y, vb.z, vb.w};
             int due[kMaxPatchVerts];
             if (nverts > 0) {
                 const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
@@ -1227,10 +1233,9 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                     if (CONTACTS && !RESIDENT && k2 < nverts) deg += __ldg(fc.vdegc + vid[k2]);
                     due[k2] = it * deg + (h & 0xff);
                     if (k2 < nverts) {
-                        unsigned long long a, b, c, d;
-                        ld_ver(xv + vid[k2], a, b, c, d);
-                        sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
-                        if (ver_min(a, b, c) < due[k2]) pending |= 1u << k2;
+                        sv[k2][tid] =
+                            make_float4(ver_val(pw[k2][0]), ver_val(pw[k2][1]), ver_val(pw[k2][2]), ver_val(pw[k2][3]));
+                        if (ver_min(pw[k2][0], pw[k2][1], pw[k2][2]) < due[k2]) pending |= 1u << k2;
                     }
                 }
                 unsigned n = 0;
