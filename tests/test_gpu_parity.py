@@ -371,6 +371,30 @@ def test_health_counts_degenerate_elements(lib):
     s.close()
 
 
+def test_versioned_sweep_careful_pass_equals_colour_launches(lib):
+    """The versioned sweep projects a patch in one straight FP32 pass and
+    redoes it from the task's start with the per-tet FP64 guard when any of
+    its tets is near-degenerate; the colour launches guard tet by tet. A mesh
+    whose top layer is squashed flat (|det F| ~ 1e-4 there) takes both paths
+    and must end bit-identical, with the same degenerate count."""
+    X, tets, faces = G.grid_mesh(6, 6, 6, 1.0 / 6)
+    x = X.copy()
+    top = X[:, 2] > 1.0 - 1e-9
+    x[top, 2] = 1.0 - 1.0 / 6 + 1e-4 / 6  # the top layer of hexes nearly flat
+    out = []
+    for var in (0, 4):
+        s = G.XPBDSolver(X, tets, None, 3e3, 0.45, 1000.0, num_iters=6, gs_variant=var)
+        s.fix_vertices(X[:, 2] == 0)
+        s.set_positions(x)
+        s.step(5)
+        s.synchronize()
+        out.append((s.positions(), s.lambdas(), s.health()))
+        s.close()
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_array_equal(out[0][1], out[1][1])
+    assert out[0][2][1] > 0 and out[0][2] == out[1][2], (out[0][2], out[1][2])
+
+
 def test_invalid_inputs_return_status(lib):
     X, tets, faces = G.grid_mesh(2, 2, 2, 0.5)
     bad = tets.copy()

@@ -1275,11 +1275,17 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 if (ok) {
                     const unsigned long long loc =
                         (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+                    // Straight-line FP32 pass: no call and no branch per tet. A
+                    // near-degenerate element or a non-finite update anywhere in
+                    // the patch (rare) sends the lane through the careful pass
+                    // below, which starts again from the patch's state before
+                    // the task: the vertex records still hold it (nothing else
+                    // writes them before this task's stores) and so does lam.
+                    bool careful = false;
 #pragma unroll
                     for (int i = 0; i < kMaxPatchTets; i++) {
                         if (i >= ntets) break;
-                        const int slot = meta.x + i;
-                        const int r = slot - s0;
+                        const int r = meta.x + i - s0;
                         TetState<float> st;
                         unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
                         int l[4];
@@ -1292,13 +1298,54 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                             st.w[q] = fabsf(xp[q].w);
                         }
                         float2 lam = slam[r];
-                        float d[4][3];
-                        double rsq;
-                        if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
+                        float d[4][3], r0, r1, dl0, dl1, J;
+                        tet_project_combined_fast(st, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
+                        careful |= !(fabsf(J) >= kDegenerateJ && isfinite(dl0) && isfinite(dl1));
+                        lam.x += dl0;
+                        lam.y += dl1;
 #pragma unroll
-                            for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
-                        }
+                        for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
                         slam[r] = lam;
+                    }
+                    if (careful) {
+                        // the per-tet rule of every other sweep kernel (FP64 guard,
+                        // non-finite updates skipped), from the start of the task
+#pragma unroll
+                        for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+                            if (k2 < nverts) {
+                                unsigned long long a, b, c, d;
+                                ld_ver(xv + vid[k2], a, b, c, d);
+                                sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
+                            }
+                        }
+                        for (int i = 0; i < ntets; i++)
+                            slam[meta.x + i - s0] =
+                                (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
+#pragma unroll
+                        for (int i = 0; i < kMaxPatchTets; i++) {
+                            if (i >= ntets) break;
+                            const int slot = meta.x + i;
+                            const int r = slot - s0;
+                            TetState<float> st;
+                            unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
+                            int l[4];
+                            float4 xp[4];
+#pragma unroll
+                            for (int q = 0; q < 4; q++) {
+                                l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+                                xp[q] = sv[l[q]][tid];
+                                st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+                                st.w[q] = fabsf(xp[q].w);
+                            }
+                            float2 lam = slam[r];
+                            float d[4][3];
+                            double rsq;
+                            if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
+#pragma unroll
+                                for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
+                            }
+                            slam[r] = lam;
+                        }
                     }
                     // every vertex goes out one version later, moved or not
 #pragma unroll
