@@ -500,6 +500,24 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
     c->sphere_tab_h.assign(3 * (size_t)n_inst * c->S, make_float4(0.f, 0.f, 0.f, -1.f));
     c->sdf_pose_h.assign(10 * (size_t)n_inst * c->S, 0.0);
 
+    // Canonical corner order of the grid generator's five-tet hexes: in a
+    // patch of split B (layout kHexLocB) tet 0's corners (a,b,c,d) become
+    // (c,a,b,d) and tet 2's (a,b,c,d) become (a,c,b,d). Its layout is then
+    // kHexLocA, so every grid hex takes the sweep's register path. A tet's
+    // corner order changes neither its element (F = Ds Dm^-1 is the same) nor
+    // its constraints; the rest shapes below follow the new order.
+    if (p.solver_type == XPBD_SOLVER_GAUSS_SEIDEL) {
+        const int cap = p.gs_patch_tets ? p.gs_patch_tets : kMaxPatchTets;
+        for (const HostPatch& hp : build_patches(c->tets_h, T, cap)) {
+            if (hp.n != 5 || hp.nv != 8 || hp.loc != kHexLocB) continue;
+            int* a = &c->tets_h[4 * (size_t)hp.first];
+            const int t0[4] = {a[2], a[0], a[1], a[3]};
+            std::copy(t0, t0 + 4, a);
+            int* b = &c->tets_h[4 * ((size_t)hp.first + 2)];
+            std::swap(b[1], b[2]);
+        }
+    }
+
     // rest shape, compliance, lumped mass (ElementConstraint.hpp:23-51;
     // HydrostaticConstraint.cpp:15-16; DeviatoricConstraint.cpp:13;
     // ElasticMaterial.hpp:31-32; XPBDMeshObject.cpp:277-331)

@@ -886,6 +886,7 @@ __global__ void __launch_bounds__(kPatchBlock, MINB) k_sweep_dataflow(TetArrays 
 constexpr int kFlowWarps = kPatchBlock / 32;
 constexpr int kTaskSlots = kTaskPatches * kMaxPatchTets;
 static_assert(kTaskSlots % 32 == 0, "whole multiplier records per lane");
+constexpr int kLamPerLane = kTaskSlots / 32;  // a task's multipliers per lane
 
 template <bool FIRST_ZERO>
 __global__ void __launch_bounds__(kPatchBlock, 6) k_sweep_dataflow_staged(TetArrays t, PatchArrays pa, TaskArrays ta,
@@ -1069,6 +1070,163 @@ __global__ void k_versions_out(float4* __restrict__ x, const VerRec* __restrict_
     x[i] = make_float4(ver_val(r.x), ver_val(r.y), ver_val(r.z), x[i].w);
 }
 
+// One lane's patch task of k_sweep_versioned after its first polls went out:
+// wait for the vertices still short of their due versions, for the task's
+// bulk-copied records and staged multipliers, project the patch's tets in
+// order and write every vertex back one version later. HEX: the patch is a
+// grid hex in the canonical layout kHexLocA (five tets on eight vertices), so
+// the layout is known at compile time and the vertices stay in registers;
+// otherwise the layout comes from the record and the vertices sit in shared
+// memory (sv).
+// The tets go through one straight FP32 pass. A near-degenerate element or a
+// non-finite update anywhere in the patch (rare) sends the lane through the
+// careful pass, which starts again from the patch's state before the task --
+// the vertex records still hold it (nothing else writes them before this
+// task's stores) and so does lam in global memory -- with the per-tet rule of
+// every other sweep kernel (FP64 guard, non-finite updates skipped).
+template <bool FIRST_ZERO, bool CONTACT_DEG, bool HEX>
+__device__ __forceinline__ void versioned_patch(const TetArrays& t, const TaskArrays& ta, const FlowContacts& fc,
+                                                VerRec* __restrict__ xv, Flags* flags, const int4& meta,
+                                                const int (&vid)[kMaxPatchVerts], const int4& vr, int it, int s0,
+                                                int ns, bool copy, float4 (*sv)[kFlowBlock],
+                                                const float4 (*srec)[kTaskSlots], float2* slam,
+                                                const float2 (&lt)[kLamPerLane], unsigned long long* bar,
+                                                unsigned& phase, bool& ok,
+                                                const unsigned long long (&pw)[kMaxPatchVerts][4]) {
+    const int tid = threadIdx.x, lane = tid & 31;
+    const bool active = (meta.y >> 8) > 0;
+    const int ntets = HEX ? kMaxPatchTets : (meta.y & 0xff);
+    const int nverts = HEX ? kMaxPatchVerts : (meta.y >> 8);
+    float4 pv[kMaxPatchVerts] = {};  // HEX: the patch's vertices
+    auto vget = [&](int l) -> float4 { return HEX ? pv[l] : sv[l][tid]; };
+    auto vset = [&](int l, const float4& p) {
+        if (HEX) pv[l] = p;
+        else sv[l][tid] = p;
+    };
+    int due[kMaxPatchVerts];
+    if (active) {
+        const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
+        unsigned pending = 0;
+#pragma unroll
+        for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+            const int h = (vw[k2 >> 1] >> (16 * (k2 & 1))) & 0xffff;  // deg << 8 | pre
+            int deg = h >> 8;
+            if (CONTACT_DEG && k2 < nverts) deg += __ldg(fc.vdegc + vid[k2]);
+            due[k2] = it * deg + (h & 0xff);
+            if (k2 < nverts) {
+                vset(k2, make_float4(ver_val(pw[k2][0]), ver_val(pw[k2][1]), ver_val(pw[k2][2]), ver_val(pw[k2][3])));
+                if (ver_min(pw[k2][0], pw[k2][1], pw[k2][2]) < due[k2]) pending |= 1u << k2;
+            }
+        }
+        unsigned n = 0;
+        while (pending) {
+            if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
+                ok = false;
+                break;
+            }
+            __nanosleep(ta.poll_ns);  // polls cost L2 bandwidth the writers need
+#pragma unroll
+            for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+                if (pending & (1u << k2)) {
+                    unsigned long long a, b, c, d;
+                    ld_ver(xv + vid[k2], a, b, c, d);
+                    if (ver_min(a, b, c) >= due[k2]) {
+                        vset(k2, make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d)));
+                        pending &= ~(1u << k2);
+                    }
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int u = 0; u < kLamPerLane; u++)
+        if (lane + 32 * u < ns) slam[lane + 32 * u] = lt[u];
+    __syncwarp();  // slam filled
+    if (copy) {
+        // the copies land (or not) whatever happened above
+        const bool staged = __all_sync(0xffffffffu, mbar_wait_bounded(bar, phase, kWaitLimit)) != 0;
+        phase ^= 1u;
+        if (!staged) {
+            ok = false;
+            if (lane == 0) mbar_wait_bounded(bar, phase ^ 1u, kWaitLimit);
+        }
+    }
+    if (!(active && ok)) return;
+    const unsigned long long loc =
+        HEX ? kHexLocA : ((unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32));
+    bool careful = false;
+#pragma unroll
+    for (int i = 0; i < kMaxPatchTets; i++) {
+        if (!HEX && i >= ntets) break;
+        const int r = meta.x + i - s0;
+        TetState<float> st;
+        unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
+        int l[4];
+        float4 xp[4];
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+            xp[q] = vget(l[q]);
+            st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+            st.w[q] = fabsf(xp[q].w);
+        }
+        float2 lam = slam[r];
+        float d[4][3], r0, r1, dl0, dl1, J;
+        tet_project_combined_fast(st, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
+        careful |= !(fabsf(J) >= kDegenerateJ && isfinite(dl0) && isfinite(dl1));
+        lam.x += dl0;
+        lam.y += dl1;
+#pragma unroll
+        for (int q = 0; q < 4; q++) vset(l[q], moved(xp[q], d[q]));
+        slam[r] = lam;
+    }
+    if (careful) {
+#pragma unroll
+        for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+            if (k2 < nverts) {
+                unsigned long long a, b, c, d;
+                ld_ver(xv + vid[k2], a, b, c, d);
+                vset(k2, make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d)));
+            }
+        }
+        for (int i = 0; i < ntets; i++)
+            slam[meta.x + i - s0] = (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
+#pragma unroll
+        for (int i = 0; i < kMaxPatchTets; i++) {
+            if (!HEX && i >= ntets) break;
+            const int slot = meta.x + i;
+            const int r = slot - s0;
+            TetState<float> st;
+            unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
+            int l[4];
+            float4 xp[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
+                xp[q] = vget(l[q]);
+                st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
+                st.w[q] = fabsf(xp[q].w);
+            }
+            float2 lam = slam[r];
+            float d[4][3];
+            double rsq;
+            if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) vset(l[q], moved(xp[q], d[q]));
+            }
+            slam[r] = lam;
+        }
+    }
+    // every vertex goes out one version later, moved or not
+#pragma unroll
+    for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
+        if (k2 < nverts) {
+            const float4 sp = vget(k2);
+            st_ver(xv + vid[k2], sp.x, sp.y, sp.z, sp.w, (unsigned)(due[k2] + 1));
+        }
+    }
+}
+
 // Warp w runs the w-th task of every colour (the task layout of
 // k_sweep_dataflow). A lane's patch reads its vertices when their versions
 // are due and writes them back one version later. The smallest unfinished
@@ -1213,7 +1371,6 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             // The task's multipliers, read and (after the task) written back by
             // coalesced accesses; only this warp touches them meanwhile. The
             // loads are in flight during the polls and land in slam after them.
-            constexpr int kLamPerLane = kTaskSlots / 32;
             const int ns = copy ? s1 - s0 : 0;
             float2 lt[kLamPerLane];
 #pragma unroll
@@ -1222,141 +1379,21 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 lt[u] = make_float2(0.f, 0.f);
                 if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = t.lam[s0 + r];
             }
-            int due[kMaxPatchVerts];
-            if (nverts > 0) {
-                const int vw[4] = {vr.x, vr.y, vr.z, vr.w};
-                unsigned pending = 0;
-#pragma unroll
-                for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
-                    const int h = (vw[k2 >> 1] >> (16 * (k2 & 1))) & 0xffff;  // deg << 8 | pre
-                    int deg = h >> 8;
-                    if (CONTACTS && !RESIDENT && k2 < nverts) deg += __ldg(fc.vdegc + vid[k2]);
-                    due[k2] = it * deg + (h & 0xff);
-                    if (k2 < nverts) {
-                        sv[k2][tid] =
-                            make_float4(ver_val(pw[k2][0]), ver_val(pw[k2][1]), ver_val(pw[k2][2]), ver_val(pw[k2][3]));
-                        if (ver_min(pw[k2][0], pw[k2][1], pw[k2][2]) < due[k2]) pending |= 1u << k2;
-                    }
-                }
-                unsigned n = 0;
-                while (pending) {
-                    if (++n > ta.poll_limit || ((n & 63) == 0 && *(volatile unsigned*)ta.abort_flag)) {
-                        ok = false;
-                        break;
-                    }
-                    __nanosleep(ta.poll_ns);  // polls cost L2 bandwidth the writers need
-#pragma unroll
-                    for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
-                        if (pending & (1u << k2)) {
-                            unsigned long long a, b, c, d;
-                            ld_ver(xv + vid[k2], a, b, c, d);
-                            if (ver_min(a, b, c) >= due[k2]) {
-                                sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
-                                pending &= ~(1u << k2);
-                            }
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kLamPerLane; u++)
-                if (lane + 32 * u < ns) slam[lane + 32 * u] = lt[u];
-            __syncwarp();  // slam filled
-            if (copy) {
-                // the copies land (or not) whatever happened above
-                const bool staged = __all_sync(0xffffffffu, mbar_wait_bounded(&bar, phase, kWaitLimit)) != 0;
-                phase ^= 1u;
-                if (!staged) {
-                    ok = false;
-                    if (lane == 0) mbar_wait_bounded(&bar, phase ^ 1u, kWaitLimit);
-                }
-            }
-            if (nverts > 0) {
-                if (ok) {
-                    const unsigned long long loc =
-                        (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
-                    // Straight-line FP32 pass: no call and no branch per tet. A
-                    // near-degenerate element or a non-finite update anywhere in
-                    // the patch (rare) sends the lane through the careful pass
-                    // below, which starts again from the patch's state before
-                    // the task: the vertex records still hold it (nothing else
-                    // writes them before this task's stores) and so does lam.
-                    bool careful = false;
-#pragma unroll
-                    for (int i = 0; i < kMaxPatchTets; i++) {
-                        if (i >= ntets) break;
-                        const int r = meta.x + i - s0;
-                        TetState<float> st;
-                        unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
-                        int l[4];
-                        float4 xp[4];
-#pragma unroll
-                        for (int q = 0; q < 4; q++) {
-                            l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
-                            xp[q] = sv[l[q]][tid];
-                            st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
-                            st.w[q] = fabsf(xp[q].w);
-                        }
-                        float2 lam = slam[r];
-                        float d[4][3], r0, r1, dl0, dl1, J;
-                        tet_project_combined_fast(st, lam.x, lam.y, r0, r1, dl0, dl1, d, J);
-                        careful |= !(fabsf(J) >= kDegenerateJ && isfinite(dl0) && isfinite(dl1));
-                        lam.x += dl0;
-                        lam.y += dl1;
-#pragma unroll
-                        for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
-                        slam[r] = lam;
-                    }
-                    if (careful) {
-                        // the per-tet rule of every other sweep kernel (FP64 guard,
-                        // non-finite updates skipped), from the start of the task
-#pragma unroll
-                        for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
-                            if (k2 < nverts) {
-                                unsigned long long a, b, c, d;
-                                ld_ver(xv + vid[k2], a, b, c, d);
-                                sv[k2][tid] = make_float4(ver_val(a), ver_val(b), ver_val(c), ver_val(d));
-                            }
-                        }
-                        for (int i = 0; i < ntets; i++)
-                            slam[meta.x + i - s0] =
-                                (FIRST_ZERO && it == 0) ? make_float2(0.f, 0.f) : t.lam[meta.x + i];
-#pragma unroll
-                        for (int i = 0; i < kMaxPatchTets; i++) {
-                            if (i >= ntets) break;
-                            const int slot = meta.x + i;
-                            const int r = slot - s0;
-                            TetState<float> st;
-                            unpack_static(srec[0][r], srec[1][r], srec[2][r], st);
-                            int l[4];
-                            float4 xp[4];
-#pragma unroll
-                            for (int q = 0; q < 4; q++) {
-                                l[q] = (int)((loc >> (12 * i + 3 * q)) & 7ull);
-                                xp[q] = sv[l[q]][tid];
-                                st.p[q][0] = xp[q].x; st.p[q][1] = xp[q].y; st.p[q][2] = xp[q].z;
-                                st.w[q] = fabsf(xp[q].w);
-                            }
-                            float2 lam = slam[r];
-                            float d[4][3];
-                            double rsq;
-                            if (project_one<false>(st, t, slot, xp, lam, d, rsq, flags)) {
-#pragma unroll
-                                for (int q = 0; q < 4; q++) sv[l[q]][tid] = moved(xp[q], d[q]);
-                            }
-                            slam[r] = lam;
-                        }
-                    }
-                    // every vertex goes out one version later, moved or not
-#pragma unroll
-                    for (int k2 = 0; k2 < kMaxPatchVerts; k2++) {
-                        if (k2 < nverts) {
-                            const float4 sp = sv[k2][tid];
-                            st_ver(xv + vid[k2], sp.x, sp.y, sp.z, sp.w, (unsigned)(due[k2] + 1));
-                        }
-                    }
-                }
-            }
+            // Grid hexes (after the build's canonical corner order every one has
+            // the layout kHexLocA) keep the patch's vertices in registers. Not
+            // with the topology pipelined in registers (!RESIDENT): the two
+            // together spill.
+            const unsigned long long loc =
+                (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
+            if (RESIDENT &&
+                __all_sync(0xffffffffu, nverts == 0 || (ntets == 5 && nverts == 8 && loc == kHexLocA)))
+                versioned_patch<FIRST_ZERO, CONTACTS && !RESIDENT, true>(t, ta, fc, xv, flags, meta, vid, vr, it, s0,
+                                                                          ns, copy, sv, srec, slam, lt, &bar, phase,
+                                                                          ok, pw);
+            else
+                versioned_patch<FIRST_ZERO, CONTACTS && !RESIDENT, false>(t, ta, fc, xv, flags, meta, vid, vr, it, s0,
+                                                                           ns, copy, sv, srec, slam, lt, &bar, phase,
+                                                                           ok, pw);
             __syncwarp();  // every lane's multipliers are in slam
 #pragma unroll
             for (int u = 0; u < kLamPerLane; u++)

@@ -67,6 +67,14 @@ struct ContactArrays {
 // kMaxPatchVerts vertices, one thread each.
 constexpr int kMaxPatchTets = 5;
 constexpr int kMaxPatchVerts = 8;
+// The local layout (the 60-bit word of a patch record, 3 bits per tet corner)
+// of a grid hex of five tets under the patch builder's first-appearance
+// numbering: tets (0,1,2,3), (0,2,4,5), (0,3,6,5), (2,3,7,5), (0,2,3,5). The
+// grid generator's split A gives it directly; split B gives kHexLocB until
+// the build reorders two of its tets' corners (tet 0: (a,b,c,d) -> (c,a,b,d),
+// tet 2: (a,b,c,d) -> (a,c,b,d)), which leaves every tet's geometry as it is.
+constexpr unsigned long long kHexLocA = 0xad0bdab98b10688ull;
+constexpr unsigned long long kHexLocB = 0xacabd9af2b0a688ull;
 constexpr int kPatchBlock = 64;
 // Gauss-Seidel sweep kernels: 0 one lane per patch, static tet records
 // prefetched into registers; 1 one lane per patch, records staged in shared
