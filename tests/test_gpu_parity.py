@@ -371,6 +371,27 @@ def test_health_counts_degenerate_elements(lib):
     s.close()
 
 
+def test_residual_reductions_are_fp64(lib):
+    """Per-tet E over six decades spreads the squared residual terms over
+    many orders of magnitude. The last history entry reduces the FP64 terms
+    of the state after the last sweep; the per-constraint vector read back
+    holds the same terms rounded to FP32, so its FP64 norm differs from the
+    entry by at most that rounding, 2^-24 relative. A reduction with FP32
+    partial sums would miss the bound by about an order of magnitude."""
+    X, tets, faces, x0 = _noisy_cube(6, seed=5, noise=5e-3)
+    E = np.exp(np.random.default_rng(9).uniform(np.log(1e2), np.log(1e8), len(tets)))
+    s = G.XPBDSolver(X, tets, None, E, 0.45, 1000.0, num_iters=4, residual_policy=G.RESIDUAL_EVERY_ITERATION)
+    s.fix_vertices(X[:, 2] == 0)
+    s.set_positions(x0)
+    s.step(2)
+    r = s.constraint_residual()
+    ref = float(np.sqrt(np.sum(r.astype(np.float64) ** 2)))
+    hs = s.residual_history()
+    assert ref > 0 and np.abs(r).max() / np.abs(r[r != 0]).min() > 1e4
+    assert abs(hs[-1] - ref) <= 2.0 ** -24 * ref, (hs[-1], ref)
+    s.close()
+
+
 def test_versioned_sweep_careful_pass_equals_colour_launches(lib):
     """The versioned sweep projects a patch in one straight FP32 pass and
     redoes it from the task's start with the per-tet FP64 guard when any of

@@ -522,7 +522,9 @@ void launch_mlp_pack(cudaStream_t s, const float* params, const MlpNet& net) {
 void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16* X, int n, const MlpNet& net, float* out,
                         const MlpCache* cache, unsigned long long* err) {
     if (n <= 0) return;
-    // persistent: at most 4 CTAs per SM (smem allows 5), weights staged once each
+    // persistent: 5 CTAs per SM (shared memory's limit; 64 tensor-memory columns each),
+    // weights staged once each; co-resident CTAs overlap one another's MMA waits with
+    // their epilogues (0.104 ms with 4 per SM, 0.099 with 5, 1.31M rows)
     static int sms = 0;
     if (!sms) {
         int dev = 0;
@@ -530,7 +532,7 @@ void launch_mlp_forward(cudaStream_t s, const __nv_bfloat16* X, int n, const Mlp
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 148;
     }
-    const int grid = std::min(nb(n, kRows), 4 * sms);
+    const int grid = std::min(nb(n, kRows), 5 * sms);
     if (cache)
         k_mlp_forward<true><<<grid, kFwdThreads, kFwdSmem, s>>>(X, n, net, out, *cache, err);
     else
