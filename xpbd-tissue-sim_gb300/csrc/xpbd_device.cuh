@@ -71,6 +71,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 
 constexpr unsigned kWaitLimit = 1u << 20;
 
+// 16-byte asynchronous copy global -> shared (cp.async, cache-global); with
+// src_bytes = 0 nothing is read and the 16 bytes are zero-filled. Completion
+// (cp_async_wait_all) makes the data visible to the issuing thread.
+__device__ __forceinline__ void cp_async16(void* dst, const void* src, unsigned src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // FP64 butterfly over the warp (each step is two 32-bit shuffles).
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll

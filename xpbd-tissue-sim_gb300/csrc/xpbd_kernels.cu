@@ -1254,6 +1254,8 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     __shared__ __align__(128) float4 srec[3][kTaskSlots];  // the task's m0, m1, m2 records
     __shared__ float2 slam[kTaskSlots];                   // and its multipliers
     __shared__ __align__(8) unsigned long long bar;
+    // !RESIDENT: the next patch task's records (meta, verts a, verts b, versions) per lane
+    __shared__ __align__(16) int4 ring[RESIDENT ? 1 : 2][4][kFlowBlock];
     const int tid = threadIdx.x, lane = tid & 31;
     const int gw = (blockIdx.x * blockDim.x + tid) >> 5;
     const int nw = (gridDim.x * blockDim.x) >> 5;
@@ -1298,29 +1300,31 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     }
     const int ntot = ta.ntasks + (CONTACTS ? *fc.ntasks : 0);
     // !RESIDENT: software pipeline over this warp's patch tasks. While a task
-    // runs, the next one's patch records are in flight and the descriptor of
-    // the one after that, so a task starts polling without a dependent load.
-    // (Each warp cycles through the same tasks every iteration: after its
-    // last patch task of an iteration comes its first one, gw.)
+    // runs, the next one's patch records are on their way into shared memory
+    // (cp.async, one ring slot per task, lanes without a patch zero-filled)
+    // and the descriptor of the one after that into a register, so a task
+    // starts polling without a dependent load. (Each warp cycles through the
+    // same tasks every iteration: after its last patch task of an iteration
+    // comes its first one, gw.)
     auto next_patch_task = [&](int j) { return j + nw < ta.ntasks ? j + nw : gw; };
     int2 tk_next = make_int2(0, 0);  // descriptor (first patch, patches) of the task after the next
-    int4 nmeta = make_int4(0, 0, 0, 0), nva = nmeta, nvb = nmeta, nvr = nmeta;
-    auto load_records = [&](int2 tk, int4& m, int4& a, int4& b, int4& r) {
-        m = a = b = r = make_int4(0, 0, 0, 0);
-        if (lane < tk.y) {
-            const int p = tk.x + lane;
-            m = __ldg(pa.meta + p);
-            a = __ldg(pa.verts + 2 * (size_t)p);
-            b = __ldg(pa.verts + 2 * (size_t)p + 1);
-            r = __ldg(pver + p);
-        }
+    int rs = 0;                      // ring slot of the next task's records
+    auto stage_records = [&](int2 tk, int slot) {
+        const bool on = lane < tk.y;
+        const size_t p = on ? (size_t)(tk.x + lane) : 0;
+        const unsigned nb = on ? 16u : 0u;
+        cp_async16(&ring[slot][0][lane], pa.meta + p, nb);
+        cp_async16(&ring[slot][1][lane], pa.verts + 2 * p, nb);
+        cp_async16(&ring[slot][2][lane], pa.verts + 2 * p + 1, nb);
+        cp_async16(&ring[slot][3][lane], pver + p, nb);
+        cp_async_commit();
     };
     auto load_desc = [&](int j) {
         const int4 d = __ldg(ta.task + j);
         return make_int2(d.x, d.y);
     };
     if (!RESIDENT && gw < ta.ntasks) {
-        load_records(load_desc(gw), nmeta, nva, nvb, nvr);
+        stage_records(load_desc(gw), 0);
         tk_next = load_desc(next_patch_task(gw));
     }
     for (int it = 0; it < iters; it++) {
@@ -1335,10 +1339,16 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 vb = topo[(4 * k + 2) * 32 + lane];
                 vr = topo[(4 * k + 3) * 32 + lane];
             } else {
-                meta = nmeta; va = nva; vb = nvb; vr = nvr;
+                cp_async_wait_all();  // this task's records (staged one task earlier)
+                const int s = RESIDENT ? 0 : rs;
+                meta = ring[s][0][lane];
+                va = ring[s][1][lane];
+                vb = ring[s][2][lane];
+                vr = ring[s][3][lane];
                 const int jn = next_patch_task(j);
-                load_records(tk_next, nmeta, nva, nvb, nvr);
+                stage_records(tk_next, s ^ 1);
                 tk_next = load_desc(next_patch_task(jn));
+                rs ^= 1;
             }
             k++;
             const int ntets = meta.y & 0xff, nverts = meta.y >> 8;
@@ -1380,13 +1390,10 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = t.lam[s0 + r];
             }
             // Grid hexes (after the build's canonical corner order every one has
-            // the layout kHexLocA) keep the patch's vertices in registers. Not
-            // with the topology pipelined in registers (!RESIDENT): the two
-            // together spill.
+            // the layout kHexLocA) keep the patch's vertices in registers.
             const unsigned long long loc =
                 (unsigned long long)(unsigned)meta.z | ((unsigned long long)(unsigned)meta.w << 32);
-            if (RESIDENT &&
-                __all_sync(0xffffffffu, nverts == 0 || (ntets == 5 && nverts == 8 && loc == kHexLocA)))
+            if (__all_sync(0xffffffffu, nverts == 0 || (ntets == 5 && nverts == 8 && loc == kHexLocA)))
                 versioned_patch<FIRST_ZERO, CONTACTS && !RESIDENT, true>(t, ta, fc, xv, flags, meta, vid, vr, it, s0,
                                                                           ns, copy, sv, srec, slam, lt, &bar, phase,
                                                                           ok, pw);
