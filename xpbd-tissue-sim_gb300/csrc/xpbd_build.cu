@@ -654,7 +654,8 @@ int build(xpbd_ctx* c, const xpbd_mesh_desc* ms, int n_inst) {
                               q[6] * (q[1] * q[5] - q[4] * q[2]);
             hm0[sidx] = make_float4((float)M[0][0], (float)M[1][1], (float)M[2][2], (float)M[0][1]);
             hm1[sidx] = make_float4((float)M[0][2], (float)M[1][2], (float)dq, atd);
-            hm2[sidx] = make_float4(ath, (float)gm[t], 0.f, 0.f);
+            const double msum = M[0][0] + M[1][1] + M[2][2] + 2.0 * (M[0][1] + M[0][2] + M[1][2]);  // |q_3|^2
+            hm2[sidx] = make_float4(ath, (float)gm[t], (float)msum, 0.f);
         }
         c->alpha_t_d[sidx] = atd;
         c->alpha_t_h[sidx] = ath;

@@ -138,6 +138,7 @@ struct TetState {
     R m[6];  // M00 M11 M22 M01 M02 M12
     R dq;    // det Q
     R atd, ath, gam;
+    R msum;  // |q_3|^2 = sum of all entries of M (q_3 = -q_0 - q_1 - q_2)
 };
 
 template <typename R>
@@ -304,8 +305,7 @@ __device__ __forceinline__ void tet_project_combined_fast(const TetState<float>&
     const float2 s01 = __ffma2_rn(splat2(s.w[0]), sq[0], __fmul2_rn(splat2(s.w[1]), sq[1]));
     const float2 s23 = __ffma2_rn(splat2(s.w[2]), sq[2], __fmul2_rn(splat2(s.w[3]), sq[3]));
     const float2 sgn = __fadd2_rn(s01, s23);  // (sum w |G|^2, sum w |N|^2)
-    const float msum = (s.m[0] + s.m[1]) + (s.m[2] + 2.f * ((s.m[3] + s.m[4]) + s.m[5]));  // |q_3|^2
-    const float sw = fmaf(s.w[0], s.m[0], s.w[1] * s.m[1]) + fmaf(s.w[2], s.m[2], s.w[3] * msum);
+    const float sw = fmaf(s.w[0], s.m[0], s.w[1] * s.m[1]) + fmaf(s.w[2], s.m[2], s.w[3] * s.msum);
     const float L00 = fmaf(invC * invC, sgn.x, s.atd);
     const float L01 = (invC * fac) * (J * sw);
     const float L11 = fmaf(fh * fh, sgn.y, s.ath);
@@ -396,7 +396,7 @@ template <typename R>
 __device__ __forceinline__ void unpack_static(const float4& a, const float4& b, const float4& c, TetState<R>& s) {
     s.m[0] = a.x; s.m[1] = a.y; s.m[2] = a.z; s.m[3] = a.w;
     s.m[4] = b.x; s.m[5] = b.y; s.dq = b.z; s.atd = b.w;
-    s.ath = c.x; s.gam = c.y;
+    s.ath = c.x; s.gam = c.y; s.msum = c.z;
 }
 
 // Static per-tet data (indices, M and det Q, compliances): never written

@@ -8,7 +8,7 @@
 //   tet_idx int4[T]   vertex indices, in solver slot order
 //   tet_m0  float4[T] M00 M11 M22 M01                  (M = Q Q^T, Q = Dm^-1)
 //   tet_m1  float4[T] M02 M12 det(Q) alpha_tilde_dev
-//   tet_m2  float4[T] alpha_tilde_hyd gamma 0 0
+//   tet_m2  float4[T] alpha_tilde_hyd gamma |q_3|^2 0   (q_3 = -q_0 - q_1 - q_2)
 //   lam     float2[T] (lambda_dev, lambda_hyd)
 //   tet_q0  float4[T] Q(0,0) Q(1,0) Q(2,0) Q(0,1)      (Q column-major; read only
 //   tet_q1  float4[T] Q(1,1) Q(2,1) Q(0,2) Q(1,2)       for the warm-start network's
