@@ -123,7 +123,7 @@ void release(xpbd_ctx* c) {
     c->local_slots.release(); c->vmask.release(); c->tmask.release(); c->gdz.release();
     c->d_att_v.release(); c->d_att_order.release(); c->d_att_target.release(); c->d_att_lam.release();
     c->flow_tasks.release(); c->flow_dep_off.release(); c->flow_dep.release(); c->flow_epoch.release();
-    c->patch_ver.release(); c->xv.release();
+    c->patch_ver.release(); c->xv.release(); c->vperm.release(); c->pverts_v.release(); c->faces_v.release();
     c->vdeg_p.release(); c->vdeg_c.release(); c->factive.release(); c->vface_off.release(); c->vface.release();
     c->fcol_d.release(); c->cm_off.release(); c->n_ctasks.release(); c->ctask.release(); c->cface.release();
     c->res_partial.release(); c->res_rows.release(); c->energy_partial.release(); c->rvec.release();
@@ -299,10 +299,41 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
             }
             ver[q] = make_int4(w[0], w[1], w[2], w[3]);
         }
+        // The sweep's own vertex numbering: records in the order in which the
+        // tasks' lanes first touch the vertices (task by task, corner by
+        // corner, lane by lane), so the 32 lanes of one poll or store mostly
+        // hit consecutive 32-byte records -- eight 128-byte lines instead of
+        // up to 32 -- on the L1 data path that bounds the phase.
+        std::vector<int> vperm(V, -1);
+        int next_rec = 0;
+        for (int j = 0; j < NTP; j++) {
+            const int4 tk = tasks[j];
+            for (int k = 0; k < kMaxPatchVerts; k++)
+                for (int L = 0; L < tk.y; L++) {
+                    const int q = tk.x + L;
+                    if (k >= (pmeta[q].y >> 8)) continue;
+                    const int v = pv(q, k);
+                    if (vperm[v] < 0) vperm[v] = next_rec++;
+                }
+        }
+        for (int v = 0; v < V; v++)
+            if (vperm[v] < 0) vperm[v] = next_rec++;
+        std::vector<int4> pvv(pverts.size());
+        for (int q = 0; q < P; q++) {
+            int r[kMaxPatchVerts];
+            for (int k = 0; k < kMaxPatchVerts; k++) r[k] = k < (pmeta[q].y >> 8) ? vperm[pv(q, k)] : -1;
+            pvv[2 * (size_t)q] = make_int4(r[0], r[1], r[2], r[3]);
+            pvv[2 * (size_t)q + 1] = make_int4(r[4], r[5], r[6], r[7]);
+        }
         c->flow_versioned = true;
         c->patch_ver_h = ver;
+        c->vperm_h = vperm;
         XPBD_CU(c, c->patch_ver.alloc(P));
         XPBD_CU(c, c->xv.alloc(V));
+        XPBD_CU(c, c->vperm.alloc(V));
+        XPBD_CU(c, c->pverts_v.alloc(pvv.size()));
+        XPBD_CU(c, cudaMemcpy(c->vperm.p, vperm.data(), sizeof(int) * V, cudaMemcpyHostToDevice));
+        XPBD_CU(c, cudaMemcpy(c->pverts_v.p, pvv.data(), sizeof(int4) * pvv.size(), cudaMemcpyHostToDevice));
         c->npatches = P;
         // the task topology stays in shared memory when every warp owns few
         // enough tasks and the grid stays co-resident with that memory
@@ -359,6 +390,14 @@ int build_flow_contacts(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::
     XPBD_CU(c, c->n_ctasks.alloc(1));
     XPBD_CU(c, c->ctask.alloc((size_t)F / 32 + c->n_face_colours + 1));
     XPBD_CU(c, c->cface.alloc(F));
+    {
+        std::vector<int4> fv(F);
+        for (int f = 0; f < F; f++)
+            fv[f] = make_int4(c->vperm_h[c->faces_h[3 * f]], c->vperm_h[c->faces_h[3 * f + 1]],
+                              c->vperm_h[c->faces_h[3 * f + 2]], 0);
+        XPBD_CU(c, c->faces_v.alloc(F));
+        XPBD_CU(c, cudaMemcpy(c->faces_v.p, fv.data(), sizeof(int4) * F, cudaMemcpyHostToDevice));
+    }
     XPBD_CU(c, cudaMemcpy(c->vdeg_p.p, dp.data(), V, cudaMemcpyHostToDevice));
     XPBD_CU(c, cudaMemset(c->vdeg_c.p, 0, V));
     XPBD_CU(c, cudaMemset(c->n_ctasks.p, 0, sizeof(int)));

@@ -315,10 +315,11 @@ int enqueue_update(xpbd_ctx* c, bool write_vel, bool solve_only) {
         }
         Scope sc(c, K_PROJECT_GS);
         if (versioned) {
-            const xg::FlowContacts fc = have_faces ? c->flowc() : xg::FlowContacts{nullptr, nullptr, nullptr, nullptr};
-            launch_sweep_versioned(c->L(), c->tets(), c->patches(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
-                                   c->xv.p, c->V, c->flags.p, c->flow_grid, p.gs_min_blocks, c->flow_resident, ca,
-                                   fc);
+            const xg::FlowContacts fc =
+                have_faces ? c->flowc() : xg::FlowContacts{nullptr, nullptr, nullptr, nullptr, nullptr};
+            launch_sweep_versioned(c->L(), c->tets(), c->patches_v(), c->patch_ver.p, c->tasks(), iters, !warm, c->x.p,
+                                   c->xv.p, c->V, c->vperm.p, c->flags.p, c->flow_grid, p.gs_min_blocks,
+                                   c->flow_resident, ca, fc);
             c->launches += 2;  // the copies into and out of the versioned positions
         } else
             launch_sweep_dataflow(c->L(), c->tets(), c->patches(), c->tasks(), iters, !warm, c->x.p, c->flags.p,
@@ -460,7 +461,7 @@ int prepare_update(xpbd_ctx* c) {
             launch_flow_contact_tables(c->L(), c->contacts(), c->act_faces.p, c->act_off.p, c->n_face_colours,
                                        c->n_inst, c->vface_off.p, c->vface.p, c->fcol_d.p, c->vdeg_p.p,
                                        c->factive.p, c->cm_off.p, c->ctask.p, c->n_ctasks.p, c->cface.p,
-                                       c->vdeg_c.p, c->V);
+                                       c->vdeg_c.p, c->vperm.p, c->V);
         c->contact_lists_dirty = false;
     }
     if (tracking(c) || c->warm_mode != XPBD_WARM_NONE) {

@@ -100,7 +100,10 @@ struct xpbd_ctx {
     DevBuf<int> flow_dep_off, flow_dep;
     DevBuf<unsigned> flow_epoch;  // ntasks epochs + the abort flag
     DevBuf<int4> patch_ver;       // variant 4: per patch, 8 x 16-bit deg << 8 | pre
-    DevBuf<xg::VerRec> xv;        // variant 4: version-stamped vertex records
+    DevBuf<xg::VerRec> xv;        // variant 4: version-stamped vertex records, in the sweep's numbering:
+    DevBuf<int> vperm;            //   vertex -> record (a task's lanes touch neighbouring records)
+    DevBuf<int4> pverts_v;        //   patch vertices and
+    DevBuf<int4> faces_v;         //   surface faces in that numbering
     bool flow_resident = false;   // variant 4: task topology kept in shared memory
     // variant 4 with static contacts inside the sweep (FlowContacts)
     bool flow_contacts = false;
@@ -118,6 +121,7 @@ struct xpbd_ctx {
     DevBuf<unsigned long long> lat;
     bool lat_on = false, lat_have = false;
     std::vector<int2> task_inst_h;  // patch task -> first and last instance it touches
+    std::vector<int> vperm_h;       // the versioned sweep's vertex numbering (vertex -> record)
     DevBuf<float4> c_bary, c_p, c_n;
     DevBuf<float> c_lam;
     int S = 4;
@@ -213,7 +217,7 @@ struct xpbd_ctx {
                               lat_on ? lat.p : nullptr};
     }
     xg::FlowContacts flowc() {
-        return xg::FlowContacts{ctask.p, cface.p, n_ctasks.p, vdeg_c.p};
+        return xg::FlowContacts{ctask.p, cface.p, n_ctasks.p, vdeg_c.p, faces_v.p};
     }
     xg::SelfArrays selfs() {
         return xg::SelfArrays{s_tets.p,        s_Q.p,          s_X0.p,         s_X0f.p,      s_surf.p,
@@ -227,6 +231,7 @@ struct xpbd_ctx {
     }
     Launch L() const { return Launch{stream, prm.use_pdl != 0}; }
     PatchArrays patches() const { return PatchArrays{patch_meta.p, patch_verts.p}; }
+    PatchArrays patches_v() const { return PatchArrays{patch_meta.p, pverts_v.p}; }  // the versioned sweep's
     ContactArrays contacts() {
         return ContactArrays{c_bary.p, c_p.p, c_n.p, c_lam.p, faces.p, F, S};
     }

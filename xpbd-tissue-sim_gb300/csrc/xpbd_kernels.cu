@@ -1053,20 +1053,23 @@ __global__ void k_stamp(unsigned long long* p) {
     *p = clock_ns();
 }
 
-// Positions at version 0, the inverse mass in the fourth word.
-__global__ void k_versions_in(VerRec* __restrict__ xv, const float4* __restrict__ x, int V) {
+// Positions at version 0, the inverse mass in the fourth word; record vperm[i]
+// holds vertex i (the sweep's numbering).
+__global__ void k_versions_in(VerRec* __restrict__ xv, const float4* __restrict__ x, const int* __restrict__ vperm,
+                              int V) {
     pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     const float4 p = x[i];
-    xv[i] = VerRec{__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z), __float_as_uint(p.w)};
+    xv[vperm[i]] = VerRec{__float_as_uint(p.x), __float_as_uint(p.y), __float_as_uint(p.z), __float_as_uint(p.w)};
 }
 
-__global__ void k_versions_out(float4* __restrict__ x, const VerRec* __restrict__ xv, int V) {
+__global__ void k_versions_out(float4* __restrict__ x, const VerRec* __restrict__ xv, const int* __restrict__ vperm,
+                               int V) {
     pdl_wait_then_release();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
-    const VerRec r = xv[i];
+    const VerRec r = xv[vperm[i]];
     x[i] = make_float4(ver_val(r.x), ver_val(r.y), ver_val(r.z), x[i].w);
 }
 
@@ -1412,7 +1415,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             const int2 ct = fc.task[j - ta.ntasks];
             if (lane < ct.y) {
                 const int4 e = fc.face[ct.x + lane];
-                const int4 fv = __ldg(ca.faces + e.x);
+                const int4 fv = __ldg(fc.vfaces + e.x);  // the sweep's vertex numbering
                 const int vid3[3] = {fv.x, fv.y, fv.z};
                 const int dw[3] = {e.y & 0xffff, (e.y >> 16) & 0xffff, e.z & 0xffff};
                 int due3[3];
@@ -1975,10 +1978,10 @@ int sweep_versioned_blocks_per_sm(int min_blocks, int tasks_per_warp, bool conta
 
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
                                    const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
-                                   Flags* flags, int grid, int min_blocks, bool resident, const ContactArrays& ca,
-                                   const FlowContacts& fc) {
+                                   const int* vperm, Flags* flags, int grid, int min_blocks, bool resident,
+                                   const ContactArrays& ca, const FlowContacts& fc) {
     if (iters <= 0 || ta.ntasks <= 0) return cudaSuccess;
-    go(k_versions_in, nblk(V, 256), 256, s, xv, (const float4*)x, V);
+    go(k_versions_in, nblk(V, 256), 256, s, xv, (const float4*)x, vperm, V);
     const int warps = grid * (kFlowBlock / 32);
     const int per_warp = (ta.ntasks + warps - 1) / warps;
     const bool contacts = fc.task != nullptr;
@@ -2010,7 +2013,7 @@ cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const Pa
 #undef XG_VER_M
 #undef XG_VER
     if (e != cudaSuccess) return e;
-    go(k_versions_out, nblk(V, 256), 256, s, x, (const VerRec*)xv, V);
+    go(k_versions_out, nblk(V, 256), 256, s, x, (const VerRec*)xv, vperm, V);
     return cudaSuccess;
 }
 
@@ -2028,13 +2031,13 @@ __global__ void k_face_active(ContactArrays c, unsigned char* __restrict__ facti
 // active faces containing each vertex
 __global__ void k_vertex_contact_degree(const int* __restrict__ vface_off, const int* __restrict__ vface,
                                         const unsigned char* __restrict__ factive, unsigned char* __restrict__ vdegc,
-                                        int V) {
+                                        const int* __restrict__ vperm, int V) {
     pdl_wait_then_release();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     int n = 0;
     for (int e = vface_off[v]; e < vface_off[v + 1]; e++) n += factive[vface[e]];
-    vdegc[v] = (unsigned char)n;
+    vdegc[vperm[v]] = (unsigned char)n;  // in the sweep's vertex numbering
 }
 
 constexpr int kScanThreads = 1024;
@@ -2137,9 +2140,10 @@ void launch_stamp(const Launch& s, unsigned long long* p) { go(k_stamp, 1, 1, s,
 void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
                                 int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,
                                 const unsigned char* vdegp, unsigned char* factive, int* cm_off, int2* ctask,
-                                int* n_ctasks, int4* cface, unsigned char* vdegc, int V) {
+                                int* n_ctasks, int4* cface, unsigned char* vdegc, const int* vperm, int V) {
     go(k_face_active, nblk(ca.F, 256), 256, s, ca, factive);
-    go(k_vertex_contact_degree, nblk(V, 256), 256, s, vface_off, vface, (const unsigned char*)factive, vdegc, V);
+    go(k_vertex_contact_degree, nblk(V, 256), 256, s, vface_off, vface, (const unsigned char*)factive, vdegc, vperm,
+       V);
     go(k_contact_task_table, 1, kScanThreads, s, act_off, ncol, n_inst, cm_off, ctask, n_ctasks);
     go(k_contact_faces_fill, n_inst, 256, s, ca, act_faces, act_off, ncol, n_inst, (const int*)cm_off, vface_off,
        vface, fcol, vdegp, (const unsigned char*)factive, cface);

@@ -157,7 +157,8 @@ struct FlowContacts {
     const int4* face;         // (face, due words of vertices 0-1, vertex 2, 0): per vertex
                               // (writes per iteration) | (writes before this face) << 8
     const int* ntasks;        // contact tasks per iteration (written after each detection)
-    const unsigned char* vdegc;  // [V] active contact faces containing the vertex
+    const unsigned char* vdegc;  // [V] active contact faces containing the vertex (sweep numbering)
+    const int4* vfaces;       // [F] face vertices in the sweep's numbering
 };
 // variant 4 keeps the topology of a warp's tasks (patch records, vertex ids,
 // version words: 64 B per lane and task) in shared memory across iterations
@@ -283,10 +284,13 @@ int sweep_dataflow_blocks_per_sm(bool staged, int min_blocks);
 // shared memory (ntasks / warps <= kResidentTasks; sweep_versioned_smem bytes
 // per block).
 // fc.task != nullptr: the static contacts of ca run inside the sweep (FlowContacts).
+// The sweep numbers the vertices its own way (vperm: vertex -> record of xv,
+// chosen so that a task's lanes touch neighbouring records); pa.verts and
+// fc.vfaces are in that numbering.
 cudaError_t launch_sweep_versioned(const Launch& s, const TetArrays& t, const PatchArrays& pa, const int4* pver,
                                    const TaskArrays& ta, int iters, bool first_zero, float4* x, VerRec* xv, int V,
-                                   Flags* flags, int grid, int min_blocks, bool resident, const ContactArrays& ca,
-                                   const FlowContacts& fc);
+                                   const int* vperm, Flags* flags, int grid, int min_blocks, bool resident,
+                                   const ContactArrays& ca, const FlowContacts& fc);
 // blocks per SM of the versioned sweep with the dynamic shared memory it
 // needs when each warp owns `tasks_per_warp` tasks (0: not resident), with or
 // without the contact phases
@@ -299,7 +303,7 @@ void launch_stamp(const Launch& s, unsigned long long* p);
 void launch_flow_contact_tables(const Launch& s, const ContactArrays& ca, const int* act_faces, const int* act_off,
                                 int ncol, int n_inst, const int* vface_off, const int* vface, const int* fcol,
                                 const unsigned char* vdegp, unsigned char* factive, int* cm_off, int2* ctask,
-                                int* n_ctasks, int4* cface, unsigned char* vdegc, int V);
+                                int* n_ctasks, int4* cface, unsigned char* vdegc, const int* vperm, int V);
 inline size_t sweep_versioned_smem(int tasks_per_warp) { return (size_t)tasks_per_warp * 4 * 32 * sizeof(int4); }
 void launch_contacts_jacobi(const Launch& s, const ContactArrays& c, const float4* x, float4* dx, bool first);
 // after a detection: per instance and face colour, the faces with an active
