@@ -125,7 +125,7 @@ typedef struct {
                                /* the closest rest-surface face; needs faces     */
     int32_t gs_poll_ns;        /* versioned sweep (gs_variant 4): back-off in ns  */
                                /* between two polls of a vertex that is not yet   */
-                               /* due; 0 = 256                                    */
+                               /* due; 0 = 128                                    */
     int32_t gs_topology_reload;/* versioned sweep: 1 reloads each task's patch    */
                                /* records from global memory every phase; 0 keeps */
                                /* a warp's task topology in shared memory when it */

@@ -143,7 +143,7 @@ struct alignas(32) VerRec {
 };
 // face colours the versioned sweep's contact phases handle (more keep their own launches)
 constexpr int kMaxFlowFaceColours = 64;
-constexpr unsigned kPollNs = 256;  // default back-off of variant 4's polls
+constexpr unsigned kPollNs = 128;  // default back-off of variant 4's polls
 
 // Static contacts inside variant 4's sweep: after each detection, the faces
 // with an active static contact in colour-major order (colour, instance,
