@@ -238,8 +238,12 @@ def run_reference(args):
     every sweep and stop at ||r|| <= 1e-3 ||r(x_pred, 0)|| (the residual
     evaluations are outside the count's cost); the count used is the most any
     of them needed. The other warm-ups and the K timed substeps run exactly
-    that many sweeps, without residual evaluations. The mesh comes from the
-    oracle's own grid generator: this arm loads no product library."""
+    that many sweeps, without residual evaluations -- unless K such substeps
+    would take more than about 90 s: then each timed substep runs a sample of
+    s sweeps and its time is the zero-sweep substep's plus n/s times the
+    sampled sweeps' (every sequential sweep does the same work, so the cost
+    is linear in the sweep count). The mesh comes from the oracle's own grid
+    generator: this arm loads no product library."""
     rank = env_int("RANK", 0)
     if rank != 0:
         return 0
@@ -274,20 +278,30 @@ def run_reference(args):
     o.set_rel_tol(0.0)
     n_it = max(cal)
     reached = n_it < args.max_iters
-    o.set_num_iter(n_it)
-    for _ in range(args.warmup - n_cal):
+    # the zero-sweep substep and one sweep's cost, to size the timed substeps
+    o.set_num_iter(0)
+    t0 = min(one_step() for _ in range(2))
+    o.set_num_iter(1)
+    t1 = one_step()
+    budget_s = 90.0
+    n_run = n_it
+    if args.steps * (t0 + n_it * max(t1 - t0, 1e-9)) > budget_s:
+        n_run = max(4, min(n_it, int(budget_s / args.steps / max(t1 - t0, 1e-9))))
+    o.set_num_iter(n_run)
+    for _ in range(max(args.warmup - n_cal, 0)):
         one_step()
     times = [one_step() for _ in range(args.steps)]
-    t_step = statistics.mean(times)
-    # per-sweep cost against a zero-sweep substep (reported, not the headline)
-    o.set_num_iter(0)
-    t0 = min(o.time_steps(1) for _ in range(2))
-    per_iter = max((t_step - t0) / max(n_it, 1), 1e-12)
+    t_run = statistics.mean(times)
+    per_iter = max((t_run - t0) / max(n_run, 1), 1e-12)
+    t_step = t0 + n_it * per_iter
     sub = 1.0 / t_step
     order = "sequential Gauss-Seidel (element order)" if solver == O.GAUSS_SEIDEL else "Jacobi (plain sum)"
     sample = (f"FP64 oracle port, {order}, 1 thread (the reference solver is single-threaded); full "
-              f"{w.T:,}-tet mesh; {args.steps} driven substeps of {n_it} sweeps each, the sweeps this order needs "
-              f"to reach 1e-3 relative residual (most over the first {n_cal} substeps: {cal})")
+              f"{w.T:,}-tet mesh; {n_it} sweeps per substep, the sweeps this order needs to reach 1e-3 "
+              f"relative residual (most over the first {n_cal} substeps: {cal}); "
+              + (f"{args.steps} driven substeps of {n_it} sweeps each" if n_run == n_it else
+                 f"{args.steps} driven substeps of {n_run} sampled sweeps each, scaled to {n_it} sweeps over a "
+                 f"zero-sweep substep of {t0 * 1e3:.0f} ms"))
     w.iters = n_it
     line = {
         "metric": METRIC, "value": sub, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
