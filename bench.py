@@ -320,6 +320,32 @@ def run_reference(args):
     return 0
 
 
+def batch_roofline(s, b, ms_step, n):
+    """Roofline of the batched step's dominant kernel, taken like the block's:
+    launch counts and the other kernels' durations from n event-bracketed
+    steps (xpbd_profile_steps), the dominant kernel's duration from the
+    event-timed step (ms_step) minus them. Algorithmic bytes per sweep as for
+    the block, 80 B/tet + 28 B/vertex, over every instance (the contact
+    projections inside the same launch are not counted)."""
+    prof = s.profile_steps(n)
+    peak, peak_kind = measured_peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0] * kv[1][1])[0]
+    if dom != "project_gs":
+        return None
+    nl_step = prof[dom][1] / n
+    others_ms = sum(v[0] * v[1] / n for k, v in prof.items() if k != dom)
+    ms_launch = max(ms_step - others_ms, 1e-6) / nl_step
+    per_launch = (80.0 * b.T + 28.0 * b.V) * b.iters / nl_step
+    achieved = per_launch / (ms_launch * 1e-3) / 1e9
+    traffic, tkey = profiled_traffic(dom, "batched", s.params.gs_variant, b.iters if nl_step == 1 else None)
+    return {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": f"{peak_kind} hbm_gbs", "algorithmic_bytes_per_launch": per_launch,
+            "avg_launch_ms": ms_launch, "launches_per_step": nl_step, "traffic": traffic,
+            "traffic_source": f"profiles/roofline_traffic.txt {tkey}" if tkey else None,
+            "timing": "event-timed step minus the other kernels' event-timed share, per launch",
+            "kernel_ms_per_step": {k: v[0] * v[1] / n for k, v in prof.items()}}
+
+
 def batched_leg(steps=10, warmup=3, variants=(4, 1)):
     """The batched configuration (256 instances, 20 Gauss-Seidel sweeps, 1-4
     spheres each) for the default run's line: each sweep variant timed with
@@ -359,6 +385,7 @@ def batched_leg(steps=10, warmup=3, variants=(4, 1)):
         legs[var] = {"ms_per_step": float(np.mean(per)), "steps_per_s": 1e3 / float(np.mean(per)),
                      "launches_per_step": (s.launch_count() - l0) / steps}
         if var == 4:
+            legs[var]["roofline"] = batch_roofline(s, b, float(np.mean(per)), steps)
             # stamped steps, outside the timed ones
             s.set_latency_stamps(True)
             lat, whole = [], []
@@ -446,6 +473,15 @@ def run_batched(args):
     launches = s.launch_count() - l0
     per = [a.elapsed_time(c) for a, c in evs]
     ms = sum(per) / args.steps
+    if args.quick:
+        # timed region only (used for profiler runs)
+        print(json.dumps({"metric": METRIC, "value": 1e3 / ms, "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+                          "warmup": args.warmup, "ms_per_step": ms, "gpu_launches": int(launches),
+                          "config": {"workload": f"batched: {len(b.instances)} instances, {b.T:,} tets",
+                                     "iterations": b.iters}, "quick": True}), flush=True)
+        s.close()
+        return 0
+    roofline = batch_roofline(s, b, ms, args.steps)
     inst_lat = {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99)),
                 "definition": "every instance completes at the end of the step: percentiles of the step time"}
     try:
@@ -502,7 +538,7 @@ def run_batched(args):
         "unbatched": {"sum_ms_per_step": float(lat.sum()), "instance_latency_ms_p50": float(np.percentile(lat, 50)),
                       "instance_latency_ms_p99": float(np.percentile(lat, 99)),
                       "speedup_of_batching": float(lat.sum() / ms)},
-        "gpu_launches": int(launches), "clocks": clk, "autotune": tune,
+        "gpu_launches": int(launches), "roofline": roofline, "clocks": clk, "autotune": tune,
     }
     print(json.dumps(line), flush=True)
     s.close()

@@ -29,7 +29,7 @@
 extern "C" {
 #endif
 
-#define XPBD_ABI_VERSION 7
+#define XPBD_ABI_VERSION 8
 
 /* status codes */
 #define XPBD_OK 0
@@ -130,6 +130,12 @@ typedef struct {
                                /* records from global memory every phase; 0 keeps */
                                /* a warp's task topology in shared memory when it */
                                /* fits (default)                                  */
+    int32_t gs_l2_stream;      /* versioned sweep: L2 priority of what it streams */
+                               /* once per sweep (tet records, multipliers, patch */
+                               /* records): 0 = evict-first when these and the    */
+                               /* vertex records exceed 3/4 of the L2, so that the*/
+                               /* vertex records stay (default); 1 = always       */
+                               /* evict-first; -1 = never                         */
 } xpbd_params;
 
 /* Fills p with the reference's defaults (XPBDMeshObjectConfig.hpp:117-125,

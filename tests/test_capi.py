@@ -23,7 +23,7 @@ def test_library_exports_every_declared_entry_point(lib):
 
 
 def test_abi_version_and_status_strings(lib):
-    assert lib.xpbd_abi_version() == 7
+    assert lib.xpbd_abi_version() == 8
     assert lib.xpbd_status_string(0) == b"ok"
     assert b"invalid" in lib.xpbd_status_string(G.XPBD_ERR_INVALID)
 

@@ -100,7 +100,26 @@ def test_batch_full_size_runs(lib):
     s.close()
 
 
-@pytest.mark.parametrize("solver,ncand", [(G.SOLVER_GAUSS_SEIDEL, 48), (G.SOLVER_JACOBI, 12)])
+def test_l2_stream_priority_leaves_results_unchanged(lib):
+    """gs_l2_stream only sets the L2 eviction priority of the sweep's streamed
+    records (evict-first or normal): every mode gives the same positions bit
+    for bit, on a batch whose sweep streams its patch records (not resident)."""
+    b = _small_batch(n=8, seed=7)
+    xs = []
+    for mode in (-1, 0, 1):
+        s = W.make_batch_solver(b, gs_l2_stream=mode)
+        for _ in range(6):
+            W.drive_batch(s, b)
+            s.step(1)
+        xs.append(s.positions())
+        s.close()
+    np.testing.assert_array_equal(xs[0], xs[1])
+    np.testing.assert_array_equal(xs[0], xs[2])
+    with pytest.raises(G.XPBDError):
+        W.make_batch_solver(b, gs_l2_stream=2)
+
+
+@pytest.mark.parametrize("solver,ncand",[(G.SOLVER_GAUSS_SEIDEL, 48), (G.SOLVER_JACOBI, 12)])
 def test_autotuner_times_every_candidate_and_keeps_the_fastest(lib, solver, ncand):
     b = _small_batch(n=3)
     inst = [(w.X, w.tets, w.faces, w.E, w.nu, w.rho) for w in b.instances]

@@ -345,6 +345,16 @@ int build_flow_tasks(xpbd_ctx* c, const std::vector<int4>& pmeta, const std::vec
             if (with_faces) res_sm = std::min(res_sm, sweep_versioned_blocks_per_sm(c->prm.gs_min_blocks, per_warp, true));
             c->flow_resident = (long long)res_sm * sms >= c->flow_grid;
         }
+        // Each sweep streams the tet records (48 B), the multipliers (8 B)
+        // and, without the resident topology, the patch records (64 B) once;
+        // the vertex records (32 B) are polled and written by every patch
+        // around the vertex. When all of it is larger than 3/4 of the L2, the
+        // streams go evict-first so that they pass through the L2 without
+        // evicting the vertex records.
+        int l2 = 0;
+        XPBD_CU(c, cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+        const double streamed = 56.0 * c->T + (c->flow_resident ? 0.0 : 64.0 * P) + 32.0 * V;
+        c->flow_l2_first = c->prm.gs_l2_stream > 0 || (c->prm.gs_l2_stream == 0 && streamed > 0.75 * l2);
         XPBD_CU(c, cudaMemcpy(c->patch_ver.p, ver.data(), sizeof(int4) * P, cudaMemcpyHostToDevice));
     }
     return XPBD_OK;

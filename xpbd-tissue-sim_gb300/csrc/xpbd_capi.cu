@@ -43,7 +43,7 @@ bool valid_params(const xpbd_params& p) {
            (p.adjust_damping_to_material == 0 || p.adjust_damping_to_material == 1) &&
            (p.first_order == 0 || (p.damping_multiplier > 0 && std::isfinite(p.damping_multiplier))) &&
            (p.self_collisions == 0 || p.self_collisions == 1) && p.gs_poll_ns >= 0 && p.gs_poll_ns <= 1000000 &&
-           (p.gs_topology_reload == 0 || p.gs_topology_reload == 1);
+           (p.gs_topology_reload == 0 || p.gs_topology_reload == 1) && p.gs_l2_stream >= -1 && p.gs_l2_stream <= 1;
 }
 
 // The colour-launch kernel that stands in for a GS variant where the one-launch

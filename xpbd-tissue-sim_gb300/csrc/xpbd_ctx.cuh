@@ -116,6 +116,7 @@ struct xpbd_ctx {
     std::vector<int4> patch_ver_h;  // host copy of patch_ver
     unsigned flow_poll_limit = xg::kFlowLimit;
     unsigned flow_poll_ns = xg::kPollNs;
+    bool flow_l2_first = false;  // variant 4: streamed records evict-first (gs_l2_stream)
     // per-instance latency stamps (xpbd_set_latency_stamps): [0] substep start,
     // [1] substep end, [2 + j] task j's end of its last iteration
     DevBuf<unsigned long long> lat;
@@ -214,7 +215,7 @@ struct xpbd_ctx {
     xg::TaskArrays tasks() {
         return xg::TaskArrays{flow_tasks.p,       flow_dep_off.p, flow_dep.p,      flow_epoch.p,
                               flow_epoch.p + ntasks, ntasks,        flow_poll_limit, flow_poll_ns,
-                              lat_on ? lat.p : nullptr};
+                              lat_on ? lat.p : nullptr, flow_l2_first ? 1u : 0u};
     }
     xg::FlowContacts flowc() {
         return xg::FlowContacts{ctask.p, cface.p, n_ctasks.p, vdeg_c.p, faces_v.p};

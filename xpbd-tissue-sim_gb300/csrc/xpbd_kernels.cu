@@ -1265,6 +1265,8 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     if (lane == 0) mbar_init(&bar, 1);
     __syncwarp();
     unsigned phase = 0;
+    // L2 priority of what every sweep streams once (ta.l2_first)
+    const unsigned long long pol = l2_policy(ta.l2_first != 0);
     if (RESIDENT) {
         int k = 0;
         for (int j = gw; j < ta.ntasks; j += nw, k++) {
@@ -1310,22 +1312,19 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
     // same tasks every iteration: after its last patch task of an iteration
     // comes its first one, gw.)
     auto next_patch_task = [&](int j) { return j + nw < ta.ntasks ? j + nw : gw; };
-    int2 tk_next = make_int2(0, 0);  // descriptor (first patch, patches) of the task after the next
-    int rs = 0;                      // ring slot of the next task's records
-    auto stage_records = [&](int2 tk, int slot) {
+    int4 tk_next = make_int4(0, 0, 0, 0);  // descriptor of the task after the next
+    int rs = 0;                            // ring slot of the next task's records
+    auto stage_records = [&](int4 tk, int slot) {
         const bool on = lane < tk.y;
         const size_t p = on ? (size_t)(tk.x + lane) : 0;
         const unsigned nb = on ? 16u : 0u;
-        cp_async16(&ring[slot][0][lane], pa.meta + p, nb);
-        cp_async16(&ring[slot][1][lane], pa.verts + 2 * p, nb);
-        cp_async16(&ring[slot][2][lane], pa.verts + 2 * p + 1, nb);
-        cp_async16(&ring[slot][3][lane], pver + p, nb);
+        cp_async16_hint(&ring[slot][0][lane], pa.meta + p, nb, pol);
+        cp_async16_hint(&ring[slot][1][lane], pa.verts + 2 * p, nb, pol);
+        cp_async16_hint(&ring[slot][2][lane], pa.verts + 2 * p + 1, nb, pol);
+        cp_async16_hint(&ring[slot][3][lane], pver + p, nb, pol);
         cp_async_commit();
     };
-    auto load_desc = [&](int j) {
-        const int4 d = __ldg(ta.task + j);
-        return make_int2(d.x, d.y);
-    };
+    auto load_desc = [&](int j) { return __ldg(ta.task + j); };
     if (!RESIDENT && gw < ta.ntasks) {
         stage_records(load_desc(gw), 0);
         tk_next = load_desc(next_patch_task(gw));
@@ -1377,9 +1376,9 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 const unsigned bytes = (unsigned)(s1 - s0) * 16u;
                 mbar_arrive_expect_tx(&bar, 3u * bytes);
-                tma_load_1d(srec[0], t.m0 + s0, bytes, &bar);
-                tma_load_1d(srec[1], t.m1 + s0, bytes, &bar);
-                tma_load_1d(srec[2], t.m2 + s0, bytes, &bar);
+                tma_load_1d_hint(srec[0], t.m0 + s0, bytes, &bar, pol);
+                tma_load_1d_hint(srec[1], t.m1 + s0, bytes, &bar, pol);
+                tma_load_1d_hint(srec[2], t.m2 + s0, bytes, &bar, pol);
             }
             // The task's multipliers, read and (after the task) written back by
             // coalesced accesses; only this warp touches them meanwhile. The
@@ -1390,7 +1389,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
             for (int u = 0; u < kLamPerLane; u++) {
                 const int r = lane + 32 * u;
                 lt[u] = make_float2(0.f, 0.f);
-                if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = t.lam[s0 + r];
+                if (!(FIRST_ZERO && it == 0) && r < ns) lt[u] = ld_f2_hint(t.lam + s0 + r, pol);
             }
             // Grid hexes (after the build's canonical corner order every one has
             // the layout kHexLocA) keep the patch's vertices in registers.
@@ -1410,7 +1409,7 @@ __global__ void __launch_bounds__(kFlowBlock, MINB)
                 if (lane + 32 * u < ns) lt[u] = slam[lane + 32 * u];
 #pragma unroll
             for (int u = 0; u < kLamPerLane; u++)
-                if (lane + 32 * u < ns) t.lam[s0 + lane + 32 * u] = lt[u];
+                if (lane + 32 * u < ns) st_f2_hint(t.lam + s0 + lane + 32 * u, lt[u], pol);
           } else if (CONTACTS) {
             const int2 ct = fc.task[j - ta.ntasks];
             if (lane < ct.y) {

@@ -131,6 +131,8 @@ struct TaskArrays {
     unsigned poll_ns;     // variant 4: back-off between two polls of a vertex not yet due
     unsigned long long* stamp;  // variant 4, optional: stamp[2 + j] = device clock (ns) when
                                 // task j ends its last iteration
+    unsigned l2_first;    // variant 4: what a sweep streams once (tet records, multipliers,
+                          // patch records) is loaded and stored evict-first in L2
 };
 
 // Variant 4's vertex record: four aligned 64-bit words (x, ver), (y, ver),

@@ -65,7 +65,7 @@ class Params(C.Structure):
         ("num_local_collision_iters", C.c_int32),
         ("first_order", C.c_int32), ("adjust_damping_to_material", C.c_int32), ("damping_multiplier", C.c_double),
         ("self_collisions", C.c_int32), ("gs_poll_ns", C.c_int32),
-        ("gs_topology_reload", C.c_int32),
+        ("gs_topology_reload", C.c_int32), ("gs_l2_stream", C.c_int32),
     ]
 
 
