@@ -72,7 +72,8 @@ def _create(lib, X, tets, params):
 def test_create_rejects_bad_parameters_before_touching_a_device(lib):
     X, tets, _ = G.grid_mesh(2, 2, 2, 0.5)
     for field, value in [("dt", -1.0), ("num_iters", -2), ("solver_type", 7), ("block_size", 48),
-                         ("max_contacts_per_face", 99)]:
+                         ("max_contacts_per_face", 99), ("gs_poll_ns", -1), ("gs_topology_reload", 2),
+                         ("gs_l2_stream", 2), ("gs_l2_stream", -2)]:
         p = G.default_params()
         setattr(p, field, value)
         st, h = _create(lib, X, tets, p)
