@@ -54,3 +54,25 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     monkeypatch.setenv("RANK", "1")
     args = types.SimpleNamespace(workload="block", solver=None, steps=1, warmup=3)
     assert bench.run_reference(args) == 0
+
+
+def test_batched_roofline_takes_the_sweep_share_of_the_step():
+    """batch_roofline: the dominant kernel's time is the event-timed step minus
+    the other kernels' event-timed share, over its launches per step; its
+    algorithmic bytes are (80 B/tet + 28 B/vertex) per sweep over the whole
+    batch."""
+    n = 4
+    prof = {"project_gs": (2.5, n), "predict": (0.02, n), "finalize": (0.03, n)}
+    s = types.SimpleNamespace(profile_steps=lambda k: prof, params=types.SimpleNamespace(gs_variant=4))
+    b = types.SimpleNamespace(T=1000, V=300, iters=20)
+    r = bench.batch_roofline(s, b, 2.05, n)
+    assert r["kernel"] == "project_gs" and r["launches_per_step"] == 1
+    assert abs(r["avg_launch_ms"] - 2.0) < 1e-12
+    per_launch = (80.0 * 1000 + 28.0 * 300) * 20
+    assert abs(r["algorithmic_bytes_per_launch"] - per_launch) < 1e-6
+    assert abs(r["achieved"] - per_launch / 2.0e-3 / 1e9) < 1e-9
+    assert abs(r["frac"] - r["achieved"] / r["peak"]) < 1e-12
+    # a step whose dominant kernel is not the sweep has no sweep roofline
+    s2 = types.SimpleNamespace(profile_steps=lambda k: {"detect": (9.0, n), "project_gs": (0.1, n)},
+                               params=s.params)
+    assert bench.batch_roofline(s2, b, 2.0, n) is None
