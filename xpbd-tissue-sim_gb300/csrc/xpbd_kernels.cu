@@ -59,9 +59,11 @@ __global__ void k_kinematic(float4* __restrict__ x, const int* __restrict__ idx,
 
 // Jacobi sweep: every tet reads the same x, its updates are summed into dx by
 // 16-byte vector reductions (XPBDJacobiSolver.hpp:79-114, plain summation).
+// Four blocks per SM (64 registers, a few bytes spilled): the launch waits on
+// its gathers and reductions, and 32 warps per SM hide more of that than 16.
 template <bool FIRST, bool SEPARATE, bool RES>
-__global__ void __launch_bounds__(256) k_project_jacobi(TetArrays t, int T, const float4* __restrict__ x,
-                                                        float4* __restrict__ dx, ResidualSink res, Flags* flags) {
+__global__ void __launch_bounds__(256, 4) k_project_jacobi(TetArrays t, int T, const float4* __restrict__ x,
+                                                           float4* __restrict__ dx, ResidualSink res, Flags* flags) {
     const int slot = blockIdx.x * blockDim.x + threadIdx.x;
     double rsq = 0.0;
     int4 e;
