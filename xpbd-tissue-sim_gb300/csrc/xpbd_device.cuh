@@ -71,16 +71,10 @@ __device__ __forceinline__ bool mbar_wait_bounded(unsigned long long* bar, unsig
 
 constexpr unsigned kWaitLimit = 1u << 20;
 
-// 16-byte asynchronous copy global -> shared (cp.async, cache-global); with
-// src_bytes = 0 nothing is read and the 16 bytes are zero-filled. Completion
-// (cp_async_wait_all) makes the data visible to the issuing thread.
-__device__ __forceinline__ void cp_async16(void* dst, const void* src, unsigned src_bytes) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(dst)), "l"(src), "r"(src_bytes)
-                 : "memory");
-}
-// The same copies with an L2 eviction-priority policy (createpolicy): data a
-// kernel reads or writes once per pass can go evict-first, so that it passes
-// through the L2 without pushing out what the pass keeps reusing.
+// Copies with an L2 eviction-priority policy (createpolicy): data a kernel
+// reads or writes once per pass can go evict-first, so that it passes through
+// the L2 without pushing out what the pass keeps reusing; evict-normal is the
+// default priority.
 __device__ __forceinline__ unsigned long long l2_policy(bool evict_first) {
     unsigned long long p;
     if (evict_first)
@@ -97,6 +91,9 @@ __device__ __forceinline__ void tma_load_1d_hint(void* dst, const void* src, uns
         "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
         : "memory");
 }
+// 16-byte asynchronous copy global -> shared (cp.async, cache-global); with
+// src_bytes = 0 nothing is read and the 16 bytes are zero-filled. Completion
+// (cp_async_wait_all) makes the data visible to the issuing thread.
 __device__ __forceinline__ void cp_async16_hint(void* dst, const void* src, unsigned src_bytes,
                                                 unsigned long long pol) {
     asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2, %3;" ::"r"(smem_u32(dst)), "l"(src),
