@@ -1244,6 +1244,10 @@ __device__ __forceinline__ void versioned_patch(const TetArrays& t, const TaskAr
 // words: four int4 per lane and task) is read once into shared memory, before
 // the wait on the previous kernel, so a phase's first poll does not wait for
 // the task, patch and vertex-id loads.
+// ta.l2_first: the tet records' bulk copies, the patch records' cp.async and
+// the multiplier loads and stores carry an evict-first L2 policy (the build
+// sets it when these streams and the vertex records outgrow the L2), so the
+// vertex records, which every patch around a vertex polls and writes, stay.
 // CONTACTS: after every iteration's patch tasks come the contact tasks
 // (FlowContacts): a lane takes one face with an active static contact,
 // polls its three vertices, projects the face's contacts in slot order
